@@ -1,0 +1,767 @@
+// assembly.cu -- element integration and scatter kernels of libifemgpu.
+//
+// Data flow of one assembly (ifemgpu_assemble):
+//   1. k_basis_tables   1D B-spline values/derivatives at the Gauss points of
+//                       every knot span (Cox-de Boor, FP64), per patch and
+//                       direction -- the GPU replacement of IFEM's
+//                       BasisFunctionCache (src/ASM/ASMs3D.C:3996-4143).
+//   2. volume passes    one launch per element colour.  Elements of one
+//                       colour share no node, so every CTA adds its element
+//                       matrix into the matrix without atomics and the sum
+//                       order is fixed (deterministic).  Replaces the element
+//                       loop of ASMs3D::integrate (src/ASM/ASMs3D.C:2118-2325)
+//                       and the scatter of assemSparse
+//                       (src/LinAlg/SparseMatrix.C:614-688).
+//   3. face passes      Neumann (traction / flux) integration on patch faces
+//                       (src/ASM/ASMs3D.C:2547-2812), also colour by colour.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "ifemgpu_internal.h"
+
+namespace ifemgpu {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Gauss-Legendre rule on [-1,1] (ascending), Newton iteration on P_n.
+void gaussRule(int n, double* x, double* w)
+{
+  for (int i = 0; i < (n + 1) / 2; i++) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; k++) {
+        double pk = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = pk;
+      }
+      if (n == 1) { p0 = 1.0; p1 = z; }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-17) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= n; k++) {
+      double pk = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+      p0 = p1;
+      p1 = pk;
+    }
+    if (n == 1) { p0 = 1.0; p1 = z; }
+    dp = n * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = -z;
+    x[n - 1 - i] = z;
+    w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+  if (n % 2) x[n / 2] = 0.0;
+}
+
+int gaussCount(int nGauss, int order, bool neumann)
+{
+  // ASMbase::getNoGaussPt semantics (src/ASM/ASMbase.C:1788-1798)
+  if (nGauss <= -order) return 0;
+  if (nGauss > 0 && nGauss < 11) return nGauss;
+  if (neumann) return order;
+  return order + nGauss % 10;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Device Cox-de Boor: values N[0..p] and first derivatives D[0..p] of the
+// degree-p B-splines that are non-zero on span k (U[k] <= u < U[k+1]).
+__device__ void bsplineDers(const double* __restrict__ U, int p, int k, double u,
+                            double* N, double* D)
+{
+  double left[kMaxDeg + 1], right[kMaxDeg + 1], lo[kMaxDeg + 1];
+  N[0] = 1.0;
+  for (int j = 1; j <= p; j++) {
+    if (j == p) {
+      for (int r = 0; r < p; r++) lo[r] = N[r];  // degree p-1 values
+    }
+    left[j] = u - U[k + 1 - j];
+    right[j] = U[k + j] - u;
+    double saved = 0.0;
+    for (int r = 0; r < j; r++) {
+      double temp = N[r] / (right[r + 1] + left[j - r]);
+      N[r] = saved + right[r + 1] * temp;
+      saved = left[j - r] * temp;
+    }
+    N[j] = saved;
+  }
+  if (p == 0) { D[0] = 0.0; return; }
+  // d/du N_{i,p} = p (N_{i,p-1}/(U_{i+p}-U_i) - N_{i+1,p-1}/(U_{i+p+1}-U_{i+1}))
+  for (int r = 0; r <= p; r++) {
+    const int i = k - p + r;
+    double a = 0.0, b = 0.0;
+    if (r >= 1) {
+      double den = U[i + p] - U[i];
+      a = den > 0.0 ? lo[r - 1] / den : 0.0;
+    }
+    if (r <= p - 1) {
+      double den = U[i + p + 1] - U[i + 1];
+      b = den > 0.0 ? lo[r] / den : 0.0;
+    }
+    D[r] = p * (a - b);
+  }
+}
+
+// 1D tables of one patch: thread per (direction, span, Gauss point).
+__global__ void k_basis_tables(DevPatch P)
+{
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = tid;
+  for (int d = 0; d < P.dim; d++) {
+    const int cnt = P.nel[d] * P.ng[d];
+    if (t < cnt) {
+      const int e = t / P.ng[d], g = t % P.ng[d];
+      const double* U = P.knots[d];
+      const int k = P.p[d] + e;
+      const double u0 = U[k], u1 = U[k + 1];
+      const double u = 0.5 * ((u1 - u0) * P.gx[d][g] + u1 + u0);
+      double N[kMaxDeg + 1], D[kMaxDeg + 1];
+      bsplineDers(U, P.p[d], k, u, N, D);
+      double* tn = P.tabN[d] + (size_t)t * (P.p[d] + 1);
+      double* td = P.tabD[d] + (size_t)t * (P.p[d] + 1);
+      for (int r = 0; r <= P.p[d]; r++) { tn[r] = N[r]; td[r] = D[r]; }
+      if (g == 0) P.span[d][e] = u1 - u0;
+      return;
+    }
+    t -= cnt;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 volume kernel: one CTA per element of one colour.
+//
+// Shared memory (doubles): Xn[nen*4] | N[nq*nen] | dX[3][nq*nen] | Jinv[nq*9]
+//                          | wq[nq] | kq[nq] | fq[nq]   then  eq[nd] (int)
+__device__ inline int elemNode(const DevPatch& P, int e, int a)
+{
+  const int q1 = P.p[0] + 1, q2 = P.p[1] + 1;
+  const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
+  const int i = a % q1, j = (a / q1) % q2, k = a / (q1 * q2);
+  return ((e3 + k) * P.n[1] + e2 + j) * P.n[0] + e1 + i;
+}
+
+// Position of row `r` (0-based) in column `c` (0-based) of the CSC pattern.
+__device__ inline int findRow(const int* __restrict__ colptr, const int* __restrict__ rowidx,
+                              int c, int r)
+{
+  int lo = colptr[c], hi = colptr[c + 1] - 1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    int v = rowidx[mid];
+    if (v == r) return mid;
+    if (v < r) lo = mid + 1; else hi = mid - 1;
+  }
+  return -1;
+}
+
+struct SysView {
+  const int* madof;
+  const int* meqn;
+  const double* c0;
+  const int* colptr;
+  const int* rowidx;
+  double* K;
+  double* b;
+  unsigned long long* counters;
+};
+
+__global__ void __launch_bounds__(256)
+k_volume_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ items,
+              SysView S)
+{
+  extern __shared__ double sm[];
+  const Item it = items[blockIdx.x];
+  const DevPatch& P = patches[it.patch];
+  const int nen = P.nen, nq = P.nq, dim = P.dim, npv = P.npv, nd = nen * npv;
+  const int e = it.elem;
+  double* Xn = sm;
+  double* Nq = Xn + nen * 4;
+  double* dX = Nq + nq * nen;          // 3 planes of nq*nen
+  double* Ji = dX + 3 * nq * nen;      // nq * 9
+  double* wq = Ji + nq * 9;
+  double* kq = wq + nq;
+  double* fq = kq + nq;
+  int* eq = reinterpret_cast<int*>(fq + nq);
+  const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
+  const int q1 = P.p[0] + 1, q2 = P.p[1] + 1;
+
+  // element nodes: coordinates and equation numbers
+  for (int a = threadIdx.x; a < nen; a += blockDim.x) {
+    const int node = elemNode(P, e, a);
+    for (int c = 0; c < 4; c++) Xn[a * 4 + c] = P.ctrl[(size_t)node * 4 + c];
+    const int g = P.firstNode + node;
+    const int d0 = S.madof[g] - 1;
+    for (int c = 0; c < npv; c++) eq[a * npv + c] = S.meqn[d0 + c];
+  }
+  __syncthreads();
+
+  // tensor-product basis (times weight) at every (Gauss point, function)
+  for (int t = threadIdx.x; t < nq * nen; t += blockDim.x) {
+    const int q = t / nen, a = t % nen;
+    const int gi = q % P.ng[0], gj = (q / P.ng[0]) % P.ng[1], gk = q / (P.ng[0] * P.ng[1]);
+    const int i = a % q1, j = (a / q1) % q2, k = a / (q1 * q2);
+    const double* n0 = P.tabN[0] + ((size_t)e1 * P.ng[0] + gi) * q1;
+    const double* d0 = P.tabD[0] + ((size_t)e1 * P.ng[0] + gi) * q1;
+    const double* n1 = P.tabN[1] + ((size_t)e2 * P.ng[1] + gj) * q2;
+    const double* d1 = P.tabD[1] + ((size_t)e2 * P.ng[1] + gj) * q2;
+    double N, du, dv, dw = 0.0;
+    if (dim == 3) {
+      const int q3 = P.p[2] + 1;
+      const double* n2 = P.tabN[2] + ((size_t)e3 * P.ng[2] + gk) * q3;
+      const double* d2 = P.tabD[2] + ((size_t)e3 * P.ng[2] + gk) * q3;
+      N = n0[i] * n1[j] * n2[k];
+      du = d0[i] * n1[j] * n2[k];
+      dv = n0[i] * d1[j] * n2[k];
+      dw = n0[i] * n1[j] * d2[k];
+    } else {
+      N = n0[i] * n1[j];
+      du = d0[i] * n1[j];
+      dv = n0[i] * d1[j];
+    }
+    Nq[t] = N;
+    dX[t] = du;
+    dX[nq * nen + t] = dv;
+    dX[2 * nq * nen + t] = dw;
+  }
+  __syncthreads();
+
+  // per Gauss point: rational weighting, Jacobian (FP64), inverse, detJxW
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    double* Nr = Nq + q * nen;
+    double* Du = dX + q * nen;
+    double* Dv = dX + nq * nen + q * nen;
+    double* Dw = dX + 2 * nq * nen + q * nen;
+    if (P.rational) {
+      double W = 0.0, Wu = 0.0, Wv = 0.0, Ww = 0.0;
+      for (int a = 0; a < nen; a++) {
+        const double w = Xn[a * 4 + 3];
+        W += w * Nr[a];
+        Wu += w * Du[a];
+        Wv += w * Dv[a];
+        Ww += w * Dw[a];
+      }
+      for (int a = 0; a < nen; a++) {
+        const double w = Xn[a * 4 + 3];
+        const double R = w * Nr[a] / W;
+        Du[a] = (w * Du[a] - R * Wu) / W;
+        Dv[a] = (w * Dv[a] - R * Wv) / W;
+        Dw[a] = (w * Dw[a] - R * Ww) / W;
+        Nr[a] = R;
+      }
+    }
+    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // column-major J(r,c) = dX_r/du_c
+    double X[3] = {0, 0, 0};
+    for (int a = 0; a < nen; a++) {
+      const double x = Xn[a * 4], y = Xn[a * 4 + 1], z = Xn[a * 4 + 2];
+      J[0] += x * Du[a]; J[1] += y * Du[a]; J[2] += z * Du[a];
+      J[3] += x * Dv[a]; J[4] += y * Dv[a]; J[5] += z * Dv[a];
+      J[6] += x * Dw[a]; J[7] += y * Dw[a]; J[8] += z * Dw[a];
+      X[0] += x * Nr[a]; X[1] += y * Nr[a]; X[2] += z * Nr[a];
+    }
+    double det, B[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (dim == 3) {
+      // matrix<T>::det / inverse (src/LinAlg/matrix.h:790-850), T(i,j)=J[(j-1)*3+i-1]
+      det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[3] * (J[1] * J[8] - J[2] * J[7]) +
+            J[6] * (J[1] * J[5] - J[2] * J[4]);
+      if (det > kEpsZ || det < -kEpsZ) {
+        B[0] = (J[4] * J[8] - J[5] * J[7]) / det;
+        B[1] = -(J[1] * J[8] - J[2] * J[7]) / det;
+        B[2] = (J[1] * J[5] - J[2] * J[4]) / det;
+        B[3] = -(J[3] * J[8] - J[5] * J[6]) / det;
+        B[4] = (J[0] * J[8] - J[2] * J[6]) / det;
+        B[5] = -(J[0] * J[5] - J[2] * J[3]) / det;
+        B[6] = (J[3] * J[7] - J[4] * J[6]) / det;
+        B[7] = -(J[0] * J[7] - J[1] * J[6]) / det;
+        B[8] = (J[0] * J[4] - J[1] * J[3]) / det;
+      }
+    } else {
+      // 2x2: J(r,c) at J[c*3+r] in the 3x3 storage above
+      det = J[0] * J[4] - J[1] * J[3];
+      if (det > kEpsZ || det < -kEpsZ) {
+        B[0] = J[4] / det; B[1] = -J[1] / det;
+        B[3] = -J[3] / det; B[4] = J[0] / det;
+      }
+    }
+    double w = 0.0;
+    if (det > kEpsZ || det < -kEpsZ) {
+      const int gi = q % P.ng[0], gj = (q / P.ng[0]) % P.ng[1], gk = q / (P.ng[0] * P.ng[1]);
+      double dV = (dim == 3 ? 0.125 : 0.25) * P.span[0][e1] * P.span[1][e2];
+      if (dim == 3) dV *= P.span[2][e3];
+      w = det * dV * P.gw[0][gi] * P.gw[1][gj];
+      if (dim == 3) w *= P.gw[2][gk];
+    } else {
+      atomicAdd(S.counters, 1ull);
+    }
+    wq[q] = w;
+    for (int c = 0; c < 9; c++) Ji[q * 9 + c] = B[c];
+    // material data at the point
+    double kap = P.kappa, f = P.source;
+    if (P.kind == IFEMGPU_POISSON) {
+      if (P.logk) {
+        double g = 0.0;
+        for (int a = 0; a < nen; a++) g += Nr[a] * P.logk[elemNode(P, e, a)];
+        kap *= exp(g);
+      }
+      if (P.source_shape == IFEMGPU_SOURCE_SINE)
+        for (int c = 0; c < dim; c++) f *= sin(M_PI * X[c]);
+      if (P.noise) {
+        double s = 0.0;
+        for (int a = 0; a < nen; a++) s += Nr[a] * P.noise[elemNode(P, e, a)];
+        f *= 1.0 + s;
+      }
+    }
+    kq[q] = kap * w;
+    fq[q] = f;
+  }
+  __syncthreads();
+
+  // dNdX = dNdu * J^-1 in place
+  for (int t = threadIdx.x; t < nq * nen; t += blockDim.x) {
+    const int q = t / nen;
+    const double* B = Ji + q * 9;
+    const double du = dX[t], dv = dX[nq * nen + t], dw = dX[2 * nq * nen + t];
+    // (dNdX)_c = sum_k dNdu_k * Jinv(k,c), Jinv column-major B[c*3+k]
+    dX[t] = du * B[0] + dv * B[1] + dw * B[2];
+    dX[nq * nen + t] = du * B[3] + dv * B[4] + dw * B[5];
+    dX[2 * nq * nen + t] = du * B[6] + dv * B[7] + dw * B[8];
+  }
+  __syncthreads();
+
+  // element matrix, node pair by node pair, scattered directly
+  const double lam = P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu));
+  const double mu = P.E / (2.0 * (1.0 + P.nu));
+  for (int t = threadIdx.x; t < nen * nen; t += blockDim.x) {
+    const int a = t % nen, bn = t / nen;
+    double Ke[9];
+    if (P.kind == IFEMGPU_POISSON) {
+      double acc = 0.0;
+      for (int q = 0; q < nq; q++) {
+        if (wq[q] == 0.0) continue;
+        const double s = kq[q];
+        double v = 0.0;
+        for (int c = 0; c < dim; c++)
+          v += dX[c * nq * nen + q * nen + a] * s * dX[c * nq * nen + q * nen + bn];
+        acc += v;
+      }
+      Ke[0] = acc;
+    } else {
+      double G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int q = 0; q < nq; q++) {
+        const double w = wq[q];
+        if (w == 0.0) continue;
+        const double ax = dX[q * nen + a] * w, ay = dX[nq * nen + q * nen + a] * w,
+                     az = dX[2 * nq * nen + q * nen + a] * w;
+        const double bx = dX[q * nen + bn], by = dX[nq * nen + q * nen + bn],
+                     bz = dX[2 * nq * nen + q * nen + bn];
+        G[0] += ax * bx; G[1] += ax * by; G[2] += ax * bz;
+        G[3] += ay * bx; G[4] += ay * by; G[5] += ay * bz;
+        G[6] += az * bx; G[7] += az * by; G[8] += az * bz;
+      }
+      const double tr = G[0] + G[4] + G[8];
+      for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++)
+          Ke[k * 3 + l] = lam * G[k * 3 + l] + mu * G[l * 3 + k] + (k == l ? mu * tr : 0.0);
+    }
+    // scatter the npv x npv block: rows of node a, columns of node bn
+    int firstCol = -1, firstRow = -1;
+    for (int l = 0; l < npv && firstCol < 0; l++)
+      if (eq[bn * npv + l] > 0) firstCol = eq[bn * npv + l] - 1;
+    for (int k = 0; k < npv && firstRow < 0; k++)
+      if (eq[a * npv + k] > 0) firstRow = eq[a * npv + k] - 1;
+    if (firstCol < 0 || firstRow < 0) continue;
+    const int pos0 = findRow(S.colptr, S.rowidx, firstCol, firstRow);
+    if (pos0 < 0) { atomicAdd(S.counters + 1, 1ull); continue; }
+    const int off = pos0 - S.colptr[firstCol];
+    for (int l = 0; l < npv; l++) {
+      const int ce = eq[bn * npv + l];
+      if (ce <= 0) continue;
+      int rank = 0;
+      for (int k = 0; k < npv; k++) {
+        const int re = eq[a * npv + k];
+        if (re <= 0) continue;
+        S.K[S.colptr[ce - 1] + off + rank] += Ke[k * npv + l];
+        rank++;
+      }
+    }
+  }
+
+  // element load vector and prescribed-DOF corrections, row by row
+  for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+    const int r = eq[i];
+    if (r <= 0) continue;
+    const int a = i / npv, k = i % npv;
+    double fe = 0.0;
+    for (int q = 0; q < nq; q++) {
+      if (wq[q] == 0.0) continue;
+      const double Na = Nq[q * nen + a];
+      if (P.kind == IFEMGPU_POISSON) fe += Na * fq[q] * wq[q];
+      else fe += P.body[k] * Na * wq[q];
+    }
+    S.b[r - 1] += fe;
+    if (S.c0 == nullptr) continue;
+    for (int j = 0; j < nd; j++) {
+      const int ce = eq[j];
+      if (ce >= 0) continue;
+      const int bn = j / npv, l = j % npv;
+      double kij = 0.0;
+      for (int q = 0; q < nq; q++) {
+        const double w = wq[q];
+        if (w == 0.0) continue;
+        if (P.kind == IFEMGPU_POISSON) {
+          double v = 0.0;
+          for (int c = 0; c < dim; c++)
+            v += dX[c * nq * nen + q * nen + a] * kq[q] * dX[c * nq * nen + q * nen + bn];
+          kij += v;
+        } else {
+          const double ak = dX[k * nq * nen + q * nen + a] * w;
+          const double al = dX[l * nq * nen + q * nen + a] * w;
+          double g = 0.0;
+          for (int c = 0; c < 3; c++)
+            g += dX[c * nq * nen + q * nen + a] * w * dX[c * nq * nen + q * nen + bn];
+          kij += lam * ak * dX[l * nq * nen + q * nen + bn] +
+                 mu * al * dX[k * nq * nen + q * nen + bn] + (k == l ? mu * g : 0.0);
+        }
+      }
+      S.b[r - 1] -= S.c0[-ce - 1] * kij;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Face (Neumann) kernel: one CTA per face element of one colour, FP64.
+// Shared memory (doubles): Xn[nen*4] | Nf[nqf*nen] | wf[nqf]  then eq[nd] (int)
+__global__ void __launch_bounds__(128)
+k_face_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ items,
+            const double* __restrict__ neumann, SysView S)
+{
+  extern __shared__ double sm[];
+  const Item it = items[blockIdx.x];
+  const DevPatch& P = patches[it.patch];
+  const int nen = P.nen, npv = P.npv, nd = nen * npv, e = it.elem;
+  const int face = it.face;
+  const int faceDir = (face % 10 + 1) / ((face % 2) ? -2 : 2);
+  const int nd0 = abs(faceDir) - 1;
+  const int t1 = 1 + abs(faceDir) % 3, t2 = 1 + t1 % 3;
+  int ng[3];
+  for (int d = 0; d < 3; d++) ng[d] = d == nd0 ? 1 : P.ngf[d];
+  const int nqf = ng[0] * ng[1] * ng[2];
+  double* Xn = sm;
+  double* Nf = Xn + nen * 4;
+  double* wf = Nf + nqf * nen;
+  int* eq = reinterpret_cast<int*>(wf + nqf);
+  const int ee[3] = {e % P.nel[0], (e / P.nel[0]) % P.nel[1], e / (P.nel[0] * P.nel[1])};
+  const int q1 = P.p[0] + 1, q2 = P.p[1] + 1;
+  for (int a = threadIdx.x; a < nen; a += blockDim.x) {
+    const int node = elemNode(P, e, a);
+    for (int c = 0; c < 4; c++) Xn[a * 4 + c] = P.ctrl[(size_t)node * 4 + c];
+    const int d0 = S.madof[P.firstNode + node] - 1;
+    for (int c = 0; c < npv; c++) eq[a * npv + c] = S.meqn[d0 + c];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nqf; q += blockDim.x) {
+    const int gi[3] = {q % ng[0], (q / ng[0]) % ng[1], q / (ng[0] * ng[1])};
+    double Nd[3][kMaxDeg + 1], Dd[3][kMaxDeg + 1];
+    double wt = 0.25;
+    for (int d = 0; d < 3; d++) {
+      const double* U = P.knots[d];
+      const int k = P.p[d] + ee[d];
+      double u;
+      if (d == nd0) {
+        u = faceDir < 0 ? U[P.p[d]] : U[P.n[d]];
+      } else {
+        const double u0 = U[k], u1 = U[k + 1];
+        u = 0.5 * ((u1 - u0) * P.fx[d][gi[d]] + u1 + u0);
+        wt *= (u1 - u0) * P.fw[d][gi[d]];
+      }
+      bsplineDers(U, P.p[d], k, u, Nd[d], Dd[d]);
+    }
+    double* Nr = Nf + q * nen;
+    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double W = 0.0, Wd[3] = {0, 0, 0};
+    // pass 1: weight function and its derivatives
+    for (int a = 0; a < nen; a++) {
+      const int i = a % q1, j = (a / q1) % q2, k = a / (q1 * q2);
+      const double w = Xn[a * 4 + 3];
+      const double N = Nd[0][i] * Nd[1][j] * Nd[2][k];
+      W += w * N;
+      Wd[0] += w * Dd[0][i] * Nd[1][j] * Nd[2][k];
+      Wd[1] += w * Nd[0][i] * Dd[1][j] * Nd[2][k];
+      Wd[2] += w * Nd[0][i] * Nd[1][j] * Dd[2][k];
+    }
+    for (int a = 0; a < nen; a++) {
+      const int i = a % q1, j = (a / q1) % q2, k = a / (q1 * q2);
+      const double w = P.rational ? Xn[a * 4 + 3] : 1.0;
+      const double N = Nd[0][i] * Nd[1][j] * Nd[2][k];
+      double d[3] = {Dd[0][i] * Nd[1][j] * Nd[2][k], Nd[0][i] * Dd[1][j] * Nd[2][k],
+                     Nd[0][i] * Nd[1][j] * Dd[2][k]};
+      double R = N;
+      if (P.rational) {
+        R = w * N / W;
+        for (int c = 0; c < 3; c++) d[c] = (w * d[c] - R * Wd[c]) / W;
+      }
+      Nr[a] = R;
+      for (int c = 0; c < 3; c++) {
+        J[c * 3 + 0] += Xn[a * 4 + 0] * d[c];
+        J[c * 3 + 1] += Xn[a * 4 + 1] * d[c];
+        J[c * 3 + 2] += Xn[a * 4 + 2] * d[c];
+      }
+    }
+    const double* ta = J + 3 * (t1 - 1);
+    const double* tb = J + 3 * (t2 - 1);
+    const double nx = ta[1] * tb[2] - ta[2] * tb[1], ny = ta[2] * tb[0] - ta[0] * tb[2],
+                 nz = ta[0] * tb[1] - ta[1] * tb[0];
+    const double dS = sqrt(nx * nx + ny * ny + nz * nz);
+    const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[3] * (J[1] * J[8] - J[2] * J[7]) +
+                       J[6] * (J[1] * J[5] - J[2] * J[4]);
+    wf[q] = (det > kEpsZ || det < -kEpsZ) ? dS * wt : 0.0;
+  }
+  __syncthreads();
+  const double* t = neumann + 3 * it.bc;
+  for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+    const int r = eq[i];
+    if (r <= 0) continue;
+    const int a = i / npv, c = i % npv;
+    double fe = 0.0;
+    for (int q = 0; q < nqf; q++)
+      if (wf[q] != 0.0) fe += t[c] * Nf[q * nen + a] * wf[q];
+    S.b[r - 1] += fe;
+  }
+}
+
+// ---------------------------------------------------------------------------
+size_t volumeSmem(const DevPatch& P)
+{
+  return sizeof(double) * ((size_t)P.nen * 4 + (size_t)P.nq * P.nen * 4 + (size_t)P.nq * 12) +
+         sizeof(int) * (size_t)P.nen * P.npv;
+}
+
+size_t faceSmem(const DevPatch& P, int nqf)
+{
+  return sizeof(double) * ((size_t)P.nen * 4 + (size_t)nqf * P.nen + nqf) +
+         sizeof(int) * (size_t)P.nen * P.npv;
+}
+
+template <typename T>
+ifemgpu_status upload(ifemgpu_ctx* ctx, T** dst, const T* src, size_t n)
+{
+  IFEMGPU_CUDA(ctx, cudaMalloc((void**)dst, sizeof(T) * std::max<size_t>(n, 1)));
+  if (n) IFEMGPU_CUDA(ctx, cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+  return IFEMGPU_OK;
+}
+
+#define IFEMGPU_TRY(x) do { ifemgpu_status s_ = (x); if (s_ != IFEMGPU_OK) return s_; } while (0)
+
+ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
+{
+  const int np = (int)ctx->patches.size();
+  ctx->h_devpatches.assign(np, DevPatch{});
+  std::vector<Item> vol, face;
+  std::vector<double> neuVals;
+  int maxColours = 0;
+  for (int pi = 0; pi < np; pi++) {
+    HostPatch& pc = ctx->patches[pi];
+    DevPatch& D = ctx->h_devpatches[pi];
+    std::memset(&D, 0, sizeof(D));
+    D.dim = pc.dim;
+    D.nen = pc.nen();
+    D.npv = pc.npv;
+    D.kind = pc.mat.kind;
+    D.rational = pc.rational;
+    D.firstNode = pc.firstNode;
+    D.kappa = pc.mat.kappa;
+    D.source = pc.mat.source;
+    D.source_shape = pc.mat.source_shape;
+    D.E = pc.mat.E;
+    D.nu = pc.mat.nu;
+    for (int c = 0; c < 3; c++) D.body[c] = pc.mat.body[c];
+    D.nq = 1;
+    for (int d = 0; d < 3; d++) {
+      D.p[d] = pc.p[d];
+      D.n[d] = pc.n[d];
+      D.nel[d] = pc.nel[d];
+      D.ng[d] = 1;
+      if (d < pc.dim) {
+        int ng = gaussCount(ctx->opts.n_gauss, pc.p[d] + 1, false);
+        int ngf = gaussCount(ctx->opts.n_gauss, pc.p[d] + 1, true);
+        if (ng < 1 || ng > kMaxGauss || ngf < 1 || ngf > kMaxGauss)
+          return setError(ctx, IFEMGPU_UNSUPPORTED, "Gauss point count outside 1..6");
+        D.ng[d] = ng;
+        D.ngf[d] = ngf;
+        gaussRule(ng, D.gx[d], D.gw[d]);
+        gaussRule(ngf, D.fx[d], D.fw[d]);
+        IFEMGPU_TRY(upload(ctx, &pc.d_knots[d], pc.knots[d].data(), pc.knots[d].size()));
+        size_t tab = (size_t)pc.nel[d] * ng * (pc.p[d] + 1);
+        IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabN[d], sizeof(double) * tab));
+        IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabD[d], sizeof(double) * tab));
+        IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_span[d], sizeof(double) * pc.nel[d]));
+      }
+      D.nq *= D.ng[d];
+      D.knots[d] = pc.d_knots[d];
+      D.tabN[d] = pc.d_tabN[d];
+      D.tabD[d] = pc.d_tabD[d];
+      D.span[d] = pc.d_span[d];
+    }
+    IFEMGPU_TRY(upload(ctx, &pc.d_ctrl, pc.ctrl4.data(), pc.ctrl4.size()));
+    D.ctrl = pc.d_ctrl;
+    if (!pc.logk.empty()) {
+      IFEMGPU_TRY(upload(ctx, &pc.d_logk, pc.logk.data(), pc.logk.size()));
+      D.logk = pc.d_logk;
+    }
+    if (!pc.noise.empty()) {
+      IFEMGPU_TRY(upload(ctx, &pc.d_noise, pc.noise.data(), pc.noise.size()));
+      D.noise = pc.d_noise;
+    }
+    if (volumeSmem(D) > 227 * 1024)
+      return setError(ctx, IFEMGPU_UNSUPPORTED, "element too large for the FP64 kernel");
+    const int nc = (pc.p[0] + 1) * (pc.p[1] + 1) * (pc.dim == 3 ? pc.p[2] + 1 : 1);
+    maxColours = std::max(maxColours, nc);
+  }
+  // volume items grouped by colour: colour = (e1 mod q1) + q1 (e2 mod q2) + ...
+  for (int c = 0; c < maxColours; c++) {
+    Pass pass{(int)vol.size(), 0, 0, 0, 0};
+    for (int pi = 0; pi < np; pi++) {
+      const HostPatch& pc = ctx->patches[pi];
+      const int q1 = pc.p[0] + 1, q2 = pc.p[1] + 1, q3 = pc.dim == 3 ? pc.p[2] + 1 : 1;
+      if (c >= q1 * q2 * q3) continue;
+      const int c1 = c % q1, c2 = (c / q1) % q2, c3 = c / (q1 * q2);
+      for (int e3 = c3; e3 < pc.nel[2]; e3 += q3)
+        for (int e2 = c2; e2 < pc.nel[1]; e2 += q2)
+          for (int e1 = c1; e1 < pc.nel[0]; e1 += q1) {
+            int e = (e3 * pc.nel[1] + e2) * pc.nel[0] + e1;
+            if (pc.active[e]) vol.push_back({pi, e, 0, 0});
+          }
+      pass.maxNd = std::max(pass.maxNd, pc.nen() * pc.npv);
+      pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi]));
+    }
+    pass.count = (int)vol.size() - pass.first;
+    if (pass.count) ctx->passes.push_back(pass);
+  }
+  // face items: per Neumann condition, face elements coloured in 2D
+  const int nVol = (int)vol.size();
+  std::vector<Pass> facePasses;
+  for (int pi = 0; pi < np; pi++) {
+    const HostPatch& pc = ctx->patches[pi];
+    for (const auto& nm : pc.neumann) {
+      const int bc = (int)neuVals.size() / 3;
+      for (int c = 0; c < 3; c++) neuVals.push_back(nm.t[c]);
+      const int faceDir = (nm.face + 1) / ((nm.face % 2) ? -2 : 2);
+      const int nd0 = std::abs(faceDir) - 1;
+      const int fixedIdx = faceDir < 0 ? 0 : pc.nel[nd0] - 1;
+      int ta = nd0 == 0 ? 1 : 0, tb = nd0 == 2 ? 1 : 2;
+      const int qa = pc.p[ta] + 1, qb = pc.p[tb] + 1;
+      int nqf = 1;
+      for (int d = 0; d < 3; d++)
+        if (d != nd0) nqf *= gaussCount(ctx->opts.n_gauss, pc.p[d] + 1, true);
+      for (int c = 0; c < qa * qb; c++) {
+        Pass pass{0, 0, nm.face, pc.nen() * pc.npv, faceSmem(ctx->h_devpatches[pi], nqf)};
+        std::vector<Item> lst;
+        for (int e = 0; e < pc.nelAll; e++) {
+          if (!pc.active[e]) continue;
+          int ee[3] = {e % pc.nel[0], (e / pc.nel[0]) % pc.nel[1], e / (pc.nel[0] * pc.nel[1])};
+          if (ee[nd0] != fixedIdx) continue;
+          if ((ee[ta] % qa) + qa * (ee[tb] % qb) != c) continue;
+          lst.push_back({pi, e, nm.face, bc});
+        }
+        pass.first = (int)(vol.size() + face.size());
+        pass.count = (int)lst.size();
+        face.insert(face.end(), lst.begin(), lst.end());
+        if (pass.count) facePasses.push_back(pass);
+      }
+    }
+  }
+  (void)nVol;
+  ctx->passes.insert(ctx->passes.end(), facePasses.begin(), facePasses.end());
+  vol.insert(vol.end(), face.begin(), face.end());
+  IFEMGPU_TRY(upload(ctx, &ctx->d_items, vol.data(), vol.size()));
+  IFEMGPU_TRY(upload(ctx, &ctx->d_neumann, neuVals.data(), neuVals.size()));
+  IFEMGPU_TRY(upload(ctx, &ctx->d_patches, ctx->h_devpatches.data(), np));
+  // system arrays
+  IFEMGPU_TRY(upload(ctx, &ctx->d_madof, ctx->madof.data(), ctx->madof.size()));
+  IFEMGPU_TRY(upload(ctx, &ctx->d_meqn, ctx->meqn.data(), ctx->meqn.size()));
+  if (!ctx->c0.empty()) IFEMGPU_TRY(upload(ctx, &ctx->d_c0, ctx->c0.data(), ctx->c0.size()));
+  IFEMGPU_TRY(upload(ctx, &ctx->d_colptr, ctx->colptr.data(), ctx->colptr.size()));
+  IFEMGPU_TRY(upload(ctx, &ctx->d_rowidx, ctx->rowidx.data(), ctx->rowidx.size()));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_K, sizeof(double) * std::max<int64_t>(ctx->nnz, 1)));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_b, sizeof(double) * std::max(ctx->neq, 1)));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 4));
+  size_t maxSmem = 0;
+  for (auto& p : ctx->passes) maxSmem = std::max(maxSmem, p.smem);
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::min<size_t>(maxSmem, 227 * 1024)));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_face_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::min<size_t>(maxSmem, 227 * 1024)));
+  return IFEMGPU_OK;
+}
+
+// raw (dim coordinates [+ weight]) -> (x, y, z, w) control net layout
+__global__ void k_pack_coefs(const double* __restrict__ raw, double* __restrict__ ctrl,
+                             int nnod, int dim, int rational)
+{
+  const int stride = dim + rational;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnod; i += gridDim.x * blockDim.x) {
+    double v[4] = {0.0, 0.0, 0.0, 1.0};
+    for (int c = 0; c < dim; c++) v[c] = raw[(size_t)i * stride + c];
+    if (rational) v[3] = raw[(size_t)i * stride + dim];
+    for (int c = 0; c < 4; c++) ctrl[(size_t)i * 4 + c] = v[c];
+  }
+}
+
+ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs)
+{
+  HostPatch& pc = ctx->patches[pi];
+  const int stride = pc.dim + (pc.rational ? 1 : 0);
+  const size_t n = (size_t)pc.nnod * stride;
+  if (!pc.d_stage) IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_stage, sizeof(double) * n));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(pc.d_stage, coefs, sizeof(double) * n,
+                                    cudaMemcpyHostToDevice, ctx->stream));
+  const int blocks = std::min(1024, (pc.nnod + 255) / 256);
+  k_pack_coefs<<<blocks, 256, 0, ctx->stream>>>(pc.d_stage, pc.d_ctrl, pc.nnod, pc.dim,
+                                                pc.rational ? 1 : 0);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
+{
+  cudaStream_t s = ctx->stream;
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_K, 0, sizeof(double) * ctx->nnz, s));
+  IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_b, 0, sizeof(double) * ctx->neq, s));
+  IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4, s));
+  for (int pi = 0; pi < (int)ctx->h_devpatches.size(); pi++) {
+    const DevPatch& D = ctx->h_devpatches[pi];
+    int work = 0;
+    for (int d = 0; d < D.dim; d++) work += D.nel[d] * D.ng[d];
+    k_basis_tables<<<(work + 127) / 128, 128, 0, s>>>(D);
+  }
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
+            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters};
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  bool faceStarted = false;
+  for (const Pass& p : ctx->passes) {
+    if (p.face && !faceStarted) {
+      IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+      faceStarted = true;
+    }
+    if (!p.face)
+      k_volume_fp64<<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
+    else
+      k_face_fp64<<<p.count, 128, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first,
+                                               ctx->d_neumann, S);
+    IFEMGPU_CUDA(ctx, cudaGetLastError());
+  }
+  if (!faceStarted) IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+  ctx->launches_per_assembly = (int)ctx->h_devpatches.size() + (int)ctx->passes.size();
+  return IFEMGPU_OK;
+}
+
+}  // namespace ifemgpu

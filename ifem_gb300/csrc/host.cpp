@@ -1,0 +1,606 @@
+// host.cpp -- model input, SAM numbering and matrix pattern of libifemgpu.
+//
+// The numbering rules are IFEM's (see include/ifemgpu.h); the implementation
+// is this library's own: node couplings of a structured patch are the index
+// box of half-width p around a node, so the pattern is generated directly in
+// compressed-column form, column by column in parallel, without IFEM's
+// per-equation std::set (SAM::getDofCouplings, src/LinAlg/SAM.C:377-427).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+
+#include "ifemgpu_internal.h"
+
+using namespace ifemgpu;
+
+namespace ifemgpu {
+
+ifemgpu_status setError(ifemgpu_ctx* ctx, ifemgpu_status st, const std::string& msg)
+{
+  if (ctx) ctx->err = msg;
+  return st;
+}
+
+ifemgpu_status cudaFail(ifemgpu_ctx* ctx, cudaError_t e, const char* what)
+{
+  std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  return setError(ctx, e == cudaErrorMemoryAllocation ? IFEMGPU_OUT_OF_MEMORY
+                                                      : IFEMGPU_CUDA_ERROR, msg);
+}
+
+}  // namespace ifemgpu
+
+namespace {
+
+void freeDevice(ifemgpu_ctx* ctx)
+{
+  auto f = [](void* p) { if (p) cudaFree(p); };
+  for (auto& pc : ctx->patches) {
+    f(pc.d_ctrl); pc.d_ctrl = nullptr;
+    f(pc.d_stage); pc.d_stage = nullptr;
+    f(pc.d_logk); pc.d_logk = nullptr;
+    f(pc.d_noise); pc.d_noise = nullptr;
+    for (int d = 0; d < 3; d++) {
+      f(pc.d_knots[d]); f(pc.d_tabN[d]); f(pc.d_tabD[d]); f(pc.d_span[d]);
+      pc.d_knots[d] = pc.d_tabN[d] = pc.d_tabD[d] = pc.d_span[d] = nullptr;
+    }
+  }
+  f(ctx->d_madof); f(ctx->d_meqn); f(ctx->d_c0); f(ctx->d_colptr);
+  f(ctx->d_rowidx); f(ctx->d_K); f(ctx->d_b); f(ctx->d_patches);
+  f(ctx->d_items); f(ctx->d_neumann); f(ctx->d_counters);
+  ctx->d_madof = ctx->d_meqn = nullptr;
+  ctx->d_c0 = nullptr;
+  ctx->d_colptr = ctx->d_rowidx = nullptr;
+  ctx->d_K = ctx->d_b = nullptr;
+  ctx->d_patches = nullptr;
+  ctx->d_items = nullptr;
+  ctx->d_neumann = nullptr;
+  ctx->d_counters = nullptr;
+  freeSolver(ctx);
+}
+
+// Patch topology: ASMs3D::generateFEMTopology (src/ASM/ASMs3D.C:487-509).
+void topology(HostPatch& pc)
+{
+  pc.nnod = 1;
+  for (int d = 0; d < 3; d++) {
+    if (d >= pc.dim) { pc.p[d] = 0; pc.n[d] = 1; pc.nel[d] = 1; continue; }
+    pc.nel[d] = pc.n[d] - pc.p[d];
+    pc.nnod *= pc.n[d];
+  }
+  pc.nelAll = pc.nel[0] * pc.nel[1] * pc.nel[2];
+  pc.active.assign(pc.nelAll, 0);
+  pc.nelActive = 0;
+  for (int e = 0; e < pc.nelAll; e++) {
+    int ee[3] = {e % pc.nel[0], (e / pc.nel[0]) % pc.nel[1], e / (pc.nel[0] * pc.nel[1])};
+    bool nz = true;
+    for (int d = 0; d < pc.dim; d++)
+      nz = nz && pc.knots[d][pc.p[d] + ee[d] + 1] > pc.knots[d][pc.p[d] + ee[d]];
+    pc.active[e] = nz;
+    pc.nelActive += nz;
+  }
+}
+
+bool boxCoupling(const HostPatch& pc)
+{
+  for (char a : pc.active)
+    if (!a) return false;
+  return true;
+}
+
+std::vector<int> faceNodes(const HostPatch& pc, int face)
+{
+  std::vector<int> out;
+  const int n1 = pc.n[0], n2 = pc.n[1], n3 = pc.n[2];
+  const int dir = (face + 1) / 2;
+  const bool hi = (face % 2) == 0;
+  auto id = [&](int i, int j, int k) { return (k * n2 + j) * n1 + i; };
+  if (dir == 1) {
+    const int i = hi ? n1 - 1 : 0;
+    for (int k = 0; k < n3; k++)
+      for (int j = 0; j < n2; j++) out.push_back(id(i, j, k));
+  } else if (dir == 2) {
+    const int j = hi ? n2 - 1 : 0;
+    for (int k = 0; k < n3; k++)
+      for (int i = 0; i < n1; i++) out.push_back(id(i, j, k));
+  } else {
+    const int k = hi ? n3 - 1 : 0;
+    for (int j = 0; j < n2; j++)
+      for (int i = 0; i < n1; i++) out.push_back(id(i, j, k));
+  }
+  return out;
+}
+
+// DOF numbering: MADOF node-major, MSC from the boundary conditions, MEQN
+// free DOFs in DOF order (SAMpatch::initNodeDofs, src/ASM/SAMpatch.C:84-161;
+// SAM::initSystemEquations, src/LinAlg/SAM.C:225-336).  Fixed DOFs win over
+// prescribed ones and the first prescription of a DOF wins, as IFEM's
+// SAMpatch::initConstraintEqs ignores constraints on already fixed or
+// constrained DOFs (src/ASM/SAMpatch.C:300-310).
+ifemgpu_status numbering(ifemgpu_ctx* ctx)
+{
+  int gNod = 0, gEl = 0;
+  for (auto& pc : ctx->patches) {
+    topology(pc);
+    pc.firstNode = gNod;
+    pc.firstElm = gEl;
+    gNod += pc.nnod;
+    gEl += pc.nelActive;
+  }
+  ctx->nnod = gNod;
+  ctx->nel = gEl;
+  ctx->madof.assign(ctx->nnod + 1, 0);
+  for (auto& pc : ctx->patches)
+    for (int i = 0; i < pc.nnod; i++) ctx->madof[pc.firstNode + i + 1] = pc.npv;
+  ctx->madof[0] = 1;
+  for (int i = 0; i < ctx->nnod; i++) ctx->madof[i + 1] += ctx->madof[i];
+  ctx->ndof = ctx->madof[ctx->nnod] - 1;
+  std::vector<int> msc(ctx->ndof, 1), slave(ctx->ndof, 0);
+  for (auto& pc : ctx->patches)
+    for (auto& bc : pc.bcs) {
+      if (bc.value != 0.0) continue;
+      for (int node : faceNodes(pc, bc.face))
+        for (char c : std::to_string(bc.dofs)) {
+          int dof = c - '0';
+          if (dof >= 1 && dof <= pc.npv)
+            msc[ctx->madof[pc.firstNode + node] - 1 + dof - 1] = 0;
+        }
+    }
+  ctx->c0.clear();
+  for (auto& pc : ctx->patches)
+    for (auto& bc : pc.bcs) {
+      if (bc.value == 0.0) continue;
+      for (int node : faceNodes(pc, bc.face))
+        for (char c : std::to_string(bc.dofs)) {
+          int dof = c - '0';
+          if (dof < 1 || dof > pc.npv) continue;
+          int idof = ctx->madof[pc.firstNode + node] - 1 + dof - 1;
+          if (msc[idof] <= 0 || slave[idof]) continue;
+          ctx->c0.push_back(bc.value);
+          slave[idof] = (int)ctx->c0.size();
+        }
+    }
+  ctx->nceq = (int)ctx->c0.size();
+  ctx->meqn.assign(ctx->ndof, 0);
+  int ieq = 0;
+  for (int i = 0; i < ctx->ndof; i++) {
+    if (slave[i]) ctx->meqn[i] = -slave[i];
+    else if (msc[i] == 1) ctx->meqn[i] = ++ieq;
+  }
+  ctx->neq = ieq;
+  return IFEMGPU_OK;
+}
+
+// Coupled nodes (patch-local) of node `node`: every node sharing an element.
+void coupledNodes(const HostPatch& pc, int node, std::vector<int>& out)
+{
+  out.clear();
+  const int i = node % pc.n[0], j = (node / pc.n[0]) % pc.n[1], k = node / (pc.n[0] * pc.n[1]);
+  const int lo[3] = {std::max(0, i - pc.p[0]), std::max(0, j - pc.p[1]), std::max(0, k - pc.p[2])};
+  const int hi[3] = {std::min(pc.n[0] - 1, i + pc.p[0]), std::min(pc.n[1] - 1, j + pc.p[1]),
+                     std::min(pc.n[2] - 1, k + pc.p[2])};
+  if (boxCoupling(pc)) {
+    for (int c = lo[2]; c <= hi[2]; c++)
+      for (int b = lo[1]; b <= hi[1]; b++)
+        for (int a = lo[0]; a <= hi[0]; a++) out.push_back((c * pc.n[1] + b) * pc.n[0] + a);
+    return;
+  }
+  // general case: union of the node sets of the active elements around node
+  const int elo[3] = {std::max(0, i - pc.p[0]), std::max(0, j - pc.p[1]), std::max(0, k - pc.p[2])};
+  const int ehi[3] = {std::min(pc.nel[0] - 1, i), std::min(pc.nel[1] - 1, j), std::min(pc.nel[2] - 1, k)};
+  for (int e3 = elo[2]; e3 <= ehi[2]; e3++)
+    for (int e2 = elo[1]; e2 <= ehi[1]; e2++)
+      for (int e1 = elo[0]; e1 <= ehi[0]; e1++) {
+        int e = (e3 * pc.nel[1] + e2) * pc.nel[0] + e1;
+        if (!pc.active[e]) continue;
+        for (int c = 0; c <= pc.p[2]; c++)
+          for (int b = 0; b <= pc.p[1]; b++)
+            for (int a = 0; a <= pc.p[0]; a++)
+              out.push_back(((e3 + c) * pc.n[1] + e2 + b) * pc.n[0] + e1 + a);
+      }
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+
+// Compressed-column pattern, identical to SAM::getDofCouplings followed by
+// SparseMatrix::optimiseCols(dofc) for patches without shared nodes.
+ifemgpu_status pattern(ifemgpu_ctx* ctx)
+{
+  const int neq = ctx->neq;
+  // equation -> (patch, node, dof)
+  std::vector<int> eqPatch(neq), eqNode(neq);
+  for (int pi = 0; pi < (int)ctx->patches.size(); pi++) {
+    auto& pc = ctx->patches[pi];
+    for (int nd = 0; nd < pc.nnod; nd++) {
+      int g = pc.firstNode + nd;
+      for (int d = ctx->madof[g]; d < ctx->madof[g + 1]; d++) {
+        int e = ctx->meqn[d - 1];
+        if (e > 0) { eqPatch[e - 1] = pi; eqNode[e - 1] = nd; }
+      }
+    }
+  }
+  // column counts (columns of one node share their row set)
+  std::vector<int64_t> cnt(neq + 1, 0);
+#pragma omp parallel
+  {
+    std::vector<int> nb;
+#pragma omp for schedule(dynamic, 256)
+    for (int c = 0; c < neq; c++) {
+      const auto& pc = ctx->patches[eqPatch[c]];
+      coupledNodes(pc, eqNode[c], nb);
+      int64_t s = 0;
+      for (int m : nb) {
+        int g = pc.firstNode + m;
+        for (int d = ctx->madof[g]; d < ctx->madof[g + 1]; d++) s += ctx->meqn[d - 1] > 0;
+      }
+      cnt[c + 1] = s;
+    }
+  }
+  for (int c = 0; c < neq; c++) cnt[c + 1] += cnt[c];
+  if (cnt[neq] >= (int64_t)INT32_MAX)
+    return setError(ctx, IFEMGPU_UNSUPPORTED, "matrix has more than 2^31-1 non-zeros");
+  ctx->nnz = cnt[neq];
+  ctx->colptr.resize(neq + 1);
+  for (int c = 0; c <= neq; c++) ctx->colptr[c] = (int)cnt[c];
+  ctx->rowidx.resize(ctx->nnz);
+#pragma omp parallel
+  {
+    std::vector<int> nb;
+#pragma omp for schedule(dynamic, 256)
+    for (int c = 0; c < neq; c++) {
+      const auto& pc = ctx->patches[eqPatch[c]];
+      coupledNodes(pc, eqNode[c], nb);
+      int64_t k = cnt[c];
+      for (int m : nb) {
+        int g = pc.firstNode + m;
+        for (int d = ctx->madof[g]; d < ctx->madof[g + 1]; d++)
+          if (ctx->meqn[d - 1] > 0) ctx->rowidx[k++] = ctx->meqn[d - 1] - 1;
+      }
+    }
+  }
+  return IFEMGPU_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int ifemgpu_abi_version(void) { return IFEMGPU_ABI_VERSION; }
+
+ifemgpu_status ifemgpu_ctx_create(ifemgpu_ctx** out, const ifemgpu_options* opts)
+{
+  if (!out) return IFEMGPU_INVALID_ARG;
+  *out = nullptr;
+  ifemgpu_ctx* ctx = new ifemgpu_ctx;
+  if (opts) ctx->opts = *opts;
+  else { ctx->opts.device = 0; ctx->opts.ke_precision = IFEMGPU_KE_FP64; ctx->opts.n_gauss = 4; }
+  if (ctx->opts.device < 0) {  // host-only: numbering and pattern, no device work
+    *out = ctx;
+    return IFEMGPU_OK;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    delete ctx;
+    return IFEMGPU_CUDA_ERROR;
+  }
+  if (ctx->opts.device < 0 || ctx->opts.device >= ndev) { delete ctx; return IFEMGPU_INVALID_ARG; }
+  if (cudaSetDevice(ctx->opts.device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return IFEMGPU_CUDA_ERROR;
+  }
+  for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+  *out = ctx;
+  return IFEMGPU_OK;
+}
+
+void ifemgpu_ctx_destroy(ifemgpu_ctx* ctx)
+{
+  if (!ctx) return;
+  if (ctx->opts.device >= 0) {
+    cudaSetDevice(ctx->opts.device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    freeDevice(ctx);
+    for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+}
+
+const char* ifemgpu_last_error(const ifemgpu_ctx* ctx)
+{
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+ifemgpu_status ifemgpu_patch_add(ifemgpu_ctx* ctx, int dim, const int* degree,
+                                 const int* ncoef, const double* const* knots,
+                                 const double* coefs, int rational, int* patch_id)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "model already preprocessed");
+  if ((dim != 2 && dim != 3) || !degree || !ncoef || !knots || !coefs)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "patch_add: bad dimension or null array");
+  HostPatch pc;
+  pc.dim = dim;
+  int nn = 1;
+  for (int d = 0; d < dim; d++) {
+    if (degree[d] < 1 || degree[d] > kMaxDeg)
+      return setError(ctx, IFEMGPU_UNSUPPORTED, "patch_add: degree must be in 1..4");
+    if (ncoef[d] < degree[d] + 1 || !knots[d])
+      return setError(ctx, IFEMGPU_INVALID_ARG, "patch_add: too few control points");
+    pc.p[d] = degree[d];
+    pc.n[d] = ncoef[d];
+    pc.knots[d].assign(knots[d], knots[d] + ncoef[d] + degree[d] + 1);
+    for (size_t i = 1; i < pc.knots[d].size(); i++)
+      if (pc.knots[d][i] < pc.knots[d][i - 1])
+        return setError(ctx, IFEMGPU_INVALID_ARG, "patch_add: decreasing knot vector");
+    nn *= ncoef[d];
+  }
+  const int stride = dim + (rational ? 1 : 0);
+  pc.rational = rational != 0;
+  pc.ctrl4.assign((size_t)nn * 4, 0.0);
+  for (int i = 0; i < nn; i++) {
+    for (int c = 0; c < dim; c++) pc.ctrl4[(size_t)i * 4 + c] = coefs[(size_t)i * stride + c];
+    pc.ctrl4[(size_t)i * 4 + 3] = rational ? coefs[(size_t)i * stride + dim] : 1.0;
+    if (!(pc.ctrl4[(size_t)i * 4 + 3] > 0.0))
+      return setError(ctx, IFEMGPU_INVALID_ARG, "patch_add: weights must be positive");
+  }
+  pc.nnod = nn;
+  ctx->patches.push_back(std::move(pc));
+  if (patch_id) *patch_id = (int)ctx->patches.size();
+  return IFEMGPU_OK;
+}
+
+static HostPatch* getPatch(ifemgpu_ctx* ctx, int pid)
+{
+  if (!ctx || pid < 1 || pid > (int)ctx->patches.size()) return nullptr;
+  return &ctx->patches[pid - 1];
+}
+
+ifemgpu_status ifemgpu_patch_set_material(ifemgpu_ctx* ctx, int patch_id,
+                                          const ifemgpu_material* mat)
+{
+  HostPatch* pc = getPatch(ctx, patch_id);
+  if (!pc || !mat) return setError(ctx, IFEMGPU_INVALID_ARG, "set_material: bad patch or material");
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "model already preprocessed");
+  if (mat->kind == IFEMGPU_ELASTICITY && pc->dim != 3)
+    return setError(ctx, IFEMGPU_UNSUPPORTED, "elasticity is implemented for 3D patches");
+  if (mat->kind != IFEMGPU_POISSON && mat->kind != IFEMGPU_ELASTICITY)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "set_material: unknown kind");
+  pc->mat = *mat;
+  pc->hasMat = true;
+  pc->npv = mat->kind == IFEMGPU_ELASTICITY ? pc->dim : 1;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_patch_set_field(ifemgpu_ctx* ctx, int patch_id, int which,
+                                       const double* values)
+{
+  HostPatch* pc = getPatch(ctx, patch_id);
+  if (!pc || !values) return setError(ctx, IFEMGPU_INVALID_ARG, "set_field: bad patch or values");
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "model already preprocessed");
+  int nn = (int)(pc->ctrl4.size() / 4);
+  if (which == IFEMGPU_FIELD_LOG_KAPPA) pc->logk.assign(values, values + nn);
+  else if (which == IFEMGPU_FIELD_SOURCE_NOISE) pc->noise.assign(values, values + nn);
+  else return setError(ctx, IFEMGPU_INVALID_ARG, "set_field: unknown field");
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_patch_constrain_face(ifemgpu_ctx* ctx, int patch_id, int face,
+                                            int dofs, double value)
+{
+  HostPatch* pc = getPatch(ctx, patch_id);
+  if (!pc || face < 1 || face > 2 * pc->dim || dofs < 1)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "constrain_face: bad patch, face or dofs");
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "model already preprocessed");
+  pc->bcs.push_back({face, dofs, value});
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_patch_add_neumann(ifemgpu_ctx* ctx, int patch_id, int face,
+                                         const double* values)
+{
+  HostPatch* pc = getPatch(ctx, patch_id);
+  if (!pc || face < 1 || face > 2 * pc->dim || !values)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "add_neumann: bad patch, face or values");
+  if (pc->dim != 3) return setError(ctx, IFEMGPU_UNSUPPORTED, "Neumann faces need 3D patches");
+  if (!pc->hasMat) return setError(ctx, IFEMGPU_NOT_READY, "add_neumann: set the material first");
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "model already preprocessed");
+  HostNeumann nm{face, {0, 0, 0}};
+  for (int c = 0; c < pc->npv; c++) nm.t[c] = values[c];
+  pc->neumann.push_back(nm);
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_preprocess(ifemgpu_ctx* ctx)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "already preprocessed");
+  if (ctx->patches.empty()) return setError(ctx, IFEMGPU_NOT_READY, "no patches");
+  for (auto& pc : ctx->patches)
+    if (!pc.hasMat) return setError(ctx, IFEMGPU_NOT_READY, "patch without material");
+  ifemgpu_status st = numbering(ctx);
+  if (st != IFEMGPU_OK) return st;
+  st = pattern(ctx);
+  if (st != IFEMGPU_OK) return st;
+  if (ctx->opts.device >= 0) {
+    IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+    st = uploadAssemblyModel(ctx);
+    if (st != IFEMGPU_OK) { freeDevice(ctx); return st; }
+  }
+  ctx->preprocessed = true;
+  if (ctx->opts.verbose)
+    std::printf("\n >>> SAM model summary <<<\nNumber of elements    %d\nNumber of nodes       %d\n"
+                "Number of dofs        %d\nNumber of unknowns    %d\nNon-zeroes            %lld\n",
+                ctx->nel, ctx->nnod, ctx->ndof, ctx->neq, (long long)ctx->nnz);
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_get_sizes(const ifemgpu_ctx* ctx, ifemgpu_sizes* out)
+{
+  if (!ctx || !out) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return IFEMGPU_NOT_READY;
+  out->npatch = (int)ctx->patches.size();
+  out->nnod = ctx->nnod;
+  out->nel = ctx->nel;
+  out->ndof = ctx->ndof;
+  out->neq = ctx->neq;
+  out->nceq = ctx->nceq;
+  out->nnz = ctx->nnz;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_get_madof(const ifemgpu_ctx* ctx, int* madof)
+{
+  if (!ctx || !madof) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return IFEMGPU_NOT_READY;
+  std::memcpy(madof, ctx->madof.data(), sizeof(int) * ctx->madof.size());
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_get_meqn(const ifemgpu_ctx* ctx, int* meqn)
+{
+  if (!ctx || !meqn) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return IFEMGPU_NOT_READY;
+  std::memcpy(meqn, ctx->meqn.data(), sizeof(int) * ctx->meqn.size());
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_get_mnpc(const ifemgpu_ctx* ctx, int patch_id, int* mnpc)
+{
+  if (!ctx || !mnpc || patch_id < 1 || patch_id > (int)ctx->patches.size())
+    return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return IFEMGPU_NOT_READY;
+  const HostPatch& pc = ctx->patches[patch_id - 1];
+  const int q1 = pc.p[0] + 1, q2 = pc.p[1] + 1, q3 = pc.p[2] + 1;
+  size_t k = 0;
+  for (int e = 0; e < pc.nelAll; e++) {
+    const int e1 = e % pc.nel[0], e2 = (e / pc.nel[0]) % pc.nel[1], e3 = e / (pc.nel[0] * pc.nel[1]);
+    for (int c = 0; c < q3; c++)
+      for (int b = 0; b < q2; b++)
+        for (int a = 0; a < q1; a++)
+          mnpc[k++] = pc.active[e] ? ((e3 + c) * pc.n[1] + e2 + b) * pc.n[0] + e1 + a : -1;
+  }
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_get_pattern(const ifemgpu_ctx* ctx, int* colptr, int* rowidx)
+{
+  if (!ctx || !colptr || !rowidx) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return IFEMGPU_NOT_READY;
+  std::memcpy(colptr, ctx->colptr.data(), sizeof(int) * ctx->colptr.size());
+  std::memcpy(rowidx, ctx->rowidx.data(), sizeof(int) * ctx->rowidx.size());
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_patch_update_coefs(ifemgpu_ctx* ctx, int patch_id, const double* coefs)
+{
+  HostPatch* pc = getPatch(ctx, patch_id);
+  if (!pc || !coefs) return setError(ctx, IFEMGPU_INVALID_ARG, "update_coefs: bad patch or array");
+  if (!ctx->preprocessed || ctx->opts.device < 0)
+    return setError(ctx, IFEMGPU_NOT_READY, "update_coefs before preprocess");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  return updateCoefs(ctx, patch_id - 1, coefs);
+}
+
+ifemgpu_status ifemgpu_get_stream(const ifemgpu_ctx* ctx, void** stream)
+{
+  if (!ctx || !stream) return IFEMGPU_INVALID_ARG;
+  *stream = (void*)ctx->stream;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_assemble(ifemgpu_ctx* ctx, int sync)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return setError(ctx, IFEMGPU_NOT_READY, "assemble before preprocess");
+  if (ctx->opts.device < 0) return setError(ctx, IFEMGPU_NOT_READY, "host-only context (device -1)");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  ifemgpu_status st = launchAssembly(ctx);
+  if (st != IFEMGPU_OK) return st;
+  ctx->assembled = true;
+  if (sync) IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_last_assembly_stats(ifemgpu_ctx* ctx, double* total_ms,
+                                           double* volume_ms, long long* singular,
+                                           int* kernel_launches)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  float t0 = 0.f, t1 = 0.f;
+  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[3]));
+  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t1, ctx->ev[1], ctx->ev[2]));
+  unsigned long long s = 0;
+  IFEMGPU_CUDA(ctx, cudaMemcpy(&s, ctx->d_counters, sizeof(s), cudaMemcpyDeviceToHost));
+  if (total_ms) *total_ms = t0;
+  if (volume_ms) *volume_ms = t1;
+  if (singular) *singular = (long long)s;
+  if (kernel_launches) *kernel_launches = ctx->launches_per_assembly;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_copy_matrix(ifemgpu_ctx* ctx, double* values)
+{
+  if (!ctx || !values) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(values, ctx->d_K, sizeof(double) * ctx->nnz,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_copy_rhs(ifemgpu_ctx* ctx, double* rhs)
+{
+  if (!ctx || !rhs) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(rhs, ctx->d_b, sizeof(double) * ctx->neq,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_device_system(ifemgpu_ctx* ctx, const double** values,
+                                     const int** colptr, const int** rowidx,
+                                     const double** rhs)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return setError(ctx, IFEMGPU_NOT_READY, "not preprocessed");
+  if (values) *values = ctx->d_K;
+  if (colptr) *colptr = ctx->d_colptr;
+  if (rowidx) *rowidx = ctx->d_rowidx;
+  if (rhs) *rhs = ctx->d_b;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_solve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* opts,
+                             double* x, ifemgpu_solve_info* info)
+{
+  if (!ctx || !opts || !x) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "solve before assemble");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  return runSolve(ctx, opts, x, info);
+}
+
+ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
+                                       double* u, double scale)
+{
+  if (!ctx || !x || !u) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return IFEMGPU_NOT_READY;
+  for (int i = 0; i < ctx->ndof; i++) {
+    int e = ctx->meqn[i];
+    u[i] = e > 0 ? x[e - 1] : (e < 0 ? ctx->c0[-e - 1] * scale : 0.0);
+  }
+  return IFEMGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,163 @@
+// Internal declarations shared by the host translation unit (host.cpp) and the
+// CUDA translation units (assembly.cu, solver.cu) of libifemgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/ifemgpu.h"
+
+namespace ifemgpu {
+
+constexpr int kMaxDeg = 4;        // highest polynomial degree handled
+constexpr int kMaxGauss = 6;      // highest Gauss point count per direction
+constexpr double kEpsZ = 1.0e-12; // singular-Jacobian tolerance (IFEM epsZ)
+
+// Device view of one patch.  All pointers are device memory.
+struct DevPatch {
+  int dim;            // 2 or 3
+  int p[3];           // degree per direction (0 in unused directions)
+  int n[3];           // control points per direction (1 in unused)
+  int nel[3];         // knot spans per direction (1 in unused)
+  int ng[3];          // Gauss points per direction (1 in unused)
+  int nen;            // basis functions per element
+  int nq;             // Gauss points per element
+  int npv;            // unknowns per node
+  int kind;           // IFEMGPU_POISSON / IFEMGPU_ELASTICITY
+  int rational;
+  int firstNode;      // global 0-based index of the patch's first node
+  double kappa, source, E, nu, body[3];
+  int source_shape;
+  const double* ctrl;     // nnod x 4: x, y, z, w (z = 0 in 2D, w = 1 if polynomial)
+  const double* knots[3]; // n+p+1 per direction
+  const double* logk;     // per node or nullptr
+  const double* noise;    // per node or nullptr
+  // 1D tables, per direction: [nel][ng][p+1] values and derivatives,
+  // [nel] span lengths; filled by the basis kernel of every assembly.
+  double* tabN[3];
+  double* tabD[3];
+  double* span[3];
+  // Gauss rules: volume (gx, gw) and face (fx, fw, ngf points)
+  double gx[3][kMaxGauss], gw[3][kMaxGauss];
+  double fx[3][kMaxGauss], fw[3][kMaxGauss];
+  int ngf[3];
+};
+
+// Work item of the volume and face passes.
+struct Item {
+  int patch;    // index into the DevPatch array
+  int elem;     // patch-local element index (first index fastest)
+  int face;     // IFEM face index for Neumann items, 0 for volume items
+  int bc;       // index into the Neumann value table for face items
+};
+
+struct HostBC { int face; int dofs; double value; };
+struct HostNeumann { int face; double t[3]; };
+
+struct HostPatch {
+  int dim = 3;
+  int p[3] = {0, 0, 0};
+  int n[3] = {1, 1, 1};
+  std::vector<double> knots[3];
+  std::vector<double> ctrl4;  // nnod x 4
+  bool rational = false;
+  ifemgpu_material mat{};
+  bool hasMat = false;
+  int npv = 1;
+  std::vector<double> logk, noise;
+  std::vector<HostBC> bcs;
+  std::vector<HostNeumann> neumann;
+  // topology
+  int nel[3] = {1, 1, 1};
+  int nelAll = 0, nnod = 0, nelActive = 0;
+  int firstNode = 0, firstElm = 0;
+  std::vector<char> active;  // per element: non-zero parametric volume
+  int nen() const {
+    return (p[0] + 1) * (p[1] + 1) * (dim == 3 ? p[2] + 1 : 1);
+  }
+  // device buffers owned by the patch
+  double* d_ctrl = nullptr;
+  double* d_stage = nullptr;  // raw coefficient upload of ifemgpu_patch_update_coefs
+  double* d_knots[3] = {nullptr, nullptr, nullptr};
+  double* d_logk = nullptr;
+  double* d_noise = nullptr;
+  double* d_tabN[3] = {nullptr, nullptr, nullptr};
+  double* d_tabD[3] = {nullptr, nullptr, nullptr};
+  double* d_span[3] = {nullptr, nullptr, nullptr};
+};
+
+// One colour pass of the volume or face integration.
+struct Pass {
+  int first;   // offset into the item array
+  int count;   // items in the pass
+  int face;    // 0 volume, else face pass
+  int maxNd;   // largest element DOF count in the pass
+  size_t smem; // dynamic shared memory of the pass' launch
+};
+
+}  // namespace ifemgpu
+
+struct ifemgpu_ctx {
+  ifemgpu_options opts{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<ifemgpu::HostPatch> patches;
+  bool preprocessed = false;
+  bool assembled = false;
+  // SAM arrays
+  int nnod = 0, nel = 0, ndof = 0, neq = 0, nceq = 0;
+  int64_t nnz = 0;
+  std::vector<int> madof, meqn;
+  std::vector<double> c0;
+  std::vector<int> colptr, rowidx;
+  // device model
+  int* d_madof = nullptr;
+  int* d_meqn = nullptr;
+  double* d_c0 = nullptr;
+  int* d_colptr = nullptr;
+  int* d_rowidx = nullptr;
+  double* d_K = nullptr;
+  double* d_b = nullptr;
+  ifemgpu::DevPatch* d_patches = nullptr;
+  std::vector<ifemgpu::DevPatch> h_devpatches;
+  ifemgpu::Item* d_items = nullptr;
+  double* d_neumann = nullptr;  // Neumann values, 3 per face condition
+  std::vector<ifemgpu::Pass> passes;
+  unsigned long long* d_counters = nullptr;  // [0] singular points
+  // statistics of the last assembly
+  double last_total_ms = 0.0, last_volume_ms = 0.0;
+  unsigned long long last_singular = 0;
+  int launches_per_assembly = 0;
+  // solver workspace (allocated on first solve)
+  float* d_K32 = nullptr;
+  double* d_work = nullptr;
+  size_t work_len = 0;
+  double* h_pinned = nullptr;
+};
+
+namespace ifemgpu {
+
+ifemgpu_status setError(ifemgpu_ctx* ctx, ifemgpu_status st, const std::string& msg);
+ifemgpu_status cudaFail(ifemgpu_ctx* ctx, cudaError_t e, const char* what);
+
+// assembly.cu
+ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx);
+ifemgpu_status launchAssembly(ifemgpu_ctx* ctx);
+ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs);
+
+// solver.cu
+ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o,
+                        double* x, ifemgpu_solve_info* info);
+void freeSolver(ifemgpu_ctx* ctx);
+
+}  // namespace ifemgpu
+
+#define IFEMGPU_CUDA(ctx, call)                                   \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) return ifemgpu::cudaFail(ctx, e_, #call); \
+  } while (0)

@@ -1,0 +1,298 @@
+"""ctypes binding of the C ABI in include/ifemgpu.h, with a host-side mirror of
+IFEM's simulator vocabulary (``SIM.preprocess``, ``SIM.getSAM``,
+``SAM.getEquation``, ``SIM.assembleSystem``, ``SIM.solveSystem``) so that
+tests read like IFEM's own unit tests.
+
+The library must be built (``ifem_gb300.build.build()``); loading fails loudly
+otherwise -- there is no CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB
+
+# ---- C structures ---------------------------------------------------------
+
+
+class Options(C.Structure):
+    _fields_ = [("device", C.c_int), ("ke_precision", C.c_int), ("n_gauss", C.c_int),
+                ("verbose", C.c_int)]
+
+
+class Sizes(C.Structure):
+    _fields_ = [("npatch", C.c_int), ("nnod", C.c_int), ("nel", C.c_int), ("ndof", C.c_int),
+                ("neq", C.c_int), ("nceq", C.c_int), ("nnz", C.c_int64)]
+
+
+class Material(C.Structure):
+    _fields_ = [("kind", C.c_int), ("kappa", C.c_double), ("source", C.c_double),
+                ("source_shape", C.c_int), ("E", C.c_double), ("nu", C.c_double),
+                ("body", C.c_double * 3)]
+
+
+class SolverOptions(C.Structure):
+    _fields_ = [("method", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
+                ("max_inner", C.c_int), ("inner_rtol", C.c_double)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("outer_iters", C.c_int), ("inner_iters", C.c_int), ("relres", C.c_double),
+                ("device_ms", C.c_double)]
+
+
+OK, INVALID_ARG, OUT_OF_MEMORY, SINGULAR_JACOBIAN, NOT_CONVERGED, DEVICE_TIMEOUT, \
+    CUDA_ERROR, NOT_READY, UNSUPPORTED = range(9)
+STATUS_NAMES = ["OK", "INVALID_ARG", "OUT_OF_MEMORY", "SINGULAR_JACOBIAN", "NOT_CONVERGED",
+                "DEVICE_TIMEOUT", "CUDA_ERROR", "NOT_READY", "UNSUPPORTED"]
+KE_FP64, KE_SPLIT_TF32 = 0, 1
+POISSON, ELASTICITY = 1, 2
+SOURCE_CONSTANT, SOURCE_SINE = 0, 1
+FIELD_LOG_KAPPA, FIELD_SOURCE_NOISE = 1, 2
+PCG_MIXED, PCG_FP64 = 1, 2
+
+# Every symbol include/ifemgpu.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "ifemgpu_ctx_create", "ifemgpu_ctx_destroy", "ifemgpu_last_error", "ifemgpu_abi_version",
+    "ifemgpu_patch_add", "ifemgpu_patch_set_material", "ifemgpu_patch_set_field",
+    "ifemgpu_patch_constrain_face", "ifemgpu_patch_add_neumann", "ifemgpu_preprocess",
+    "ifemgpu_get_sizes", "ifemgpu_get_madof", "ifemgpu_get_meqn", "ifemgpu_get_mnpc",
+    "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
+    "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_solve",
+    "ifemgpu_expand_solution", "ifemgpu_patch_update_coefs", "ifemgpu_get_stream",
+]
+
+
+class IfemGpuError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES[status] if 0 <= status < 9 else status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libifemgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB
+    if not os.path.exists(path):
+        raise OSError(f"{path} not built: run ifem_gb300.build.build()")
+    lib = C.CDLL(path)
+    P, I, D, V = C.c_void_p, C.c_int, C.c_double, C.c_void_p
+    sig = {
+        "ifemgpu_ctx_create": (I, [C.POINTER(P), C.POINTER(Options)]),
+        "ifemgpu_ctx_destroy": (None, [P]),
+        "ifemgpu_last_error": (C.c_char_p, [P]),
+        "ifemgpu_abi_version": (I, []),
+        "ifemgpu_patch_add": (I, [P, I, V, V, V, V, I, C.POINTER(I)]),
+        "ifemgpu_patch_set_material": (I, [P, I, C.POINTER(Material)]),
+        "ifemgpu_patch_set_field": (I, [P, I, I, V]),
+        "ifemgpu_patch_constrain_face": (I, [P, I, I, I, D]),
+        "ifemgpu_patch_add_neumann": (I, [P, I, I, V]),
+        "ifemgpu_preprocess": (I, [P]),
+        "ifemgpu_get_sizes": (I, [P, C.POINTER(Sizes)]),
+        "ifemgpu_get_madof": (I, [P, V]),
+        "ifemgpu_get_meqn": (I, [P, V]),
+        "ifemgpu_get_mnpc": (I, [P, I, V]),
+        "ifemgpu_get_pattern": (I, [P, V, V]),
+        "ifemgpu_assemble": (I, [P, I]),
+        "ifemgpu_copy_matrix": (I, [P, V]),
+        "ifemgpu_copy_rhs": (I, [P, V]),
+        "ifemgpu_device_system": (I, [P, V, V, V, V]),
+        "ifemgpu_last_assembly_stats": (I, [P, C.POINTER(D), C.POINTER(D),
+                                            C.POINTER(C.c_longlong), C.POINTER(I)]),
+        "ifemgpu_solve": (I, [P, C.POINTER(SolverOptions), V, C.POINTER(SolveInfo)]),
+        "ifemgpu_expand_solution": (I, [P, V, V, D]),
+        "ifemgpu_patch_update_coefs": (I, [P, I, V]),
+        "ifemgpu_get_stream": (I, [P, C.POINTER(C.c_void_p)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class SAM:
+    """Read-only view of the DOF numbering (IFEM SAM, src/LinAlg/SAM.h)."""
+
+    def __init__(self, madof: np.ndarray, meqn: np.ndarray, colptr: np.ndarray,
+                 rowidx: np.ndarray):
+        self.madof, self.meqn, self.colptr, self.rowidx = madof, meqn, colptr, rowidx
+
+    def getNoNodes(self) -> int:
+        return len(self.madof) - 1
+
+    def getNoEquations(self) -> int:
+        return len(self.colptr) - 1
+
+    def getEquation(self, inod: int, ldof: int) -> int:
+        """SAM::getEquation (src/LinAlg/SAM.C:746-755): 1-based node and DOF."""
+        if inod < 1 or inod > self.getNoNodes() or ldof < 1:
+            return -1
+        idof = self.madof[inod - 1] + ldof - 1
+        if idof >= self.madof[inod]:
+            return -2
+        ieq = int(self.meqn[idof - 1])
+        return ieq if ieq > 0 else 0
+
+    def getDofCouplings(self) -> list[list[int]]:
+        """Sorted 1-based coupled equations per equation (SAM::getDofCouplings)."""
+        return [list((self.rowidx[self.colptr[j]:self.colptr[j + 1]] + 1).tolist())
+                for j in range(self.getNoEquations())]
+
+
+class SIM:
+    """One GPU model: patches, numbering, system (mirrors SIMbase usage)."""
+
+    def __init__(self, n_gauss: int = 4, ke_precision: int = KE_FP64, device: int = 0,
+                 verbose: int = 0):
+        self.lib = load_library()
+        self.ctx = C.c_void_p()
+        opts = Options(device, ke_precision, n_gauss, verbose)
+        st = self.lib.ifemgpu_ctx_create(C.byref(self.ctx), C.byref(opts))
+        if st != OK:
+            raise IfemGpuError(st, "ifemgpu_ctx_create failed (no CUDA device?)")
+        self.sizes = None
+        self._patches = []
+
+    def _check(self, st: int):
+        if st != OK:
+            raise IfemGpuError(st, self.lib.ifemgpu_last_error(self.ctx).decode())
+
+    def close(self):
+        if self.ctx:
+            self.lib.ifemgpu_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- model input -------------------------------------------------------
+    def add_patch(self, patch) -> int:
+        """patch: ifem_gb300.workloads.SplinePatch (degree, ncoef, knots, coefs, rational)."""
+        dim = patch.dim
+        deg = np.ascontiguousarray(patch.degree, dtype=np.int32)
+        nco = np.ascontiguousarray(patch.ncoef, dtype=np.int32)
+        kn = [np.ascontiguousarray(k, dtype=np.float64) for k in patch.knots]
+        karr = (C.c_void_p * 3)(*[_ptr(k) for k in kn] + [None] * (3 - dim))
+        coefs = np.ascontiguousarray(patch.coefs, dtype=np.float64)
+        pid = C.c_int()
+        self._check(self.lib.ifemgpu_patch_add(self.ctx, dim, _ptr(deg), _ptr(nco),
+                                               C.cast(karr, C.c_void_p), _ptr(coefs),
+                                               int(patch.rational), C.byref(pid)))
+        self._patches.append((patch, kn, coefs))
+        return pid.value
+
+    def set_material(self, pid: int, kind: int, kappa=1.0, source=0.0, source_shape=0,
+                     E=1.0, nu=0.3, body=(0.0, 0.0, 0.0)):
+        m = Material(kind, kappa, source, source_shape, E, nu, (C.c_double * 3)(*body))
+        self._check(self.lib.ifemgpu_patch_set_material(self.ctx, pid, C.byref(m)))
+
+    def set_field(self, pid: int, which: int, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self.lib.ifemgpu_patch_set_field(self.ctx, pid, which, _ptr(v)))
+
+    def constrain_face(self, pid: int, face: int, dofs: int, value: float = 0.0):
+        self._check(self.lib.ifemgpu_patch_constrain_face(self.ctx, pid, face, dofs, value))
+
+    def add_neumann(self, pid: int, face: int, values):
+        v = np.zeros(3)
+        v[:len(values)] = values
+        self._check(self.lib.ifemgpu_patch_add_neumann(self.ctx, pid, face, _ptr(v)))
+
+    # ---- preprocessing -------------------------------------------------------
+    def preprocess(self):
+        self._check(self.lib.ifemgpu_preprocess(self.ctx))
+        s = Sizes()
+        self._check(self.lib.ifemgpu_get_sizes(self.ctx, C.byref(s)))
+        self.sizes = s
+        return s
+
+    def getSAM(self) -> SAM:
+        s = self.sizes
+        madof = np.zeros(s.nnod + 1, dtype=np.int32)
+        meqn = np.zeros(s.ndof, dtype=np.int32)
+        colptr = np.zeros(s.neq + 1, dtype=np.int32)
+        rowidx = np.zeros(max(s.nnz, 1), dtype=np.int32)
+        self._check(self.lib.ifemgpu_get_madof(self.ctx, _ptr(madof)))
+        self._check(self.lib.ifemgpu_get_meqn(self.ctx, _ptr(meqn)))
+        self._check(self.lib.ifemgpu_get_pattern(self.ctx, _ptr(colptr), _ptr(rowidx)))
+        return SAM(madof, meqn, colptr, rowidx[:s.nnz])
+
+    def mnpc(self, pid: int) -> np.ndarray:
+        patch = self._patches[pid - 1][0]
+        nel = int(np.prod([n - p for n, p in zip(patch.ncoef, patch.degree)]))
+        nen = int(np.prod([p + 1 for p in patch.degree]))
+        out = np.zeros(nel * nen, dtype=np.int32)
+        self._check(self.lib.ifemgpu_get_mnpc(self.ctx, pid, _ptr(out)))
+        return out.reshape(nel, nen)
+
+    def update_coefs(self, pid: int, coefs: np.ndarray):
+        """Asynchronous upload: `coefs` must stay alive until the next sync."""
+        assert coefs.flags.c_contiguous and coefs.dtype == np.float64
+        self._check(self.lib.ifemgpu_patch_update_coefs(self.ctx, pid, _ptr(coefs)))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.ifemgpu_get_stream(self.ctx, C.byref(s)))
+        return s.value or 0
+
+    # ---- assembly / solve ----------------------------------------------------
+    def assembleSystem(self, sync: bool = True):
+        self._check(self.lib.ifemgpu_assemble(self.ctx, 1 if sync else 0))
+
+    def assembly_stats(self):
+        t, v, s, n = C.c_double(), C.c_double(), C.c_longlong(), C.c_int()
+        self._check(self.lib.ifemgpu_last_assembly_stats(self.ctx, C.byref(t), C.byref(v),
+                                                         C.byref(s), C.byref(n)))
+        self.kernel_launches = n.value
+        return t.value, v.value, s.value
+
+    def matrix_values(self) -> np.ndarray:
+        out = np.zeros(self.sizes.nnz, dtype=np.float64)
+        self._check(self.lib.ifemgpu_copy_matrix(self.ctx, _ptr(out)))
+        return out
+
+    def rhs(self) -> np.ndarray:
+        out = np.zeros(self.sizes.neq, dtype=np.float64)
+        self._check(self.lib.ifemgpu_copy_rhs(self.ctx, _ptr(out)))
+        return out
+
+    def copy_matrix_into(self, out: np.ndarray):
+        assert out.dtype == np.float64 and out.size >= self.sizes.nnz
+        self._check(self.lib.ifemgpu_copy_matrix(self.ctx, _ptr(out)))
+
+    def copy_rhs_into(self, out: np.ndarray):
+        assert out.dtype == np.float64 and out.size >= self.sizes.neq
+        self._check(self.lib.ifemgpu_copy_rhs(self.ctx, _ptr(out)))
+
+    def solveSystem(self, method=PCG_MIXED, rtol=1e-10, max_outer=20, max_inner=20000,
+                    inner_rtol=1e-4, check=True):
+        x = np.zeros(self.sizes.neq, dtype=np.float64)
+        o = SolverOptions(method, rtol, max_outer, max_inner, inner_rtol)
+        info = SolveInfo()
+        st = self.lib.ifemgpu_solve(self.ctx, C.byref(o), _ptr(x), C.byref(info))
+        if check:
+            self._check(st)
+        return x, info
+
+    def expand_solution(self, x: np.ndarray, scale: float = 1.0) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        u = np.zeros(self.sizes.ndof, dtype=np.float64)
+        self._check(self.lib.ifemgpu_expand_solution(self.ctx, _ptr(x), _ptr(u), scale))
+        return u

@@ -1,0 +1,264 @@
+/*
+ * ifemgpu.h -- C ABI of the GB300 element-integration, assembly and solve
+ * path for tensor-product spline (B-spline / NURBS) patches.
+ *
+ * One context (ifemgpu_ctx) is one simulator model: a set of structured
+ * spline patches, their SAM-style DOF numbering, one sparse system matrix in
+ * compressed-column storage and its right-hand side, all resident in the
+ * memory of one GPU.  Every entry point returns an ifemgpu_status; the text
+ * of the last failure is available from ifemgpu_last_error().  There is no
+ * CPU fallback: a configuration the GPU path cannot handle is rejected with
+ * IFEMGPU_UNSUPPORTED.
+ *
+ * Each declaration names the IFEM interface it replaces (file:line within
+ * the IFEM source tree).  Conventions that follow IFEM exactly:
+ *   - nodes of a patch are numbered with the first parametric index fastest
+ *     (ASMs3D::generateFEMTopology, src/ASM/ASMs3D.C:487-509);
+ *   - element-to-node lists are ascending, first index fastest
+ *     (ASMs3D::createMNPC, src/ASM/ASMs3D.C:3899-3924);
+ *   - DOFs are node-major, free DOFs are numbered in DOF order
+ *     (SAM::initSystemEquations, src/LinAlg/SAM.C:317-323);
+ *   - the matrix pattern is SuperLU compressed-column storage with 0-based,
+ *     ascending row indices (SparseMatrix::optimiseCols, SparseMatrix.C:984).
+ * Equation numbers returned by this API are 1-based like IFEM's MEQN;
+ * 0 marks a fixed DOF and a negative value -i marks the i-th prescribed DOF.
+ *
+ * Threading: a context is used by one host thread at a time.  All device
+ * work of a context is ordered on one CUDA stream owned by the context.
+ */
+#ifndef IFEMGPU_H
+#define IFEMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IFEMGPU_ABI_VERSION 1
+
+typedef enum ifemgpu_status {
+  IFEMGPU_OK = 0,
+  IFEMGPU_INVALID_ARG = 1,       /* bad argument or call order            */
+  IFEMGPU_OUT_OF_MEMORY = 2,     /* device or host allocation failed      */
+  IFEMGPU_SINGULAR_JACOBIAN = 3, /* |det J| <= 1e-12 at an integration pt */
+  IFEMGPU_NOT_CONVERGED = 4,     /* iterative solve hit its iteration cap */
+  IFEMGPU_DEVICE_TIMEOUT = 5,    /* a bounded device wait gave up          */
+  IFEMGPU_CUDA_ERROR = 6,        /* CUDA runtime error                    */
+  IFEMGPU_NOT_READY = 7,         /* step required before this call missing */
+  IFEMGPU_UNSUPPORTED = 8        /* configuration not handled on the GPU  */
+} ifemgpu_status;
+
+typedef struct ifemgpu_ctx ifemgpu_ctx;
+
+/* Arithmetic of the element matrices. */
+enum ifemgpu_ke_precision {
+  IFEMGPU_KE_FP64 = 0,       /* FP64 on CUDA cores (exact-parity mode)     */
+  IFEMGPU_KE_SPLIT_TF32 = 1  /* FP32 via 3xTF32 tcgen05 products, FP32 acc */
+};
+
+typedef struct ifemgpu_options {
+  int device;        /* CUDA device ordinal; -1 = host-only context (model
+                        input, numbering and pattern; no device work)       */
+  int ke_precision;  /* enum ifemgpu_ke_precision                            */
+  int n_gauss;       /* IFEM nGauss: 1..10 points per direction, or 10+k for
+                        degree+1+k points (ASMbase::getNoGaussPt,
+                        src/ASM/ASMbase.C:1788-1798)                          */
+  int verbose;       /* 0 silent, 1 model summary on stdout                  */
+} ifemgpu_options;
+
+typedef struct ifemgpu_sizes {
+  int npatch;
+  int nnod;          /* total nodes                                  */
+  int nel;           /* total elements (non-zero parametric volume)  */
+  int ndof;          /* total DOFs                                   */
+  int neq;           /* free equations                               */
+  int nceq;          /* prescribed (constraint) equations            */
+  int64_t nnz;       /* non-zeros of the system matrix               */
+} ifemgpu_sizes;
+
+/* Weak form of a patch: the GPU counterpart of the application Integrand.
+ * Poisson:     -div(kappa grad u) = f,   Ke = sum_q kappa dNdX dNdX^T detJxW
+ *              (EqualOrderOperators::Weak::LaplacianCoeff,
+ *               Apps/Utils/EqualOrderOperators.C:194-211; Source :243-265)
+ * Elasticity:  isotropic linear elasticity, Ke = sum_q B^T D B detJxW with
+ *              node-interleaved DOFs (IntegrandBase.C:68-77,
+ *              EqualOrderOperators.C:27-33 for the component ordering).     */
+enum ifemgpu_kind { IFEMGPU_POISSON = 1, IFEMGPU_ELASTICITY = 2 };
+enum ifemgpu_source_shape {
+  IFEMGPU_SOURCE_CONSTANT = 0,  /* f = source                           */
+  IFEMGPU_SOURCE_SINE = 1       /* f = source * prod_d sin(pi x_d)      */
+};
+enum ifemgpu_field {
+  IFEMGPU_FIELD_LOG_KAPPA = 1,   /* g_a: kappa = kappa0 * exp(sum_a R_a g_a) */
+  IFEMGPU_FIELD_SOURCE_NOISE = 2 /* eta_a: f *= (1 + sum_a R_a eta_a)        */
+};
+
+typedef struct ifemgpu_material {
+  int kind;            /* enum ifemgpu_kind                               */
+  double kappa;        /* Poisson conductivity (scale of the field)       */
+  double source;       /* Poisson source scale f0                         */
+  int source_shape;    /* enum ifemgpu_source_shape                       */
+  double E, nu;        /* elasticity: Young's modulus, Poisson's ratio    */
+  double body[3];      /* elasticity: body force per unit volume          */
+} ifemgpu_material;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Replaces IFEM::Init + SIMbase construction (src/IFEM.C:41-46). */
+ifemgpu_status ifemgpu_ctx_create(ifemgpu_ctx** ctx, const ifemgpu_options* opts);
+void ifemgpu_ctx_destroy(ifemgpu_ctx* ctx);
+const char* ifemgpu_last_error(const ifemgpu_ctx* ctx);
+int ifemgpu_abi_version(void);
+
+/* ---- model input ------------------------------------------------------ */
+
+/* Adds one structured spline patch; replaces ASMs3D::read/ASMs2D::read plus
+ * generateFEMTopology (src/ASM/ASMs3D.C:433-516, ASMs2D.C:501).
+ *   dim       2 or 3 (parametric = spatial dimension)
+ *   degree    polynomial degree per direction (GoTools order minus one)
+ *   ncoef     control points per direction
+ *   knots     per direction, ncoef+degree+1 non-decreasing values
+ *   coefs     node-major, first index fastest; per node dim Euclidean
+ *             coordinates followed by the weight when rational != 0
+ * The arrays are copied.  patch_id receives a 1-based patch index.        */
+ifemgpu_status ifemgpu_patch_add(ifemgpu_ctx* ctx, int dim, const int* degree,
+                                 const int* ncoef, const double* const* knots,
+                                 const double* coefs, int rational,
+                                 int* patch_id);
+
+/* Sets the weak form integrated over a patch (Integrand / IntegrandBase::npv,
+ * src/ASM/IntegrandBase.h:363).  Must precede ifemgpu_preprocess.        */
+ifemgpu_status ifemgpu_patch_set_material(ifemgpu_ctx* ctx, int patch_id,
+                                          const ifemgpu_material* mat);
+
+/* Per-control-point coefficient field (enum ifemgpu_field), nnod values.  */
+ifemgpu_status ifemgpu_patch_set_field(ifemgpu_ctx* ctx, int patch_id,
+                                       int which, const double* values);
+
+/* Dirichlet condition on a patch face; replaces ASMs3D::constrainFace
+ * (src/ASM/ASMs3D.C:1025-1102) and ASMs2D::constrainEdge.  face follows the
+ * IFEM face index (1:-u 2:+u 3:-v 4:+v 5:-w 6:+w), dofs is a digit list
+ * such as 123.  value 0 fixes the DOFs (MSC=0, ASMbase::fix,
+ * src/ASM/ASMbase.C:963); a non-zero value prescribes them through a
+ * constraint equation with coefficient c0=value (ASMbase::prescribe, :884). */
+ifemgpu_status ifemgpu_patch_constrain_face(ifemgpu_ctx* ctx, int patch_id,
+                                            int face, int dofs, double value);
+
+/* Constant Neumann data on a face: traction vector (elasticity, npv values)
+ * or normal flux (Poisson, 1 value); integrated by the face overload of
+ * ASMs3D::integrate (src/ASM/ASMs3D.C:2547-2812).                        */
+ifemgpu_status ifemgpu_patch_add_neumann(ifemgpu_ctx* ctx, int patch_id,
+                                         int face, const double* values);
+
+/* ---- preprocessing ---------------------------------------------------- */
+
+/* Node/DOF numbering and matrix pattern; replaces SIMbase::preprocessC
+ * (src/SIM/SIMbase.C:209-443) -> SAMpatch::init (src/ASM/SAMpatch.C:21-81)
+ * and SIMbase::initSystem -> SparseMatrix::preAssemble/optimiseCols
+ * (src/LinAlg/SparseMatrix.C:731-762, :984-1023).  Uploads the model to the
+ * device and builds the element colouring.                                */
+ifemgpu_status ifemgpu_preprocess(ifemgpu_ctx* ctx);
+
+ifemgpu_status ifemgpu_get_sizes(const ifemgpu_ctx* ctx, ifemgpu_sizes* out);
+
+/* SAM arrays (src/LinAlg/SAM.h:333-342): MADOF (nnod+1, 1-based
+ * accumulated DOFs) and MEQN (ndof).                                      */
+ifemgpu_status ifemgpu_get_madof(const ifemgpu_ctx* ctx, int* madof);
+ifemgpu_status ifemgpu_get_meqn(const ifemgpu_ctx* ctx, int* meqn);
+
+/* Element connectivity of a patch: nel x nen patch-local 0-based nodes
+ * (ASMbase::MNPC, src/ASM/ASMbase.h:1085).                                */
+ifemgpu_status ifemgpu_get_mnpc(const ifemgpu_ctx* ctx, int patch_id,
+                                int* mnpc);
+
+/* Compressed-column pattern (SparseMatrix IA/JA, SparseMatrix.h:294-297):
+ * colptr has neq+1 entries, rowidx nnz entries.                           */
+ifemgpu_status ifemgpu_get_pattern(const ifemgpu_ctx* ctx, int* colptr,
+                                   int* rowidx);
+
+/* Replaces the control net of a preprocessed patch (same layout as
+ * ifemgpu_patch_add), e.g. for a moved or optimised geometry; the topology
+ * and numbering are kept.  The host array is read by an asynchronous copy
+ * on the context's stream: it must stay valid until the next synchronising
+ * call (pinned memory makes the copy truly asynchronous).  Counterpart of
+ * updating the spline coefficients of ASMs3D's Go::SplineVolume before the
+ * next SIMbase::assembleSystem.                                           */
+ifemgpu_status ifemgpu_patch_update_coefs(ifemgpu_ctx* ctx, int patch_id,
+                                          const double* coefs);
+
+/* The CUDA stream (cudaStream_t) all device work of the context runs on. */
+ifemgpu_status ifemgpu_get_stream(const ifemgpu_ctx* ctx, void** stream);
+
+/* ---- assembly --------------------------------------------------------- */
+
+/* Zeroes the system and integrates every patch (interior and Neumann
+ * faces), scattering into the matrix and right-hand side; replaces
+ * SIMbase::assembleSystem (src/SIM/SIMbase.C:1229-1429) with
+ * ASMs3D::integrate (src/ASM/ASMs3D.C:2071-2335) and
+ * AlgEqSystem::assemble -> SAM::assembleSystem -> assemSparse
+ * (src/ASM/AlgEqSystem.C:215-303, src/LinAlg/SAM.C:430-467,
+ * src/LinAlg/SparseMatrix.C:614-688).  Stream-ordered; returns once the
+ * work is enqueued unless sync != 0.                                      */
+ifemgpu_status ifemgpu_assemble(ifemgpu_ctx* ctx, int sync);
+
+/* Copies the assembled matrix values (nnz, FP64, compressed-column order)
+ * and the right-hand side (neq) to host memory.                           */
+ifemgpu_status ifemgpu_copy_matrix(ifemgpu_ctx* ctx, double* values);
+ifemgpu_status ifemgpu_copy_rhs(ifemgpu_ctx* ctx, double* rhs);
+
+/* Device pointers of the system, owned by the context (read-only use).   */
+ifemgpu_status ifemgpu_device_system(ifemgpu_ctx* ctx, const double** values,
+                                     const int** colptr, const int** rowidx,
+                                     const double** rhs);
+
+/* Statistics of the last ifemgpu_assemble: device time in milliseconds of
+ * the whole assembly and of its volume integration + scatter passes alone,
+ * and the number of integration points skipped because |det J| <= 1e-12
+ * (IFEM skips them the same way, src/ASM/ASMs3D.C:2286), and the number of
+ * kernels one assembly launches.  Synchronises.  Null pointers are skipped. */
+ifemgpu_status ifemgpu_last_assembly_stats(ifemgpu_ctx* ctx, double* total_ms,
+                                           double* volume_ms,
+                                           long long* singular_points,
+                                           int* kernel_launches);
+
+/* ---- solve ------------------------------------------------------------ */
+
+enum ifemgpu_solver_method {
+  IFEMGPU_PCG_MIXED = 1,  /* FP32 Jacobi-PCG inner, FP64 residual refinement */
+  IFEMGPU_PCG_FP64 = 2    /* FP64 Jacobi-PCG                                 */
+};
+
+typedef struct ifemgpu_solver_options {
+  int method;          /* enum ifemgpu_solver_method                     */
+  double rtol;         /* target ||b - A x|| / ||b|| in FP64 (e.g. 1e-10) */
+  int max_outer;       /* refinement steps (mixed)                       */
+  int max_inner;       /* PCG iterations per refinement step / total     */
+  double inner_rtol;   /* FP32 residual reduction per refinement step    */
+} ifemgpu_solver_options;
+
+typedef struct ifemgpu_solve_info {
+  int outer_iters;
+  int inner_iters;     /* total PCG iterations                           */
+  double relres;       /* final FP64 relative residual                   */
+  double device_ms;    /* device time of the solve                       */
+} ifemgpu_solve_info;
+
+/* Solves K x = b with the assembled system; replaces SIMbase::solveSystem
+ * -> SparseMatrix::solve (src/SIM/SIMbase.C:1487-1550,
+ * src/LinAlg/SparseMatrix.C:1026-1042).  x (neq) is host memory.          */
+ifemgpu_status ifemgpu_solve(ifemgpu_ctx* ctx,
+                             const ifemgpu_solver_options* opts, double* x,
+                             ifemgpu_solve_info* info);
+
+/* Equation order -> DOF order, fixed DOFs 0 and prescribed DOFs their value
+ * times scale; replaces SAM::expandSolution (src/LinAlg/SAM.C:768-810).   */
+ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
+                                       double* u, double scale);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IFEMGPU_H */
