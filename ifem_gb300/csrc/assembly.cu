@@ -625,7 +625,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   }
   // volume items grouped by colour: colour = (e1 mod q1) + q1 (e2 mod q2) + ...
   for (int c = 0; c < maxColours; c++) {
-    Pass pass{(int)vol.size(), 0, 0, 0, 0};
+    Pass pass{(int)vol.size(), 0, 0, 0, 0, ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32};
     for (int pi = 0; pi < np; pi++) {
       const HostPatch& pc = ctx->patches[pi];
       const int q1 = pc.p[0] + 1, q2 = pc.p[1] + 1, q3 = pc.dim == 3 ? pc.p[2] + 1 : 1;
@@ -639,6 +639,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
           }
       pass.maxNd = std::max(pass.maxNd, pc.nen() * pc.npv);
       pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi]));
+      pass.tc = pass.tc && tcSupports(ctx->h_devpatches[pi]);
     }
     pass.count = (int)vol.size() - pass.first;
     if (pass.count) ctx->passes.push_back(pass);
@@ -660,7 +661,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
       for (int d = 0; d < 3; d++)
         if (d != nd0) nqf *= gaussCount(ctx->opts.n_gauss, pc.p[d] + 1, true);
       for (int c = 0; c < qa * qb; c++) {
-        Pass pass{0, 0, nm.face, pc.nen() * pc.npv, faceSmem(ctx->h_devpatches[pi], nqf)};
+        Pass pass{0, 0, nm.face, pc.nen() * pc.npv, faceSmem(ctx->h_devpatches[pi], nqf), false};
         std::vector<Item> lst;
         for (int e = 0; e < pc.nelAll; e++) {
           if (!pc.active[e]) continue;
@@ -697,6 +698,13 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
                                          (int)std::min<size_t>(maxSmem, 227 * 1024)));
   IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_face_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::min<size_t>(maxSmem, 227 * 1024)));
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&ctx->numSMs, cudaDevAttrMultiProcessorCount,
+                                           ctx->opts.device));
+  for (auto& p : ctx->passes)
+    if (p.tc) {
+      IFEMGPU_TRY(tcPrepare(ctx));
+      break;
+    }
   return IFEMGPU_OK;
 }
 
@@ -751,7 +759,9 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
       IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
       faceStarted = true;
     }
-    if (!p.face)
+    if (p.tc)
+      IFEMGPU_TRY(tcLaunchVolume(ctx, p, std::min(p.count, 3 * ctx->numSMs)));
+    else if (!p.face)
       k_volume_fp64<<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
     else
       k_face_fp64<<<p.count, 128, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first,

@@ -96,7 +96,12 @@ struct Pass {
   int face;    // 0 volume, else face pass
   int maxNd;   // largest element DOF count in the pass
   size_t smem; // dynamic shared memory of the pass' launch
+  bool tc;     // volume pass on the tensor-core kernel
 };
+
+// tc_volume.cu
+bool tcSupports(const DevPatch& P);
+size_t tcVolumeSmem();
 
 }  // namespace ifemgpu
 
@@ -132,6 +137,7 @@ struct ifemgpu_ctx {
   double last_total_ms = 0.0, last_volume_ms = 0.0;
   unsigned long long last_singular = 0;
   int launches_per_assembly = 0;
+  int numSMs = 1;
   // solver workspace (allocated on first solve)
   float* d_K32 = nullptr;
   double* d_work = nullptr;
@@ -148,6 +154,10 @@ ifemgpu_status cudaFail(ifemgpu_ctx* ctx, cudaError_t e, const char* what);
 ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx);
 ifemgpu_status launchAssembly(ifemgpu_ctx* ctx);
 ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs);
+
+// tc_volume.cu
+ifemgpu_status tcPrepare(ifemgpu_ctx* ctx);
+ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid);
 
 // solver.cu
 ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o,

@@ -1,0 +1,157 @@
+// tc_common.cuh -- inline-PTX building blocks for the sm_103a tensor-core
+// path: tcgen05 MMA (kind::tf32, cta_group::1), tensor-memory allocation and
+// loads, mbarrier waits with an iteration bound, and the shared-memory
+// operand layout.
+//
+// Operand layout ("K-major, no swizzle"): a tile of R rows x 32 K-elements
+// (FP32/TF32) is stored as 8x4 core matrices of 128 bytes; the core matrices
+// of one 8-row group are adjacent along K (leading byte offset 128 B) and the
+// 8-row groups follow each other every 1024 B (stride byte offset).
+#pragma once
+
+#include <cstdint>
+
+namespace ifemgpu {
+namespace tc {
+
+constexpr int kK = 32;                 // K extent of one operand tile (elements)
+constexpr uint32_t kLBO = 128;         // bytes between K-adjacent core matrices
+constexpr uint32_t kSBO = 1024;        // bytes between 8-row groups
+constexpr uint32_t kSpinLimit = 1u << 22;  // bounded mbarrier polling
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// float offset of (row r, k) in a K-major tile with kK = 32
+__device__ __forceinline__ int kmaj(int r, int k)
+{
+  return (r >> 3) * 256 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3);
+}
+
+// shared-memory matrix descriptor (sm_100 family): start address, LBO, SBO
+// (all >> 4), descriptor version 1 at bit 46, no swizzle, base offset 0.
+__device__ __forceinline__ uint64_t smemDesc(uint32_t saddr)
+{
+  return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) |
+         (static_cast<uint64_t>(kLBO >> 4) << 16) |
+         (static_cast<uint64_t>(kSBO >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
+// (bits 7-9 and 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t instrDescTF32(int M, int N)
+{
+  return (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mmaTF32(uint32_t tmemD, uint64_t adesc, uint64_t bdesc,
+                                        uint32_t idesc, uint32_t accumulate)
+{
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+      :
+      : "r"(tmemD), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mmaCommit(uint32_t mbar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               :
+               : "r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbarInit(uint32_t mbar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(mbar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" : : : "memory");
+}
+
+__device__ __forceinline__ bool mbarTryWait(uint32_t mbar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Polls the barrier phase at most kSpinLimit times; false on give-up.
+__device__ __forceinline__ bool mbarWait(uint32_t mbar, uint32_t parity)
+{
+  for (uint32_t i = 0; i < kSpinLimit; i++)
+    if (mbarTryWait(mbar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void fenceProxyAsync()
+{
+  asm volatile("fence.proxy.async.shared::cta;" : : : "memory");
+}
+
+__device__ __forceinline__ void tcFenceBefore()
+{
+  asm volatile("tcgen05.fence::before_thread_sync;" : : : "memory");
+}
+
+__device__ __forceinline__ void tcFenceAfter()
+{
+  asm volatile("tcgen05.fence::after_thread_sync;" : : : "memory");
+}
+
+// one warp: allocate ncols TMEM columns, base address written to smem slot
+__device__ __forceinline__ void tmemAlloc(uint32_t* slot, uint32_t ncols)
+{
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+               :
+               : "r"(smemAddr(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" : : : "memory");
+}
+
+__device__ __forceinline__ void tmemDealloc(uint32_t taddr, uint32_t ncols)
+{
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+               :
+               : "r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+// 32 lanes x 16 columns of 32-bit words: thread t of the warp receives lane
+// (quadrant base + t), columns col..col+15
+__device__ __forceinline__ void tmemLoad16(uint32_t taddr, float* v)
+{
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : : : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// x = hi + lo with hi rounded to TF32 (10 explicit mantissa bits)
+__device__ __forceinline__ void splitTF32(float x, float& hi, float& lo)
+{
+  const uint32_t b = __float_as_uint(x);
+  hi = __uint_as_float((b + 0x1000u) & 0xFFFFE000u);
+  lo = x - hi;
+}
+
+}  // namespace tc
+}  // namespace ifemgpu

@@ -63,6 +63,7 @@ EXPORTS = [
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
     "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_solve",
     "ifemgpu_expand_solution", "ifemgpu_patch_update_coefs", "ifemgpu_get_stream",
+    "ifemgpu_selftest_tc_gemm",
 ]
 
 
@@ -111,6 +112,7 @@ def load_library(path: str | None = None):
         "ifemgpu_expand_solution": (I, [P, V, V, D]),
         "ifemgpu_patch_update_coefs": (I, [P, I, V]),
         "ifemgpu_get_stream": (I, [P, C.POINTER(C.c_void_p)]),
+        "ifemgpu_selftest_tc_gemm": (I, [V, V, V]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -122,6 +124,19 @@ def load_library(path: str | None = None):
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def selftest_tc_gemm(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """D = A B^T on the tensor cores (A 128x32, B 96x32 float32)."""
+    lib = load_library()
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    assert A.shape == (128, 32) and B.shape == (96, 32)
+    D = np.zeros((128, 96), dtype=np.float32)
+    st = lib.ifemgpu_selftest_tc_gemm(_ptr(A), _ptr(B), _ptr(D))
+    if st != OK:
+        raise IfemGpuError(st, "tensor-core self-test failed")
+    return D
 
 
 class SAM:

@@ -257,6 +257,14 @@ ifemgpu_status ifemgpu_solve(ifemgpu_ctx* ctx,
 ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
                                        double* u, double scale);
 
+/* ---- diagnostics ------------------------------------------------------ */
+
+/* Runs the tensor-core building block of the element kernel once on the
+ * current device: D (128 x 96) = A (128 x 32) * B (96 x 32)^T in 3xTF32
+ * split precision with FP32 accumulation, all row-major host arrays.  No
+ * IFEM counterpart: it checks the sm_103a MMA path in isolation.          */
+ifemgpu_status ifemgpu_selftest_tc_gemm(const float* A, const float* B, float* D);
+
 #ifdef __cplusplus
 }
 #endif
