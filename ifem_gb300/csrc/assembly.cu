@@ -609,6 +609,10 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
       D.span[d] = pc.d_span[d];
     }
     IFEMGPU_TRY(upload(ctx, &pc.d_ctrl, pc.ctrl4.data(), pc.ctrl4.size()));
+    if (!pc.lineOff.empty()) {
+      IFEMGPU_TRY(upload(ctx, &pc.d_lineOff, pc.lineOff.data(), pc.lineOff.size()));
+      D.lineOff = pc.d_lineOff;
+    }
     D.ctrl = pc.d_ctrl;
     if (!pc.logk.empty()) {
       IFEMGPU_TRY(upload(ctx, &pc.d_logk, pc.logk.data(), pc.logk.size()));
@@ -689,6 +693,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   if (!ctx->c0.empty()) IFEMGPU_TRY(upload(ctx, &ctx->d_c0, ctx->c0.data(), ctx->c0.size()));
   IFEMGPU_TRY(upload(ctx, &ctx->d_colptr, ctx->colptr.data(), ctx->colptr.size()));
   IFEMGPU_TRY(upload(ctx, &ctx->d_rowidx, ctx->rowidx.data(), ctx->rowidx.size()));
+  IFEMGPU_TRY(upload(ctx, &ctx->d_freeBefore, ctx->freeBefore.data(), ctx->freeBefore.size()));
   IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_K, sizeof(double) * std::max<int64_t>(ctx->nnz, 1)));
   IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_b, sizeof(double) * std::max(ctx->neq, 1)));
   IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 4));
@@ -736,10 +741,10 @@ ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs)
   return IFEMGPU_OK;
 }
 
-ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
+// The kernel sequence of one assembly; captured once into a CUDA graph.
+static ifemgpu_status enqueueAssembly(ifemgpu_ctx* ctx)
 {
   cudaStream_t s = ctx->stream;
-  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_K, 0, sizeof(double) * ctx->nnz, s));
   IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_b, 0, sizeof(double) * ctx->neq, s));
   IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4, s));
@@ -769,6 +774,27 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
     IFEMGPU_CUDA(ctx, cudaGetLastError());
   }
   if (!faceStarted) IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
+{
+  cudaStream_t s = ctx->stream;
+  if (!ctx->graphExec) {
+    IFEMGPU_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    ifemgpu_status st = enqueueAssembly(ctx);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (st != IFEMGPU_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    IFEMGPU_CUDA(ctx, e);
+    ctx->graph = g;
+    IFEMGPU_CUDA(ctx, cudaGraphInstantiate(&ctx->graphExec, g, 0));
+  }
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec, s));
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   ctx->launches_per_assembly = (int)ctx->h_devpatches.size() + (int)ctx->passes.size();
   return IFEMGPU_OK;

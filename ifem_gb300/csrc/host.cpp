@@ -41,6 +41,7 @@ void freeDevice(ifemgpu_ctx* ctx)
   for (auto& pc : ctx->patches) {
     f(pc.d_ctrl); pc.d_ctrl = nullptr;
     f(pc.d_stage); pc.d_stage = nullptr;
+    f(pc.d_lineOff); pc.d_lineOff = nullptr;
     f(pc.d_logk); pc.d_logk = nullptr;
     f(pc.d_noise); pc.d_noise = nullptr;
     for (int d = 0; d < 3; d++) {
@@ -50,7 +51,12 @@ void freeDevice(ifemgpu_ctx* ctx)
   }
   f(ctx->d_madof); f(ctx->d_meqn); f(ctx->d_c0); f(ctx->d_colptr);
   f(ctx->d_rowidx); f(ctx->d_K); f(ctx->d_b); f(ctx->d_patches);
-  f(ctx->d_items); f(ctx->d_neumann); f(ctx->d_counters);
+  f(ctx->d_items); f(ctx->d_neumann); f(ctx->d_counters); f(ctx->d_freeBefore);
+  ctx->d_freeBefore = nullptr;
+  if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graphExec = nullptr;
+  ctx->graph = nullptr;
   ctx->d_madof = ctx->d_meqn = nullptr;
   ctx->d_c0 = nullptr;
   ctx->d_colptr = ctx->d_rowidx = nullptr;
@@ -258,6 +264,39 @@ ifemgpu_status pattern(ifemgpu_ctx* ctx)
         int g = pc.firstNode + m;
         for (int d = ctx->madof[g]; d < ctx->madof[g + 1]; d++)
           if (ctx->meqn[d - 1] > 0) ctx->rowidx[k++] = ctx->meqn[d - 1] - 1;
+      }
+    }
+  }
+  // F(n), and the line-offset tables that give pattern positions without a
+  // search for patches whose couplings are the index box
+  ctx->freeBefore.assign(ctx->nnod + 1, 0);
+  for (int n = 0; n < ctx->nnod; n++) {
+    int f = 0;
+    for (int d = ctx->madof[n]; d < ctx->madof[n + 1]; d++) f += ctx->meqn[d - 1] > 0;
+    ctx->freeBefore[n + 1] = ctx->freeBefore[n] + f;
+  }
+  const std::vector<int>& F = ctx->freeBefore;
+  for (auto& pc : ctx->patches) {
+    pc.lineOff.clear();
+    if (!boxCoupling(pc)) continue;
+    const int w1 = 2 * pc.p[1] + 1, w2 = 2 * pc.p[2] + 1;
+    pc.lineOff.assign((size_t)pc.nnod * w1 * w2, 0);
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < pc.nnod; b++) {
+      const int xb = b % pc.n[0], yb = (b / pc.n[0]) % pc.n[1], zb = b / (pc.n[0] * pc.n[1]);
+      const int x0 = std::max(0, xb - pc.p[0]), x1 = std::min(pc.n[0] - 1, xb + pc.p[0]);
+      int acc = 0;
+      for (int dz = -pc.p[2]; dz <= pc.p[2]; dz++) {
+        const int z = zb + dz;
+        if (z < 0 || z >= pc.n[2]) continue;
+        for (int dy = -pc.p[1]; dy <= pc.p[1]; dy++) {
+          const int y = yb + dy;
+          if (y < 0 || y >= pc.n[1]) continue;
+          const int s = pc.firstNode + (z * pc.n[1] + y) * pc.n[0] + x0;
+          const int e = pc.firstNode + (z * pc.n[1] + y) * pc.n[0] + x1 + 1;
+          pc.lineOff[(size_t)b * w1 * w2 + (dz + pc.p[2]) * w1 + dy + pc.p[1]] = acc - F[s];
+          acc += F[e] - F[s];
+        }
       }
     }
   }

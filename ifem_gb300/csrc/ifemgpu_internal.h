@@ -40,6 +40,13 @@ struct DevPatch {
   double* tabN[3];
   double* tabD[3];
   double* span[3];
+  // Position table of the compressed-column pattern for patches whose
+  // couplings are the index box of half-width p (nullptr otherwise): for
+  // node b and the box line (dz, dy), lineOff[b*(2p+1)^2 + (dz+p)(2p+1) +
+  // dy+p] = (free DOFs of the box lines before it) - F(first node of the
+  // line), so that row (a, k) sits in column (b, l) at
+  // colptr[c] + lineOff[...] + F(a) + rank of k among a's free DOFs.
+  const int* lineOff;
   // Gauss rules: volume (gx, gw) and face (fx, fw, ngf points)
   double gx[3][kMaxGauss], gw[3][kMaxGauss];
   double fx[3][kMaxGauss], fw[3][kMaxGauss];
@@ -87,6 +94,8 @@ struct HostPatch {
   double* d_tabN[3] = {nullptr, nullptr, nullptr};
   double* d_tabD[3] = {nullptr, nullptr, nullptr};
   double* d_span[3] = {nullptr, nullptr, nullptr};
+  std::vector<int> lineOff;       // see DevPatch::lineOff (empty: no box coupling)
+  int* d_lineOff = nullptr;
 };
 
 // One colour pass of the volume or face integration.
@@ -119,6 +128,10 @@ struct ifemgpu_ctx {
   std::vector<int> madof, meqn;
   std::vector<double> c0;
   std::vector<int> colptr, rowidx;
+  std::vector<int> freeBefore;  // F(n): free DOFs of the nodes before node n (nnod+1)
+  int* d_freeBefore = nullptr;
+  cudaGraph_t graph = nullptr;  // captured pass sequence of one assembly
+  cudaGraphExec_t graphExec = nullptr;
   // device model
   int* d_madof = nullptr;
   int* d_meqn = nullptr;

@@ -52,6 +52,9 @@ struct TcSmem {
   float wq[kNq];           // detJ * dV * Gauss weights (0 at skipped points)
   float X[kNen][4];        // control points relative to the element's first, weight
   int eq[kNen * 3];
+  int colStart[kNen * 3];  // colptr of the element's free columns
+  int Fa[kNen];            // F(a): free DOFs before node a
+  int lo[kNen][9];         // line offset of row node line (j + 3k) in column node b
   unsigned long long mbar;
   uint32_t tmemSlot;
   int fail;
@@ -80,6 +83,7 @@ __device__ __forceinline__ void redAdd(double* p, double v)
 struct TcSys {
   const int* madof;
   const int* meqn;
+  const int* F;
   const double* c0;
   const int* colptr;
   const int* rowidx;
@@ -132,6 +136,16 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.eq[3 * a] = S.meqn[d0];
       sm.eq[3 * a + 1] = S.meqn[d0 + 1];
       sm.eq[3 * a + 2] = S.meqn[d0 + 2];
+      sm.Fa[a] = S.F[P.firstNode + node];
+    }
+    if (P.lineOff) {
+      // line offsets of the 9 row lines of the element in each column node
+      for (int idx = tid; idx < kNen * 9; idx += blockDim.x) {
+        const int bn = idx / 9, la = idx % 9;
+        const int nodeb = n0 + ((bn / 9) * P.n[1] + (bn / 3) % 3) * P.n[0] + bn % 3;
+        const int dy = la % 3 - (bn / 3) % 3, dz = la / 3 - bn / 9;
+        sm.lo[bn][la] = P.lineOff[(size_t)nodeb * 25 + (dz + 2) * 5 + dy + 2];
+      }
     }
     // zero padding of the operand tiles (rows a >= 27 per component block,
     // rows >= 96 of A, columns q >= 27)
@@ -148,6 +162,8 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       }
     }
     __syncthreads();
+
+    if (tid < kNen * 3) sm.colStart[tid] = sm.eq[tid] > 0 ? S.colptr[sm.eq[tid] - 1] : 0;
 
     // ---- 2. weighted tensor-product basis at every (Gauss point, function)
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
@@ -319,16 +335,21 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
 #pragma unroll
         for (int l = 0; l < 3; l++) g[k][l] = G[(32 * k + a) * kGld + 32 * l + bn];
       const double tr = (double)g[0][0] + (double)g[1][1] + (double)g[2][2];
-      const int pos0 = findRowTc(S.colptr, S.rowidx, firstCol, firstRow);
-      if (pos0 < 0) {
-        atomicAdd(S.counters + 1, 1ull);
-        continue;
+      int off;
+      if (P.lineOff) {
+        off = sm.lo[bn][(a / 3) % 3 + 3 * (a / 9)] + sm.Fa[a];
+      } else {
+        const int pos0 = findRowTc(S.colptr, S.rowidx, firstCol, firstRow);
+        if (pos0 < 0) {
+          atomicAdd(S.counters + 1, 1ull);
+          continue;
+        }
+        off = pos0 - S.colptr[firstCol];
       }
-      const int off = pos0 - S.colptr[firstCol];
       for (int l = 0; l < 3; l++) {
         const int ce = sm.eq[3 * bn + l];
         if (ce <= 0) continue;
-        double* col = S.K + S.colptr[ce - 1] + off;
+        double* col = S.K + sm.colStart[3 * bn + l] + off;
         int rank = 0;
         for (int k = 0; k < 3; k++) {
           if (sm.eq[3 * a + k] <= 0) continue;
@@ -450,8 +471,8 @@ ifemgpu_status tcPrepare(ifemgpu_ctx* ctx)
 
 ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid)
 {
-  TcSys S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
-          ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters};
+  TcSys S{ctx->d_madof, ctx->d_meqn, ctx->d_freeBefore, ctx->nceq ? ctx->d_c0 : nullptr,
+          ctx->d_colptr, ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters};
   // dynamic shared memory is 1024-aligned by the __align__ of the buffer
   k_volume_tc_elast_p2<<<grid, 128, tcVolumeSmem(), ctx->stream>>>(ctx->d_patches,
                                                                    ctx->d_items + p.first,
