@@ -741,29 +741,29 @@ ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs)
   return IFEMGPU_OK;
 }
 
-// The kernel sequence of one assembly; captured once into a CUDA graph.
-static ifemgpu_status enqueueAssembly(ifemgpu_ctx* ctx)
+// The kernel sequence of one assembly in three segments -- prologue (zeroing,
+// basis tables), volume passes, face passes -- each captured once into a CUDA
+// graph; the timing events are recorded between the graph launches.
+static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
 {
   cudaStream_t s = ctx->stream;
-  IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_K, 0, sizeof(double) * ctx->nnz, s));
-  IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_b, 0, sizeof(double) * ctx->neq, s));
-  IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4, s));
-  for (int pi = 0; pi < (int)ctx->h_devpatches.size(); pi++) {
-    const DevPatch& D = ctx->h_devpatches[pi];
-    int work = 0;
-    for (int d = 0; d < D.dim; d++) work += D.nel[d] * D.ng[d];
-    k_basis_tables<<<(work + 127) / 128, 128, 0, s>>>(D);
+  if (seg == 0) {
+    IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_K, 0, sizeof(double) * ctx->nnz, s));
+    IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_b, 0, sizeof(double) * ctx->neq, s));
+    IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4, s));
+    for (int pi = 0; pi < (int)ctx->h_devpatches.size(); pi++) {
+      const DevPatch& D = ctx->h_devpatches[pi];
+      int work = 0;
+      for (int d = 0; d < D.dim; d++) work += D.nel[d] * D.ng[d];
+      k_basis_tables<<<(work + 127) / 128, 128, 0, s>>>(D);
+    }
+    IFEMGPU_CUDA(ctx, cudaGetLastError());
+    return IFEMGPU_OK;
   }
-  IFEMGPU_CUDA(ctx, cudaGetLastError());
   SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
             ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters};
-  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
-  bool faceStarted = false;
   for (const Pass& p : ctx->passes) {
-    if (p.face && !faceStarted) {
-      IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
-      faceStarted = true;
-    }
+    if ((p.face != 0) != (seg == 2)) continue;
     if (p.tc)
       IFEMGPU_TRY(tcLaunchVolume(ctx, p, std::min(p.count, 3 * ctx->numSMs)));
     else if (!p.face)
@@ -773,16 +773,16 @@ static ifemgpu_status enqueueAssembly(ifemgpu_ctx* ctx)
                                                ctx->d_neumann, S);
     IFEMGPU_CUDA(ctx, cudaGetLastError());
   }
-  if (!faceStarted) IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
   return IFEMGPU_OK;
 }
 
 ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
 {
   cudaStream_t s = ctx->stream;
-  if (!ctx->graphExec) {
+  for (int seg = 0; seg < 3; seg++) {
+    if (ctx->graphExec[seg]) continue;
     IFEMGPU_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    ifemgpu_status st = enqueueAssembly(ctx);
+    ifemgpu_status st = enqueueSegment(ctx, seg);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s, &g);
     if (st != IFEMGPU_OK) {
@@ -790,11 +790,15 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
       return st;
     }
     IFEMGPU_CUDA(ctx, e);
-    ctx->graph = g;
-    IFEMGPU_CUDA(ctx, cudaGraphInstantiate(&ctx->graphExec, g, 0));
+    ctx->graph[seg] = g;
+    IFEMGPU_CUDA(ctx, cudaGraphInstantiate(&ctx->graphExec[seg], g, 0));
   }
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
-  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec, s));
+  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[0], s));
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[1], s));
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[2], s));
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   ctx->launches_per_assembly = (int)ctx->h_devpatches.size() + (int)ctx->passes.size();
   return IFEMGPU_OK;

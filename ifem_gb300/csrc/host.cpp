@@ -53,10 +53,12 @@ void freeDevice(ifemgpu_ctx* ctx)
   f(ctx->d_rowidx); f(ctx->d_K); f(ctx->d_b); f(ctx->d_patches);
   f(ctx->d_items); f(ctx->d_neumann); f(ctx->d_counters); f(ctx->d_freeBefore);
   ctx->d_freeBefore = nullptr;
-  if (ctx->graphExec) cudaGraphExecDestroy(ctx->graphExec);
-  if (ctx->graph) cudaGraphDestroy(ctx->graph);
-  ctx->graphExec = nullptr;
-  ctx->graph = nullptr;
+  for (int g = 0; g < 3; g++) {
+    if (ctx->graphExec[g]) cudaGraphExecDestroy(ctx->graphExec[g]);
+    if (ctx->graph[g]) cudaGraphDestroy(ctx->graph[g]);
+    ctx->graphExec[g] = nullptr;
+    ctx->graph[g] = nullptr;
+  }
   ctx->d_madof = ctx->d_meqn = nullptr;
   ctx->d_c0 = nullptr;
   ctx->d_colptr = ctx->d_rowidx = nullptr;

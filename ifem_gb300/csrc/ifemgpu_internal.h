@@ -130,8 +130,8 @@ struct ifemgpu_ctx {
   std::vector<int> colptr, rowidx;
   std::vector<int> freeBefore;  // F(n): free DOFs of the nodes before node n (nnod+1)
   int* d_freeBefore = nullptr;
-  cudaGraph_t graph = nullptr;  // captured pass sequence of one assembly
-  cudaGraphExec_t graphExec = nullptr;
+  cudaGraph_t graph[3] = {nullptr, nullptr, nullptr};  // captured assembly segments
+  cudaGraphExec_t graphExec[3] = {nullptr, nullptr, nullptr};
   // device model
   int* d_madof = nullptr;
   int* d_meqn = nullptr;
