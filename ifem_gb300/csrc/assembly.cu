@@ -779,8 +779,10 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
 ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
 {
   cudaStream_t s = ctx->stream;
+  bool hasSeg[3] = {true, false, false};
+  for (const Pass& p : ctx->passes) hasSeg[p.face ? 2 : 1] = true;
   for (int seg = 0; seg < 3; seg++) {
-    if (ctx->graphExec[seg]) continue;
+    if (ctx->graphExec[seg] || !hasSeg[seg]) continue;
     IFEMGPU_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     ifemgpu_status st = enqueueSegment(ctx, seg);
     cudaGraph_t g = nullptr;
@@ -793,12 +795,10 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
     ctx->graph[seg] = g;
     IFEMGPU_CUDA(ctx, cudaGraphInstantiate(&ctx->graphExec[seg], g, 0));
   }
-  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
-  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[0], s));
-  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
-  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[1], s));
-  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
-  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[2], s));
+  for (int seg = 0; seg < 3; seg++) {
+    IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[seg], s));
+    if (hasSeg[seg]) IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[seg], s));
+  }
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
   ctx->launches_per_assembly = (int)ctx->h_devpatches.size() + (int)ctx->passes.size();
   return IFEMGPU_OK;
