@@ -132,6 +132,20 @@ __global__ void k_basis_tables(DevPatch P)
     }
     t -= cnt;
   }
+  // boundary tables: the first and last span evaluated at the patch ends
+  if (t < 2 * P.dim) {
+    const int d = t >> 1, side = t & 1;
+    const double* U = P.knots[d];
+    const int k = side ? P.n[d] - 1 : P.p[d];
+    const double u = side ? U[P.n[d]] : U[P.p[d]];
+    double N[kMaxDeg + 1], D[kMaxDeg + 1];
+    bsplineDers(U, P.p[d], k, u, N, D);
+    double* tb = P.tabB[d] + side * 2 * (P.p[d] + 1);
+    for (int r = 0; r <= P.p[d]; r++) {
+      tb[r] = N[r];
+      tb[P.p[d] + 1 + r] = D[r];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -470,48 +484,55 @@ k_face_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ items
     double Nd[3][kMaxDeg + 1], Dd[3][kMaxDeg + 1];
     double wt = 0.25;
     for (int d = 0; d < 3; d++) {
-      const double* U = P.knots[d];
-      const int k = P.p[d] + ee[d];
-      double u;
-      if (d == nd0) {
-        u = faceDir < 0 ? U[P.p[d]] : U[P.n[d]];
-      } else {
-        const double u0 = U[k], u1 = U[k + 1];
-        u = 0.5 * ((u1 - u0) * P.fx[d][gi[d]] + u1 + u0);
-        wt *= (u1 - u0) * P.fw[d][gi[d]];
+      const int p1 = P.p[d] + 1;
+      if (d == nd0) {  // normal direction: the boundary table of this side
+        const double* tb = P.tabB[d] + (faceDir < 0 ? 0 : 2 * p1);
+        for (int r = 0; r < p1; r++) {
+          Nd[d][r] = tb[r];
+          Dd[d][r] = tb[p1 + r];
+        }
+        continue;
       }
-      bsplineDers(U, P.p[d], k, u, Nd[d], Dd[d]);
+      wt *= P.span[d][ee[d]] * P.fw[d][gi[d]];
+      if (P.faceTables) {  // face rule = volume rule: the volume tables apply
+        const size_t o = ((size_t)ee[d] * P.ng[d] + gi[d]) * p1;
+        for (int r = 0; r < p1; r++) {
+          Nd[d][r] = P.tabN[d][o + r];
+          Dd[d][r] = P.tabD[d][o + r];
+        }
+      } else {
+        const double* U = P.knots[d];
+        const int k = P.p[d] + ee[d];
+        const double u0 = U[k], u1 = U[k + 1];
+        bsplineDers(U, P.p[d], k, 0.5 * ((u1 - u0) * P.fx[d][gi[d]] + u1 + u0), Nd[d], Dd[d]);
+      }
     }
+    // homogeneous sums S[c][0] = sum_a wN_a X_a,c, S[c][1+d] = sum_a w dN_a/du_d X_a,c
+    // (X_a,3 = 1 gives W and its derivatives); one reciprocal per point
+    double Sm[4][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
     double* Nr = Nf + q * nen;
-    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    double W = 0.0, Wd[3] = {0, 0, 0};
-    // pass 1: weight function and its derivatives
     for (int a = 0; a < nen; a++) {
       const int i = a % q1, j = (a / q1) % q2, k = a / (q1 * q2);
       const double w = Xn[a * 4 + 3];
-      const double N = Nd[0][i] * Nd[1][j] * Nd[2][k];
-      W += w * N;
-      Wd[0] += w * Dd[0][i] * Nd[1][j] * Nd[2][k];
-      Wd[1] += w * Nd[0][i] * Dd[1][j] * Nd[2][k];
-      Wd[2] += w * Nd[0][i] * Nd[1][j] * Dd[2][k];
+      const double wN = w * (Nd[0][i] * Nd[1][j] * Nd[2][k]);
+      const double w0 = w * (Dd[0][i] * Nd[1][j] * Nd[2][k]);
+      const double w1 = w * (Nd[0][i] * Dd[1][j] * Nd[2][k]);
+      const double w2 = w * (Nd[0][i] * Nd[1][j] * Dd[2][k]);
+      Nr[a] = wN;
+      for (int c = 0; c < 4; c++) {
+        const double x = c < 3 ? Xn[a * 4 + c] : 1.0;
+        Sm[c][0] += wN * x;
+        Sm[c][1] += w0 * x;
+        Sm[c][2] += w1 * x;
+        Sm[c][3] += w2 * x;
+      }
     }
-    for (int a = 0; a < nen; a++) {
-      const int i = a % q1, j = (a / q1) % q2, k = a / (q1 * q2);
-      const double w = P.rational ? Xn[a * 4 + 3] : 1.0;
-      const double N = Nd[0][i] * Nd[1][j] * Nd[2][k];
-      double d[3] = {Dd[0][i] * Nd[1][j] * Nd[2][k], Nd[0][i] * Dd[1][j] * Nd[2][k],
-                     Nd[0][i] * Nd[1][j] * Dd[2][k]};
-      double R = N;
-      if (P.rational) {
-        R = w * N / W;
-        for (int c = 0; c < 3; c++) d[c] = (w * d[c] - R * Wd[c]) / W;
-      }
-      Nr[a] = R;
-      for (int c = 0; c < 3; c++) {
-        J[c * 3 + 0] += Xn[a * 4 + 0] * d[c];
-        J[c * 3 + 1] += Xn[a * 4 + 1] * d[c];
-        J[c * 3 + 2] += Xn[a * 4 + 2] * d[c];
-      }
+    const double iW = 1.0 / Sm[3][0];
+    for (int a = 0; a < nen; a++) Nr[a] *= iW;
+    double J[9];  // J[d*3 + c] = dX_c/du_d
+    for (int c = 0; c < 3; c++) {
+      const double Xc = Sm[c][0] * iW;
+      for (int d = 0; d < 3; d++) J[d * 3 + c] = (Sm[c][1 + d] - Xc * Sm[3][1 + d]) * iW;
     }
     const double* ta = J + 3 * (t1 - 1);
     const double* tb = J + 3 * (t2 - 1);
@@ -582,6 +603,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     D.nu = pc.mat.nu;
     for (int c = 0; c < 3; c++) D.body[c] = pc.mat.body[c];
     D.nq = 1;
+    D.faceTables = 1;
     for (int d = 0; d < 3; d++) {
       D.p[d] = pc.p[d];
       D.n[d] = pc.n[d];
@@ -601,12 +623,15 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
         IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabN[d], sizeof(double) * tab));
         IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabD[d], sizeof(double) * tab));
         IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_span[d], sizeof(double) * pc.nel[d]));
+        IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabB[d], sizeof(double) * 4 * (pc.p[d] + 1)));
+        if (ngf != ng) D.faceTables = 0;
       }
       D.nq *= D.ng[d];
       D.knots[d] = pc.d_knots[d];
       D.tabN[d] = pc.d_tabN[d];
       D.tabD[d] = pc.d_tabD[d];
       D.span[d] = pc.d_span[d];
+      D.tabB[d] = pc.d_tabB[d];
     }
     IFEMGPU_TRY(upload(ctx, &pc.d_ctrl, pc.ctrl4.data(), pc.ctrl4.size()));
     if (!pc.lineOff.empty()) {
@@ -755,6 +780,7 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
       const DevPatch& D = ctx->h_devpatches[pi];
       int work = 0;
       for (int d = 0; d < D.dim; d++) work += D.nel[d] * D.ng[d];
+      work += 2 * D.dim;  // boundary tables
       k_basis_tables<<<(work + 127) / 128, 128, 0, s>>>(D);
     }
     IFEMGPU_CUDA(ctx, cudaGetLastError());

@@ -45,8 +45,8 @@ void freeDevice(ifemgpu_ctx* ctx)
     f(pc.d_logk); pc.d_logk = nullptr;
     f(pc.d_noise); pc.d_noise = nullptr;
     for (int d = 0; d < 3; d++) {
-      f(pc.d_knots[d]); f(pc.d_tabN[d]); f(pc.d_tabD[d]); f(pc.d_span[d]);
-      pc.d_knots[d] = pc.d_tabN[d] = pc.d_tabD[d] = pc.d_span[d] = nullptr;
+      f(pc.d_knots[d]); f(pc.d_tabN[d]); f(pc.d_tabD[d]); f(pc.d_span[d]); f(pc.d_tabB[d]);
+      pc.d_knots[d] = pc.d_tabN[d] = pc.d_tabD[d] = pc.d_span[d] = pc.d_tabB[d] = nullptr;
     }
   }
   f(ctx->d_madof); f(ctx->d_meqn); f(ctx->d_c0); f(ctx->d_colptr);

@@ -40,6 +40,9 @@ struct DevPatch {
   double* tabN[3];
   double* tabD[3];
   double* span[3];
+  // boundary tables per direction: [side 0 = start, 1 = end][N, dN/du][p+1]
+  double* tabB[3];
+  int faceTables;     // face Gauss rule equals the volume rule in every direction
   // Position table of the compressed-column pattern for patches whose
   // couplings are the index box of half-width p (nullptr otherwise): for
   // node b and the box line (dz, dy), lineOff[b*(2p+1)^2 + (dz+p)(2p+1) +
@@ -94,6 +97,7 @@ struct HostPatch {
   double* d_tabN[3] = {nullptr, nullptr, nullptr};
   double* d_tabD[3] = {nullptr, nullptr, nullptr};
   double* d_span[3] = {nullptr, nullptr, nullptr};
+  double* d_tabB[3] = {nullptr, nullptr, nullptr};
   std::vector<int> lineOff;       // see DevPatch::lineOff (empty: no box coupling)
   int* d_lineOff = nullptr;
 };

@@ -145,6 +145,21 @@ __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float* v)
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Exact float -> double widening on the integer pipe (GB300's FP64 units run
+// at a small fraction of the FP32 rate, and the conversion instruction uses
+// them).  Normal numbers and zero are exact; subnormal floats (< 1.2e-38)
+// flush to a signed zero; infinities and NaN keep their class.
+__device__ __forceinline__ double widenF32(float f)
+{
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  const uint64_t sign = static_cast<uint64_t>(b & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double(static_cast<long long>(sign));
+  const uint64_t ed = e == 0xFFu ? 0x7FFull : static_cast<uint64_t>(e + 896u);
+  const uint64_t m = static_cast<uint64_t>(b & 0x7FFFFFu) << 29;
+  return __longlong_as_double(static_cast<long long>(sign | (ed << 52) | m));
+}
+
 // x = hi + lo with hi rounded to TF32 (10 explicit mantissa bits)
 __device__ __forceinline__ void splitTF32(float x, float& hi, float& lo)
 {

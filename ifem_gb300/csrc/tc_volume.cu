@@ -318,9 +318,11 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     __syncthreads();
     if (sm.fail) break;
 
-    // ---- 8. element matrix and scatter, node pair by node pair
+    // ---- 8. element matrix and scatter, node pair by node pair (FP32
+    //         arithmetic; the FP64 additions happen in the L2 reductions)
     const double lam = P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu));
     const double mu = P.E / (2.0 * (1.0 + P.nu));
+    const float lamf = (float)lam, muf = (float)mu;
     for (int pr = tid; pr < kNen * kNen; pr += blockDim.x) {
       const int a = pr % kNen, bn = pr / kNen;
       int firstCol = -1, firstRow = -1;
@@ -334,7 +336,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       for (int k = 0; k < 3; k++)
 #pragma unroll
         for (int l = 0; l < 3; l++) g[k][l] = G[(32 * k + a) * kGld + 32 * l + bn];
-      const double tr = (double)g[0][0] + (double)g[1][1] + (double)g[2][2];
+      const float trm = muf * (g[0][0] + g[1][1] + g[2][2]);
       int off;
       if (P.lineOff) {
         off = sm.lo[bn][(a / 3) % 3 + 3 * (a / 9)] + sm.Fa[a];
@@ -353,8 +355,8 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
         int rank = 0;
         for (int k = 0; k < 3; k++) {
           if (sm.eq[3 * a + k] <= 0) continue;
-          const double ke = lam * g[k][l] + mu * g[l][k] + (k == l ? mu * tr : 0.0);
-          redAdd(col + rank, ke);
+          const float ke = fmaf(lamf, g[k][l], fmaf(muf, g[l][k], k == l ? trm : 0.f));
+          redAdd(col + rank, widenF32(ke));
           rank++;
         }
       }
@@ -365,7 +367,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       const int a = tid / 3, k = tid % 3;
       const int r = sm.eq[tid];
       if (r > 0) {
-        double acc = fe;
+        double acc = widenF32(fe);
         if (S.c0) {
           for (int j = 0; j < kNen * 3; j++) {
             const int ce = sm.eq[j];
