@@ -127,6 +127,11 @@ __global__ void k_basis_tables(DevPatch P)
       double* tn = P.tabN[d] + (size_t)t * (P.p[d] + 1);
       double* td = P.tabD[d] + (size_t)t * (P.p[d] + 1);
       for (int r = 0; r <= P.p[d]; r++) { tn[r] = N[r]; td[r] = D[r]; }
+      if (P.tabNf[d]) {
+        float* fn = P.tabNf[d] + (size_t)t * (P.p[d] + 1);
+        float* fd = P.tabDf[d] + (size_t)t * (P.p[d] + 1);
+        for (int r = 0; r <= P.p[d]; r++) { fn[r] = (float)N[r]; fd[r] = (float)D[r]; }
+      }
       if (g == 0) P.span[d][e] = u1 - u0;
       return;
     }
@@ -624,6 +629,8 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
         IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabD[d], sizeof(double) * tab));
         IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_span[d], sizeof(double) * pc.nel[d]));
         IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabB[d], sizeof(double) * 4 * (pc.p[d] + 1)));
+        IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabNf[d], sizeof(float) * tab));
+        IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabDf[d], sizeof(float) * tab));
         if (ngf != ng) D.faceTables = 0;
       }
       D.nq *= D.ng[d];
@@ -632,6 +639,8 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
       D.tabD[d] = pc.d_tabD[d];
       D.span[d] = pc.d_span[d];
       D.tabB[d] = pc.d_tabB[d];
+      D.tabNf[d] = pc.d_tabNf[d];
+      D.tabDf[d] = pc.d_tabDf[d];
     }
     IFEMGPU_TRY(upload(ctx, &pc.d_ctrl, pc.ctrl4.data(), pc.ctrl4.size()));
     if (!pc.lineOff.empty()) {
@@ -652,27 +661,53 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     const int nc = (pc.p[0] + 1) * (pc.p[1] + 1) * (pc.dim == 3 ? pc.p[2] + 1 : 1);
     maxColours = std::max(maxColours, nc);
   }
-  // volume items grouped by colour: colour = (e1 mod q1) + q1 (e2 mod q2) + ...
+  // Patches on the tensor-core path: all their elements in one colour-major
+  // pass (one persistent launch ordered by per-element done flags); the
+  // other patches: one FP64 launch per colour.
+  // colour = (e1 mod q1) + q1 (e2 mod q2) + q1 q2 (e3 mod q3)
+  std::vector<char> onTc(np, 0);
+  int nflags = 0;
+  for (int pi = 0; pi < np; pi++) {
+    DevPatch& D = ctx->h_devpatches[pi];
+    onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) &&
+               D.lineOff != nullptr;
+    D.flagBase = nflags;
+    if (onTc[pi]) nflags += ctx->patches[pi].nelAll;
+  }
+  auto colourItems = [&](int pi, int c, std::vector<Item>& out) {
+    const HostPatch& pc = ctx->patches[pi];
+    const int q1 = pc.p[0] + 1, q2 = pc.p[1] + 1, q3 = pc.dim == 3 ? pc.p[2] + 1 : 1;
+    if (c >= q1 * q2 * q3) return;
+    const int c1 = c % q1, c2 = (c / q1) % q2, c3 = c / (q1 * q2);
+    for (int e3 = c3; e3 < pc.nel[2]; e3 += q3)
+      for (int e2 = c2; e2 < pc.nel[1]; e2 += q2)
+        for (int e1 = c1; e1 < pc.nel[0]; e1 += q1) {
+          const int e = (e3 * pc.nel[1] + e2) * pc.nel[0] + e1;
+          if (pc.active[e]) out.push_back({pi, e, 0, 0});
+        }
+  };
+  if (nflags > 0) {
+    Pass pass{(int)vol.size(), 0, 0, 81, tcVolumeSmem(), true};
+    for (int c = 0; c < maxColours; c++)
+      for (int pi = 0; pi < np; pi++)
+        if (onTc[pi]) colourItems(pi, c, vol);
+    pass.count = (int)vol.size() - pass.first;
+    ctx->passes.push_back(pass);
+  }
   for (int c = 0; c < maxColours; c++) {
-    Pass pass{(int)vol.size(), 0, 0, 0, 0, ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32};
+    Pass pass{(int)vol.size(), 0, 0, 0, 0, false};
     for (int pi = 0; pi < np; pi++) {
+      if (onTc[pi]) continue;
       const HostPatch& pc = ctx->patches[pi];
-      const int q1 = pc.p[0] + 1, q2 = pc.p[1] + 1, q3 = pc.dim == 3 ? pc.p[2] + 1 : 1;
-      if (c >= q1 * q2 * q3) continue;
-      const int c1 = c % q1, c2 = (c / q1) % q2, c3 = c / (q1 * q2);
-      for (int e3 = c3; e3 < pc.nel[2]; e3 += q3)
-        for (int e2 = c2; e2 < pc.nel[1]; e2 += q2)
-          for (int e1 = c1; e1 < pc.nel[0]; e1 += q1) {
-            int e = (e3 * pc.nel[1] + e2) * pc.nel[0] + e1;
-            if (pc.active[e]) vol.push_back({pi, e, 0, 0});
-          }
+      colourItems(pi, c, vol);
       pass.maxNd = std::max(pass.maxNd, pc.nen() * pc.npv);
       pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi]));
-      pass.tc = pass.tc && tcSupports(ctx->h_devpatches[pi]);
     }
     pass.count = (int)vol.size() - pass.first;
     if (pass.count) ctx->passes.push_back(pass);
   }
+  ctx->nflags = nflags;
+  if (nflags) IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_flags, sizeof(int) * nflags));
   // face items: per Neumann condition, face elements coloured in 2D
   const int nVol = (int)vol.size();
   std::vector<Pass> facePasses;
@@ -776,6 +811,8 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
     IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_K, 0, sizeof(double) * ctx->nnz, s));
     IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_b, 0, sizeof(double) * ctx->neq, s));
     IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4, s));
+    if (ctx->nflags)
+      IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * ctx->nflags, s));
     for (int pi = 0; pi < (int)ctx->h_devpatches.size(); pi++) {
       const DevPatch& D = ctx->h_devpatches[pi];
       int work = 0;
@@ -791,7 +828,7 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
   for (const Pass& p : ctx->passes) {
     if ((p.face != 0) != (seg == 2)) continue;
     if (p.tc)
-      IFEMGPU_TRY(tcLaunchVolume(ctx, p, std::min(p.count, 3 * ctx->numSMs)));
+      IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
     else if (!p.face)
       k_volume_fp64<<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
     else

@@ -46,13 +46,17 @@ void freeDevice(ifemgpu_ctx* ctx)
     f(pc.d_noise); pc.d_noise = nullptr;
     for (int d = 0; d < 3; d++) {
       f(pc.d_knots[d]); f(pc.d_tabN[d]); f(pc.d_tabD[d]); f(pc.d_span[d]); f(pc.d_tabB[d]);
+      f(pc.d_tabNf[d]); f(pc.d_tabDf[d]);
       pc.d_knots[d] = pc.d_tabN[d] = pc.d_tabD[d] = pc.d_span[d] = pc.d_tabB[d] = nullptr;
+      pc.d_tabNf[d] = pc.d_tabDf[d] = nullptr;
     }
   }
   f(ctx->d_madof); f(ctx->d_meqn); f(ctx->d_c0); f(ctx->d_colptr);
   f(ctx->d_rowidx); f(ctx->d_K); f(ctx->d_b); f(ctx->d_patches);
   f(ctx->d_items); f(ctx->d_neumann); f(ctx->d_counters); f(ctx->d_freeBefore);
+  f(ctx->d_flags);
   ctx->d_freeBefore = nullptr;
+  ctx->d_flags = nullptr;
   for (int g = 0; g < 3; g++) {
     if (ctx->graphExec[g]) cudaGraphExecDestroy(ctx->graphExec[g]);
     if (ctx->graph[g]) cudaGraphDestroy(ctx->graph[g]);
@@ -565,7 +569,12 @@ ifemgpu_status ifemgpu_assemble(ifemgpu_ctx* ctx, int sync)
   ifemgpu_status st = launchAssembly(ctx);
   if (st != IFEMGPU_OK) return st;
   ctx->assembled = true;
-  if (sync) IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (sync) {
+    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    unsigned long long c[4] = {0, 0, 0, 0};
+    IFEMGPU_CUDA(ctx, cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+    if (c[2]) return setError(ctx, IFEMGPU_DEVICE_TIMEOUT, "a bounded device wait gave up");
+  }
   return IFEMGPU_OK;
 }
 

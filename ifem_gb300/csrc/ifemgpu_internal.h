@@ -42,6 +42,10 @@ struct DevPatch {
   double* span[3];
   // boundary tables per direction: [side 0 = start, 1 = end][N, dN/du][p+1]
   double* tabB[3];
+  // FP32 copies of tabN/tabD for the tensor-core kernel
+  float* tabNf[3];
+  float* tabDf[3];
+  int flagBase;       // first slot of this patch's elements in the done-flag array
   int faceTables;     // face Gauss rule equals the volume rule in every direction
   // Position table of the compressed-column pattern for patches whose
   // couplings are the index box of half-width p (nullptr otherwise): for
@@ -98,6 +102,8 @@ struct HostPatch {
   double* d_tabD[3] = {nullptr, nullptr, nullptr};
   double* d_span[3] = {nullptr, nullptr, nullptr};
   double* d_tabB[3] = {nullptr, nullptr, nullptr};
+  float* d_tabNf[3] = {nullptr, nullptr, nullptr};
+  float* d_tabDf[3] = {nullptr, nullptr, nullptr};
   std::vector<int> lineOff;       // see DevPatch::lineOff (empty: no box coupling)
   int* d_lineOff = nullptr;
 };
@@ -150,6 +156,8 @@ struct ifemgpu_ctx {
   double* d_neumann = nullptr;  // Neumann values, 3 per face condition
   std::vector<ifemgpu::Pass> passes;
   unsigned long long* d_counters = nullptr;  // [0] singular points
+  int* d_flags = nullptr;        // per-element done flags of the tensor-core pass
+  int nflags = 0;
   // statistics of the last assembly
   double last_total_ms = 0.0, last_volume_ms = 0.0;
   unsigned long long last_singular = 0;

@@ -4,19 +4,25 @@
 // with the linear-elasticity integrand, and the scatter of assemSparse
 // (src/LinAlg/SparseMatrix.C:614-688).
 //
-// Per element (one CTA of 128 threads processes the elements of a colour):
+// One persistent launch processes every element of the eligible patches.
+// Per element (one CTA of 128 threads, elements in colour-major order):
 //   1. rational basis and Jacobian at the 27 Gauss points (FP32 sums of the
 //      homogeneous control net; determinant and inverse in FP64);
-//   2. Gram matrix G = A^T B on the tensor cores, A[(a,k),q] = w_q dN_a/dx_k,
-//      B[(b,l),q] = dN_b/dx_l (rows m = 32k + a), in 3xTF32 split precision:
-//      G = Ahi Bhi + Ahi Blo + Alo Bhi, FP32 accumulation in tensor memory;
-//   3. Ke[(a,k),(b,l)] = lambda G[(a,k),(b,l)] + mu G[(a,l),(b,k)]
+//   2. operand tile T[(a,k), q] = sqrt|w_q| dN_a/dx_k (rows m = 32k + a), so
+//      that the Gram matrix G = sum_q w_q dN dN^T = s T^T T with the sign s of
+//      the weights.  Elements whose weights change sign (folded geometry) run
+//      one pass per sign, the negative one with the negate-A bit of the MMA;
+//   3. G on the tensor cores in 3xTF32 split precision,
+//      G = Thi^T Thi + Thi^T Tlo + Tlo^T Thi, FP32 accumulation in tensor memory;
+//   4. Ke[(a,k),(b,l)] = lambda G[(a,k),(b,l)] + mu G[(a,l),(b,k)]
 //                        + mu delta_kl sum_m G[(a,m),(b,m)]
-//      -- the B^T D B product of isotropic elasticity regrouped so that the
-//      tensor cores contract over Gauss points once;
-//   4. FP64 reductions of Ke into the compressed-column matrix in L2
-//      (red.global.add.f64).  Elements of one colour share no node, so no
-//      address is reduced twice within a launch and the sum order is fixed.
+//      -- B^T D B of isotropic elasticity regrouped so the tensor cores
+//      contract over the Gauss points once;
+//   5. FP64 reductions of Ke into the compressed-column matrix in L2
+//      (red.global.add.f64).  An element reduces only after every
+//      lower-colour neighbour (sharing a node) has published its done flag,
+//      and elements of one colour share no node: every matrix entry receives
+//      its contributions in colour order, so the sums are deterministic.
 #include <algorithm>
 #include <cstdio>
 
@@ -33,23 +39,18 @@ constexpr int kNen = 27;      // p = 2: 3x3x3 functions
 constexpr int kNq = 27;       // 3x3x3 Gauss points
 constexpr int kM = 128;       // MMA M (rows 32k + a, k < 3, a < 27)
 constexpr int kN = 96;        // MMA N (columns 32l + b)
-constexpr int kGld = 97;      // row stride of the staged Gram matrix (floats)
+constexpr int kGs = 81;       // row stride of the compact Gram matrix (conflict-free)
+constexpr uint32_t kFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wait
 
 struct TcSmem {
-  // operand tiles (K-major core-matrix layout); the staged Gram matrix
-  // G[96][97] aliases the first 37 KB once the MMAs have completed
-  float Ahi[kM * kK];
-  float Alo[kM * kK];
-  float Bhi[kN * kK];
-  float Blo[kN * kK];
-  float N[kNq][kNen];      // weighted basis wN, later the rational basis R
-  float Du[kNq][kNen];     // weighted parametric derivatives w dN/du_d
+  float Thi[kM * kK];      // operand tile, K-major core-matrix layout
+  float Tlo[kM * kK];
+  float Gc[81 * kGs];      // G[(3a+k)][(3b+l)]; before the epilogue: per-point scratch
+  float N[kNq][kNen];      // weighted basis wN, then the rational basis R
+  float Du[kNq][kNen];     // weighted parametric derivatives, then dR/du_d
   float Dv[kNq][kNen];
   float Dw[kNq][kNen];
-  float P[kNq][4][4];      // homogeneous sums: [q][x,y,z,w][value, d/du, d/dv, d/dw]
-  float Jinv[kNq][9];      // column-major inverse Jacobian
-  float Wq[kNq][4];        // W and dW/du_d
-  float wq[kNq];           // detJ * dV * Gauss weights (0 at skipped points)
+  float wq[kNq];           // signed integration weight (0 at skipped points)
   float X[kNen][4];        // control points relative to the element's first, weight
   int eq[kNen * 3];
   int colStart[kNen * 3];  // colptr of the element's free columns
@@ -58,24 +59,36 @@ struct TcSmem {
   unsigned long long mbar;
   uint32_t tmemSlot;
   int fail;
+  int signs;               // bit 0: some w_q > 0, bit 1: some w_q < 0
 };
 
-__device__ inline int findRowTc(const int* __restrict__ colptr, const int* __restrict__ rowidx,
-                                int c, int r)
+// scratch views inside Gc (dead before the epilogue writes G)
+struct Scratch {
+  float* P;     // [27][4][4] homogeneous sums
+  float* Jinv;  // [27][9] column-major inverse Jacobian
+  float* Wq;    // [27][4] 1/W and dW/du_d
+};
+
+__device__ __forceinline__ Scratch scratch(TcSmem& sm)
 {
-  int lo = colptr[c], hi = colptr[c + 1] - 1;
-  while (lo <= hi) {
-    const int mid = (lo + hi) >> 1;
-    const int v = rowidx[mid];
-    if (v == r) return mid;
-    if (v < r) lo = mid + 1; else hi = mid - 1;
-  }
-  return -1;
+  return Scratch{sm.Gc, sm.Gc + 27 * 16, sm.Gc + 27 * 16 + 27 * 9};
 }
 
 __device__ __forceinline__ void redAdd(double* p, double v)
 {
   atomicAdd(p, v);  // result unused: compiles to an L2 reduction
+}
+
+__device__ __forceinline__ int loadAcquire(const int* p)
+{
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void storeRelease(int* p, int v)
+{
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
 
 }  // namespace
@@ -85,11 +98,11 @@ struct TcSys {
   const int* meqn;
   const int* F;
   const double* c0;
-  const int* colptr;
-  const int* rowidx;
   double* K;
   double* b;
-  unsigned long long* counters;  // [0] singular points, [1] pattern misses, [2] device timeouts
+  const int* colptr;
+  int* flags;
+  unsigned long long* counters;  // [0] singular points, [2] device timeouts
 };
 
 __global__ void __launch_bounds__(128)
@@ -100,19 +113,23 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mbar = smemAddr(&sm.mbar);
+  const Scratch sc = scratch(sm);
   if (tid == 0) {
     mbarInit(mbar, 1);
     sm.fail = 0;
+  }
+  // the padding of the operand tile (rows >= 96, rows with a >= 27, q >= 27)
+  // is never written again
+  for (int i = tid; i < kM * kK; i += blockDim.x) {
+    sm.Thi[i] = 0.f;
+    sm.Tlo[i] = 0.f;
   }
   if (warp == 0) tmemAlloc(&sm.tmemSlot, 128);
   tcFenceBefore();
   __syncthreads();
   tcFenceAfter();
   const uint32_t tmem = sm.tmemSlot;
-  constexpr uint32_t idesc = instrDescTF32(kM, kN);
-  const uint32_t aHi = smemAddr(sm.Ahi), aLo = smemAddr(sm.Alo);
-  const uint32_t bHi = smemAddr(sm.Bhi), bLo = smemAddr(sm.Blo);
-  float* G = sm.Ahi;  // staged Gram matrix, [96][kGld]
+  const uint32_t tHi = smemAddr(sm.Thi), tLo = smemAddr(sm.Tlo);
   uint32_t phase = 0;
 
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
@@ -122,7 +139,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
     const int n0 = (e3 * P.n[1] + e2) * P.n[0] + e1;
 
-    // ---- 1. element nodes ------------------------------------------------
+    // ---- 1. element nodes, equation numbers, pattern positions -----------
     if (tid < kNen) {
       const int a = tid;
       const int node = n0 + ((a / 9) * P.n[1] + (a / 3) % 3) * P.n[0] + a % 3;
@@ -138,52 +155,34 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.eq[3 * a + 2] = S.meqn[d0 + 2];
       sm.Fa[a] = S.F[P.firstNode + node];
     }
-    if (P.lineOff) {
-      // line offsets of the 9 row lines of the element in each column node
-      for (int idx = tid; idx < kNen * 9; idx += blockDim.x) {
-        const int bn = idx / 9, la = idx % 9;
-        const int nodeb = n0 + ((bn / 9) * P.n[1] + (bn / 3) % 3) * P.n[0] + bn % 3;
-        const int dy = la % 3 - (bn / 3) % 3, dz = la / 3 - bn / 9;
-        sm.lo[bn][la] = P.lineOff[(size_t)nodeb * 25 + (dz + 2) * 5 + dy + 2];
-      }
+    if (tid == 0) sm.signs = 0;
+    for (int idx = tid; idx < kNen * 9; idx += blockDim.x) {
+      const int bn = idx / 9, la = idx % 9;
+      const int nodeb = n0 + ((bn / 9) * P.n[1] + (bn / 3) % 3) * P.n[0] + bn % 3;
+      const int dy = la % 3 - (bn / 3) % 3, dz = la / 3 - bn / 9;
+      sm.lo[bn][la] = P.lineOff[(size_t)nodeb * 25 + (dz + 2) * 5 + dy + 2];
     }
-    // zero padding of the operand tiles (rows a >= 27 per component block,
-    // rows >= 96 of A, columns q >= 27)
-    for (int idx = tid; idx < kM * kK; idx += blockDim.x) {
-      const int r = idx >> 5, k = idx & 31;
-      if ((r & 31) >= kNen || r >= 96 || k >= kNq) {
-        const int o = kmaj(r, k);
-        sm.Ahi[o] = 0.f;
-        sm.Alo[o] = 0.f;
-        if (r < kN) {
-          sm.Bhi[o] = 0.f;
-          sm.Blo[o] = 0.f;
-        }
-      }
-    }
-    __syncthreads();
-
-    if (tid < kNen * 3) sm.colStart[tid] = sm.eq[tid] > 0 ? S.colptr[sm.eq[tid] - 1] : 0;
-
     // ---- 2. weighted tensor-product basis at every (Gauss point, function)
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
       const int q = idx / kNen, a = idx % kNen;
       const int gi = q % 3, gj = (q / 3) % 3, gk = q / 9;
       const int i = a % 3, j = (a / 3) % 3, k = a / 9;
-      const double* t0 = P.tabN[0] + (e1 * 3 + gi) * 3;
-      const double* t1 = P.tabN[1] + (e2 * 3 + gj) * 3;
-      const double* t2 = P.tabN[2] + (e3 * 3 + gk) * 3;
-      const double* d0 = P.tabD[0] + (e1 * 3 + gi) * 3;
-      const double* d1 = P.tabD[1] + (e2 * 3 + gj) * 3;
-      const double* d2 = P.tabD[2] + (e3 * 3 + gk) * 3;
-      const float nx = (float)t0[i], ny = (float)t1[j], nz = (float)t2[k];
-      const float w = sm.X[a][3];
+      const float* t0 = P.tabNf[0] + (e1 * 3 + gi) * 3;
+      const float* t1 = P.tabNf[1] + (e2 * 3 + gj) * 3;
+      const float* t2 = P.tabNf[2] + (e3 * 3 + gk) * 3;
+      const float nx = t0[i], ny = t1[j], nz = t2[k];
+      const float dx = P.tabDf[0][(e1 * 3 + gi) * 3 + i];
+      const float dy = P.tabDf[1][(e2 * 3 + gj) * 3 + j];
+      const float dz = P.tabDf[2][(e3 * 3 + gk) * 3 + k];
+      const double* c = P.ctrl + (size_t)(n0 + (k * P.n[1] + j) * P.n[0] + i) * 4;
+      const float w = (float)c[3];
       sm.N[q][a] = w * nx * ny * nz;
-      sm.Du[q][a] = w * (float)d0[i] * ny * nz;
-      sm.Dv[q][a] = w * nx * (float)d1[j] * nz;
-      sm.Dw[q][a] = w * nx * ny * (float)d2[k];
+      sm.Du[q][a] = w * dx * ny * nz;
+      sm.Dv[q][a] = w * nx * dy * nz;
+      sm.Dw[q][a] = w * nx * ny * dz;
     }
     __syncthreads();
+    if (tid < kNen * 3) sm.colStart[tid] = sm.eq[tid] > 0 ? S.colptr[sm.eq[tid] - 1] : 0;
 
     // ---- 3. homogeneous sums per Gauss point: sum_a (wN)_a (X_a, 1) and derivatives
     if (tid < kNq * 4) {
@@ -197,23 +196,24 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
         s2 = fmaf(sm.Dv[q][a], x, s2);
         s3 = fmaf(sm.Dw[q][a], x, s3);
       }
-      sm.P[q][c][0] = s0;
-      sm.P[q][c][1] = s1;
-      sm.P[q][c][2] = s2;
-      sm.P[q][c][3] = s3;
+      float* Pq = sc.P + q * 16 + c * 4;
+      Pq[0] = s0;
+      Pq[1] = s1;
+      Pq[2] = s2;
+      Pq[3] = s3;
     }
     __syncthreads();
 
     // ---- 4. Jacobian, FP64 determinant and inverse, integration weight
     if (tid < kNq) {
       const int q = tid;
-      const float W = sm.P[q][3][0];
-      const float iW = 1.f / W;
+      const float* Pq = sc.P + q * 16;
+      const float iW = 1.f / Pq[12];
       double J[9];  // column-major: J[d*3 + r] = dX_r/du_d
       for (int r = 0; r < 3; r++) {
-        const float Xr = sm.P[q][r][0] * iW;
+        const float Xr = Pq[r * 4] * iW;
         for (int d = 0; d < 3; d++)
-          J[d * 3 + r] = (double)((sm.P[q][r][1 + d] - Xr * sm.P[q][3][1 + d]) * iW);
+          J[d * 3 + r] = (double)((Pq[r * 4 + 1 + d] - Xr * Pq[12 + 1 + d]) * iW);
       }
       const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[3] * (J[1] * J[8] - J[2] * J[7]) +
                          J[6] * (J[1] * J[5] - J[2] * J[4]);
@@ -232,127 +232,159 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
         B[8] = (float)((J[0] * J[4] - J[1] * J[3]) * id);
         const double dV = 0.125 * P.span[0][e1] * P.span[1][e2] * P.span[2][e3];
         w = (float)(det * dV * P.gw[0][q % 3] * P.gw[1][(q / 3) % 3] * P.gw[2][q / 9]);
+        atomicOr(&sm.signs, w > 0.f ? 1 : 2);
       } else {
         atomicAdd(S.counters, 1ull);
       }
       sm.wq[q] = w;
-      for (int c = 0; c < 9; c++) sm.Jinv[q][c] = B[c];
-      sm.Wq[q][0] = iW;
-      sm.Wq[q][1] = sm.P[q][3][1];
-      sm.Wq[q][2] = sm.P[q][3][2];
-      sm.Wq[q][3] = sm.P[q][3][3];
+      for (int c = 0; c < 9; c++) sc.Jinv[q * 9 + c] = B[c];
+      sc.Wq[q * 4 + 0] = iW;
+      sc.Wq[q * 4 + 1] = Pq[13];
+      sc.Wq[q * 4 + 2] = Pq[14];
+      sc.Wq[q * 4 + 3] = Pq[15];
     }
     __syncthreads();
 
-    // ---- 5. dN/dX into the split-TF32 operand tiles
+    // ---- 5. rational basis R and dR/du in place
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
       const int q = idx / kNen, a = idx % kNen;
-      const float iW = sm.Wq[q][0];
-      const float R = sm.N[q][a] * iW;
-      const float ru = (sm.Du[q][a] - R * sm.Wq[q][1]) * iW;
-      const float rv = (sm.Dv[q][a] - R * sm.Wq[q][2]) * iW;
-      const float rw = (sm.Dw[q][a] - R * sm.Wq[q][3]) * iW;
-      const float* B = sm.Jinv[q];
-      const float w = sm.wq[q];
-      const float g[3] = {ru * B[0] + rv * B[1] + rw * B[2], ru * B[3] + rv * B[4] + rw * B[5],
-                          ru * B[6] + rv * B[7] + rw * B[8]};
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const int o = kmaj(32 * c + a, q);
-        float hi, lo;
-        splitTF32(g[c], hi, lo);
-        sm.Bhi[o] = hi;
-        sm.Blo[o] = lo;
-        splitTF32(w * g[c], hi, lo);
-        sm.Ahi[o] = hi;
-        sm.Alo[o] = lo;
-      }
+      const float* Wq = sc.Wq + q * 4;
+      const float R = sm.N[q][a] * Wq[0];
+      sm.Du[q][a] = (sm.Du[q][a] - R * Wq[1]) * Wq[0];
+      sm.Dv[q][a] = (sm.Dv[q][a] - R * Wq[2]) * Wq[0];
+      sm.Dw[q][a] = (sm.Dw[q][a] - R * Wq[3]) * Wq[0];
       sm.N[q][a] = R;
     }
-    fenceProxyAsync();
     __syncthreads();
 
-    // ---- 6. tensor cores: G = Ahi Bhi + Ahi Blo + Alo Bhi over 4 K-steps
-    if (tid == 0) {
-      tcFenceAfter();
-      for (int s = 0; s < kK / 8; s++) {
-        const uint32_t off = s * 256;
-        mmaTF32(tmem, smemDesc(aHi + off), smemDesc(bHi + off), idesc, s > 0);
-        mmaTF32(tmem, smemDesc(aHi + off), smemDesc(bLo + off), idesc, 1);
-        mmaTF32(tmem, smemDesc(aLo + off), smemDesc(bHi + off), idesc, 1);
+    // ---- 6. operand tile and tensor-core Gram matrix, one pass per weight sign
+    const int signs = sm.signs;
+    bool first = true, ok = true;
+    for (int pass = 0; pass < 2 && ok; pass++) {
+      const float s = pass == 0 ? 1.f : -1.f;
+      if (!(signs & (1 << pass))) continue;
+      // rows r = 32k + a (k < 3, a < 27), 4 consecutive Gauss points per chunk
+      for (int ch = tid; ch < 12 * 7 * 8; ch += blockDim.x) {
+        const int r = (ch / 56) * 8 + (ch & 7), q0 = ((ch >> 3) % 7) * 4;
+        const int a = r & 31, k = r >> 5;
+        if (a >= kNen) continue;
+        float hi[4], lo[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int q = q0 + j;
+          float v = 0.f;
+          if (q < kNq) {
+            const float ws = s * sm.wq[q];
+            if (ws > 0.f) {
+              const float* B = sc.Jinv + q * 9 + k * 3;
+              v = sqrtf(ws) * (sm.Du[q][a] * B[0] + sm.Dv[q][a] * B[1] + sm.Dw[q][a] * B[2]);
+            }
+          }
+          splitTF32(v, hi[j], lo[j]);
+        }
+        const int o = kmaj(r, q0);
+        *reinterpret_cast<float4*>(sm.Thi + o) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<float4*>(sm.Tlo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
       }
-      mmaCommit(mbar);
+      fenceProxyAsync();
+      __syncthreads();
+      if (tid == 0) {
+        tcFenceAfter();
+        const uint32_t idesc = instrDescTF32(kM, kN) | (s < 0.f ? (1u << 13) : 0u);
+        for (int st = 0; st < kK / 8; st++) {
+          const uint32_t off = st * 256;
+          mmaTF32(tmem, smemDesc(tHi + off), smemDesc(tHi + off), idesc, first ? 0u : 1u);
+          mmaTF32(tmem, smemDesc(tHi + off), smemDesc(tLo + off), idesc, 1);
+          mmaTF32(tmem, smemDesc(tLo + off), smemDesc(tHi + off), idesc, 1);
+          first = false;
+        }
+        mmaCommit(mbar);
+      }
+      first = false;
+      ok = mbarWait(mbar, phase);
+      phase ^= 1u;
+      tcFenceAfter();
+    }
+    if (!ok && tid == 0) {
+      atomicAdd(S.counters + 2, 1ull);
+      sm.fail = 1;
     }
 
-    // element load vector (body force), overlapping the MMAs
+    // element load vector (body force)
     float fe = 0.f;
     if (tid < kNen * 3) {
       const int a = tid / 3, k = tid % 3;
-      const double bk = P.body[k];
-      if (bk != 0.0) {
-        float s = 0.f;
-        for (int q = 0; q < kNq; q++) s = fmaf(sm.N[q][a], sm.wq[q], s);
-        fe = (float)bk * s;
+      const float bk = (float)P.body[k];
+      if (bk != 0.f) {
+        float acc = 0.f;
+        for (int q = 0; q < kNq; q++) acc = fmaf(sm.N[q][a], sm.wq[q], acc);
+        fe = bk * acc;
       }
     }
 
-    // ---- 7. wait for the MMAs (bounded), stage G in shared memory
-    const bool ok = mbarWait(mbar, phase);
-    phase ^= 1u;
-    if (!ok) {
-      if (tid == 0) {
-        atomicAdd(S.counters + 2, 1ull);
-        sm.fail = 1;
-      }
-    }
-    tcFenceAfter();
-    if (ok && warp < 3) {
+    // ---- 7. tensor memory -> compact Gram matrix in shared memory
+    if (ok && warp < 3 && signs) {
       float v[16];
       for (int c16 = 0; c16 < kN / 16; c16++) {
         tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
+        if (lane < kNen) {
 #pragma unroll
-        for (int i = 0; i < 16; i++) G[(32 * warp + lane) * kGld + 16 * c16 + i] = v[i];
+          for (int i = 0; i < 16; i++) {
+            const int n = 16 * c16 + i, l = n >> 5, bcol = n & 31;
+            if (bcol < kNen) sm.Gc[(3 * lane + warp) * kGs + 3 * bcol + l] = v[i];
+          }
+        }
       }
+    } else if (!signs) {
+      for (int i = tid; i < 81 * kGs; i += blockDim.x) sm.Gc[i] = 0.f;
     }
     tcFenceBefore();
     __syncthreads();
     if (sm.fail) break;
 
-    // ---- 8. element matrix and scatter, node pair by node pair (FP32
+    // ---- 8. wait for the lower-colour neighbours (they share nodes)
+    if (tid < 124) {
+      const int t = tid < 62 ? tid : tid + 1;  // skip the element itself
+      const int dx = t % 5 - 2, dy = (t / 5) % 5 - 2, dz = t / 25 - 2;
+      const int f1 = e1 + dx, f2 = e2 + dy, f3 = e3 + dz;
+      if (f1 >= 0 && f1 < P.nel[0] && f2 >= 0 && f2 < P.nel[1] && f3 >= 0 && f3 < P.nel[2]) {
+        const int myc = e1 % 3 + 3 * (e2 % 3) + 9 * (e3 % 3);
+        const int nc = f1 % 3 + 3 * (f2 % 3) + 9 * (f3 % 3);
+        if (nc < myc) {
+          const int* flag = S.flags + P.flagBase + (f3 * P.nel[1] + f2) * P.nel[0] + f1;
+          uint32_t spin = 0;
+          while (loadAcquire(flag) == 0) {
+            if (++spin > kFlagSpin) {
+              atomicAdd(S.counters + 2, 1ull);
+              break;
+            }
+            __nanosleep(64);
+          }
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- 9. element matrix and scatter, node pair by node pair (FP32
     //         arithmetic; the FP64 additions happen in the L2 reductions)
-    const double lam = P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu));
-    const double mu = P.E / (2.0 * (1.0 + P.nu));
-    const float lamf = (float)lam, muf = (float)mu;
+    const float lamf = (float)(P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu)));
+    const float muf = (float)(P.E / (2.0 * (1.0 + P.nu)));
     for (int pr = tid; pr < kNen * kNen; pr += blockDim.x) {
       const int a = pr % kNen, bn = pr / kNen;
-      int firstCol = -1, firstRow = -1;
-      for (int l = 0; l < 3 && firstCol < 0; l++)
-        if (sm.eq[3 * bn + l] > 0) firstCol = sm.eq[3 * bn + l] - 1;
-      for (int k = 0; k < 3 && firstRow < 0; k++)
-        if (sm.eq[3 * a + k] > 0) firstRow = sm.eq[3 * a + k] - 1;
-      if (firstCol < 0 || firstRow < 0) continue;
+      const float* ga = sm.Gc + 3 * a * kGs + 3 * bn;
       float g[3][3];
 #pragma unroll
       for (int k = 0; k < 3; k++)
 #pragma unroll
-        for (int l = 0; l < 3; l++) g[k][l] = G[(32 * k + a) * kGld + 32 * l + bn];
+        for (int l = 0; l < 3; l++) g[k][l] = ga[k * kGs + l];
       const float trm = muf * (g[0][0] + g[1][1] + g[2][2]);
-      int off;
-      if (P.lineOff) {
-        off = sm.lo[bn][(a / 3) % 3 + 3 * (a / 9)] + sm.Fa[a];
-      } else {
-        const int pos0 = findRowTc(S.colptr, S.rowidx, firstCol, firstRow);
-        if (pos0 < 0) {
-          atomicAdd(S.counters + 1, 1ull);
-          continue;
-        }
-        off = pos0 - S.colptr[firstCol];
-      }
+      const int off = sm.lo[bn][(a / 3) % 3 + 3 * (a / 9)] + sm.Fa[a];
+#pragma unroll
       for (int l = 0; l < 3; l++) {
-        const int ce = sm.eq[3 * bn + l];
-        if (ce <= 0) continue;
+        if (sm.eq[3 * bn + l] <= 0) continue;
         double* col = S.K + sm.colStart[3 * bn + l] + off;
         int rank = 0;
+#pragma unroll
         for (int k = 0; k < 3; k++) {
           if (sm.eq[3 * a + k] <= 0) continue;
           const float ke = fmaf(lamf, g[k][l], fmaf(muf, g[l][k], k == l ? trm : 0.f));
@@ -362,7 +394,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       }
     }
 
-    // ---- 9. right-hand side: load vector minus prescribed-DOF terms
+    // ---- 10. right-hand side: load vector minus prescribed-DOF terms
     if (tid < kNen * 3) {
       const int a = tid / 3, k = tid % 3;
       const int r = sm.eq[tid];
@@ -373,21 +405,25 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
             const int ce = sm.eq[j];
             if (ce >= 0) continue;
             const int bn = j / 3, l = j % 3;
-            double tr = 0.0;
-            for (int m = 0; m < 3; m++) tr += G[(32 * m + a) * kGld + 32 * m + bn];
-            const double ke = lam * G[(32 * k + a) * kGld + 32 * l + bn] +
-                              mu * G[(32 * l + a) * kGld + 32 * k + bn] + (k == l ? mu * tr : 0.0);
+            const float* ga = sm.Gc + 3 * a * kGs + 3 * bn;
+            const double tr = (double)ga[0] + ga[kGs + 1] + ga[2 * kGs + 2];
+            const double ke = lamf * (double)ga[k * kGs + l] + muf * (double)ga[l * kGs + k] +
+                              (k == l ? muf * tr : 0.0);
             acc -= S.c0[-ce - 1] * ke;
           }
         }
         if (acc != 0.0) redAdd(S.b + r - 1, acc);
       }
     }
+
+    // ---- 11. publish: all reductions of this element precede its flag
     __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      storeRelease(S.flags + P.flagBase + e, 1);
+    }
   }
 
-  // after a timed-out wait, give the MMAs in flight one more bounded wait
-  if (sm.fail) mbarWait(mbar, phase ^ 1u);
   // release tensor memory (all tcgen05 traffic of this CTA has completed)
   tcFenceBefore();
   __syncthreads();
@@ -455,7 +491,7 @@ k_selftest_gemm(const float* __restrict__ A, const float* __restrict__ B, float*
   if (warp == 0) tmemDealloc(tmem, 128);
 }
 
-size_t tcVolumeSmem() { return sizeof(TcSmem) + 1024; }
+size_t tcVolumeSmem() { return sizeof(TcSmem); }
 
 bool tcSupports(const DevPatch& P)
 {
@@ -471,15 +507,32 @@ ifemgpu_status tcPrepare(ifemgpu_ctx* ctx)
   return IFEMGPU_OK;
 }
 
-ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid)
+ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int)
 {
   TcSys S{ctx->d_madof, ctx->d_meqn, ctx->d_freeBefore, ctx->nceq ? ctx->d_c0 : nullptr,
-          ctx->d_colptr, ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters};
-  // dynamic shared memory is 1024-aligned by the __align__ of the buffer
-  k_volume_tc_elast_p2<<<grid, 128, tcVolumeSmem(), ctx->stream>>>(ctx->d_patches,
-                                                                   ctx->d_items + p.first,
-                                                                   p.count, S);
-  IFEMGPU_CUDA(ctx, cudaGetLastError());
+          ctx->d_K, ctx->d_b, ctx->d_colptr, ctx->d_flags, ctx->d_counters};
+  // every CTA must be resident (CTAs wait on each other's done flags):
+  // cooperative launch with the occupancy-limited grid
+  int perSM = 0;
+  IFEMGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_volume_tc_elast_p2, 128,
+                                                                  tcVolumeSmem()));
+  if (perSM < 1) return setError(ctx, IFEMGPU_UNSUPPORTED, "tensor-core kernel does not fit an SM");
+  const int grid = std::min(p.count, perSM * ctx->numSMs);
+  const DevPatch* patches = ctx->d_patches;
+  const Item* items = ctx->d_items + p.first;
+  int count = p.count;
+  void* args[] = {(void*)&patches, (void*)&items, (void*)&count, (void*)&S};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = tcVolumeSmem();
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  IFEMGPU_CUDA(ctx, cudaLaunchKernelExC(&cfg, (const void*)k_volume_tc_elast_p2, args));
   return IFEMGPU_OK;
 }
 
