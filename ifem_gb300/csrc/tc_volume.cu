@@ -56,6 +56,7 @@ struct TcSmem {
   int colStart[kNen * 3];  // colptr of the element's free columns
   int Fa[kNen];            // F(a): free DOFs before node a
   int lo[kNen][9];         // line offset of row node line (j + 3k) in column node b
+  uint32_t dec[kNq * kNen];  // (q, a) decode: q | a<<5 | gi<<10 | gj<<12 | gk<<14 | i<<16 | j<<18 | k<<20
   unsigned long long mbar;
   uint32_t tmemSlot;
   int fail;
@@ -67,11 +68,12 @@ struct Scratch {
   float* P;     // [27][4][4] homogeneous sums
   float* Jinv;  // [27][9] column-major inverse Jacobian
   float* Wq;    // [27][4] 1/W and dW/du_d
+  float* C;     // [27][9] sqrt(max(s w_q, 0)) * Jinv of the current sign pass
 };
 
 __device__ __forceinline__ Scratch scratch(TcSmem& sm)
 {
-  return Scratch{sm.Gc, sm.Gc + 27 * 16, sm.Gc + 27 * 16 + 27 * 9};
+  return Scratch{sm.Gc, sm.Gc + 27 * 16, sm.Gc + 27 * 16 + 27 * 9, sm.Gc + 27 * 16 + 27 * 13};
 }
 
 __device__ __forceinline__ void redAdd(double* p, double v)
@@ -124,6 +126,11 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     sm.Thi[i] = 0.f;
     sm.Tlo[i] = 0.f;
   }
+  for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
+    const uint32_t q = idx / kNen, a = idx % kNen;
+    sm.dec[idx] = q | (a << 5) | ((q % 3) << 10) | (((q / 3) % 3) << 12) | ((q / 9) << 14) |
+                  ((a % 3) << 16) | (((a / 3) % 3) << 18) | ((a / 9) << 20);
+  }
   if (warp == 0) tmemAlloc(&sm.tmemSlot, 128);
   tcFenceBefore();
   __syncthreads();
@@ -163,23 +170,25 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.lo[bn][la] = P.lineOff[(size_t)nodeb * 25 + (dz + 2) * 5 + dy + 2];
     }
     // ---- 2. weighted tensor-product basis at every (Gauss point, function)
+    const float* tn0 = P.tabNf[0] + e1 * 9;
+    const float* tn1 = P.tabNf[1] + e2 * 9;
+    const float* tn2 = P.tabNf[2] + e3 * 9;
+    const float* td0 = P.tabDf[0] + e1 * 9;
+    const float* td1 = P.tabDf[1] + e2 * 9;
+    const float* td2 = P.tabDf[2] + e3 * 9;
+    __syncthreads();  // X, eq visible
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
-      const int q = idx / kNen, a = idx % kNen;
-      const int gi = q % 3, gj = (q / 3) % 3, gk = q / 9;
-      const int i = a % 3, j = (a / 3) % 3, k = a / 9;
-      const float* t0 = P.tabNf[0] + (e1 * 3 + gi) * 3;
-      const float* t1 = P.tabNf[1] + (e2 * 3 + gj) * 3;
-      const float* t2 = P.tabNf[2] + (e3 * 3 + gk) * 3;
-      const float nx = t0[i], ny = t1[j], nz = t2[k];
-      const float dx = P.tabDf[0][(e1 * 3 + gi) * 3 + i];
-      const float dy = P.tabDf[1][(e2 * 3 + gj) * 3 + j];
-      const float dz = P.tabDf[2][(e3 * 3 + gk) * 3 + k];
-      const double* c = P.ctrl + (size_t)(n0 + (k * P.n[1] + j) * P.n[0] + i) * 4;
-      const float w = (float)c[3];
+      const uint32_t d = sm.dec[idx];
+      const int q = d & 31, a = (d >> 5) & 31;
+      const int g0 = ((d >> 10) & 3) * 3 + ((d >> 16) & 3);  // gi*3 + i
+      const int g1 = ((d >> 12) & 3) * 3 + ((d >> 18) & 3);
+      const int g2 = ((d >> 14) & 3) * 3 + ((d >> 20) & 3);
+      const float nx = tn0[g0], ny = tn1[g1], nz = tn2[g2];
+      const float w = sm.X[a][3];
       sm.N[q][a] = w * nx * ny * nz;
-      sm.Du[q][a] = w * dx * ny * nz;
-      sm.Dv[q][a] = w * nx * dy * nz;
-      sm.Dw[q][a] = w * nx * ny * dz;
+      sm.Du[q][a] = w * td0[g0] * ny * nz;
+      sm.Dv[q][a] = w * nx * td1[g1] * nz;
+      sm.Dw[q][a] = w * nx * ny * td2[g2];
     }
     __syncthreads();
     if (tid < kNen * 3) sm.colStart[tid] = sm.eq[tid] > 0 ? S.colptr[sm.eq[tid] - 1] : 0;
@@ -247,7 +256,8 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
 
     // ---- 5. rational basis R and dR/du in place
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
-      const int q = idx / kNen, a = idx % kNen;
+      const uint32_t d = sm.dec[idx];
+      const int q = d & 31, a = (d >> 5) & 31;
       const float* Wq = sc.Wq + q * 4;
       const float R = sm.N[q][a] * Wq[0];
       sm.Du[q][a] = (sm.Du[q][a] - R * Wq[1]) * Wq[0];
@@ -263,28 +273,37 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     for (int pass = 0; pass < 2 && ok; pass++) {
       const float s = pass == 0 ? 1.f : -1.f;
       if (!(signs & (1 << pass))) continue;
-      // rows r = 32k + a (k < 3, a < 27), 4 consecutive Gauss points per chunk
-      for (int ch = tid; ch < 12 * 7 * 8; ch += blockDim.x) {
-        const int r = (ch / 56) * 8 + (ch & 7), q0 = ((ch >> 3) % 7) * 4;
-        const int a = r & 31, k = r >> 5;
-        if (a >= kNen) continue;
-        float hi[4], lo[4];
+      // C[q] = sqrt(max(s w_q, 0)) Jinv_q
+      if (tid < kNq) {
+        const float ws = s * sm.wq[tid];
+        const float sw = ws > 0.f ? sqrtf(ws) : 0.f;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int q = q0 + j;
-          float v = 0.f;
-          if (q < kNq) {
-            const float ws = s * sm.wq[q];
-            if (ws > 0.f) {
-              const float* B = sc.Jinv + q * 9 + k * 3;
-              v = sqrtf(ws) * (sm.Du[q][a] * B[0] + sm.Dv[q][a] * B[1] + sm.Dw[q][a] * B[2]);
+        for (int c = 0; c < 9; c++) sc.C[tid * 9 + c] = sw * sc.Jinv[tid * 9 + c];
+      }
+      __syncthreads();
+      // one operand row per thread: r = 32k + a (k < 3, a < 27), 4 Gauss
+      // points per 16-byte store (conflict-free: lanes cover whole core rows)
+      {
+        const int r = tid, a = r & 31, k = r >> 5;
+        if (a < kNen && k < 3) {
+#pragma unroll
+          for (int kb = 0; kb < 7; kb++) {
+            float hi[4], lo[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int q = kb * 4 + j;
+              float v = 0.f;
+              if (q < kNq) {
+                const float* C = sc.C + q * 9 + k * 3;
+                v = sm.Du[q][a] * C[0] + sm.Dv[q][a] * C[1] + sm.Dw[q][a] * C[2];
+              }
+              splitTF32(v, hi[j], lo[j]);
             }
+            const int o = kmaj(r, kb * 4);
+            *reinterpret_cast<float4*>(sm.Thi + o) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<float4*>(sm.Tlo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
           }
-          splitTF32(v, hi[j], lo[j]);
         }
-        const int o = kmaj(r, q0);
-        *reinterpret_cast<float4*>(sm.Thi + o) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<float4*>(sm.Tlo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
       }
       fenceProxyAsync();
       __syncthreads();
@@ -325,13 +344,15 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     // ---- 7. tensor memory -> compact Gram matrix in shared memory
     if (ok && warp < 3 && signs) {
       float v[16];
+      float* grow = sm.Gc + (3 * lane + warp) * kGs;
+#pragma unroll
       for (int c16 = 0; c16 < kN / 16; c16++) {
         tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
         if (lane < kNen) {
 #pragma unroll
           for (int i = 0; i < 16; i++) {
             const int n = 16 * c16 + i, l = n >> 5, bcol = n & 31;
-            if (bcol < kNen) sm.Gc[(3 * lane + warp) * kGs + 3 * bcol + l] = v[i];
+            if (bcol < kNen) grow[3 * bcol + l] = v[i];
           }
         }
       }
@@ -369,27 +390,26 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     //         arithmetic; the FP64 additions happen in the L2 reductions)
     const float lamf = (float)(P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu)));
     const float muf = (float)(P.E / (2.0 * (1.0 + P.nu)));
-    for (int pr = tid; pr < kNen * kNen; pr += blockDim.x) {
-      const int a = pr % kNen, bn = pr / kNen;
-      const float* ga = sm.Gc + 3 * a * kGs + 3 * bn;
-      float g[3][3];
+    // one matrix row (a, k) per thread: the lanes of a warp cover consecutive
+    // rows, so each reduction instruction touches contiguous column segments
+    if (tid < kNen * 3 && sm.eq[tid] > 0) {
+      const int a = tid / 3, k = tid - 3 * a;
+      int rank = 0;
+      for (int m = 0; m < k; m++) rank += sm.eq[3 * a + m] > 0;
+      const int base = sm.Fa[a] + rank;
+      const int la = (a / 3) % 3 + 3 * (a / 9);
+      const float* Grow = sm.Gc + tid * kGs;    // row (a, k)
+      const float* Ga = sm.Gc + 3 * a * kGs;     // rows (a, 0..2)
+      for (int bn = 0; bn < kNen; bn++) {
+        const float trm =
+            muf * (Ga[3 * bn] + Ga[kGs + 3 * bn + 1] + Ga[2 * kGs + 3 * bn + 2]);
+        const int off = sm.lo[bn][la] + base;
 #pragma unroll
-      for (int k = 0; k < 3; k++)
-#pragma unroll
-        for (int l = 0; l < 3; l++) g[k][l] = ga[k * kGs + l];
-      const float trm = muf * (g[0][0] + g[1][1] + g[2][2]);
-      const int off = sm.lo[bn][(a / 3) % 3 + 3 * (a / 9)] + sm.Fa[a];
-#pragma unroll
-      for (int l = 0; l < 3; l++) {
-        if (sm.eq[3 * bn + l] <= 0) continue;
-        double* col = S.K + sm.colStart[3 * bn + l] + off;
-        int rank = 0;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          if (sm.eq[3 * a + k] <= 0) continue;
-          const float ke = fmaf(lamf, g[k][l], fmaf(muf, g[l][k], k == l ? trm : 0.f));
-          redAdd(col + rank, widenF32(ke));
-          rank++;
+        for (int l = 0; l < 3; l++) {
+          if (sm.eq[3 * bn + l] <= 0) continue;
+          const float ke = fmaf(lamf, Grow[3 * bn + l],
+                                fmaf(muf, Ga[l * kGs + 3 * bn + k], k == l ? trm : 0.f));
+          redAdd(S.K + sm.colStart[3 * bn + l] + off, widenF32(ke));
         }
       }
     }
@@ -504,6 +524,9 @@ ifemgpu_status tcPrepare(ifemgpu_ctx* ctx)
   IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_tc_elast_p2,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tcVolumeSmem()));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_tc_elast_p2,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
   return IFEMGPU_OK;
 }
 
