@@ -45,11 +45,16 @@ constexpr uint32_t kFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wai
 struct TcSmem {
   float Thi[kM * kK];      // operand tile, K-major core-matrix layout
   float Tlo[kM * kK];
-  float Gc[81 * kGs];      // G[(3a+k)][(3b+l)]; before the epilogue: per-point scratch
-  float N[kNq][kNen];      // weighted basis wN, then the rational basis R
-  float Du[kNq][kNen];     // weighted parametric derivatives, then dR/du_d
-  float Dv[kNq][kNen];
-  float Dw[kNq][kNen];
+  union {
+    struct {
+      float N[kNq][kNen];   // weighted basis wN, then the rational basis R
+      float Du[kNq][kNen];  // weighted parametric derivatives, then dR/du_d
+      float Dv[kNq][kNen];
+      float Dw[kNq][kNen];
+      float scr[1026];      // per-point scratch (see Scratch)
+    } b;
+    float Gc[81 * kGs];     // G[(3a+k)][(3b+l)], written once the basis data is dead
+  } u;
   float wq[kNq];           // signed integration weight (0 at skipped points)
   float X[kNen][4];        // control points relative to the element's first, weight
   int eq[kNen * 3];
@@ -63,7 +68,7 @@ struct TcSmem {
   int signs;               // bit 0: some w_q > 0, bit 1: some w_q < 0
 };
 
-// scratch views inside Gc (dead before the epilogue writes G)
+// scratch views (dead before the epilogue writes G)
 struct Scratch {
   float* P;     // [27][4][4] homogeneous sums
   float* Jinv;  // [27][9] column-major inverse Jacobian
@@ -73,7 +78,8 @@ struct Scratch {
 
 __device__ __forceinline__ Scratch scratch(TcSmem& sm)
 {
-  return Scratch{sm.Gc, sm.Gc + 27 * 16, sm.Gc + 27 * 16 + 27 * 9, sm.Gc + 27 * 16 + 27 * 13};
+  float* b = sm.u.b.scr;
+  return Scratch{b, b + 27 * 16, b + 27 * 16 + 27 * 9, b + 27 * 16 + 27 * 13};
 }
 
 __device__ __forceinline__ void redAdd(double* p, double v)
@@ -185,10 +191,10 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       const int g2 = ((d >> 14) & 3) * 3 + ((d >> 20) & 3);
       const float nx = tn0[g0], ny = tn1[g1], nz = tn2[g2];
       const float w = sm.X[a][3];
-      sm.N[q][a] = w * nx * ny * nz;
-      sm.Du[q][a] = w * td0[g0] * ny * nz;
-      sm.Dv[q][a] = w * nx * td1[g1] * nz;
-      sm.Dw[q][a] = w * nx * ny * td2[g2];
+      sm.u.b.N[q][a] = w * nx * ny * nz;
+      sm.u.b.Du[q][a] = w * td0[g0] * ny * nz;
+      sm.u.b.Dv[q][a] = w * nx * td1[g1] * nz;
+      sm.u.b.Dw[q][a] = w * nx * ny * td2[g2];
     }
     __syncthreads();
     if (tid < kNen * 3) sm.colStart[tid] = sm.eq[tid] > 0 ? S.colptr[sm.eq[tid] - 1] : 0;
@@ -200,10 +206,10 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
 #pragma unroll 9
       for (int a = 0; a < kNen; a++) {
         const float x = c < 3 ? sm.X[a][c] : 1.f;
-        s0 = fmaf(sm.N[q][a], x, s0);
-        s1 = fmaf(sm.Du[q][a], x, s1);
-        s2 = fmaf(sm.Dv[q][a], x, s2);
-        s3 = fmaf(sm.Dw[q][a], x, s3);
+        s0 = fmaf(sm.u.b.N[q][a], x, s0);
+        s1 = fmaf(sm.u.b.Du[q][a], x, s1);
+        s2 = fmaf(sm.u.b.Dv[q][a], x, s2);
+        s3 = fmaf(sm.u.b.Dw[q][a], x, s3);
       }
       float* Pq = sc.P + q * 16 + c * 4;
       Pq[0] = s0;
@@ -259,11 +265,11 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       const uint32_t d = sm.dec[idx];
       const int q = d & 31, a = (d >> 5) & 31;
       const float* Wq = sc.Wq + q * 4;
-      const float R = sm.N[q][a] * Wq[0];
-      sm.Du[q][a] = (sm.Du[q][a] - R * Wq[1]) * Wq[0];
-      sm.Dv[q][a] = (sm.Dv[q][a] - R * Wq[2]) * Wq[0];
-      sm.Dw[q][a] = (sm.Dw[q][a] - R * Wq[3]) * Wq[0];
-      sm.N[q][a] = R;
+      const float R = sm.u.b.N[q][a] * Wq[0];
+      sm.u.b.Du[q][a] = (sm.u.b.Du[q][a] - R * Wq[1]) * Wq[0];
+      sm.u.b.Dv[q][a] = (sm.u.b.Dv[q][a] - R * Wq[2]) * Wq[0];
+      sm.u.b.Dw[q][a] = (sm.u.b.Dw[q][a] - R * Wq[3]) * Wq[0];
+      sm.u.b.N[q][a] = R;
     }
     __syncthreads();
 
@@ -295,7 +301,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
               float v = 0.f;
               if (q < kNq) {
                 const float* C = sc.C + q * 9 + k * 3;
-                v = sm.Du[q][a] * C[0] + sm.Dv[q][a] * C[1] + sm.Dw[q][a] * C[2];
+                v = sm.u.b.Du[q][a] * C[0] + sm.u.b.Dv[q][a] * C[1] + sm.u.b.Dw[q][a] * C[2];
               }
               splitTF32(v, hi[j], lo[j]);
             }
@@ -336,15 +342,16 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       const float bk = (float)P.body[k];
       if (bk != 0.f) {
         float acc = 0.f;
-        for (int q = 0; q < kNq; q++) acc = fmaf(sm.N[q][a], sm.wq[q], acc);
+        for (int q = 0; q < kNq; q++) acc = fmaf(sm.u.b.N[q][a], sm.wq[q], acc);
         fe = bk * acc;
       }
     }
+    __syncthreads();  // the Gram stage below overlays the basis arrays
 
     // ---- 7. tensor memory -> compact Gram matrix in shared memory
     if (ok && warp < 3 && signs) {
       float v[16];
-      float* grow = sm.Gc + (3 * lane + warp) * kGs;
+      float* grow = sm.u.Gc + (3 * lane + warp) * kGs;
 #pragma unroll
       for (int c16 = 0; c16 < kN / 16; c16++) {
         tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
@@ -357,7 +364,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
         }
       }
     } else if (!signs) {
-      for (int i = tid; i < 81 * kGs; i += blockDim.x) sm.Gc[i] = 0.f;
+      for (int i = tid; i < 81 * kGs; i += blockDim.x) sm.u.Gc[i] = 0.f;
     }
     tcFenceBefore();
     __syncthreads();
@@ -398,8 +405,8 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       for (int m = 0; m < k; m++) rank += sm.eq[3 * a + m] > 0;
       const int base = sm.Fa[a] + rank;
       const int la = (a / 3) % 3 + 3 * (a / 9);
-      const float* Grow = sm.Gc + tid * kGs;    // row (a, k)
-      const float* Ga = sm.Gc + 3 * a * kGs;     // rows (a, 0..2)
+      const float* Grow = sm.u.Gc + tid * kGs;    // row (a, k)
+      const float* Ga = sm.u.Gc + 3 * a * kGs;     // rows (a, 0..2)
       for (int bn = 0; bn < kNen; bn++) {
         const float trm =
             muf * (Ga[3 * bn] + Ga[kGs + 3 * bn + 1] + Ga[2 * kGs + 3 * bn + 2]);
@@ -425,7 +432,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
             const int ce = sm.eq[j];
             if (ce >= 0) continue;
             const int bn = j / 3, l = j % 3;
-            const float* ga = sm.Gc + 3 * a * kGs + 3 * bn;
+            const float* ga = sm.u.Gc + 3 * a * kGs + 3 * bn;
             const double tr = (double)ga[0] + ga[kGs + 1] + ga[2 * kGs + 2];
             const double ke = lamf * (double)ga[k * kGs + l] + muf * (double)ga[l * kGs + k] +
                               (k == l ? muf * tr : 0.0);
@@ -541,6 +548,18 @@ ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int)
                                                                   tcVolumeSmem()));
   if (perSM < 1) return setError(ctx, IFEMGPU_UNSUPPORTED, "tensor-core kernel does not fit an SM");
   const int grid = std::min(p.count, perSM * ctx->numSMs);
+  if (ctx->opts.verbose) {
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, k_volume_tc_elast_p2);
+    int smemSM = 0, resv = 0, optin = 0;
+    cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->opts.device);
+    cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, ctx->opts.device);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->opts.device);
+    std::printf("tc kernel: smem/block %zu, regs %d, static smem %zu, max dyn %d, carveout %d; "
+                "SM smem %d, reserved %d, optin %d -> %d blocks/SM, grid %d\n",
+                tcVolumeSmem(), fa.numRegs, fa.sharedSizeBytes, fa.maxDynamicSharedSizeBytes,
+                fa.preferredShmemCarveout, smemSM, resv, optin, perSM, grid);
+  }
   const DevPatch* patches = ctx->d_patches;
   const Item* items = ctx->d_items + p.first;
   int count = p.count;
