@@ -541,25 +541,27 @@ ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int)
 {
   TcSys S{ctx->d_madof, ctx->d_meqn, ctx->d_freeBefore, ctx->nceq ? ctx->d_c0 : nullptr,
           ctx->d_K, ctx->d_b, ctx->d_colptr, ctx->d_flags, ctx->d_counters};
-  // every CTA must be resident (CTAs wait on each other's done flags):
-  // cooperative launch with the occupancy-limited grid
-  int perSM = 0;
-  IFEMGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_volume_tc_elast_p2, 128,
-                                                                  tcVolumeSmem()));
+  // every CTA must be resident (CTAs wait on each other's done flags): the
+  // grid is sized from the SM's shared memory, registers and tensor memory
+  // (4 x 128 columns).  Should residency ever fail, the bounded flag waits
+  // end with a reported device timeout instead of a hang.
+  cudaFuncAttributes fa{};
+  IFEMGPU_CUDA(ctx, cudaFuncGetAttributes(&fa, k_volume_tc_elast_p2));
+  int smemSM = 0, resv = 0, regsSM = 0;
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                           ctx->opts.device));
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock,
+                                           ctx->opts.device));
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&regsSM, cudaDevAttrMaxRegistersPerMultiprocessor,
+                                           ctx->opts.device));
+  const int bySmem = smemSM / (int)(tcVolumeSmem() + resv);
+  const int byRegs = regsSM / (((fa.numRegs + 7) / 8) * 8 * 128);
+  const int perSM = std::min(std::min(bySmem, byRegs), 3);
   if (perSM < 1) return setError(ctx, IFEMGPU_UNSUPPORTED, "tensor-core kernel does not fit an SM");
   const int grid = std::min(p.count, perSM * ctx->numSMs);
-  if (ctx->opts.verbose) {
-    cudaFuncAttributes fa{};
-    cudaFuncGetAttributes(&fa, k_volume_tc_elast_p2);
-    int smemSM = 0, resv = 0, optin = 0;
-    cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->opts.device);
-    cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, ctx->opts.device);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->opts.device);
-    std::printf("tc kernel: smem/block %zu, regs %d, static smem %zu, max dyn %d, carveout %d; "
-                "SM smem %d, reserved %d, optin %d -> %d blocks/SM, grid %d\n",
-                tcVolumeSmem(), fa.numRegs, fa.sharedSizeBytes, fa.maxDynamicSharedSizeBytes,
-                fa.preferredShmemCarveout, smemSM, resv, optin, perSM, grid);
-  }
+  if (ctx->opts.verbose)
+    std::printf("tensor-core volume kernel: %zu B shared memory, %d registers, %d blocks/SM, grid %d\n",
+                tcVolumeSmem(), fa.numRegs, perSM, grid);
   const DevPatch* patches = ctx->d_patches;
   const Item* items = ctx->d_items + p.first;
   int count = p.count;
@@ -569,11 +571,7 @@ ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int)
   cfg.blockDim = dim3(128);
   cfg.dynamicSmemBytes = tcVolumeSmem();
   cfg.stream = ctx->stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 0;
   IFEMGPU_CUDA(ctx, cudaLaunchKernelExC(&cfg, (const void*)k_volume_tc_elast_p2, args));
   return IFEMGPU_OK;
 }
