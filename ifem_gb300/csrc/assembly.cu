@@ -670,9 +670,17 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   for (int pi = 0; pi < np; pi++) {
     DevPatch& D = ctx->h_devpatches[pi];
     onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) &&
-               D.lineOff != nullptr;
+               D.lineOff != nullptr && D.faceTables && ctx->patches[pi].neumann.size() <= 6;
     D.flagBase = nflags;
-    if (onTc[pi]) nflags += ctx->patches[pi].nelAll;
+    if (onTc[pi]) {
+      nflags += ctx->patches[pi].nelAll;
+      // the element kernel integrates this patch's Neumann faces itself
+      D.nneu = (int)ctx->patches[pi].neumann.size();
+      for (int f = 0; f < D.nneu; f++) {
+        D.neuFace[f] = ctx->patches[pi].neumann[f].face;
+        for (int c = 0; c < 3; c++) D.neuT[f][c] = (float)ctx->patches[pi].neumann[f].t[c];
+      }
+    }
   }
   auto colourItems = [&](int pi, int c, std::vector<Item>& out) {
     const HostPatch& pc = ctx->patches[pi];
@@ -713,6 +721,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   std::vector<Pass> facePasses;
   for (int pi = 0; pi < np; pi++) {
     const HostPatch& pc = ctx->patches[pi];
+    if (onTc[pi]) continue;  // integrated by the tensor-core element kernel
     for (const auto& nm : pc.neumann) {
       const int bc = (int)neuVals.size() / 3;
       for (int c = 0; c < 3; c++) neuVals.push_back(nm.t[c]);

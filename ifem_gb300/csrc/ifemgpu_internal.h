@@ -46,6 +46,10 @@ struct DevPatch {
   float* tabNf[3];
   float* tabDf[3];
   int flagBase;       // first slot of this patch's elements in the done-flag array
+  // Neumann faces integrated inside the tensor-core element kernel
+  int nneu;
+  int neuFace[6];
+  float neuT[6][3];
   int faceTables;     // face Gauss rule equals the volume rule in every direction
   // Position table of the compressed-column pattern for patches whose
   // couplings are the index box of half-width p (nullptr otherwise): for

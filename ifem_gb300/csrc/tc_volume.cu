@@ -346,6 +346,81 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
         fe = bk * acc;
       }
     }
+
+    // Neumann faces of the patch that this element touches: constant
+    // traction t, Fe += t R dS w at the 3x3 face points (face overload of
+    // ASMs3D::integrate, src/ASM/ASMs3D.C:2547-2812)
+    for (int f = 0; f < P.nneu; f++) {
+      const int face = P.neuFace[f];
+      const int nd0 = (face - 1) >> 1, side = (face - 1) & 1;
+      const int ee[3] = {e1, e2, e3};
+      if (ee[nd0] != (side ? P.nel[nd0] - 1 : 0)) continue;  // uniform in the CTA
+      float* fR = sc.P;            // [9][27] rational basis at the face points
+      float* fW = sc.P + 9 * 27;   // [9] dS * weights
+      if (tid < 9) {
+        const int ta = nd0 == 0 ? 1 : 0, tb = nd0 == 2 ? 1 : 2;
+        int g[3] = {0, 0, 0};
+        g[ta] = tid % 3;
+        g[tb] = tid / 3;
+        float Nd[3][3], Dd[3][3];
+        for (int d = 0; d < 3; d++)
+          for (int r = 0; r < 3; r++) {
+            if (d == nd0) {
+              Nd[d][r] = (float)P.tabB[d][side * 6 + r];
+              Dd[d][r] = (float)P.tabB[d][side * 6 + 3 + r];
+            } else {
+              Nd[d][r] = P.tabNf[d][ee[d] * 9 + g[d] * 3 + r];
+              Dd[d][r] = P.tabDf[d][ee[d] * 9 + g[d] * 3 + r];
+            }
+          }
+        float S4[4][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f},
+                          {0.f, 0.f, 0.f, 0.f}};
+        for (int a = 0; a < kNen; a++) {
+          const int i = a % 3, j = (a / 3) % 3, k = a / 9;
+          const float w = sm.X[a][3];
+          const float wN = w * Nd[0][i] * Nd[1][j] * Nd[2][k];
+          const float w0 = w * Dd[0][i] * Nd[1][j] * Nd[2][k];
+          const float w1 = w * Nd[0][i] * Dd[1][j] * Nd[2][k];
+          const float w2 = w * Nd[0][i] * Nd[1][j] * Dd[2][k];
+          fR[tid * 27 + a] = wN;
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            const float x = c < 3 ? sm.X[a][c] : 1.f;
+            S4[c][0] = fmaf(wN, x, S4[c][0]);
+            S4[c][1] = fmaf(w0, x, S4[c][1]);
+            S4[c][2] = fmaf(w1, x, S4[c][2]);
+            S4[c][3] = fmaf(w2, x, S4[c][3]);
+          }
+        }
+        const float iW = 1.f / S4[3][0];
+        float J[9];  // J[d*3 + c] = dX_c/du_d
+        for (int c = 0; c < 3; c++)
+          for (int d = 0; d < 3; d++)
+            J[d * 3 + c] = (S4[c][1 + d] - S4[c][0] * iW * S4[3][1 + d]) * iW;
+        const int t1 = 1 + (nd0 + 1) % 3, t2 = 1 + t1 % 3;
+        const float* u = J + 3 * (t1 - 1);
+        const float* v = J + 3 * (t2 - 1);
+        const float nx = u[1] * v[2] - u[2] * v[1], ny = u[2] * v[0] - u[0] * v[2],
+                    nz = u[0] * v[1] - u[1] * v[0];
+        const double det = (double)J[0] * ((double)J[4] * J[8] - (double)J[5] * J[7]) -
+                           (double)J[3] * ((double)J[1] * J[8] - (double)J[2] * J[7]) +
+                           (double)J[6] * ((double)J[1] * J[5] - (double)J[2] * J[4]);
+        float wgt = 0.f;
+        if (det > kEpsZ || det < -kEpsZ)
+          wgt = sqrtf(nx * nx + ny * ny + nz * nz) * 0.25f * (float)P.span[ta][ee[ta]] *
+                (float)P.span[tb][ee[tb]] * (float)P.fw[ta][g[ta]] * (float)P.fw[tb][g[tb]];
+        for (int a = 0; a < kNen; a++) fR[tid * 27 + a] *= iW;
+        fW[tid] = wgt;
+      }
+      __syncthreads();
+      if (tid < kNen * 3) {
+        const int a = tid / 3, c = tid % 3;
+        float acc = 0.f;
+        for (int gq = 0; gq < 9; gq++) acc = fmaf(fR[gq * 27 + a], fW[gq], acc);
+        fe = fmaf(P.neuT[f][c], acc, fe);
+      }
+      __syncthreads();
+    }
     __syncthreads();  // the Gram stage below overlays the basis arrays
 
     // ---- 7. tensor memory -> compact Gram matrix in shared memory
