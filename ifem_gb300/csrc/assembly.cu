@@ -20,6 +20,7 @@
 #include <cstring>
 
 #include "ifemgpu_internal.h"
+#include "tc_common.cuh"
 
 namespace ifemgpu {
 
@@ -189,39 +190,55 @@ struct SysView {
   double* K;
   double* b;
   unsigned long long* counters;
+  const int* F;  // free DOFs before each node
 };
 
+// Generic element kernel, one CTA per element of one colour; T = double is
+// the exact-parity mode (FP64 arithmetic, plain adds: no two CTAs of a colour
+// touch one entry), T = float the split mode on the CUDA cores (FP32
+// arithmetic, FP64 determinant/inverse, FP64 additions in L2 reductions).
+// Node pairs a <= b are computed once; the (b, a) block is the transpose.
+//
+// Shared memory (T): Xn[nen*4] | N[nq*nen] | dX[3][nq*nen] | Jinv[nq*9]
+//                    | wq[nq] | kq[nq] | fq[nq]   then  eq[nd] (int)
+__device__ __forceinline__ void addEntry(double* p, double v) { *p += v; }
+__device__ __forceinline__ void addEntry(double* p, float v) { atomicAdd(p, tc::widenF32(v)); }
+
+template <typename T>
 __global__ void __launch_bounds__(256)
-k_volume_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ items,
-              SysView S)
+k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ items,
+             SysView S)
 {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
   const Item it = items[blockIdx.x];
   const DevPatch& P = patches[it.patch];
   const int nen = P.nen, nq = P.nq, dim = P.dim, npv = P.npv, nd = nen * npv;
   const int e = it.elem;
-  double* Xn = sm;
-  double* Nq = Xn + nen * 4;
-  double* dX = Nq + nq * nen;          // 3 planes of nq*nen
-  double* Ji = dX + 3 * nq * nen;      // nq * 9
-  double* wq = Ji + nq * 9;
-  double* kq = wq + nq;
-  double* fq = kq + nq;
+  T* Xn = sm;
+  T* Nq = Xn + nen * 4;
+  T* dX = Nq + nq * nen;          // 3 planes of nq*nen
+  T* Ji = dX + 3 * nq * nen;      // nq * 9
+  T* wq = Ji + nq * 9;
+  T* kq = wq + nq;
+  T* fq = kq + nq;
   int* eq = reinterpret_cast<int*>(fq + nq);
   const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
   const int q1 = P.p[0] + 1, q2 = P.p[1] + 1;
+  const double* c00 = P.ctrl + (size_t)elemNode(P, e, 0) * 4;
 
-  // element nodes: coordinates and equation numbers
+  // element nodes: coordinates (relative to the first node) and equation numbers
   for (int a = threadIdx.x; a < nen; a += blockDim.x) {
     const int node = elemNode(P, e, a);
-    for (int c = 0; c < 4; c++) Xn[a * 4 + c] = P.ctrl[(size_t)node * 4 + c];
+    for (int c = 0; c < 3; c++) Xn[a * 4 + c] = (T)(P.ctrl[(size_t)node * 4 + c] - c00[c]);
+    Xn[a * 4 + 3] = (T)P.ctrl[(size_t)node * 4 + 3];
     const int g = P.firstNode + node;
     const int d0 = S.madof[g] - 1;
     for (int c = 0; c < npv; c++) eq[a * npv + c] = S.meqn[d0 + c];
   }
   __syncthreads();
 
-  // tensor-product basis (times weight) at every (Gauss point, function)
+  // tensor-product basis at every (Gauss point, function)
   for (int t = threadIdx.x; t < nq * nen; t += blockDim.x) {
     const int q = t / nen, a = t % nen;
     const int gi = q % P.ng[0], gj = (q / P.ng[0]) % P.ng[1], gk = q / (P.ng[0] * P.ng[1]);
@@ -230,19 +247,19 @@ k_volume_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ ite
     const double* d0 = P.tabD[0] + ((size_t)e1 * P.ng[0] + gi) * q1;
     const double* n1 = P.tabN[1] + ((size_t)e2 * P.ng[1] + gj) * q2;
     const double* d1 = P.tabD[1] + ((size_t)e2 * P.ng[1] + gj) * q2;
-    double N, du, dv, dw = 0.0;
+    T N, du, dv, dw = 0;
     if (dim == 3) {
       const int q3 = P.p[2] + 1;
       const double* n2 = P.tabN[2] + ((size_t)e3 * P.ng[2] + gk) * q3;
       const double* d2 = P.tabD[2] + ((size_t)e3 * P.ng[2] + gk) * q3;
-      N = n0[i] * n1[j] * n2[k];
-      du = d0[i] * n1[j] * n2[k];
-      dv = n0[i] * d1[j] * n2[k];
-      dw = n0[i] * n1[j] * d2[k];
+      N = (T)(n0[i] * n1[j] * n2[k]);
+      du = (T)(d0[i] * n1[j] * n2[k]);
+      dv = (T)(n0[i] * d1[j] * n2[k]);
+      dw = (T)(n0[i] * n1[j] * d2[k]);
     } else {
-      N = n0[i] * n1[j];
-      du = d0[i] * n1[j];
-      dv = n0[i] * d1[j];
+      N = (T)(n0[i] * n1[j]);
+      du = (T)(d0[i] * n1[j]);
+      dv = (T)(n0[i] * d1[j]);
     }
     Nq[t] = N;
     dX[t] = du;
@@ -251,39 +268,42 @@ k_volume_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ ite
   }
   __syncthreads();
 
-  // per Gauss point: rational weighting, Jacobian (FP64), inverse, detJxW
+  // per Gauss point: rational weighting, Jacobian, FP64 determinant and inverse
   for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-    double* Nr = Nq + q * nen;
-    double* Du = dX + q * nen;
-    double* Dv = dX + nq * nen + q * nen;
-    double* Dw = dX + 2 * nq * nen + q * nen;
+    T* Nr = Nq + q * nen;
+    T* Du = dX + q * nen;
+    T* Dv = dX + nq * nen + q * nen;
+    T* Dw = dX + 2 * nq * nen + q * nen;
     if (P.rational) {
-      double W = 0.0, Wu = 0.0, Wv = 0.0, Ww = 0.0;
+      T W = 0, Wu = 0, Wv = 0, Ww = 0;
       for (int a = 0; a < nen; a++) {
-        const double w = Xn[a * 4 + 3];
+        const T w = Xn[a * 4 + 3];
         W += w * Nr[a];
         Wu += w * Du[a];
         Wv += w * Dv[a];
         Ww += w * Dw[a];
       }
       for (int a = 0; a < nen; a++) {
-        const double w = Xn[a * 4 + 3];
-        const double R = w * Nr[a] / W;
+        const T w = Xn[a * 4 + 3];
+        const T R = w * Nr[a] / W;
         Du[a] = (w * Du[a] - R * Wu) / W;
         Dv[a] = (w * Dv[a] - R * Wv) / W;
         Dw[a] = (w * Dw[a] - R * Ww) / W;
         Nr[a] = R;
       }
     }
-    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // column-major J(r,c) = dX_r/du_c
-    double X[3] = {0, 0, 0};
+    T Jt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // column-major J(r,c) = dX_r/du_c
+    T Xt[3] = {0, 0, 0};
     for (int a = 0; a < nen; a++) {
-      const double x = Xn[a * 4], y = Xn[a * 4 + 1], z = Xn[a * 4 + 2];
-      J[0] += x * Du[a]; J[1] += y * Du[a]; J[2] += z * Du[a];
-      J[3] += x * Dv[a]; J[4] += y * Dv[a]; J[5] += z * Dv[a];
-      J[6] += x * Dw[a]; J[7] += y * Dw[a]; J[8] += z * Dw[a];
-      X[0] += x * Nr[a]; X[1] += y * Nr[a]; X[2] += z * Nr[a];
+      const T x = Xn[a * 4], y = Xn[a * 4 + 1], z = Xn[a * 4 + 2];
+      Jt[0] += x * Du[a]; Jt[1] += y * Du[a]; Jt[2] += z * Du[a];
+      Jt[3] += x * Dv[a]; Jt[4] += y * Dv[a]; Jt[5] += z * Dv[a];
+      Jt[6] += x * Dw[a]; Jt[7] += y * Dw[a]; Jt[8] += z * Dw[a];
+      Xt[0] += x * Nr[a]; Xt[1] += y * Nr[a]; Xt[2] += z * Nr[a];
     }
+    double J[9], X[3];
+    for (int c = 0; c < 9; c++) J[c] = (double)Jt[c];
+    for (int c = 0; c < 3; c++) X[c] = (double)Xt[c] + c00[c];
     double det, B[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (dim == 3) {
       // matrix<T>::det / inverse (src/LinAlg/matrix.h:790-850), T(i,j)=J[(j-1)*3+i-1]
@@ -318,34 +338,34 @@ k_volume_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ ite
     } else {
       atomicAdd(S.counters, 1ull);
     }
-    wq[q] = w;
-    for (int c = 0; c < 9; c++) Ji[q * 9 + c] = B[c];
+    wq[q] = (T)w;
+    for (int c = 0; c < 9; c++) Ji[q * 9 + c] = (T)B[c];
     // material data at the point
     double kap = P.kappa, f = P.source;
     if (P.kind == IFEMGPU_POISSON) {
       if (P.logk) {
         double g = 0.0;
-        for (int a = 0; a < nen; a++) g += Nr[a] * P.logk[elemNode(P, e, a)];
+        for (int a = 0; a < nen; a++) g += (double)Nr[a] * P.logk[elemNode(P, e, a)];
         kap *= exp(g);
       }
       if (P.source_shape == IFEMGPU_SOURCE_SINE)
         for (int c = 0; c < dim; c++) f *= sin(M_PI * X[c]);
       if (P.noise) {
         double s = 0.0;
-        for (int a = 0; a < nen; a++) s += Nr[a] * P.noise[elemNode(P, e, a)];
+        for (int a = 0; a < nen; a++) s += (double)Nr[a] * P.noise[elemNode(P, e, a)];
         f *= 1.0 + s;
       }
     }
-    kq[q] = kap * w;
-    fq[q] = f;
+    kq[q] = (T)(kap * w);
+    fq[q] = (T)f;
   }
   __syncthreads();
 
   // dNdX = dNdu * J^-1 in place
   for (int t = threadIdx.x; t < nq * nen; t += blockDim.x) {
     const int q = t / nen;
-    const double* B = Ji + q * 9;
-    const double du = dX[t], dv = dX[nq * nen + t], dw = dX[2 * nq * nen + t];
+    const T* B = Ji + q * 9;
+    const T du = dX[t], dv = dX[nq * nen + t], dw = dX[2 * nq * nen + t];
     // (dNdX)_c = sum_k dNdu_k * Jinv(k,c), Jinv column-major B[c*3+k]
     dX[t] = du * B[0] + dv * B[1] + dw * B[2];
     dX[nq * nen + t] = du * B[3] + dv * B[4] + dw * B[5];
@@ -353,60 +373,135 @@ k_volume_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ ite
   }
   __syncthreads();
 
-  // element matrix, node pair by node pair, scattered directly
-  const double lam = P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu));
-  const double mu = P.E / (2.0 * (1.0 + P.nu));
-  for (int t = threadIdx.x; t < nen * nen; t += blockDim.x) {
-    const int a = t % nen, bn = t / nen;
-    double Ke[9];
+  // Poisson in split mode: 4x4 register tiles of node pairs (ta <= tb),
+  // Ke[a][b] = sum over (Gauss point, direction) of kq dX_a dX_b
+  if (sizeof(T) == sizeof(float) && P.kind == IFEMGPU_POISSON && S.c0 == nullptr) {
+    const int nt = (nen + 3) / 4, ntp = nt * (nt + 1) / 2, K = nq * dim;
+    for (int t = threadIdx.x; t < ntp; t += blockDim.x) {
+      int tb = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+      while (tb * (tb + 1) / 2 > t) tb--;
+      while ((tb + 1) * (tb + 2) / 2 <= t) tb++;
+      const int ta = t - tb * (tb + 1) / 2;
+      T acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0;
+      for (int k = 0; k < K; k++) {
+        const int c = k / nq, q = k - c * nq;
+        const T* row = dX + c * nq * nen + q * nen;
+        const T s = kq[q];
+        T va[4], vb[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int a = 4 * ta + i, b = 4 * tb + i;
+          va[i] = a < nen ? row[a] * s : T(0);
+          vb[i] = b < nen ? row[b] : T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+          for (int j = 0; j < 4; j++) acc[i][j] += va[i] * vb[j];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int a = 4 * ta + i, bn = 4 * tb + j;
+          if (a >= nen || bn >= nen || a > bn) continue;
+          for (int side = 0; side < (a == bn ? 1 : 2); side++) {
+            const int ra = side ? bn : a, cb = side ? a : bn;
+            const int r = eq[ra], ce = eq[cb];
+            if (r <= 0 || ce <= 0) continue;
+            int off;
+            if (P.lineOff) {
+              const int w1 = 2 * P.p[1] + 1, w2 = 2 * P.p[2] + 1;
+              const int dy = (ra / q1) % q2 - (cb / q1) % q2, dz = ra / (q1 * q2) - cb / (q1 * q2);
+              off = P.lineOff[(size_t)elemNode(P, e, cb) * w1 * w2 + (dz + P.p[2]) * w1 + dy +
+                              P.p[1]] +
+                    S.F[P.firstNode + elemNode(P, e, ra)];
+            } else {
+              const int pos0 = findRow(S.colptr, S.rowidx, ce - 1, r - 1);
+              if (pos0 < 0) { atomicAdd(S.counters + 1, 1ull); continue; }
+              off = pos0 - S.colptr[ce - 1];
+            }
+            addEntry(S.K + S.colptr[ce - 1] + off, acc[i][j]);
+          }
+        }
+    }
+  }
+
+  // element matrix for node pairs a <= bn, scattered as the (a, bn) block and
+  // its transpose (bn, a)
+  const T lam = (T)(P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu)));
+  const T mu = (T)(P.E / (2.0 * (1.0 + P.nu)));
+  const bool tiled = sizeof(T) == sizeof(float) && P.kind == IFEMGPU_POISSON && S.c0 == nullptr;
+  const int npairs = tiled ? 0 : nen * (nen + 1) / 2;
+  for (int t = threadIdx.x; t < npairs; t += blockDim.x) {
+    int bn = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+    while (bn * (bn + 1) / 2 > t) bn--;
+    while ((bn + 1) * (bn + 2) / 2 <= t) bn++;
+    const int a = t - bn * (bn + 1) / 2;
+    T Ke[9];
     if (P.kind == IFEMGPU_POISSON) {
-      double acc = 0.0;
+      T acc = 0;
       for (int q = 0; q < nq; q++) {
-        if (wq[q] == 0.0) continue;
-        const double s = kq[q];
-        double v = 0.0;
+        const T s = kq[q];
+        if (s == T(0)) continue;
+        T v = 0;
         for (int c = 0; c < dim; c++)
           v += dX[c * nq * nen + q * nen + a] * s * dX[c * nq * nen + q * nen + bn];
         acc += v;
       }
       Ke[0] = acc;
     } else {
-      double G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      T G[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (int q = 0; q < nq; q++) {
-        const double w = wq[q];
-        if (w == 0.0) continue;
-        const double ax = dX[q * nen + a] * w, ay = dX[nq * nen + q * nen + a] * w,
-                     az = dX[2 * nq * nen + q * nen + a] * w;
-        const double bx = dX[q * nen + bn], by = dX[nq * nen + q * nen + bn],
-                     bz = dX[2 * nq * nen + q * nen + bn];
+        const T w = wq[q];
+        if (w == T(0)) continue;
+        const T ax = dX[q * nen + a] * w, ay = dX[nq * nen + q * nen + a] * w,
+                az = dX[2 * nq * nen + q * nen + a] * w;
+        const T bx = dX[q * nen + bn], by = dX[nq * nen + q * nen + bn],
+                bz = dX[2 * nq * nen + q * nen + bn];
         G[0] += ax * bx; G[1] += ax * by; G[2] += ax * bz;
         G[3] += ay * bx; G[4] += ay * by; G[5] += ay * bz;
         G[6] += az * bx; G[7] += az * by; G[8] += az * bz;
       }
-      const double tr = G[0] + G[4] + G[8];
+      const T tr = G[0] + G[4] + G[8];
       for (int k = 0; k < 3; k++)
         for (int l = 0; l < 3; l++)
-          Ke[k * 3 + l] = lam * G[k * 3 + l] + mu * G[l * 3 + k] + (k == l ? mu * tr : 0.0);
+          Ke[k * 3 + l] = lam * G[k * 3 + l] + mu * G[l * 3 + k] + (k == l ? mu * tr : T(0));
     }
-    // scatter the npv x npv block: rows of node a, columns of node bn
-    int firstCol = -1, firstRow = -1;
-    for (int l = 0; l < npv && firstCol < 0; l++)
-      if (eq[bn * npv + l] > 0) firstCol = eq[bn * npv + l] - 1;
-    for (int k = 0; k < npv && firstRow < 0; k++)
-      if (eq[a * npv + k] > 0) firstRow = eq[a * npv + k] - 1;
-    if (firstCol < 0 || firstRow < 0) continue;
-    const int pos0 = findRow(S.colptr, S.rowidx, firstCol, firstRow);
-    if (pos0 < 0) { atomicAdd(S.counters + 1, 1ull); continue; }
-    const int off = pos0 - S.colptr[firstCol];
-    for (int l = 0; l < npv; l++) {
-      const int ce = eq[bn * npv + l];
-      if (ce <= 0) continue;
-      int rank = 0;
-      for (int k = 0; k < npv; k++) {
-        const int re = eq[a * npv + k];
-        if (re <= 0) continue;
-        S.K[S.colptr[ce - 1] + off + rank] += Ke[k * npv + l];
-        rank++;
+    // scatter: block (rows of a, columns of bn), then (rows of bn, columns of a)
+    for (int side = 0; side < (a == bn ? 1 : 2); side++) {
+      const int ra = side ? bn : a, cb = side ? a : bn;
+      int firstCol = -1, firstRow = -1;
+      for (int l = 0; l < npv && firstCol < 0; l++)
+        if (eq[cb * npv + l] > 0) firstCol = eq[cb * npv + l] - 1;
+      for (int k = 0; k < npv && firstRow < 0; k++)
+        if (eq[ra * npv + k] > 0) firstRow = eq[ra * npv + k] - 1;
+      if (firstCol < 0 || firstRow < 0) continue;
+      int off;
+      if (P.lineOff) {  // structured patch: position from the line-offset table
+        const int w1 = 2 * P.p[1] + 1, w2 = 2 * P.p[2] + 1;
+        const int dy = (ra / q1) % q2 - (cb / q1) % q2, dz = ra / (q1 * q2) - cb / (q1 * q2);
+        off = P.lineOff[(size_t)elemNode(P, e, cb) * w1 * w2 + (dz + P.p[2]) * w1 + dy + P.p[1]] +
+              S.F[P.firstNode + elemNode(P, e, ra)];
+      } else {
+        const int pos0 = findRow(S.colptr, S.rowidx, firstCol, firstRow);
+        if (pos0 < 0) { atomicAdd(S.counters + 1, 1ull); continue; }
+        off = pos0 - S.colptr[firstCol];
+      }
+      for (int l = 0; l < npv; l++) {
+        const int ce = eq[cb * npv + l];
+        if (ce <= 0) continue;
+        int rank = 0;
+        for (int k = 0; k < npv; k++) {
+          const int re = eq[ra * npv + k];
+          if (re <= 0) continue;
+          addEntry(S.K + S.colptr[ce - 1] + off + rank, side ? Ke[l * npv + k] : Ke[k * npv + l]);
+          rank++;
+        }
       }
     }
   }
@@ -416,40 +511,43 @@ k_volume_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ ite
     const int r = eq[i];
     if (r <= 0) continue;
     const int a = i / npv, k = i % npv;
-    double fe = 0.0;
+    T fe = 0;
     for (int q = 0; q < nq; q++) {
-      if (wq[q] == 0.0) continue;
-      const double Na = Nq[q * nen + a];
+      if (wq[q] == T(0)) continue;
+      const T Na = Nq[q * nen + a];
       if (P.kind == IFEMGPU_POISSON) fe += Na * fq[q] * wq[q];
-      else fe += P.body[k] * Na * wq[q];
+      else fe += (T)P.body[k] * Na * wq[q];
     }
-    S.b[r - 1] += fe;
-    if (S.c0 == nullptr) continue;
-    for (int j = 0; j < nd; j++) {
-      const int ce = eq[j];
-      if (ce >= 0) continue;
-      const int bn = j / npv, l = j % npv;
-      double kij = 0.0;
-      for (int q = 0; q < nq; q++) {
-        const double w = wq[q];
-        if (w == 0.0) continue;
-        if (P.kind == IFEMGPU_POISSON) {
-          double v = 0.0;
-          for (int c = 0; c < dim; c++)
-            v += dX[c * nq * nen + q * nen + a] * kq[q] * dX[c * nq * nen + q * nen + bn];
-          kij += v;
-        } else {
-          const double ak = dX[k * nq * nen + q * nen + a] * w;
-          const double al = dX[l * nq * nen + q * nen + a] * w;
-          double g = 0.0;
-          for (int c = 0; c < 3; c++)
-            g += dX[c * nq * nen + q * nen + a] * w * dX[c * nq * nen + q * nen + bn];
-          kij += lam * ak * dX[l * nq * nen + q * nen + bn] +
-                 mu * al * dX[k * nq * nen + q * nen + bn] + (k == l ? mu * g : 0.0);
+    double acc = (double)fe;
+    if (S.c0 != nullptr) {
+      for (int j = 0; j < nd; j++) {
+        const int ce = eq[j];
+        if (ce >= 0) continue;
+        const int bn = j / npv, l = j % npv;
+        T kij = 0;
+        for (int q = 0; q < nq; q++) {
+          const T w = wq[q];
+          if (w == T(0)) continue;
+          if (P.kind == IFEMGPU_POISSON) {
+            T v = 0;
+            for (int c = 0; c < dim; c++)
+              v += dX[c * nq * nen + q * nen + a] * kq[q] * dX[c * nq * nen + q * nen + bn];
+            kij += v;
+          } else {
+            const T ak = dX[k * nq * nen + q * nen + a] * w;
+            const T al = dX[l * nq * nen + q * nen + a] * w;
+            T g = 0;
+            for (int c = 0; c < 3; c++)
+              g += dX[c * nq * nen + q * nen + a] * w * dX[c * nq * nen + q * nen + bn];
+            kij += lam * ak * dX[l * nq * nen + q * nen + bn] +
+                   mu * al * dX[k * nq * nen + q * nen + bn] + (k == l ? mu * g : T(0));
+          }
         }
+        acc -= S.c0[-ce - 1] * (double)kij;
       }
-      S.b[r - 1] -= S.c0[-ce - 1] * kij;
     }
+    if (sizeof(T) == sizeof(double)) S.b[r - 1] += acc;
+    else atomicAdd(S.b + r - 1, acc);
   }
 }
 
@@ -562,9 +660,9 @@ k_face_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ items
 }
 
 // ---------------------------------------------------------------------------
-size_t volumeSmem(const DevPatch& P)
+size_t volumeSmem(const DevPatch& P, size_t real)
 {
-  return sizeof(double) * ((size_t)P.nen * 4 + (size_t)P.nq * P.nen * 4 + (size_t)P.nq * 12) +
+  return real * ((size_t)P.nen * 4 + (size_t)P.nq * P.nen * 4 + (size_t)P.nq * 12) +
          sizeof(int) * (size_t)P.nen * P.npv;
 }
 
@@ -587,6 +685,8 @@ ifemgpu_status upload(ifemgpu_ctx* ctx, T** dst, const T* src, size_t n)
 ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
 {
   const int np = (int)ctx->patches.size();
+  const size_t realBytes = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 ? sizeof(float)
+                                                                          : sizeof(double);
   ctx->h_devpatches.assign(np, DevPatch{});
   std::vector<Item> vol, face;
   std::vector<double> neuVals;
@@ -656,8 +756,8 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
       IFEMGPU_TRY(upload(ctx, &pc.d_noise, pc.noise.data(), pc.noise.size()));
       D.noise = pc.d_noise;
     }
-    if (volumeSmem(D) > 227 * 1024)
-      return setError(ctx, IFEMGPU_UNSUPPORTED, "element too large for the FP64 kernel");
+    if (volumeSmem(D, realBytes) > 227 * 1024)
+      return setError(ctx, IFEMGPU_UNSUPPORTED, "element too large for the element kernel");
     const int nc = (pc.p[0] + 1) * (pc.p[1] + 1) * (pc.dim == 3 ? pc.p[2] + 1 : 1);
     maxColours = std::max(maxColours, nc);
   }
@@ -709,7 +809,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
       const HostPatch& pc = ctx->patches[pi];
       colourItems(pi, c, vol);
       pass.maxNd = std::max(pass.maxNd, pc.nen() * pc.npv);
-      pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi]));
+      pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi], realBytes));
     }
     pass.count = (int)vol.size() - pass.first;
     if (pass.count) ctx->passes.push_back(pass);
@@ -768,7 +868,11 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_counters, sizeof(unsigned long long) * 4));
   size_t maxSmem = 0;
   for (auto& p : ctx->passes) maxSmem = std::max(maxSmem, p.smem);
-  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_gen<double>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::min<size_t>(maxSmem, 227 * 1024)));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_gen<float>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::min<size_t>(maxSmem, 227 * 1024)));
   IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_face_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::min<size_t>(maxSmem, 227 * 1024)));
@@ -833,13 +937,15 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
     return IFEMGPU_OK;
   }
   SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
-            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters};
+            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore};
   for (const Pass& p : ctx->passes) {
     if ((p.face != 0) != (seg == 2)) continue;
     if (p.tc)
       IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
+    else if (!p.face && ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32)
+      k_volume_gen<float><<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
     else if (!p.face)
-      k_volume_fp64<<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
+      k_volume_gen<double><<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
     else
       k_face_fp64<<<p.count, 128, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first,
                                                ctx->d_neumann, S);
