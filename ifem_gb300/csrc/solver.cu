@@ -376,4 +376,149 @@ ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o, doubl
   return IFEMGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free FP64 solve (ifemgpu_solve_noalloc).  Its workspace is one
+// file-scope device array, the same on every call: 11 * 65,536 doubles for
+// the vectors plus the reduction partials, about 5.8 MB, held by every GPU
+// that loads the library.  Host code reaches it through the address that
+// cudaGetSymbolAddress returns for the current device (the array's name in
+// host code is only a host-side stand-in).
+constexpr int kNoAllocMaxEq = 65536;
+constexpr size_t kNoAllocWords = (size_t)kNoAllocMaxEq * 11 + 2 * kRedBlocks + 16;
+static __device__ __align__(256) double g_noallocWork[kNoAllocWords];
+constexpr int kMaxDevices = 64;
+static double* g_noallocAddr[kMaxDevices] = {};  // device address per device ordinal
+static double g_noallocScalar[2];                // pageable host copy of one reduced scalar
+
+static Work carveFrom(double* base, size_t n)
+{
+  Work w{};
+  w.x64 = base; base += n;
+  w.r64 = base; base += n;
+  w.d64 = base; base += n;
+  w.part = base; base += 2 * kRedBlocks;
+  w.scal = base; base += 16;
+  w.rD = base; base += n;
+  w.xD = base; base += n;
+  w.zD = base; base += n;
+  w.pD = base; base += n;
+  w.qD = base; base += n;
+  float* fb = reinterpret_cast<float*>(base);
+  w.r32 = fb; fb += n;
+  w.x32 = fb; fb += n;
+  w.z32 = fb; fb += n;
+  w.p32 = fb; fb += n;
+  w.q32 = fb; fb += n;
+  w.dinv32 = fb; fb += n;
+  return w;
+}
+
+// FP64 Jacobi-PCG of innerPCG with the convergence scalar read through a
+// caller-given host buffer instead of the context's pinned buffer.
+static ifemgpu_status innerPCG64(ifemgpu_ctx* ctx, const Work& w, double rtol, int maxit,
+                                 double* hostScalar, int* iters)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  k_pcg_start<double><<<vb, kThreads, 0, s>>>(w.r64, w.scal, 9, w.rD, w.xD, w.zD, w.pD, w.d64, n,
+                                              w.part);
+  k_finish<<<1, kThreads, 0, s>>>(w.part, vb, 1, w.scal + 0);
+  int it = 0;
+  while (it < maxit) {
+    for (int k = 0; k < 16 && it < maxit; k++, it++) {
+      k_spmv<double><<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K, w.pD, w.qD, n,
+                                             w.part);
+      k_finish<<<1, kThreads, 0, s>>>(w.part, sb, 1, w.scal + 1);
+      k_pcg_update<double><<<vb, kThreads, 0, s>>>(w.xD, w.rD, w.zD, w.pD, w.qD, w.d64, w.scal, n,
+                                                   w.part);
+      k_finish<<<1, kThreads, 0, s>>>(w.part, vb, 2, w.scal + 2);
+      k_pcg_dir<double><<<vb, kThreads, 0, s>>>(w.pD, w.zD, w.scal, n);
+      k_shift_scalars<<<1, 1, 0, s>>>(w.scal);
+    }
+    IFEMGPU_CUDA(ctx, cudaGetLastError());
+    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(hostScalar, w.scal + 3, sizeof(double),
+                                      cudaMemcpyDeviceToHost, s));
+    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+    const double rr = hostScalar[0];
+    if (!(rr == rr)) { *iters = it; return setError(ctx, IFEMGPU_NOT_CONVERGED, "PCG breakdown (NaN)"); }
+    if (std::sqrt(rr) <= rtol) break;
+  }
+  *iters = it;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status solveNoAlloc(ifemgpu_ctx* ctx, double rtol, int maxit, double* xh,
+                            ifemgpu_solve_info* info)
+{
+  const int n = ctx->neq;
+  if (n > kNoAllocMaxEq)
+    return setError(ctx, IFEMGPU_INVALID_ARG,
+                    "ifemgpu_solve_noalloc: more than 65536 equations (its fixed workspace)");
+  if (ctx->opts.device < 0 || ctx->opts.device >= kMaxDevices)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "ifemgpu_solve_noalloc: unsupported device ordinal");
+  if (n == 0) {
+    if (info) *info = ifemgpu_solve_info{0, 0, 0.0, 0.0};
+    return IFEMGPU_OK;
+  }
+  double*& base = g_noallocAddr[ctx->opts.device];
+  if (!base) IFEMGPU_CUDA(ctx, cudaGetSymbolAddress((void**)&base, g_noallocWork));
+  cudaStream_t s = ctx->stream;
+  const Work w = carveFrom(base, (size_t)n);
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  k_diag<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K,
+                                                              n, w.d64, w.dinv32);
+  // the accumulated solution starts at zero; every other workspace entry is
+  // written before it is read
+  IFEMGPU_CUDA(ctx, cudaMemsetAsync(w.x64, 0, sizeof(double) * n, s));
+  k_norm2<double><<<vb, kThreads, 0, s>>>(ctx->d_b, n, w.part);
+  k_finish<<<1, kThreads, 0, s>>>(w.part, vb, 1, w.scal + 8);
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.r64, ctx->d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.scal + 9, w.scal + 8, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(g_noallocScalar, w.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  const double bn = std::sqrt(g_noallocScalar[0]);
+  int inner = 0, outer = 0;
+  double relres = bn > 0 ? 1.0 : 0.0;
+  ifemgpu_status st = IFEMGPU_OK;
+  if (bn > 0) {
+    st = innerPCG64(ctx, w, rtol, maxit, g_noallocScalar, &inner);
+    outer = 1;
+    if (st == IFEMGPU_OK) {
+      k_accumulate<double><<<vb, kThreads, 0, s>>>(w.x64, w.xD, w.scal, 9, n);
+      k_residual<<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K, w.x64, ctx->d_b,
+                                         w.r64, n, w.part);
+      k_finish<<<1, kThreads, 0, s>>>(w.part, sb, 1, w.scal + 9);
+      IFEMGPU_CUDA(ctx, cudaGetLastError());
+      IFEMGPU_CUDA(ctx, cudaMemcpyAsync(g_noallocScalar, w.scal + 9, sizeof(double),
+                                        cudaMemcpyDeviceToHost, s));
+      IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+      relres = std::sqrt(g_noallocScalar[0]) / bn;
+    }
+  }
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(xh, w.x64, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+  if (info) *info = ifemgpu_solve_info{outer, inner, relres, (double)ms};
+  if (st != IFEMGPU_OK) return st;
+  if (bn > 0 && relres > rtol)
+    return setError(ctx, IFEMGPU_NOT_CONVERGED, "relative residual above tolerance");
+  return IFEMGPU_OK;
+}
+
 }  // namespace ifemgpu
+
+extern "C" ifemgpu_status ifemgpu_solve_noalloc(ifemgpu_ctx* ctx, double rtol, int max_iter,
+                                                double* x, ifemgpu_solve_info* info)
+{
+  if (!ctx || !x || max_iter < 1) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled)
+    return ifemgpu::setError(ctx, IFEMGPU_NOT_READY, "solve before assemble");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  return ifemgpu::solveNoAlloc(ctx, rtol, max_iter, x, info);
+}

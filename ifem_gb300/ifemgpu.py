@@ -63,7 +63,7 @@ EXPORTS = [
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
     "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_solve",
     "ifemgpu_expand_solution", "ifemgpu_patch_update_coefs", "ifemgpu_get_stream",
-    "ifemgpu_selftest_tc_gemm",
+    "ifemgpu_selftest_tc_gemm", "ifemgpu_solve_noalloc",
 ]
 
 
@@ -113,6 +113,7 @@ def load_library(path: str | None = None):
         "ifemgpu_patch_update_coefs": (I, [P, I, V]),
         "ifemgpu_get_stream": (I, [P, C.POINTER(C.c_void_p)]),
         "ifemgpu_selftest_tc_gemm": (I, [V, V, V]),
+        "ifemgpu_solve_noalloc": (I, [P, D, I, V, C.POINTER(SolveInfo)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -305,6 +306,16 @@ class SIM:
         if check:
             self._check(st)
         return x, info
+
+    def solve_noalloc(self, rtol=1e-10, max_iter=20000, check=True):
+        """FP64 Jacobi-PCG through the allocation-free entry point (fixed
+        library workspace, at most 65,536 equations)."""
+        x = np.zeros(self.sizes.neq, dtype=np.float64)
+        info = SolveInfo()
+        st = self.lib.ifemgpu_solve_noalloc(self.ctx, rtol, max_iter, _ptr(x), C.byref(info))
+        if check:
+            self._check(st)
+        return x, info, st
 
     def expand_solution(self, x: np.ndarray, scale: float = 1.0) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)

@@ -252,6 +252,27 @@ ifemgpu_status ifemgpu_solve(ifemgpu_ctx* ctx,
                              const ifemgpu_solver_options* opts, double* x,
                              ifemgpu_solve_info* info);
 
+/* FP64 Jacobi-PCG solve of the assembled system that allocates nothing, for
+ * callers that cannot allocate device or pinned host memory at solve time:
+ * an application that hands its whole device memory to its own pool, a
+ * time-stepping or Newton loop that must not synchronise on cudaMalloc, or a
+ * host framework that owns the allocator.  No IFEM counterpart: it is the
+ * IFEMGPU_PCG_FP64 branch of ifemgpu_solve with a fixed workspace.
+ *   - The workspace is a file-scope device array of the library, about
+ *     5.8 MB, held by every GPU that loads the library until the process
+ *     exits; it limits the system to 65,536 equations (larger systems are
+ *     rejected with IFEMGPU_INVALID_ARG).
+ *   - The first call on a device looks the array's device address up; make
+ *     that first call before any stream capture.
+ *   - All calls share the one array: calls that overlap on the GPU (two
+ *     contexts of one device on different streams, or from several host
+ *     threads) race and give wrong results.  Calls of one context are
+ *     ordered on its stream and are safe.
+ * rtol is the FP64 relative residual target, max_iter the PCG iteration cap,
+ * x (neq, host) receives the solution; info is optional.                   */
+ifemgpu_status ifemgpu_solve_noalloc(ifemgpu_ctx* ctx, double rtol, int max_iter,
+                                     double* x, ifemgpu_solve_info* info);
+
 /* Equation order -> DOF order, fixed DOFs 0 and prescribed DOFs their value
  * times scale; replaces SAM::expandSolution (src/LinAlg/SAM.C:768-810).   */
 ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
