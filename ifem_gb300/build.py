@@ -1,6 +1,6 @@
 """Build recipe of libifemgpu.so (CUDA sm_103a) -- plain nvcc, no cmake.
 
-The three translation units are compiled in parallel and linked into
+The translation units are compiled in parallel and linked into
 ``ifem_gb300/libifemgpu.so`` next to this file (in-tree, git-ignored).
 """
 from __future__ import annotations
@@ -16,7 +16,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libifemgpu.so")
 OBJDIR = os.path.join(HERE, "_build")
 
-SOURCES = ["host.cpp", "assembly.cu", "solver.cu", "tc_volume.cu"]
+SOURCES = ["host.cpp", "assembly.cu", "solver.cu", "tc_volume.cu", "learned.cu", "fdprec.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "-I", INCLUDE]
 

@@ -60,6 +60,12 @@ void gaussRule(int n, double* x, double* w)
   if (n % 2) x[n / 2] = 0.0;
 }
 
+}  // namespace
+
+void gaussLegendre(int n, double* x, double* w) { gaussRule(n, x, w); }
+
+namespace {
+
 int gaussCount(int nGauss, int order, bool neumann)
 {
   // ASMbase::getNoGaussPt semantics (src/ASM/ASMbase.C:1788-1798)

@@ -72,6 +72,10 @@ void freeDevice(ifemgpu_ctx* ctx)
   ctx->d_neumann = nullptr;
   ctx->d_counters = nullptr;
   freeSolver(ctx);
+  destroyLearn(ctx);
+  destroyFd(ctx);
+  f(ctx->d_rhsAlt);
+  ctx->d_rhsAlt = nullptr;
 }
 
 // Patch topology: ASMs3D::generateFEMTopology (src/ASM/ASMs3D.C:487-509).
@@ -650,6 +654,107 @@ ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
     int e = ctx->meqn[i];
     u[i] = e > 0 ? x[e - 1] : (e < 0 ? ctx->c0[-e - 1] * scale : 0.0);
   }
+  return IFEMGPU_OK;
+}
+
+// ---- learned coarse correction (learned.cu, solver.cu) ----------------------
+
+static ifemgpu_status deviceReady(ifemgpu_ctx* ctx)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed) return setError(ctx, IFEMGPU_NOT_READY, "not preprocessed");
+  if (ctx->opts.device < 0) return setError(ctx, IFEMGPU_NOT_READY, "host-only context (device -1)");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_learn_setup(ifemgpu_ctx* ctx, const ifemgpu_learn_options* o)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  if (!o) return setError(ctx, IFEMGPU_INVALID_ARG, "learn_setup: null options");
+  return learnSetup(ctx, o->coarse_cells, o->hidden, o->capacity, o->seed, o->field_inputs);
+}
+
+ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs, const double* xstar,
+                                     int stride, int max_iter, double rtol, int* pairs)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  if (!ctx->learn) return setError(ctx, IFEMGPU_NOT_READY, "learn_collect before learn_setup");
+  if (!rhs && !ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "learn_collect before assemble");
+  if (stride < 1 || max_iter < 1 || !(rtol > 0))
+    return setError(ctx, IFEMGPU_INVALID_ARG, "learn_collect: bad stride, cap or tolerance");
+  st = collectPairs(ctx, rhs, xstar, stride, max_iter, rtol);
+  if (pairs) *pairs = learnCount(ctx);
+  return st;
+}
+
+ifemgpu_status ifemgpu_learn_clear(ifemgpu_ctx* ctx)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  learnClear(ctx);
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_learn_train(ifemgpu_ctx* ctx, int epochs, int batch, float lr,
+                                   unsigned seed, float* final_loss)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  return learnTrain(ctx, epochs, batch, lr, seed, final_loss);
+}
+
+ifemgpu_status ifemgpu_learn_evaluate(ifemgpu_ctx* ctx, float* mse)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  return learnEvaluate(ctx, mse);
+}
+
+ifemgpu_status ifemgpu_learn_gradients(ifemgpu_ctx* ctx, const float* X, const float* Y, int n,
+                                       float* grad, float* loss)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  return learnGradients(ctx, X, Y, n, grad, loss);
+}
+
+ifemgpu_status ifemgpu_learn_get_weights(ifemgpu_ctx* ctx, float* theta, int* count, float* scale)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  return learnWeights(ctx, theta, count, scale, 0);
+}
+
+ifemgpu_status ifemgpu_learn_set_weights(ifemgpu_ctx* ctx, const float* theta, int count,
+                                         float scale)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  if (!theta) return setError(ctx, IFEMGPU_INVALID_ARG, "learn_set_weights: null array");
+  return learnWeights(ctx, const_cast<float*>(theta), &count, &scale, 1);
+}
+
+ifemgpu_status ifemgpu_patch_update_field(ifemgpu_ctx* ctx, int patch_id, int which,
+                                          const double* values)
+{
+  ifemgpu_status st = deviceReady(ctx);
+  if (st != IFEMGPU_OK) return st;
+  HostPatch* pc = getPatch(ctx, patch_id);
+  if (!pc || !values) return setError(ctx, IFEMGPU_INVALID_ARG, "update_field: bad patch or values");
+  std::vector<double>* host = nullptr;
+  double* dev = nullptr;
+  if (which == IFEMGPU_FIELD_LOG_KAPPA) { host = &pc->logk; dev = pc->d_logk; }
+  else if (which == IFEMGPU_FIELD_SOURCE_NOISE) { host = &pc->noise; dev = pc->d_noise; }
+  else return setError(ctx, IFEMGPU_INVALID_ARG, "update_field: unknown field");
+  if (host->empty() || !dev)
+    return setError(ctx, IFEMGPU_NOT_READY, "update_field: the field was not set before preprocess");
+  std::copy(values, values + host->size(), host->begin());
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaMemcpy(dev, host->data(), sizeof(double) * host->size(), cudaMemcpyHostToDevice));
+  ctx->assembled = false;
+  ctx->fieldVersion++;
   return IFEMGPU_OK;
 }
 

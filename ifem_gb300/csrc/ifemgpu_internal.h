@@ -126,6 +126,9 @@ struct Pass {
 bool tcSupports(const DevPatch& P);
 size_t tcVolumeSmem();
 
+struct LearnState;  // learned.cu
+struct FdState;     // fdprec.cu
+
 }  // namespace ifemgpu
 
 struct ifemgpu_ctx {
@@ -172,6 +175,19 @@ struct ifemgpu_ctx {
   double* d_work = nullptr;
   size_t work_len = 0;
   double* h_pinned = nullptr;
+  // captured inner-solve loops: [0] FP32 Jacobi-PCG, [1 + fine + 2 coarse] FP32
+  // flexible CG (fine: 0 Jacobi, 1 Kronecker; coarse: learned correction on)
+  static constexpr int kLoops = 5;
+  cudaGraphExec_t loopExec[kLoops] = {};
+  const void* loopKey[kLoops] = {};
+  int loopGen[kLoops] = {};
+  ifemgpu::FdState* fd = nullptr;  // Kronecker preconditioner (built on first use)
+  int workGen = 0;               // bumped whenever the solver workspace moves
+  // learned coarse correction
+  ifemgpu::LearnState* learn = nullptr;
+  int learnGen = 0;              // bumped by every setup
+  int fieldVersion = 0;          // bumped by every field update
+  double* d_rhsAlt = nullptr;    // right-hand side of a collecting solve (neq)
 };
 
 namespace ifemgpu {
@@ -190,8 +206,37 @@ ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid);
 
 // solver.cu
 ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o,
-                        double* x, ifemgpu_solve_info* info);
+                        double* x, ifemgpu_solve_info* info, const double* bdev = nullptr);
+ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* xstar,
+                            int stride, int maxit, double rtol);
 void freeSolver(ifemgpu_ctx* ctx);
+
+// learned.cu
+ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigned seed,
+                          int fieldInputs);
+ifemgpu_status learnPrepare(ifemgpu_ctx* ctx);
+void destroyLearn(ifemgpu_ctx* ctx);
+double* learnXstar(ifemgpu_ctx* ctx);
+ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx);
+ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* q,
+                          double* part, int nparts, unsigned* counter, double* dotOut,
+                          const double* guard);
+ifemgpu_status learnTrain(ifemgpu_ctx* ctx, int epochs, int B, float lr, unsigned seed,
+                          float* lossOut);
+ifemgpu_status learnEvaluate(ifemgpu_ctx* ctx, float* mse);
+ifemgpu_status learnGradients(ifemgpu_ctx* ctx, const float* X, const float* Y, int n,
+                              float* gradOut, float* lossOut);
+ifemgpu_status learnWeights(ifemgpu_ctx* ctx, float* theta, int* count, float* scale, int set);
+int learnCount(const ifemgpu_ctx* ctx);
+bool learnReady(const ifemgpu_ctx* ctx);
+void learnClear(ifemgpu_ctx* ctx);
+
+// fdprec.cu
+ifemgpu_status fdSetup(ifemgpu_ctx* ctx);
+void destroyFd(ifemgpu_ctx* ctx);
+ifemgpu_status fdRescale(ifemgpu_ctx* ctx, const double* dinv);
+ifemgpu_status fdApply(ifemgpu_ctx* ctx, const float* r, float* z, const double* guard);
+int fdLaunches(const ifemgpu_ctx* ctx);
 
 }  // namespace ifemgpu
 

@@ -1,0 +1,820 @@
+// learned.cu -- learned coarse correction of the flexible PCG solve.
+//
+// No IFEM counterpart (IFEM solves with SuperLU or a PETSc/ISTL Krylov
+// method).  For a patch with npv unknowns per node the correction works on a
+// coarse grid of (m+1)^3 vertices over the patch's parameter domain, npv
+// values per vertex (nc = npv (m+1)^3 coarse unknowns):
+//   restriction   rc_(v,c) = sum_e w_ve r_e     over the free equations e of
+//                                               component c; w_ve is the
+//                                               trilinear weight of vertex v
+//                                               at e's Greville point
+//   network       y = MLP([rc / |rc|, g])       3 layers, width nh, ReLU
+//   prolongation  z_e += S |rc| sum_v w_ve y_(v,c(e))
+// g (optional) is the patch's log-conductivity field restricted to the
+// coarse vertices, so that one network can serve many coefficient fields.
+// The network is trained by the kernels of this file on pairs
+// ([rc/|rc|, g], ec/|rc|), ec the weight-normalised restriction of the error
+// x* - x_k of plain PCG iterates; S, the RMS of the targets, keeps the
+// network's outputs of order one.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "ifemgpu_internal.h"
+#include "reduce.cuh"
+
+namespace ifemgpu {
+
+struct LearnState {
+  int m = 8;             // coarse cells per direction
+  int npv = 1;           // unknowns per node
+  int nc = 0;            // coarse unknowns, npv (m+1)^3
+  int nf = 0;            // field inputs: (m+1)^3 or 0
+  int nin = 0;           // network inputs, nc + nf
+  int nh = 256;          // hidden width
+  float* feat = nullptr; // nf: coarse log-conductivity of the current field
+  int featVersion = -1;  // field version the features were computed from
+  std::vector<int> featEq;     // per feature weight list: equations (component 0)
+  std::vector<float> featW;
+  std::vector<int> featPtr;
+  int nparam = 0;
+  int oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0;
+  // transfer operators
+  int* eqCell = nullptr;      // neq: coarse cell of the equation's Greville point
+  float4* eqFrac = nullptr;   // neq: position inside the cell (x, y, z), component (w)
+  int* vPtr = nullptr;        // nc+1: equations in the support of each coarse unknown
+  int* vEq = nullptr;
+  float* vW = nullptr;        // trilinear weights
+  float* vWn = nullptr;       // weights divided by their sum per coarse unknown
+  // network: FP32 master weights, BF16 copy for the solve
+  float* theta = nullptr;
+  float* grad = nullptr;
+  float* am = nullptr;
+  float* av = nullptr;
+  __nv_bfloat16* wbf = nullptr;
+  int adamStep = 0;
+  float scale = 1.f;          // S
+  bool trained = false;
+  // dataset
+  float* X = nullptr;
+  float* Y = nullptr;
+  int cap = 0, count = 0;
+  double* xstar = nullptr;    // neq: reference solution of the collecting solve
+  // training scratch (batch B)
+  int B = 0;
+  float *Xb = nullptr, *Yb = nullptr, *H1 = nullptr, *H2 = nullptr, *Yp = nullptr;
+  float *dH1 = nullptr, *dH2 = nullptr, *dY = nullptr, *loss = nullptr;
+  int* perm = nullptr;
+  // solve scratch
+  float *rc = nullptr, *h1 = nullptr, *h2 = nullptr, *yc = nullptr;
+  float* nrm = nullptr;        // [0] |rc| of the last restriction, [1] S
+};
+
+namespace {
+
+constexpr int kT = 256;
+
+__device__ inline bool stopped(const double* guard) { return guard && guard[0] != 0.0; }
+
+// ---- transfer kernels --------------------------------------------------------
+
+// rc = R r: warp per coarse unknown, fixed order (deterministic)
+__global__ void k_restrict(const int* __restrict__ vPtr, const int* __restrict__ vEq,
+                           const float* __restrict__ vW, const float* __restrict__ r,
+                           float* __restrict__ rc, int nc, const double* guard)
+{
+  if (stopped(guard)) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nc) return;
+  float s = 0.f;
+  for (int k = vPtr[warp] + lane; k < vPtr[warp + 1]; k += 32) s += vW[k] * r[vEq[k]];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) rc[warp] = s;
+}
+
+// ec = Rn (x* sx - x) for the error of an iterate
+__global__ void k_restrict_err(const int* __restrict__ vPtr, const int* __restrict__ vEq,
+                               const float* __restrict__ vWn, const double* __restrict__ xs,
+                               double sx, const float* __restrict__ x, float* __restrict__ ec,
+                               int nc)
+{
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nc) return;
+  float s = 0.f;
+  for (int k = vPtr[warp] + lane; k < vPtr[warp + 1]; k += 32) {
+    const int e = vEq[k];
+    s += vWn[k] * (float)(xs[e] * sx - (double)x[e]);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) ec[warp] = s;
+}
+
+__device__ float blockSumF(float v, float* sh)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float s = 0.f;
+  for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[i];
+  __syncthreads();
+  return s;  // every thread
+}
+
+// dataset row: X = [rc/|rc|, feat], Y = ec/|rc| (single block)
+__global__ void k_store_pair(const float* __restrict__ rc, const float* __restrict__ ec,
+                             const float* __restrict__ feat, float* __restrict__ X,
+                             float* __restrict__ Y, int nc, int nf)
+{
+  __shared__ float sh[32];
+  float s = 0.f;
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) s += rc[i] * rc[i];
+  const float n = sqrtf(blockSumF(s, sh));
+  const float inv = n > 0.f ? 1.f / n : 0.f;
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    X[i] = rc[i] * inv;
+    Y[i] = ec[i] * inv;
+  }
+  for (int i = threadIdx.x; i < nf; i += blockDim.x) X[nc + i] = feat[i];
+}
+
+// z_e += S |rc| sum_v w_ve y_(v,c); with q != 0 also (z, q): per-block
+// partials, summed in fixed order by the last block into *dotOut
+__global__ void __launch_bounds__(kT)
+k_prolong_add(const int* __restrict__ eqCell, const float4* __restrict__ eqFrac,
+              const float* __restrict__ y, const float* __restrict__ nrm, int m, int npv,
+              float* __restrict__ z, int n, const float* __restrict__ q, double* __restrict__ part,
+              unsigned* counter, double* dotOut, const double* guard)
+{
+  if (stopped(guard)) return;
+  __shared__ double sh[32];
+  const float sc = nrm[0] * nrm[1];  // |rc| S
+  const int m1 = m + 1;
+  double dot = 0.0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int c = eqCell[e];
+    const int ci = c % m, cj = (c / m) % m, ck = c / (m * m);
+    const float4 f = eqFrac[e];
+    const int comp = (int)f.w;
+    float s = 0.f;
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+      const int di = d & 1, dj = (d >> 1) & 1, dk = d >> 2;
+      const float w = (di ? f.x : 1.f - f.x) * (dj ? f.y : 1.f - f.y) * (dk ? f.z : 1.f - f.z);
+      s += w * y[(((ck + dk) * m1 + cj + dj) * m1 + ci + di) * npv + comp];
+    }
+    const float zi = z[e] + sc * s;
+    z[e] = zi;
+    if (q) dot += (double)zi * (double)q[e];
+  }
+  if (!q) return;
+  const double t = blockReduceSum(dot, sh);
+  if (lastBlockDone(part, t, counter)) {
+    const double v = finalSum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) *dotOut = v;
+  }
+}
+
+// ---- network kernels -----------------------------------------------------------
+
+// y = act(W [x / |x|, x2] + b) with |x| taken when normOut != 0 (first
+// layer; block 0 stores it), else y = act(W [x, x2] + b); W rows hold
+// cols + cols2 weights.  Warp per output row, BF16 weights, FP32 sums.
+__global__ void __launch_bounds__(kT)
+k_gemv_bf16(const __nv_bfloat16* __restrict__ W, const float* __restrict__ b,
+            const float* __restrict__ x, int cols, const float* __restrict__ x2, int cols2,
+            float* __restrict__ y, int rows, int relu, float* normOut, const double* guard)
+{
+  if (stopped(guard)) return;
+  __shared__ float sh[32];
+  float inv = 1.f;
+  if (normOut) {
+    float s = 0.f;
+    for (int i = threadIdx.x; i < cols; i += blockDim.x) s += x[i] * x[i];
+    const float nx = sqrtf(blockSumF(s, sh));
+    if (blockIdx.x == 0 && threadIdx.x == 0) normOut[0] = nx;
+    inv = nx > 0.f ? 1.f / nx : 0.f;
+  }
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= rows) return;
+  const __nv_bfloat16* w = W + (size_t)warp * (cols + cols2);
+  float s = 0.f, s2 = 0.f;
+  for (int k = lane; k < cols; k += 32) s = fmaf(__bfloat162float(w[k]), x[k], s);
+  for (int k = lane; k < cols2; k += 32) s2 = fmaf(__bfloat162float(w[cols + k]), x2[k], s2);
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+  }
+  if (lane == 0) {
+    const float v = s * inv + s2 + b[warp];
+    y[warp] = relu ? fmaxf(v, 0.f) : v;
+  }
+}
+
+__global__ void k_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = __float2bfloat16(a[i]);
+}
+
+// C (M x N) = op(A) op(B) (+ C when accumulate); row-major; op transposes
+// when its flag is set (A is M x K or K x M, B is K x N or N x K).  64 x 64
+// tiles, 16 x 16 threads of 4 x 4 outputs, K in steps of 16 through shared
+// memory.
+__global__ void __launch_bounds__(256)
+k_sgemm(const float* __restrict__ A, const float* __restrict__ B, float* __restrict__ C, int M,
+        int N, int K, int lda, int ldb, int ldc, int transA, int transB, int accumulate)
+{
+  __shared__ float As[16][64 + 4];
+  __shared__ float Bs[16][64 + 4];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  float acc[4][4] = {{0.f}};
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int i = threadIdx.x; i < 16 * 64; i += 256) {
+      int kk, mm;
+      if (transA) { kk = i / 64; mm = i % 64; }  // consecutive threads along m
+      else { mm = i / 16; kk = i % 16; }         // consecutive threads along k
+      const int gm = m0 + mm, gk = k0 + kk;
+      float va = 0.f;
+      if (gm < M && gk < K) va = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+      As[kk][mm] = va;
+      int kb, nn;
+      if (transB) { nn = i / 16; kb = i % 16; }
+      else { kb = i / 64; nn = i % 64; }
+      const int gn = n0 + nn, gkb = k0 + kb;
+      float vb = 0.f;
+      if (gn < N && gkb < K) vb = transB ? B[(size_t)gn * ldb + gkb] : B[(size_t)gkb * ldb + gn];
+      Bs[kb][nn] = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; kk++) {
+      float a[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        a[i] = As[kk][ty * 4 + i];
+        bv[i] = Bs[kk][tx * 4 + i];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+      if (gm < M && gn < N) {
+        float* c = C + (size_t)gm * ldc + gn;
+        *c = accumulate ? *c + acc[i][j] : acc[i][j];
+      }
+    }
+}
+
+// H = act(H + b) row-wise
+__global__ void k_bias_act(float* __restrict__ H, const float* __restrict__ b, int rows, int cols,
+                           int relu)
+{
+  const size_t n = (size_t)rows * cols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float v = H[i] + b[i % cols];
+    H[i] = relu ? fmaxf(v, 0.f) : v;
+  }
+}
+
+// dH *= (H > 0)
+__global__ void k_relu_back(float* __restrict__ dH, const float* __restrict__ H, size_t n)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    if (!(H[i] > 0.f)) dH[i] = 0.f;
+}
+
+// g = column sums of D (rows x cols), fixed order per column
+__global__ void k_colsum(const float* __restrict__ D, float* __restrict__ g, int rows, int cols)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (int r = 0; r < rows; r++) s += D[(size_t)r * cols + c];
+  g[c] = s;
+}
+
+// dY = 2 (Yp - Y/S) / n (when dY != 0), per-block partial sums of (Yp - Y/S)^2
+__global__ void k_mse(const float* __restrict__ Yp, const float* __restrict__ Y, float invS,
+                      float* __restrict__ dY, size_t n, float* __restrict__ part)
+{
+  __shared__ float sh[32];
+  float s = 0.f;
+  const float g = 2.f / (float)n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float d = Yp[i] - Y[i] * invS;
+    if (dY) dY[i] = d * g;
+    s += d * d;
+  }
+  const float t = blockSumF(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_adam(float* __restrict__ th, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, int n, float lr, float b1, float b2, float c1,
+                       float c2, float eps)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    th[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// batch rows gathered through a permutation
+__global__ void k_gather_rows(const float* __restrict__ src, const int* __restrict__ idx,
+                              float* __restrict__ dst, int rows, int cols)
+{
+  const size_t n = (size_t)rows * cols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    dst[i] = src[(size_t)idx[r] * cols + c];
+  }
+}
+
+__global__ void k_sum_sq(const float* __restrict__ v, size_t n, float* __restrict__ part)
+{
+  __shared__ float sh[32];
+  float s = 0.f;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    s += v[i] * v[i];
+  const float t = blockSumF(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+void sgemm(cudaStream_t s, const float* A, const float* B, float* C, int M, int N, int K, int lda,
+           int ldb, int ldc, int tA, int tB, int acc)
+{
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  k_sgemm<<<grid, 256, 0, s>>>(A, B, C, M, N, K, lda, ldb, ldc, tA, tB, acc);
+}
+
+void freeLearn(LearnState* L)
+{
+  void* ptrs[] = {L->eqCell, L->eqFrac, L->vPtr, L->vEq, L->vW, L->vWn, L->theta, L->grad,
+                  L->am, L->av, L->wbf, L->X, L->Y, L->xstar, L->Xb, L->Yb, L->H1, L->H2,
+                  L->Yp, L->dH1, L->dH2, L->dY, L->loss, L->perm, L->rc, L->h1, L->h2,
+                  L->yc, L->nrm, L->feat};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+constexpr int kLossParts = 128;
+
+// forward (+ backward when grad) of one batch of Bn rows in Xb/Yb; the
+// per-block loss partials go to L->loss[0..kLossParts)
+void batchPass(cudaStream_t s, LearnState* L, int Bn, float invS, bool grad)
+{
+  const int nc = L->nc, nh = L->nh, nin = L->nin;
+  const float* th = L->theta;
+  float* g = L->grad;
+  sgemm(s, L->Xb, th + L->oW1, L->H1, Bn, nh, nin, nin, nin, nh, 0, 1, 0);
+  k_bias_act<<<256, kT, 0, s>>>(L->H1, th + L->ob1, Bn, nh, 1);
+  sgemm(s, L->H1, th + L->oW2, L->H2, Bn, nh, nh, nh, nh, nh, 0, 1, 0);
+  k_bias_act<<<256, kT, 0, s>>>(L->H2, th + L->ob2, Bn, nh, 1);
+  sgemm(s, L->H2, th + L->oW3, L->Yp, Bn, nc, nh, nh, nh, nc, 0, 1, 0);
+  k_bias_act<<<256, kT, 0, s>>>(L->Yp, th + L->ob3, Bn, nc, 0);
+  k_mse<<<kLossParts, kT, 0, s>>>(L->Yp, L->Yb, invS, grad ? L->dY : nullptr, (size_t)Bn * nc,
+                                  L->loss);
+  if (!grad) return;
+  sgemm(s, L->dY, L->H2, g + L->oW3, nc, nh, Bn, nc, nh, nh, 1, 0, 0);
+  k_colsum<<<(nc + kT - 1) / kT, kT, 0, s>>>(L->dY, g + L->ob3, Bn, nc);
+  sgemm(s, L->dY, th + L->oW3, L->dH2, Bn, nh, nc, nc, nh, nh, 0, 0, 0);
+  k_relu_back<<<256, kT, 0, s>>>(L->dH2, L->H2, (size_t)Bn * nh);
+  sgemm(s, L->dH2, L->H1, g + L->oW2, nh, nh, Bn, nh, nh, nh, 1, 0, 0);
+  k_colsum<<<(nh + kT - 1) / kT, kT, 0, s>>>(L->dH2, g + L->ob2, Bn, nh);
+  sgemm(s, L->dH2, th + L->oW2, L->dH1, Bn, nh, nh, nh, nh, nh, 0, 0, 0);
+  k_relu_back<<<256, kT, 0, s>>>(L->dH1, L->H1, (size_t)Bn * nh);
+  sgemm(s, L->dH1, L->Xb, g + L->oW1, nh, nin, Bn, nh, nin, nin, 1, 0, 0);
+  k_colsum<<<(nh + kT - 1) / kT, kT, 0, s>>>(L->dH1, g + L->ob1, Bn, nh);
+}
+
+ifemgpu_status readLoss(ifemgpu_ctx* ctx, LearnState* L, double denom, double* out)
+{
+  float part[kLossParts];
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(part, L->loss, sizeof(part), cudaMemcpyDeviceToHost, ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double sl = 0.0;
+  for (float v : part) sl += v;
+  *out = sl / denom;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ensureBatch(ifemgpu_ctx* ctx, LearnState* L, int B)
+{
+  if (L->B >= B) return IFEMGPU_OK;
+  float** bufs[] = {&L->Xb, &L->Yb, &L->H1, &L->H2, &L->Yp, &L->dH1, &L->dH2, &L->dY};
+  for (float** p : bufs)
+    if (*p) { cudaFree(*p); *p = nullptr; }
+  L->B = 0;
+  const size_t nc = L->nc, nh = L->nh, nin = L->nin;
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->Xb, sizeof(float) * B * nin));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->Yb, sizeof(float) * B * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->Yp, sizeof(float) * B * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->dY, sizeof(float) * B * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->H1, sizeof(float) * B * nh));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->H2, sizeof(float) * B * nh));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->dH1, sizeof(float) * B * nh));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->dH2, sizeof(float) * B * nh));
+  L->B = B;
+  return IFEMGPU_OK;
+}
+
+}  // namespace
+
+void destroyLearn(ifemgpu_ctx* ctx)
+{
+  if (!ctx->learn) return;
+  freeLearn(ctx->learn);
+  delete ctx->learn;
+  ctx->learn = nullptr;
+}
+
+ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigned seed,
+                          int fieldInputs)
+{
+  if (ctx->patches.size() != 1)
+    return setError(ctx, IFEMGPU_UNSUPPORTED, "learned correction: one patch per context");
+  const HostPatch& pc = ctx->patches[0];
+  if (pc.dim != 3)
+    return setError(ctx, IFEMGPU_UNSUPPORTED, "learned correction: 3D patches");
+  if (m < 1 || m > 32 || nh < 8 || nh > 1024 || capacity < 1)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "learned correction: bad sizes");
+  if (fieldInputs && pc.logk.empty())
+    return setError(ctx, IFEMGPU_NOT_READY, "learned correction: field inputs without a log-conductivity field");
+  destroyLearn(ctx);
+  LearnState* L = new LearnState;
+  ctx->learn = L;
+  ctx->learnGen++;
+  L->m = m;
+  L->nh = nh;
+  L->npv = pc.npv;
+  const int nv = (m + 1) * (m + 1) * (m + 1);
+  L->nc = nv * pc.npv;
+  L->nf = fieldInputs ? nv : 0;
+  L->nin = L->nc + L->nf;
+  const int nc = L->nc, neq = ctx->neq, npv = pc.npv, nin = L->nin;
+  std::vector<std::vector<std::pair<int, float>>> flist(L->nf);
+  // coarse cell and trilinear weights of every free equation's Greville point
+  std::vector<double> gr[3];
+  for (int d = 0; d < 3; d++) {
+    const auto& U = pc.knots[d];
+    const int p = pc.p[d], n = pc.n[d];
+    const double u0 = U[p], u1 = U[n];
+    gr[d].resize(n);
+    for (int i = 0; i < n; i++) {
+      double s = 0.0;
+      for (int k = 1; k <= p; k++) s += U[i + k];
+      gr[d][i] = p > 0 ? (s / p - u0) / (u1 - u0) : 0.0;
+    }
+  }
+  std::vector<int> cell(neq, 0);
+  std::vector<float4> frac(neq, make_float4(0.f, 0.f, 0.f, 0.f));
+  std::vector<std::vector<std::pair<int, float>>> vlist(nc);
+  for (int node = 0; node < pc.nnod; node++) {
+    const int ii = node % pc.n[0], jj = (node / pc.n[0]) % pc.n[1],
+              kk = node / (pc.n[0] * pc.n[1]);
+    const double t[3] = {gr[0][ii] * m, gr[1][jj] * m, gr[2][kk] * m};
+    int c[3];
+    float f[3];
+    for (int d = 0; d < 3; d++) {
+      c[d] = std::min(m - 1, std::max(0, (int)std::floor(t[d])));
+      f[d] = (float)std::min(1.0, std::max(0.0, t[d] - c[d]));
+    }
+    for (int dd = 0; dd < 8 && L->nf; dd++) {  // field inputs: every control point
+      const int di = dd & 1, dj = (dd >> 1) & 1, dk = dd >> 2;
+      const float w = (di ? f[0] : 1.f - f[0]) * (dj ? f[1] : 1.f - f[1]) *
+                      (dk ? f[2] : 1.f - f[2]);
+      flist[((c[2] + dk) * (m + 1) + c[1] + dj) * (m + 1) + c[0] + di].push_back({node, w});
+    }
+    const int first = ctx->madof[pc.firstNode + node] - 1;
+    for (int comp = 0; comp < npv; comp++) {
+      const int eq = ctx->meqn[first + comp];
+      if (eq <= 0) continue;
+      cell[eq - 1] = (c[2] * m + c[1]) * m + c[0];
+      frac[eq - 1] = make_float4(f[0], f[1], f[2], (float)comp);
+      for (int dd = 0; dd < 8; dd++) {
+        const int di = dd & 1, dj = (dd >> 1) & 1, dk = dd >> 2;
+        const float w = (di ? f[0] : 1.f - f[0]) * (dj ? f[1] : 1.f - f[1]) *
+                        (dk ? f[2] : 1.f - f[2]);
+        const int v = ((c[2] + dk) * (m + 1) + c[1] + dj) * (m + 1) + c[0] + di;
+        vlist[v * npv + comp].push_back({eq - 1, w});
+      }
+    }
+  }
+  std::vector<int> vptr(nc + 1, 0), veq;
+  std::vector<float> vw, vwn;
+  for (int v = 0; v < nc; v++) {
+    double sw = 0.0;
+    for (auto& pr : vlist[v]) sw += pr.second;
+    for (auto& pr : vlist[v]) {
+      veq.push_back(pr.first);
+      vw.push_back(pr.second);
+      vwn.push_back(sw > 0 ? (float)(pr.second / sw) : 0.f);
+    }
+    vptr[v + 1] = (int)veq.size();
+  }
+  L->featPtr.assign(L->nf + 1, 0);
+  for (int v = 0; v < L->nf; v++) {
+    double sw = 0.0;
+    for (auto& pr : flist[v]) sw += pr.second;
+    for (auto& pr : flist[v]) {
+      L->featEq.push_back(pr.first);
+      L->featW.push_back(sw > 0 ? (float)(pr.second / sw) : 0.f);
+    }
+    L->featPtr[v + 1] = (int)L->featEq.size();
+  }
+  auto up = [&](auto** dst, const auto* src, size_t n) -> ifemgpu_status {
+    IFEMGPU_CUDA(ctx, cudaMalloc((void**)dst, sizeof(**dst) * std::max<size_t>(n, 1)));
+    if (n) IFEMGPU_CUDA(ctx, cudaMemcpy(*dst, src, sizeof(**dst) * n, cudaMemcpyHostToDevice));
+    return IFEMGPU_OK;
+  };
+  ifemgpu_status st;
+  if ((st = up(&L->eqCell, cell.data(), cell.size())) != IFEMGPU_OK) return st;
+  if ((st = up(&L->eqFrac, frac.data(), frac.size())) != IFEMGPU_OK) return st;
+  if ((st = up(&L->vPtr, vptr.data(), vptr.size())) != IFEMGPU_OK) return st;
+  if ((st = up(&L->vEq, veq.data(), veq.size())) != IFEMGPU_OK) return st;
+  if ((st = up(&L->vW, vw.data(), vw.size())) != IFEMGPU_OK) return st;
+  if ((st = up(&L->vWn, vwn.data(), vwn.size())) != IFEMGPU_OK) return st;
+  // parameters: W1 (nh x nin), b1, W2 (nh x nh), b2, W3 (nc x nh), b3; He
+  // initialisation from the seed, zero biases
+  L->oW1 = 0;
+  L->ob1 = L->oW1 + nh * nin;
+  L->oW2 = L->ob1 + nh;
+  L->ob2 = L->oW2 + nh * nh;
+  L->oW3 = L->ob2 + nh;
+  L->ob3 = L->oW3 + nc * nh;
+  L->nparam = L->ob3 + nc;
+  std::vector<float> th(L->nparam, 0.f);
+  std::mt19937 rng(seed);
+  auto fill = [&](int off, int count, double sd) {
+    std::normal_distribution<double> nd(0.0, sd);
+    for (int i = 0; i < count; i++) th[off + i] = (float)nd(rng);
+  };
+  fill(L->oW1, nh * nin, std::sqrt(2.0 / nin));
+  fill(L->oW2, nh * nh, std::sqrt(2.0 / nh));
+  fill(L->oW3, nc * nh, std::sqrt(1.0 / nh));
+  if ((st = up(&L->theta, th.data(), th.size())) != IFEMGPU_OK) return st;
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->grad, sizeof(float) * L->nparam));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->am, sizeof(float) * L->nparam));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->av, sizeof(float) * L->nparam));
+  IFEMGPU_CUDA(ctx, cudaMemset(L->am, 0, sizeof(float) * L->nparam));
+  IFEMGPU_CUDA(ctx, cudaMemset(L->av, 0, sizeof(float) * L->nparam));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->wbf, sizeof(__nv_bfloat16) * L->nparam));
+  L->cap = capacity;
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->X, sizeof(float) * (size_t)capacity * nin));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->Y, sizeof(float) * (size_t)capacity * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->feat, sizeof(float) * std::max(L->nf, 1)));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->xstar, sizeof(double) * std::max(neq, 1)));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->perm, sizeof(int) * capacity));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->loss, sizeof(float) * kLossParts));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->rc, sizeof(float) * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->yc, sizeof(float) * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->h1, sizeof(float) * nh));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->h2, sizeof(float) * nh));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->nrm, sizeof(float) * 4));
+  IFEMGPU_CUDA(ctx, cudaMemcpy(L->nrm + 1, &L->scale, sizeof(float), cudaMemcpyHostToDevice));
+  return IFEMGPU_OK;
+}
+
+double* learnXstar(ifemgpu_ctx* ctx) { return ctx->learn ? ctx->learn->xstar : nullptr; }
+
+// field inputs of the current log-conductivity field (host restriction,
+// uploaded when the field changed); call outside stream capture
+ifemgpu_status learnPrepare(ifemgpu_ctx* ctx)
+{
+  LearnState* L = ctx->learn;
+  if (!L || !L->nf || L->featVersion == ctx->fieldVersion) return IFEMGPU_OK;
+  const std::vector<double>& g = ctx->patches[0].logk;
+  std::vector<float> f(L->nf, 0.f);
+  for (int v = 0; v < L->nf; v++) {
+    double s = 0.0;
+    for (int k = L->featPtr[v]; k < L->featPtr[v + 1]; k++) s += L->featW[k] * g[L->featEq[k]];
+    f[v] = (float)s;
+  }
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaMemcpy(L->feat, f.data(), sizeof(float) * L->nf, cudaMemcpyHostToDevice));
+  L->featVersion = ctx->fieldVersion;
+  return IFEMGPU_OK;
+}
+
+// one plain-PCG iterate (r, x of the system scaled by sx) -> one pair
+ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx)
+{
+  LearnState* L = ctx->learn;
+  if (!L || L->count >= L->cap) return IFEMGPU_OK;
+  cudaStream_t s = ctx->stream;
+  const int nc = L->nc;
+  const int blocks = (nc * 32 + kT - 1) / kT;
+  k_restrict<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, L->rc, nc, nullptr);
+  k_restrict_err<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vWn, L->xstar, sx, x, L->yc, nc);
+  k_store_pair<<<1, kT, 0, s>>>(L->rc, L->yc, L->feat, L->X + (size_t)L->count * L->nin,
+                                L->Y + (size_t)L->count * nc, nc, L->nf);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  L->count++;
+  return IFEMGPU_OK;
+}
+
+// z += coarse correction of r with the BF16 network.  With q != 0 the
+// prolongation also forms (z, q) over its grid of nparts blocks and the last
+// block stores it in *dotOut.  Every kernel returns at once when *guard != 0.
+ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* q,
+                          double* part, int nparts, unsigned* counter, double* dotOut,
+                          const double* guard)
+{
+  LearnState* L = ctx->learn;
+  cudaStream_t s = ctx->stream;
+  const int nc = L->nc, nh = L->nh;
+  k_restrict<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, L->rc, nc, guard);
+  k_gemv_bf16<<<(nh * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW1, L->theta + L->ob1, L->rc,
+                                                      nc, L->feat, L->nf, L->h1, nh, 1, L->nrm,
+                                                      guard);
+  k_gemv_bf16<<<(nh * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW2, L->theta + L->ob2, L->h1,
+                                                      nh, nullptr, 0, L->h2, nh, 1, nullptr, guard);
+  k_gemv_bf16<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW3, L->theta + L->ob3, L->h2,
+                                                      nh, nullptr, 0, L->yc, nc, 0, nullptr, guard);
+  k_prolong_add<<<nparts, kT, 0, s>>>(L->eqCell, L->eqFrac, L->yc, L->nrm, L->m, L->npv,
+                                      z, ctx->neq, q, part, counter, dotOut, guard);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status learnTrain(ifemgpu_ctx* ctx, int epochs, int B, float lr, unsigned seed,
+                          float* lossOut)
+{
+  LearnState* L = ctx->learn;
+  if (!L || L->count < 1) return setError(ctx, IFEMGPU_NOT_READY, "no training pairs collected");
+  if (epochs < 0 || B < 1 || !(lr > 0.f))
+    return setError(ctx, IFEMGPU_INVALID_ARG, "learn_train: bad arguments");
+  const int N = L->count, nc = L->nc;
+  B = std::min(B, N);
+  ifemgpu_status st = ensureBatch(ctx, L, B);
+  if (st != IFEMGPU_OK) return st;
+  cudaStream_t s = ctx->stream;
+  // S = RMS of the targets
+  k_sum_sq<<<kLossParts, kT, 0, s>>>(L->Y, (size_t)N * nc, L->loss);
+  double ms = 0.0;
+  if ((st = readLoss(ctx, L, (double)N * nc, &ms)) != IFEMGPU_OK) return st;
+  L->scale = ms > 0 ? (float)std::sqrt(ms) : 1.f;
+  IFEMGPU_CUDA(ctx, cudaMemcpy(L->nrm + 1, &L->scale, sizeof(float), cudaMemcpyHostToDevice));
+  std::mt19937 rng(seed);
+  std::vector<int> perm(N);
+  double lastLoss = 0.0;
+  const float b1 = 0.9f, b2 = 0.999f;
+  for (int ep = 0; ep < epochs; ep++) {
+    for (int i = 0; i < N; i++) perm[i] = i;
+    std::shuffle(perm.begin(), perm.end(), rng);
+    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(L->perm, perm.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s));
+    for (int b0 = 0; b0 + B <= N; b0 += B) {
+      k_gather_rows<<<256, kT, 0, s>>>(L->X, L->perm + b0, L->Xb, B, L->nin);
+      k_gather_rows<<<256, kT, 0, s>>>(L->Y, L->perm + b0, L->Yb, B, nc);
+      batchPass(s, L, B, 1.f / L->scale, true);
+      L->adamStep++;
+      const float c1 = 1.f - std::pow(b1, (float)L->adamStep);
+      const float c2 = 1.f - std::pow(b2, (float)L->adamStep);
+      k_adam<<<512, kT, 0, s>>>(L->theta, L->grad, L->am, L->av, L->nparam, lr, b1, b2, c1, c2, 1e-8f);
+    }
+    if (ep == epochs - 1) {  // loss of the epoch's last batch
+      if ((st = readLoss(ctx, L, (double)B * nc, &lastLoss)) != IFEMGPU_OK) return st;
+    }
+    // the host permutation is rewritten next epoch: wait for its copy
+    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  }
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  k_to_bf16<<<512, kT, 0, s>>>(L->theta, L->wbf, L->nparam);
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  L->trained = true;
+  if (lossOut) *lossOut = (float)lastLoss;
+  return IFEMGPU_OK;
+}
+
+// mean squared error of the FP32 network on the collected pairs, targets in units of S
+ifemgpu_status learnEvaluate(ifemgpu_ctx* ctx, float* mse)
+{
+  LearnState* L = ctx->learn;
+  if (!L || L->count < 1) return setError(ctx, IFEMGPU_NOT_READY, "no pairs collected");
+  const int N = L->count, nc = L->nc;
+  const int B = std::min(N, 1024);
+  ifemgpu_status st = ensureBatch(ctx, L, B);
+  if (st != IFEMGPU_OK) return st;
+  cudaStream_t s = ctx->stream;
+  double total = 0.0;
+  std::vector<int> idx(B);
+  for (int b0 = 0; b0 < N; b0 += B) {
+    const int nb = std::min(B, N - b0);
+    for (int i = 0; i < nb; i++) idx[i] = b0 + i;
+    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(L->perm, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+    k_gather_rows<<<256, kT, 0, s>>>(L->X, L->perm, L->Xb, nb, L->nin);
+    k_gather_rows<<<256, kT, 0, s>>>(L->Y, L->perm, L->Yb, nb, nc);
+    batchPass(s, L, nb, 1.f / L->scale, false);
+    double l = 0.0;
+    if ((st = readLoss(ctx, L, 1.0, &l)) != IFEMGPU_OK) return st;  // also waits for idx
+    total += l;
+  }
+  if (mse) *mse = (float)(total / ((double)N * nc));
+  return IFEMGPU_OK;
+}
+
+// loss mean((Yp - Y)^2) and its gradient for host pairs (targets unscaled)
+ifemgpu_status learnGradients(ifemgpu_ctx* ctx, const float* X, const float* Y, int n,
+                              float* gradOut, float* lossOut)
+{
+  LearnState* L = ctx->learn;
+  if (!L) return setError(ctx, IFEMGPU_NOT_READY, "learned correction not set up");
+  if (n < 1 || !X || !Y) return setError(ctx, IFEMGPU_INVALID_ARG, "learn_gradients: bad arguments");
+  ifemgpu_status st = ensureBatch(ctx, L, n);
+  if (st != IFEMGPU_OK) return st;
+  cudaStream_t s = ctx->stream;
+  const int nc = L->nc;
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(L->Xb, X, sizeof(float) * (size_t)n * L->nin, cudaMemcpyHostToDevice, s));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(L->Yb, Y, sizeof(float) * (size_t)n * nc, cudaMemcpyHostToDevice, s));
+  batchPass(s, L, n, 1.f, true);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  double l = 0.0;
+  if ((st = readLoss(ctx, L, (double)n * nc, &l)) != IFEMGPU_OK) return st;
+  if (gradOut)
+    IFEMGPU_CUDA(ctx, cudaMemcpy(gradOut, L->grad, sizeof(float) * L->nparam, cudaMemcpyDeviceToHost));
+  if (lossOut) *lossOut = (float)l;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status learnWeights(ifemgpu_ctx* ctx, float* theta, int* count, float* scale, int set)
+{
+  LearnState* L = ctx->learn;
+  if (!L) return setError(ctx, IFEMGPU_NOT_READY, "learned correction not set up");
+  if (set && count && *count != L->nparam)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "learn_weights: parameter count mismatch");
+  if (count) *count = L->nparam;
+  if (!theta) return IFEMGPU_OK;
+  if (set) {
+    IFEMGPU_CUDA(ctx, cudaMemcpy(L->theta, theta, sizeof(float) * L->nparam, cudaMemcpyHostToDevice));
+    if (scale) L->scale = *scale;
+    IFEMGPU_CUDA(ctx, cudaMemcpy(L->nrm + 1, &L->scale, sizeof(float), cudaMemcpyHostToDevice));
+    k_to_bf16<<<512, kT, 0, ctx->stream>>>(L->theta, L->wbf, L->nparam);
+    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    L->trained = true;
+  } else {
+    IFEMGPU_CUDA(ctx, cudaMemcpy(theta, L->theta, sizeof(float) * L->nparam, cudaMemcpyDeviceToHost));
+    if (scale) *scale = L->scale;
+  }
+  return IFEMGPU_OK;
+}
+
+int learnCount(const ifemgpu_ctx* ctx) { return ctx->learn ? ctx->learn->count : 0; }
+bool learnReady(const ifemgpu_ctx* ctx) { return ctx->learn && ctx->learn->trained; }
+void learnClear(ifemgpu_ctx* ctx)
+{
+  if (ctx->learn) ctx->learn->count = 0;
+}
+
+}  // namespace ifemgpu
+
+extern "C" ifemgpu_status ifemgpu_learn_info(const ifemgpu_ctx* ctx, int* coarse_unknowns,
+                                             int* inputs, int* hidden, int* nparam, int* pairs)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  const ifemgpu::LearnState* L = ctx->learn;
+  if (!L) return IFEMGPU_NOT_READY;
+  if (coarse_unknowns) *coarse_unknowns = L->nc;
+  if (inputs) *inputs = L->nin;
+  if (hidden) *hidden = L->nh;
+  if (nparam) *nparam = L->nparam;
+  if (pairs) *pairs = L->count;
+  return IFEMGPU_OK;
+}
+
+extern "C" ifemgpu_status ifemgpu_learn_get_pairs(ifemgpu_ctx* ctx, int first, int count,
+                                                  float* X, float* Y)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  const ifemgpu::LearnState* L = ctx->learn;
+  if (!L) return ifemgpu::setError(ctx, IFEMGPU_NOT_READY, "learned correction not set up");
+  if (first < 0 || count < 0 || first + count > L->count || !X || !Y)
+    return ifemgpu::setError(ctx, IFEMGPU_INVALID_ARG, "learn_get_pairs: bad range or arrays");
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaMemcpy(X, L->X + (size_t)first * L->nin, sizeof(float) * (size_t)count * L->nin,
+                               cudaMemcpyDeviceToHost));
+  IFEMGPU_CUDA(ctx, cudaMemcpy(Y, L->Y + (size_t)first * L->nc, sizeof(float) * (size_t)count * L->nc,
+                               cudaMemcpyDeviceToHost));
+  return IFEMGPU_OK;
+}

@@ -15,8 +15,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <vector>
 
 #include "ifemgpu_internal.h"
+#include "reduce.cuh"
 
 namespace ifemgpu {
 
@@ -222,9 +224,251 @@ __global__ void k_accumulate(double* __restrict__ x, const T* __restrict__ d,
     x[i] += sc * (double)d[i];
 }
 
+// ---- kernels of the captured inner loops --------------------------------------
+// The loops run as CUDA graphs of kLoopBlock iterations.  Their scalars live
+// on the device; the kernel that updates the residual sets S_DONE once the
+// recurrence residual reaches the tolerance (or the iteration cap, or NaN),
+// after which every later kernel of the graph returns at once.  Dot products
+// finish inside the kernel that forms them (last-block reduction).
+enum : int {
+  S_RZ = 0, S_PQ = 1, S_RZN = 2, S_RR = 3, S_DONE = 4, S_ITS = 5, S_TOL2 = 6, S_MAXIT = 7,
+  // [8] ||b||^2 and [9] the refinement residual^2 belong to runSolve
+  S_PR = 10, S_ZQ = 11,
+  S_STAG = 12, S_RREF = 13, S_ITREF = 14,  // stagnation test (learned loops)
+  S_CNT = 24  // [24..28): eight unsigned ticket counters
+};
+constexpr int kScal = 32;
+constexpr int kLoopBlock = 8;
+constexpr int kStagWindow = 32;      // iterations per stagnation test
+constexpr double kStagFactor = 0.25; // required reduction of ||r||^2 per window
+
+// S_DONE: 1 converged or capped, 2 NaN, 3 stagnated
+__device__ inline unsigned* tickets(double* s) { return reinterpret_cast<unsigned*>(s + S_CNT); }
+__device__ inline bool loopStopped(const double* s) { return s[S_DONE] != 0.0; }
+
+__global__ void k_loop_init(double* s, double tol2, double maxit, double stagnation)
+{
+  s[S_DONE] = 0.0;
+  s[S_ITS] = 0.0;
+  s[S_TOL2] = tol2;
+  s[S_MAXIT] = maxit;
+  s[S_PQ] = 1.0;
+  s[S_ZQ] = 0.0;
+  s[S_STAG] = stagnation;
+  s[S_RREF] = 1.0;  // the loops start from a unit right-hand side
+  s[S_ITREF] = 0.0;
+  unsigned* c = tickets(s);
+  for (int i = 0; i < 8; i++) c[i] = 0u;
+}
+
+// after a residual update: count the iteration, stop on convergence, cap,
+// NaN or (when enabled) too little progress over the last window
+__device__ inline void loopCheck(double* s, double rr)
+{
+  s[S_RR] = rr;
+  const double its = s[S_ITS] + 1.0;
+  s[S_ITS] = its;
+  if (!(rr == rr)) {
+    s[S_DONE] = 2.0;
+  } else if (rr <= s[S_TOL2] || its >= s[S_MAXIT]) {
+    s[S_DONE] = 1.0;
+  } else if (s[S_STAG] != 0.0 && its - s[S_ITREF] >= kStagWindow) {
+    if (rr > kStagFactor * s[S_RREF]) {
+      s[S_DONE] = 3.0;
+    } else {
+      s[S_RREF] = rr;
+      s[S_ITREF] = its;
+    }
+  }
+}
+
+// rhs = r64 / sqrt(scal[9]); x = 0; z = Dinv r; p = z; rz -> S_RZ, S_RZN
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+g_pcg_start(const double* __restrict__ r64, double* s, T* __restrict__ r, T* __restrict__ x,
+            T* __restrict__ z, T* __restrict__ p, const T* __restrict__ dinv, int n,
+            double* __restrict__ part)
+{
+  __shared__ double sh[32];
+  const double inv = 1.0 / sqrt(s[9]);
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const T ri = (T)(r64[i] * inv);
+    const T zi = dinv[i] * ri;
+    r[i] = ri;
+    x[i] = 0;
+    z[i] = zi;
+    p[i] = zi;
+    acc += (double)ri * (double)zi;
+  }
+  const double t = blockReduceSum(acc, sh);
+  if (lastBlockDone(part, t, tickets(s) + 4)) {
+    const double v = finalSum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) s[S_RZ] = s[S_RZN] = v;
+  }
+}
+
+// q = A p (warp per row); (p, q) -> S_PQ; with shift also S_RZ <- S_RZN
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+g_spmv(const int* __restrict__ colptr, const int* __restrict__ rowidx, const T* __restrict__ A,
+       const T* __restrict__ p, T* __restrict__ q, int n, double* __restrict__ part, double* s,
+       int shift)
+{
+  if (loopStopped(s)) return;
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31;
+  const int warpsPerGrid = gridDim.x * (blockDim.x >> 5);
+  double dot = 0.0;
+  for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += warpsPerGrid) {
+    const int b = colptr[row], e = colptr[row + 1];
+    T acc = 0;
+    for (int k = b + lane; k < e; k += 32) acc += A[k] * p[rowidx[k]];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      q[row] = acc;
+      dot += (double)acc * (double)p[row];
+    }
+  }
+  const double t = blockReduceSum(dot, sh);
+  if (lastBlockDone(part, t, tickets(s) + 0)) {
+    const double v = finalSum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      s[S_PQ] = v;
+      if (shift) s[S_RZ] = s[S_RZN];
+    }
+  }
+}
+
+// x += a p; r -= a q; z = Dinv r with a = rz / pq; (r, z) -> S_RZN, (r, r) -> check
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+g_pcg_update(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
+             const T* __restrict__ q, const T* __restrict__ dinv, double* s, int n,
+             double* __restrict__ part)
+{
+  if (loopStopped(s)) return;
+  __shared__ double sh[32];
+  const T alpha = (T)(s[S_RZ] / s[S_PQ]);
+  double a1 = 0.0, a2 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const T ri = r[i] - alpha * q[i];
+    const T zi = dinv[i] * ri;
+    r[i] = ri;
+    z[i] = zi;
+    a1 += (double)ri * (double)zi;
+    a2 += (double)ri * (double)ri;
+  }
+  const double t1 = blockReduceSum(a1, sh);
+  const double t2 = blockReduceSum(a2, sh);
+  if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = t2;
+  if (lastBlockDone(part, t1, tickets(s) + 1)) {
+    const double rz = finalSum(part, gridDim.x, sh);
+    const double rr = finalSum(part + gridDim.x, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      s[S_RZN] = rz;
+      loopCheck(s, rr);
+    }
+  }
+}
+
+// p = z + (rz_new / rz) p
+template <typename T>
+__global__ void g_pcg_dir(T* __restrict__ p, const T* __restrict__ z, const double* s, int n)
+{
+  if (loopStopped(s)) return;
+  const T beta = (T)(s[S_RZN] / s[S_RZ]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+// flexible CG (Notay's FCG(1)): rhs = r64 / sqrt(scal[9]); x = p = q = 0; z = Dinv r
+__global__ void g_fcg_start(const double* __restrict__ r64, const double* s, float* __restrict__ r,
+                            float* __restrict__ x, float* __restrict__ z, float* __restrict__ p,
+                            float* __restrict__ q, const float* __restrict__ dinv, int n)
+{
+  const double inv = 1.0 / sqrt(s[9]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float ri = (float)(r64[i] * inv);
+    r[i] = ri;
+    x[i] = 0.f;
+    z[i] = dinv[i] * ri;
+    p[i] = 0.f;
+    q[i] = 0.f;
+  }
+}
+
+// x += a p; r -= a q; z = Dinv r with a = (p, r) / (p, q); (r, r) -> check
+__global__ void __launch_bounds__(kThreads)
+g_fcg_update(float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
+             const float* __restrict__ p, const float* __restrict__ q,
+             const float* __restrict__ dinv, double* s, int n, double* __restrict__ part)
+{
+  if (loopStopped(s)) return;
+  __shared__ double sh[32];
+  const float alpha = (float)(s[S_PR] / s[S_PQ]);
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const float ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    z[i] = dinv[i] * ri;
+    acc += (double)ri * (double)ri;
+  }
+  const double t = blockReduceSum(acc, sh);
+  if (lastBlockDone(part, t, tickets(s) + 1)) {
+    const double rr = finalSum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) loopCheck(s, rr);
+  }
+}
+
+// p = z - ((z, q) / (p, q)) p, q = A p of the previous direction; (p, r) -> S_PR
+__global__ void __launch_bounds__(kThreads)
+g_fcg_dir(float* __restrict__ p, const float* __restrict__ z, const float* __restrict__ r,
+          double* s, int n, double* __restrict__ part)
+{
+  if (loopStopped(s)) return;
+  __shared__ double sh[32];
+  const float beta = (float)(-s[S_ZQ] / s[S_PQ]);
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float pi = z[i] + beta * p[i];
+    p[i] = pi;
+    acc += (double)pi * (double)r[i];
+  }
+  const double t = blockReduceSum(acc, sh);
+  if (lastBlockDone(part, t, tickets(s) + 3)) {
+    const double v = finalSum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) s[S_PR] = v;
+  }
+}
+
+// (a, b) -> *out
+__global__ void __launch_bounds__(kThreads)
+g_dot(const float* __restrict__ a, const float* __restrict__ b, int n, double* __restrict__ part,
+      unsigned* counter, double* out, const double* s)
+{
+  if (loopStopped(s)) return;
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    acc += (double)a[i] * (double)b[i];
+  const double t = blockReduceSum(acc, sh);
+  if (lastBlockDone(part, t, counter)) {
+    const double v = finalSum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) *out = v;
+  }
+}
+
+__global__ void k_copy_d(const double* __restrict__ a, double* __restrict__ b, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+
 }  // namespace
 
-// Workspace layout (doubles): x64, r64, dinv64 | part (2*kRedBlocks) | scal(16)
+// Workspace layout (doubles): x64, r64, dinv64 | part (2*kRedBlocks) | scal(kScal)
 // then typed vectors for the inner PCG (FP32: 6 n floats; FP64: 5 n doubles)
 struct Work {
   double *x64, *r64, *d64, *part, *scal;
@@ -241,7 +485,7 @@ static Work carve(ifemgpu_ctx* ctx)
   w.r64 = base; base += n;
   w.d64 = base; base += n;
   w.part = base; base += 2 * kRedBlocks;
-  w.scal = base; base += 16;
+  w.scal = base; base += kScal;
   w.rD = base; base += n;
   w.xD = base; base += n;
   w.zD = base; base += n;
@@ -257,8 +501,19 @@ static Work carve(ifemgpu_ctx* ctx)
   return w;
 }
 
+static void dropLoopGraphs(ifemgpu_ctx* ctx)
+{
+  for (int g = 0; g < 3; g++) {
+    if (ctx->loopExec[g]) cudaGraphExecDestroy(ctx->loopExec[g]);
+    ctx->loopExec[g] = nullptr;
+    ctx->loopKey[g] = nullptr;
+  }
+  ctx->workGen++;
+}
+
 void freeSolver(ifemgpu_ctx* ctx)
 {
+  dropLoopGraphs(ctx);
   if (ctx->d_K32) cudaFree(ctx->d_K32);
   if (ctx->d_work) cudaFree(ctx->d_work);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
@@ -302,77 +557,376 @@ static ifemgpu_status innerPCG(ifemgpu_ctx* ctx, const Work& w, const T* A, cons
   return IFEMGPU_OK;
 }
 
-ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o, double* xh,
-                        ifemgpu_solve_info* info)
+// Captures kLoopBlock iterations of body into the slot's graph, once per
+// workspace (and network) generation.
+template <typename Body>
+static ifemgpu_status captureLoop(ifemgpu_ctx* ctx, int slot, int gen, Body body)
 {
-  const int n = ctx->neq;
-  cudaStream_t s = ctx->stream;
-  if (n == 0) {
-    if (info) *info = ifemgpu_solve_info{0, 0, 0.0, 0.0};
+  if (ctx->loopExec[slot] && ctx->loopKey[slot] == ctx->d_work && ctx->loopGen[slot] == gen)
     return IFEMGPU_OK;
+  if (ctx->loopExec[slot]) cudaGraphExecDestroy(ctx->loopExec[slot]);
+  ctx->loopExec[slot] = nullptr;
+  cudaStream_t s = ctx->stream;
+  IFEMGPU_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  ifemgpu_status st = IFEMGPU_OK;
+  for (int k = 0; k < kLoopBlock && st == IFEMGPU_OK; k++) st = body();
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (st == IFEMGPU_OK && e != cudaSuccess) st = cudaFail(ctx, e, "cudaStreamEndCapture");
+  if (st == IFEMGPU_OK) {
+    const cudaError_t e2 = cudaGraphInstantiate(&ctx->loopExec[slot], g, 0);
+    if (e2 != cudaSuccess) {
+      ctx->loopExec[slot] = nullptr;
+      st = cudaFail(ctx, e2, "cudaGraphInstantiate");
+    }
   }
-  const size_t need = sizeof(double) * ((size_t)n * 8 + 2 * kRedBlocks + 16) + sizeof(float) * (size_t)n * 6;
+  if (g) cudaGraphDestroy(g);
+  if (st != IFEMGPU_OK) return st;
+  ctx->loopKey[slot] = ctx->d_work;
+  ctx->loopGen[slot] = gen;
+  return IFEMGPU_OK;
+}
+
+// Replays a captured loop until its stop flag is set (bounded by the cap).
+static ifemgpu_status replayLoop(ifemgpu_ctx* ctx, const Work& w, int slot, int maxit,
+                                 int* iters, int* flag)
+{
+  cudaStream_t s = ctx->stream;
+  double* h = ctx->h_pinned;
+  h[1] = 0.0;
+  h[2] = 0.0;
+  const int maxLaunch = maxit / kLoopBlock + 2;
+  for (int l = 0; l < maxLaunch; l++) {
+    IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->loopExec[slot], s));
+    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(h, w.scal + S_RR, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+    if (h[1] != 0.0) break;  // S_DONE
+  }
+  *iters = (int)h[2];        // S_ITS
+  *flag = (int)h[1];
+  return IFEMGPU_OK;
+}
+
+static inline unsigned* hostTickets(const Work& w)
+{
+  return reinterpret_cast<unsigned*>(w.scal + S_CNT);
+}
+
+// FP32 Jacobi-PCG on rhs r64 / sqrt(scal[9]) from x = 0 (captured loop)
+static ifemgpu_status loopPCG32(ifemgpu_ctx* ctx, const Work& w, double rtol, int maxit,
+                                int* iters)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  auto body = [&]() -> ifemgpu_status {
+    g_spmv<float><<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, w.p32, w.q32,
+                                          n, w.part, w.scal, 1);
+    g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32,
+                                                w.scal, n, w.part);
+    g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
+    IFEMGPU_CUDA(ctx, cudaGetLastError());
+    return IFEMGPU_OK;
+  };
+  ifemgpu_status st = captureLoop(ctx, 0, ctx->workGen, body);
+  if (st != IFEMGPU_OK) return st;
+  k_loop_init<<<1, 1, 0, s>>>(w.scal, rtol * rtol, (double)maxit, 0.0);
+  g_pcg_start<float><<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.dinv32,
+                                             n, w.part);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  int flag = 0;
+  if ((st = replayLoop(ctx, w, 0, maxit, iters, &flag)) != IFEMGPU_OK) return st;
+  if (flag == 2) return setError(ctx, IFEMGPU_NOT_CONVERGED, "PCG breakdown (NaN)");
+  return IFEMGPU_OK;
+}
+
+// FP32 flexible CG (captured loop).  Preconditioner: the fine level (Jacobi,
+// or the Kronecker preconditioner when kron) plus, when learned, the network's
+// coarse correction.  *nan is set when the recurrence produced NaN.
+static ifemgpu_status loopFCG(ifemgpu_ctx* ctx, const Work& w, bool kron, bool learned,
+                              double rtol, int maxit, int* iters, bool* nan)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  unsigned* tk = hostTickets(w);
+  const double* guard = w.scal + S_DONE;
+  // z = M r after the Jacobi step of the update kernel; (z, q) -> S_ZQ
+  auto precondition = [&](bool withDot) -> ifemgpu_status {
+    ifemgpu_status st2;
+    if (kron && (st2 = fdApply(ctx, w.r32, w.z32, guard)) != IFEMGPU_OK) return st2;
+    if (learned)
+      return learnApply(ctx, w.r32, w.z32, withDot ? w.q32 : nullptr, w.part, vb, tk + 2,
+                        w.scal + S_ZQ, guard);
+    if (withDot) g_dot<<<vb, kThreads, 0, s>>>(w.z32, w.q32, n, w.part, tk + 2, w.scal + S_ZQ, w.scal);
+    return IFEMGPU_OK;
+  };
+  auto body = [&]() -> ifemgpu_status {
+    g_spmv<float><<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, w.p32, w.q32,
+                                          n, w.part, w.scal, 0);
+    g_fcg_update<<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32, w.scal, n,
+                                         w.part);
+    ifemgpu_status st2 = precondition(true);
+    if (st2 != IFEMGPU_OK) return st2;
+    g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
+    IFEMGPU_CUDA(ctx, cudaGetLastError());
+    return IFEMGPU_OK;
+  };
+  const int slot = 1 + (kron ? 1 : 0) + (learned ? 2 : 0);
+  ifemgpu_status st = captureLoop(ctx, slot, ctx->workGen * 65536 + (learned ? ctx->learnGen : 0), body);
+  if (st != IFEMGPU_OK) return st;
+  // a learned loop must keep shrinking its residual or it stops (and the
+  // caller continues without the network)
+  k_loop_init<<<1, 1, 0, s>>>(w.scal, rtol * rtol, (double)maxit, learned ? 1.0 : 0.0);
+  g_fcg_start<<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.q32, w.dinv32, n);
+  if ((st = precondition(false)) != IFEMGPU_OK) return st;  // p = q = 0: (z, q) = 0
+  g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  int flag = 0;
+  if ((st = replayLoop(ctx, w, slot, maxit, iters, &flag)) != IFEMGPU_OK) return st;
+  *nan = flag >= 2;  // NaN or stagnation
+  return IFEMGPU_OK;
+}
+
+// workspace, pinned scalars and (mixed) the FP32 matrix copy
+static ifemgpu_status ensureWork(ifemgpu_ctx* ctx, bool mixed)
+{
+  const size_t n = ctx->neq;
+  const size_t need = sizeof(double) * (n * 8 + 2 * kRedBlocks + kScal) + sizeof(float) * n * 6;
   if (ctx->work_len < need) {
+    dropLoopGraphs(ctx);
     if (ctx->d_work) cudaFree(ctx->d_work);
+    ctx->d_work = nullptr;
+    ctx->work_len = 0;
     IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_work, need));
     ctx->work_len = need;
   }
   if (!ctx->h_pinned) IFEMGPU_CUDA(ctx, cudaMallocHost(&ctx->h_pinned, 64));
-  const bool mixed = o->method != IFEMGPU_PCG_FP64;
   if (mixed && !ctx->d_K32) IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_K32, sizeof(float) * ctx->nnz));
-  Work w = carve(ctx);
+  return IFEMGPU_OK;
+}
+
+// FP32 matrix copy, inverse diagonal, x64 = 0, r64 = b, ||b||^2 in scal[8]
+// and scal[9]; returns ||b||
+static ifemgpu_status solvePrologue(ifemgpu_ctx* ctx, const Work& w, const double* b, bool mixed,
+                                    double* bn)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
-  const int sb = std::min(kRedBlocks, (n + 7) / 8);
-  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   if (mixed) k_convert<float><<<1024, kThreads, 0, s>>>(ctx->d_K, ctx->d_K32, ctx->nnz);
   k_diag<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K,
                                                               n, w.d64, w.dinv32);
   IFEMGPU_CUDA(ctx, cudaMemsetAsync(w.x64, 0, sizeof(double) * n, s));
-  // ||b||^2 -> scal[8]
-  k_norm2<double><<<vb, kThreads, 0, s>>>(ctx->d_b, n, w.part);
+  k_norm2<double><<<vb, kThreads, 0, s>>>(b, n, w.part);
   k_finish<<<1, kThreads, 0, s>>>(w.part, vb, 1, w.scal + 8);
-  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.r64, ctx->d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.r64, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.scal + 9, w.scal + 8, sizeof(double), cudaMemcpyDeviceToDevice, s));
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
-  const double bn = std::sqrt(ctx->h_pinned[0]);
-  int outer = 0, inner = 0;
+  *bn = std::sqrt(ctx->h_pinned[0]);
+  return IFEMGPU_OK;
+}
+
+// r64 = b - A x64 in FP64; returns ||r64||
+static ifemgpu_status refineResidual(ifemgpu_ctx* ctx, const Work& w, const double* b, double* rn)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  k_residual<<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K, w.x64, b, w.r64, n,
+                                     w.part);
+  k_finish<<<1, kThreads, 0, s>>>(w.part, sb, 1, w.scal + 9);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + 9, sizeof(double), cudaMemcpyDeviceToHost, s));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  *rn = std::sqrt(ctx->h_pinned[0]);
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o, double* xh,
+                        ifemgpu_solve_info* info, const double* bdev)
+{
+  const int n = ctx->neq;
+  cudaStream_t s = ctx->stream;
+  const double* b = bdev ? bdev : ctx->d_b;
+  if (n == 0) {
+    if (info) *info = ifemgpu_solve_info{0, 0, 0.0, 0.0, 0};
+    return IFEMGPU_OK;
+  }
+  if (o->method != IFEMGPU_PCG_MIXED && o->method != IFEMGPU_PCG_FP64 &&
+      o->method != IFEMGPU_FCG_LEARNED)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "solve: unknown method");
+  bool learned = o->method == IFEMGPU_FCG_LEARNED;
+  if (learned && !learnReady(ctx))
+    return setError(ctx, IFEMGPU_NOT_READY, "solve: no trained coarse correction");
+  const bool mixed = o->method != IFEMGPU_PCG_FP64;
+  if (o->precond != IFEMGPU_PRECOND_JACOBI && o->precond != IFEMGPU_PRECOND_KRONECKER)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "solve: unknown preconditioner");
+  const bool kron = o->precond == IFEMGPU_PRECOND_KRONECKER;
+  if (kron && !mixed)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "solve: the FP64 method takes the Jacobi preconditioner");
+  ifemgpu_status st = ensureWork(ctx, mixed);
+  if (st != IFEMGPU_OK) return st;
+  if (kron && (st = fdSetup(ctx)) != IFEMGPU_OK) return st;
+  if (learned && (st = learnPrepare(ctx)) != IFEMGPU_OK) return st;
+  Work w = carve(ctx);
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  double bn = 0.0;
+  if ((st = solvePrologue(ctx, w, b, mixed, &bn)) != IFEMGPU_OK) return st;
+  if (kron && (st = fdRescale(ctx, w.d64)) != IFEMGPU_OK) return st;
+  int outer = 0, inner = 0, fallbacks = 0;
   double relres = bn > 0 ? 1.0 : 0.0;
-  ifemgpu_status st = IFEMGPU_OK;
   const int maxOuter = mixed ? std::max(1, o->max_outer) : 1;
   const double innerTol = mixed ? (o->inner_rtol > 0 ? o->inner_rtol : 1e-4) : o->rtol;
   while (bn > 0 && relres > o->rtol && outer < maxOuter) {
     int it = 0;
-    if (mixed)
-      st = innerPCG<float>(ctx, w, ctx->d_K32, w.dinv32, w.r32, w.x32, w.z32, w.p32, w.q32, 9,
-                           innerTol, o->max_inner, &it);
-    else
+    bool nan = false;
+    if (learned || kron) {
+      st = loopFCG(ctx, w, kron, learned, innerTol, o->max_inner, &it, &nan);
+    } else if (mixed) {
+      st = loopPCG32(ctx, w, innerTol, o->max_inner, &it);
+    } else {
       st = innerPCG<double>(ctx, w, ctx->d_K, w.d64, w.rD, w.xD, w.zD, w.pD, w.qD, 9, innerTol,
                             o->max_inner, &it);
+    }
     inner += it;
     outer++;
     if (st != IFEMGPU_OK) break;
+    if (nan) {  // the learned step broke down: continue without the network
+      if (!learned) {
+        st = setError(ctx, IFEMGPU_NOT_CONVERGED, "flexible CG breakdown (NaN)");
+        break;
+      }
+      learned = false;
+      fallbacks++;
+      continue;
+    }
+    if (learned) k_copy_d<<<vb, kThreads, 0, s>>>(w.x64, w.rD, n);  // x before the step
     if (mixed)
       k_accumulate<float><<<vb, kThreads, 0, s>>>(w.x64, w.x32, w.scal, 9, n);
     else
       k_accumulate<double><<<vb, kThreads, 0, s>>>(w.x64, w.xD, w.scal, 9, n);
-    k_residual<<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K, w.x64, ctx->d_b,
-                                       w.r64, n, w.part);
-    k_finish<<<1, kThreads, 0, s>>>(w.part, sb, 1, w.scal + 9);
-    IFEMGPU_CUDA(ctx, cudaGetLastError());
-    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + 9, sizeof(double), cudaMemcpyDeviceToHost, s));
-    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
-    relres = std::sqrt(ctx->h_pinned[0]) / bn;
+    double rn = 0.0;
+    if ((st = refineResidual(ctx, w, b, &rn)) != IFEMGPU_OK) return st;
+    const double next = rn / bn;
+    if (learned && !(next < relres)) {
+      // the FP64 residual judges the learned step: no progress -> undo it
+      // and continue with plain Jacobi-PCG
+      k_copy_d<<<vb, kThreads, 0, s>>>(w.rD, w.x64, n);
+      if ((st = refineResidual(ctx, w, b, &rn)) != IFEMGPU_OK) return st;
+      learned = false;
+      fallbacks++;
+      relres = rn / bn;
+      continue;
+    }
+    relres = next;
   }
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(xh, w.x64, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-  if (info) *info = ifemgpu_solve_info{outer, inner, relres, (double)ms};
+  if (info) *info = ifemgpu_solve_info{outer, inner, relres, (double)ms, fallbacks};
   if (st != IFEMGPU_OK) return st;
   if (bn > 0 && relres > o->rtol)
     return setError(ctx, IFEMGPU_NOT_CONVERGED, "relative residual above tolerance");
+  return IFEMGPU_OK;
+}
+
+// Training pairs from one plain FP32 Jacobi-PCG solve of A x = rhs (the
+// assembled b when rhs is null) from x = 0: every stride-th iterate gives
+// (R r_k, Rn (x* - x_k)).  x* is the caller's reference solution, or the
+// FP64-refined mixed solve to 1e-12 when xstar is null.
+// z = M r for the FP32 preconditioner precond of the assembled matrix (host
+// vectors; diagnostic)
+ifemgpu_status applyPreconditioner(ifemgpu_ctx* ctx, int precond, const double* r, double* z)
+{
+  const int n = ctx->neq;
+  cudaStream_t s = ctx->stream;
+  if (precond != IFEMGPU_PRECOND_JACOBI && precond != IFEMGPU_PRECOND_KRONECKER)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "apply_preconditioner: unknown preconditioner");
+  ifemgpu_status st = ensureWork(ctx, true);
+  if (st != IFEMGPU_OK) return st;
+  if (precond == IFEMGPU_PRECOND_KRONECKER && (st = fdSetup(ctx)) != IFEMGPU_OK) return st;
+  if (n == 0) return IFEMGPU_OK;
+  Work w = carve(ctx);
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  k_diag<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K,
+                                                              n, w.d64, w.dinv32);
+  const double one = 1.0;
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.scal + 9, &one, sizeof(double), cudaMemcpyHostToDevice, s));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.r64, r, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  g_fcg_start<<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.q32, w.dinv32, n);
+  if (precond == IFEMGPU_PRECOND_KRONECKER) {
+    if ((st = fdRescale(ctx, w.d64)) != IFEMGPU_OK) return st;
+    if ((st = fdApply(ctx, w.r32, w.z32, nullptr)) != IFEMGPU_OK) return st;
+  }
+  std::vector<float> zf(n);
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(zf.data(), w.z32, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  for (int i = 0; i < n; i++) z[i] = zf[i];
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* xstar, int stride,
+                            int maxit, double rtol)
+{
+  const int n = ctx->neq;
+  cudaStream_t s = ctx->stream;
+  double* xs = learnXstar(ctx);
+  if (!xs) return setError(ctx, IFEMGPU_NOT_READY, "learn_collect before learn_setup");
+  if (n == 0) return IFEMGPU_OK;
+  const double* b = ctx->d_b;
+  if (rhs) {
+    if (!ctx->d_rhsAlt) IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_rhsAlt, sizeof(double) * n));
+    IFEMGPU_CUDA(ctx, cudaMemcpy(ctx->d_rhsAlt, rhs, sizeof(double) * n, cudaMemcpyHostToDevice));
+    b = ctx->d_rhsAlt;
+  }
+  ifemgpu_status st;
+  if (xstar) {
+    IFEMGPU_CUDA(ctx, cudaMemcpy(xs, xstar, sizeof(double) * n, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<double> xh(n);
+    ifemgpu_solver_options so{IFEMGPU_PCG_MIXED, 1e-12, 40, 100000, 1e-5};
+    ifemgpu_solve_info si{};
+    st = runSolve(ctx, &so, xh.data(), &si, b);
+    if (st != IFEMGPU_OK && !(st == IFEMGPU_NOT_CONVERGED && si.relres < 1e-9)) return st;
+    IFEMGPU_CUDA(ctx, cudaMemcpy(xs, xh.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  }
+  if ((st = ensureWork(ctx, true)) != IFEMGPU_OK) return st;
+  if ((st = learnPrepare(ctx)) != IFEMGPU_OK) return st;
+  Work w = carve(ctx);
+  double bn = 0.0;
+  if ((st = solvePrologue(ctx, w, b, true, &bn)) != IFEMGPU_OK) return st;
+  if (!(bn > 0)) return IFEMGPU_OK;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  const double sx = 1.0 / bn;  // the loop solves the system scaled by 1/||b||
+  k_loop_init<<<1, 1, 0, s>>>(w.scal, rtol * rtol, (double)maxit, 0.0);
+  g_pcg_start<float><<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.dinv32,
+                                             n, w.part);
+  if ((st = learnRecord(ctx, w.r32, w.x32, sx)) != IFEMGPU_OK) return st;
+  stride = std::max(1, stride);
+  for (int l = 0; l <= maxit / stride; l++) {
+    for (int k = 0; k < stride; k++) {
+      g_spmv<float><<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, w.p32, w.q32,
+                                            n, w.part, w.scal, 1);
+      g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32,
+                                                  w.scal, n, w.part);
+      g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
+    }
+    IFEMGPU_CUDA(ctx, cudaGetLastError());
+    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + S_DONE, sizeof(double),
+                                      cudaMemcpyDeviceToHost, s));
+    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+    if (ctx->h_pinned[0] != 0.0) break;
+    if ((st = learnRecord(ctx, w.r32, w.x32, sx)) != IFEMGPU_OK) return st;
+  }
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
   return IFEMGPU_OK;
 }
 
@@ -512,6 +1066,16 @@ ifemgpu_status solveNoAlloc(ifemgpu_ctx* ctx, double rtol, int maxit, double* xh
 }
 
 }  // namespace ifemgpu
+
+extern "C" ifemgpu_status ifemgpu_apply_preconditioner(ifemgpu_ctx* ctx, int precond,
+                                                       const double* r, double* z)
+{
+  if (!ctx || !r || !z) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled)
+    return ifemgpu::setError(ctx, IFEMGPU_NOT_READY, "apply_preconditioner before assemble");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  return ifemgpu::applyPreconditioner(ctx, precond, r, z);
+}
 
 extern "C" ifemgpu_status ifemgpu_solve_noalloc(ifemgpu_ctx* ctx, double rtol, int max_iter,
                                                 double* x, ifemgpu_solve_info* info)

@@ -36,12 +36,17 @@ class Material(C.Structure):
 
 class SolverOptions(C.Structure):
     _fields_ = [("method", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
-                ("max_inner", C.c_int), ("inner_rtol", C.c_double)]
+                ("max_inner", C.c_int), ("inner_rtol", C.c_double), ("precond", C.c_int)]
 
 
 class SolveInfo(C.Structure):
     _fields_ = [("outer_iters", C.c_int), ("inner_iters", C.c_int), ("relres", C.c_double),
-                ("device_ms", C.c_double)]
+                ("device_ms", C.c_double), ("fallbacks", C.c_int)]
+
+
+class LearnOptions(C.Structure):
+    _fields_ = [("coarse_cells", C.c_int), ("hidden", C.c_int), ("capacity", C.c_int),
+                ("seed", C.c_uint), ("field_inputs", C.c_int)]
 
 
 OK, INVALID_ARG, OUT_OF_MEMORY, SINGULAR_JACOBIAN, NOT_CONVERGED, DEVICE_TIMEOUT, \
@@ -52,7 +57,8 @@ KE_FP64, KE_SPLIT_TF32 = 0, 1
 POISSON, ELASTICITY = 1, 2
 SOURCE_CONSTANT, SOURCE_SINE = 0, 1
 FIELD_LOG_KAPPA, FIELD_SOURCE_NOISE = 1, 2
-PCG_MIXED, PCG_FP64 = 1, 2
+PCG_MIXED, PCG_FP64, FCG_LEARNED = 1, 2, 3
+PRECOND_JACOBI, PRECOND_KRONECKER = 0, 1
 
 # Every symbol include/ifemgpu.h declares (checked by the CPU test suite).
 EXPORTS = [
@@ -63,7 +69,11 @@ EXPORTS = [
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
     "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_solve",
     "ifemgpu_expand_solution", "ifemgpu_patch_update_coefs", "ifemgpu_get_stream",
-    "ifemgpu_selftest_tc_gemm", "ifemgpu_solve_noalloc",
+    "ifemgpu_selftest_tc_gemm", "ifemgpu_solve_noalloc", "ifemgpu_learn_setup",
+    "ifemgpu_learn_collect", "ifemgpu_learn_clear", "ifemgpu_learn_train",
+    "ifemgpu_learn_evaluate", "ifemgpu_learn_gradients", "ifemgpu_learn_info",
+    "ifemgpu_learn_get_weights", "ifemgpu_learn_set_weights", "ifemgpu_patch_update_field",
+    "ifemgpu_learn_get_pairs", "ifemgpu_apply_preconditioner",
 ]
 
 
@@ -114,6 +124,19 @@ def load_library(path: str | None = None):
         "ifemgpu_get_stream": (I, [P, C.POINTER(C.c_void_p)]),
         "ifemgpu_selftest_tc_gemm": (I, [V, V, V]),
         "ifemgpu_solve_noalloc": (I, [P, D, I, V, C.POINTER(SolveInfo)]),
+        "ifemgpu_learn_setup": (I, [P, C.POINTER(LearnOptions)]),
+        "ifemgpu_learn_collect": (I, [P, V, V, I, I, D, C.POINTER(I)]),
+        "ifemgpu_learn_clear": (I, [P]),
+        "ifemgpu_learn_get_pairs": (I, [P, I, I, V, V]),
+        "ifemgpu_apply_preconditioner": (I, [P, I, V, V]),
+        "ifemgpu_learn_train": (I, [P, I, I, C.c_float, C.c_uint, C.POINTER(C.c_float)]),
+        "ifemgpu_learn_evaluate": (I, [P, C.POINTER(C.c_float)]),
+        "ifemgpu_learn_gradients": (I, [P, V, V, I, V, C.POINTER(C.c_float)]),
+        "ifemgpu_learn_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I),
+                                   C.POINTER(I)]),
+        "ifemgpu_learn_get_weights": (I, [P, V, C.POINTER(I), C.POINTER(C.c_float)]),
+        "ifemgpu_learn_set_weights": (I, [P, V, I, C.c_float]),
+        "ifemgpu_patch_update_field": (I, [P, I, I, V]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -298,9 +321,9 @@ class SIM:
         self._check(self.lib.ifemgpu_copy_rhs(self.ctx, _ptr(out)))
 
     def solveSystem(self, method=PCG_MIXED, rtol=1e-10, max_outer=20, max_inner=20000,
-                    inner_rtol=1e-4, check=True):
+                    inner_rtol=1e-4, check=True, precond=PRECOND_JACOBI):
         x = np.zeros(self.sizes.neq, dtype=np.float64)
-        o = SolverOptions(method, rtol, max_outer, max_inner, inner_rtol)
+        o = SolverOptions(method, rtol, max_outer, max_inner, inner_rtol, precond)
         info = SolveInfo()
         st = self.lib.ifemgpu_solve(self.ctx, C.byref(o), _ptr(x), C.byref(info))
         if check:
@@ -322,3 +345,89 @@ class SIM:
         u = np.zeros(self.sizes.ndof, dtype=np.float64)
         self._check(self.lib.ifemgpu_expand_solution(self.ctx, _ptr(x), _ptr(u), scale))
         return u
+
+    def apply_preconditioner(self, r: np.ndarray, precond=PRECOND_KRONECKER) -> np.ndarray:
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros(self.sizes.neq, dtype=np.float64)
+        self._check(self.lib.ifemgpu_apply_preconditioner(self.ctx, precond, _ptr(r), _ptr(z)))
+        return z
+
+    # ---- learned coarse correction -----------------------------------------
+    def update_field(self, pid: int, which: int, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self.lib.ifemgpu_patch_update_field(self.ctx, pid, which, _ptr(v)))
+
+    def learn_setup(self, coarse_cells=8, hidden=256, capacity=20000, seed=1, field_inputs=0):
+        o = LearnOptions(coarse_cells, hidden, capacity, seed, field_inputs)
+        self._check(self.lib.ifemgpu_learn_setup(self.ctx, C.byref(o)))
+        return self.learn_info()
+
+    def learn_info(self) -> dict:
+        nc, nin, nh, npar, pairs = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._check(self.lib.ifemgpu_learn_info(self.ctx, C.byref(nc), C.byref(nin), C.byref(nh),
+                                                C.byref(npar), C.byref(pairs)))
+        return {"coarse_unknowns": nc.value, "inputs": nin.value, "hidden": nh.value,
+                "nparam": npar.value, "pairs": pairs.value}
+
+    def learn_collect(self, rhs=None, xstar=None, stride=1, max_iter=20000, rtol=1e-6) -> int:
+        keep = []
+        args = []
+        for a in (rhs, xstar):
+            if a is None:
+                args.append(None)
+            else:
+                v = np.ascontiguousarray(a, dtype=np.float64)
+                assert v.size == self.sizes.neq
+                keep.append(v)
+                args.append(_ptr(v))
+        n = C.c_int()
+        self._check(self.lib.ifemgpu_learn_collect(self.ctx, args[0], args[1], stride, max_iter,
+                                                   rtol, C.byref(n)))
+        return n.value
+
+    def learn_clear(self):
+        self._check(self.lib.ifemgpu_learn_clear(self.ctx))
+
+    def learn_pairs(self, first=0, count=None):
+        info = self.learn_info()
+        count = info["pairs"] - first if count is None else count
+        X = np.zeros((count, info["inputs"]), dtype=np.float32)
+        Y = np.zeros((count, info["coarse_unknowns"]), dtype=np.float32)
+        self._check(self.lib.ifemgpu_learn_get_pairs(self.ctx, first, count, _ptr(X), _ptr(Y)))
+        return X, Y
+
+    def learn_train(self, epochs=20, batch=256, lr=1e-3, seed=7) -> float:
+        loss = C.c_float()
+        self._check(self.lib.ifemgpu_learn_train(self.ctx, epochs, batch, lr, seed,
+                                                 C.byref(loss)))
+        return loss.value
+
+    def learn_evaluate(self) -> float:
+        mse = C.c_float()
+        self._check(self.lib.ifemgpu_learn_evaluate(self.ctx, C.byref(mse)))
+        return mse.value
+
+    def learn_gradients(self, X: np.ndarray, Y: np.ndarray):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        info = self.learn_info()
+        assert X.shape[0] == Y.shape[0]
+        assert X.shape[1] == info["inputs"] and Y.shape[1] == info["coarse_unknowns"]
+        grad = np.zeros(info["nparam"], dtype=np.float32)
+        loss = C.c_float()
+        self._check(self.lib.ifemgpu_learn_gradients(self.ctx, _ptr(X), _ptr(Y), X.shape[0],
+                                                     _ptr(grad), C.byref(loss)))
+        return loss.value, grad
+
+    def learn_get_weights(self):
+        n = C.c_int()
+        s = C.c_float()
+        self._check(self.lib.ifemgpu_learn_get_weights(self.ctx, None, C.byref(n), C.byref(s)))
+        theta = np.zeros(n.value, dtype=np.float32)
+        self._check(self.lib.ifemgpu_learn_get_weights(self.ctx, _ptr(theta), C.byref(n),
+                                                       C.byref(s)))
+        return theta, s.value
+
+    def learn_set_weights(self, theta: np.ndarray, scale: float):
+        theta = np.ascontiguousarray(theta, dtype=np.float32)
+        self._check(self.lib.ifemgpu_learn_set_weights(self.ctx, _ptr(theta), theta.size, scale))

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define IFEMGPU_ABI_VERSION 1
+#define IFEMGPU_ABI_VERSION 2
 
 typedef enum ifemgpu_status {
   IFEMGPU_OK = 0,
@@ -227,7 +227,25 @@ ifemgpu_status ifemgpu_last_assembly_stats(ifemgpu_ctx* ctx, double* total_ms,
 
 enum ifemgpu_solver_method {
   IFEMGPU_PCG_MIXED = 1,  /* FP32 Jacobi-PCG inner, FP64 residual refinement */
-  IFEMGPU_PCG_FP64 = 2    /* FP64 Jacobi-PCG                                 */
+  IFEMGPU_PCG_FP64 = 2,   /* FP64 Jacobi-PCG                                 */
+  IFEMGPU_FCG_LEARNED = 3 /* FP32 flexible CG preconditioned by the fine
+                             level (precond) plus the learned coarse
+                             correction (ifemgpu_learn_*), FP64 residual
+                             refinement; an inner solve that breaks down or
+                             does not lower the FP64 residual is undone and
+                             the solve continues without the network
+                             (counted in info->fallbacks)                  */
+};
+
+enum ifemgpu_precond {
+  IFEMGPU_PRECOND_JACOBI = 0,    /* point Jacobi                              */
+  IFEMGPU_PRECOND_KRONECKER = 1  /* per patch and component: the parameter-cube
+                                    Laplacian K0xM1xM2 + M0xK1xM2 + M0xM1xK2 of
+                                    the 1D spline stiffness K_d and mass M_d,
+                                    inverted by fast diagonalisation and scaled
+                                    to the matrix diagonal; 3D patches whose
+                                    free DOFs form boxes, no shared nodes,
+                                    FP32 methods only                         */
 };
 
 typedef struct ifemgpu_solver_options {
@@ -236,6 +254,8 @@ typedef struct ifemgpu_solver_options {
   int max_outer;       /* refinement steps (mixed)                       */
   int max_inner;       /* PCG iterations per refinement step / total     */
   double inner_rtol;   /* FP32 residual reduction per refinement step    */
+  int precond;         /* enum ifemgpu_precond (fine level of the FP32
+                          methods; IFEMGPU_PCG_FP64 takes Jacobi only)    */
 } ifemgpu_solver_options;
 
 typedef struct ifemgpu_solve_info {
@@ -243,6 +263,7 @@ typedef struct ifemgpu_solve_info {
   int inner_iters;     /* total PCG iterations                           */
   double relres;       /* final FP64 relative residual                   */
   double device_ms;    /* device time of the solve                       */
+  int fallbacks;       /* learned inner solves replaced by plain PCG     */
 } ifemgpu_solve_info;
 
 /* Solves K x = b with the assembled system; replaces SIMbase::solveSystem
@@ -278,7 +299,95 @@ ifemgpu_status ifemgpu_solve_noalloc(ifemgpu_ctx* ctx, double rtol, int max_iter
 ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
                                        double* u, double scale);
 
+/* ---- learned coarse correction ---------------------------------------- */
+/* No IFEM counterpart: IFEM's solvers are SuperLU and PETSc/ISTL Krylov
+ * methods with algebraic preconditioners.  For a context of one 3D patch a
+ * small network maps the residual, restricted to a coarse grid of
+ * (m+1)^3 vertices over the patch's parameter domain (trilinear weights at
+ * the Greville points, npv values per vertex), to a coarse error estimate
+ * that is interpolated back and added to the Jacobi step of flexible CG
+ * (IFEMGPU_FCG_LEARNED).  The network (3 layers of width `hidden`, ReLU) is
+ * trained on the device by the library's own kernels on (residual, error)
+ * pairs that plain PCG solves of the same patch generate.                 */
+
+typedef struct ifemgpu_learn_options {
+  int coarse_cells;   /* m, coarse cells per direction (1..32)            */
+  int hidden;         /* hidden width (8..1024)                           */
+  int capacity;       /* training pairs kept on the device                */
+  unsigned seed;      /* initial weights                                  */
+  int field_inputs;   /* 1: the network also reads the patch's
+                         log-conductivity field averaged onto the coarse
+                         vertices (one network for many fields)          */
+} ifemgpu_learn_options;
+
+/* Builds the coarse transfer operators and a freshly initialised network
+ * for the preprocessed one-patch 3D model (discards earlier training).    */
+ifemgpu_status ifemgpu_learn_setup(ifemgpu_ctx* ctx, const ifemgpu_learn_options* o);
+
+/* Solves A x = rhs (rhs: neq host values, or null for the assembled b)
+ * with plain FP32 Jacobi-PCG from x = 0 to the relative residual rtol (at
+ * most max_iter iterations) and stores one pair per stride-th iterate:
+ * (R r_k / |R r_k|, Rn (x* - x_k) / |R r_k|), Rn the weight-normalised
+ * restriction.  x* is xstar (neq host values) or, when null, the library's
+ * FP64-refined solve to 1e-12.  *pairs receives the stored total.          */
+ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs,
+                                     const double* xstar, int stride,
+                                     int max_iter, double rtol, int* pairs);
+
+/* Forgets the stored pairs (the network is kept).                         */
+ifemgpu_status ifemgpu_learn_clear(ifemgpu_ctx* ctx);
+
+/* Copies stored pairs first .. first+count-1 to host rows X (`inputs`
+ * floats each) and Y (`coarse_unknowns` floats each): the training set's
+ * checkpoint, and the check of the restriction.                           */
+ifemgpu_status ifemgpu_learn_get_pairs(ifemgpu_ctx* ctx, int first, int count,
+                                       float* X, float* Y);
+
+/* Adam on the stored pairs: mean squared error against targets divided by
+ * their RMS S, minibatches of `batch`, `epochs` passes, shuffled from seed.
+ * The last batch's loss goes to *final_loss (optional).                   */
+ifemgpu_status ifemgpu_learn_train(ifemgpu_ctx* ctx, int epochs, int batch,
+                                   float lr, unsigned seed, float* final_loss);
+
+/* Mean squared error (targets / S) of the FP32 network on the stored pairs. */
+ifemgpu_status ifemgpu_learn_evaluate(ifemgpu_ctx* ctx, float* mse);
+
+/* Loss mean((net(X) - Y)^2) over n host pairs (rows of X hold `inputs`
+ * floats, rows of Y `coarse_unknowns`, targets taken as they are) and its
+ * gradient with respect to all parameters (layout of
+ * ifemgpu_learn_get_weights).                                             */
+ifemgpu_status ifemgpu_learn_gradients(ifemgpu_ctx* ctx, const float* X,
+                                       const float* Y, int n, float* grad,
+                                       float* loss);
+
+/* Sizes of the coarse problem and the network; null pointers skipped.     */
+ifemgpu_status ifemgpu_learn_info(const ifemgpu_ctx* ctx, int* coarse_unknowns,
+                                  int* inputs, int* hidden, int* nparam,
+                                  int* pairs);
+
+/* Parameters as one FP32 array: W1 (hidden x inputs, row-major), b1, W2
+ * (hidden x hidden), b2, W3 (nc x hidden), b3, and the target scale S.
+ * get with theta null returns only the count; set marks the network
+ * trained (checkpoint restore).                                           */
+ifemgpu_status ifemgpu_learn_get_weights(ifemgpu_ctx* ctx, float* theta,
+                                         int* count, float* scale);
+ifemgpu_status ifemgpu_learn_set_weights(ifemgpu_ctx* ctx, const float* theta,
+                                         int count, float scale);
+
+/* Replaces the values of a field set before preprocessing (same length),
+ * for a new assembly of the same model; the random-coefficient solves that
+ * feed the network use it.  No IFEM counterpart (IFEM re-reads a field
+ * function per assembly).                                                 */
+ifemgpu_status ifemgpu_patch_update_field(ifemgpu_ctx* ctx, int patch_id,
+                                          int which, const double* values);
+
 /* ---- diagnostics ------------------------------------------------------ */
+
+/* z = M r with the FP32 preconditioner `precond` (enum ifemgpu_precond) of
+ * the assembled matrix, r and z neq host values.  No IFEM counterpart: it
+ * checks the preconditioner kernels in isolation.                         */
+ifemgpu_status ifemgpu_apply_preconditioner(ifemgpu_ctx* ctx, int precond,
+                                            const double* r, double* z);
 
 /* Runs the tensor-core building block of the element kernel once on the
  * current device: D (128 x 96) = A (128 x 32) * B (96 x 32)^T in 3xTF32

@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(gpulib):
     for s in sorted(syms):
         assert hasattr(gpulib, s), f"{s} declared in include/ but not exported"
     assert set(G.EXPORTS) <= syms
-    assert gpulib.ifemgpu_abi_version() == 1
+    assert gpulib.ifemgpu_abi_version() == 2
 
 
 def host_sim(n_gauss=4):

@@ -1,0 +1,188 @@
+"""Kronecker preconditioner and learned coarse correction, through the C ABI.
+
+- the network's loss and gradient from the library's training kernels
+  against the FP64 numpy oracle (oracle/mlp.py);
+- the stored (residual, error) pairs against the oracle's restriction of
+  the FP64 solution;
+- flexible CG with the Kronecker preconditioner and with the learned
+  correction reaching the FP64 relative residual 1e-10 on the 3D Poisson
+  family with a log-normal conductivity (p = 3), with the solution equal to
+  plain mixed-precision PCG's;
+- the A/B comparison of what the trained network gains over the method
+  without it, on a held-out seed;
+- the fallback when the network returns NaN, and the weight checkpoint.
+"""
+import numpy as np
+import pytest
+
+from ifem_gb300 import ifemgpu as G
+from ifem_gb300 import workloads as W
+from oracle import mlp
+
+pytestmark = pytest.mark.gpu
+
+SEED0 = 4100
+
+
+def poisson_model(nel=12, p=3, seed=SEED0, ke=G.KE_SPLIT_TF32):
+    patches, ng = W.config4(nel=nel, p=p, seed=seed)
+    sim = G.SIM(n_gauss=ng, ke_precision=ke)
+    W.load_into(sim, patches)
+    sim.preprocess()
+    sim.assembleSystem()
+    return sim, patches
+
+
+def new_field(patches, seed):
+    rng = np.random.default_rng(seed)
+    return W.gaussian_field_3d(rng, patches[0].coefs[:, :3])
+
+
+def test_training_gradients_match_oracle(gpulib):
+    sim, _ = poisson_model(nel=6)
+    info = sim.learn_setup(coarse_cells=2, hidden=16, capacity=8, seed=3, field_inputs=1)
+    nin, nc, nh = info["inputs"], info["coarse_unknowns"], info["hidden"]
+    assert nc == 27 and nin == 54
+    rng = np.random.default_rng(11)
+    X = rng.standard_normal((37, nin)).astype(np.float32)
+    Y = rng.standard_normal((37, nc)).astype(np.float32)
+    theta, _ = sim.learn_get_weights()
+    theta = theta + 0.05 * rng.standard_normal(theta.size).astype(np.float32)  # non-zero biases
+    sim.learn_set_weights(theta, 1.0)
+    loss, grad = sim.learn_gradients(X, Y)
+    ref_loss, ref_grad = mlp.loss_and_grad(theta.astype(np.float64), X, Y, nh)
+    assert abs(loss - ref_loss) <= 1e-5 * ref_loss
+    # FP32 sums of at most a few hundred terms: 1e-4 of the largest entry
+    assert np.abs(grad - ref_grad).max() <= 1e-4 * np.abs(ref_grad).max()
+
+
+def test_collected_pairs_match_oracle_restriction(gpulib):
+    sim, patches = poisson_model(nel=8)
+    m = 3
+    sim.learn_setup(coarse_cells=m, hidden=16, capacity=64, seed=1, field_inputs=1)
+    x_ref, _ = sim.solveSystem(method=G.PCG_FP64, rtol=1e-12, max_inner=20000)
+    n = sim.learn_collect(xstar=x_ref, stride=4, rtol=1e-6)
+    assert n >= 2
+    X, Y = sim.learn_pairs()
+    sam = sim.getSAM()
+    pc = patches[0]
+    R = mlp.restriction(pc.knots, pc.degree, pc.ncoef, sam.meqn, sam.madof, 1, m)
+    b = sim.rhs()
+    # the first pair is iterate 0: residual b/|b|, error x*/|b|
+    rc = R @ (b / np.linalg.norm(b))
+    nrm = np.linalg.norm(rc)
+    Rn = R / np.maximum(R.sum(1, keepdims=True), 1e-300)
+    nc = R.shape[0]
+    assert np.abs(X[0, :nc] - rc / nrm).max() <= 1e-5
+    ec = Rn @ (x_ref / np.linalg.norm(b)) / nrm
+    assert np.abs(Y[0] - ec).max() <= 1e-4 * np.abs(ec).max()
+    # field inputs: normalised trilinear average of log kappa over all control points
+    g = np.asarray(pc.log_kappa)
+    madof_all = np.arange(1, pc.nnod + 2, dtype=np.int32)
+    meqn_all = np.arange(1, pc.nnod + 1, dtype=np.int32)
+    Rf = mlp.restriction(pc.knots, pc.degree, pc.ncoef, meqn_all, madof_all, 1, m)
+    f = (Rf @ g) / Rf.sum(1)
+    assert np.abs(X[0, nc:] - f).max() <= 1e-5 * max(1.0, np.abs(f).max())
+
+
+def test_kronecker_pcg_matches_plain_pcg(gpulib):
+    sim, _ = poisson_model(nel=16)
+    x0, i0 = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10)
+    x1, i1 = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    assert i0.relres <= 1e-10 and i1.relres <= 1e-10
+    assert np.abs(x1 - x0).max() <= 1e-8 * np.abs(x0).max()
+    print(f"\nJacobi PCG {i0.inner_iters} its {i0.device_ms:.2f} ms, "
+          f"Kronecker {i1.inner_iters} its {i1.device_ms:.2f} ms")
+    assert i1.inner_iters * 3 <= i0.inner_iters
+
+
+def test_kronecker_elasticity(gpulib):
+    patches, ng = W.config2(nel=8)
+    sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
+    W.load_into(sim, patches)
+    sim.preprocess()
+    sim.assembleSystem()
+    x0, i0 = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10)
+    x1, i1 = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    assert i1.relres <= 1e-10
+    assert np.abs(x1 - x0).max() <= 1e-8 * np.abs(x0).max()
+    assert i1.inner_iters < i0.inner_iters
+
+
+def test_kronecker_rejects_fp64_method(gpulib):
+    sim, _ = poisson_model(nel=4)
+    x = np.zeros(sim.sizes.neq)
+    info = G.SolveInfo()
+    o = G.SolverOptions(G.PCG_FP64, 1e-10, 1, 100, 1e-4, G.PRECOND_KRONECKER)
+    assert sim.lib.ifemgpu_solve(sim.ctx, G.C.byref(o), G._ptr(x), G.C.byref(info)) == G.INVALID_ARG
+
+
+def train_on_seeds(sim, patches, seeds, stride=1):
+    for s in seeds:
+        sim.update_field(1, G.FIELD_LOG_KAPPA, new_field(patches, s))
+        sim.assembleSystem()
+        sim.learn_collect(stride=stride, rtol=1e-6)
+    return sim.learn_train(epochs=40, batch=64, lr=1e-3, seed=5)
+
+
+def test_learned_fcg_ab_on_held_out_seed(gpulib):
+    sim, patches = poisson_model(nel=16)
+    sim.learn_setup(coarse_cells=4, hidden=256, capacity=20000, seed=2, field_inputs=1)
+    loss = train_on_seeds(sim, patches, range(SEED0 + 1, SEED0 + 13))
+    train_mse = sim.learn_evaluate()
+    # held-out seed
+    sim.update_field(1, G.FIELD_LOG_KAPPA, new_field(patches, SEED0 + 999))
+    sim.assembleSystem()
+    sim.learn_clear()
+    sim.learn_collect(stride=1, rtol=1e-6)
+    test_mse = sim.learn_evaluate()
+    xp, ip = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10)
+    xk, ik = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    xl, il = sim.solveSystem(method=G.FCG_LEARNED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    xj, ij = sim.solveSystem(method=G.FCG_LEARNED, rtol=1e-10, precond=G.PRECOND_JACOBI)
+    print(f"\ntrain loss {loss:.3e} mse {train_mse:.3e}, held-out mse {test_mse:.3e}"
+          f"\nplain Jacobi PCG   {ip.inner_iters:5d} its {ip.device_ms:8.2f} ms"
+          f"\nKronecker FCG      {ik.inner_iters:5d} its {ik.device_ms:8.2f} ms"
+          f"\nKronecker+network  {il.inner_iters:5d} its {il.device_ms:8.2f} ms fallbacks {il.fallbacks}"
+          f"\nJacobi+network     {ij.inner_iters:5d} its {ij.device_ms:8.2f} ms fallbacks {ij.fallbacks}")
+    for x, i in ((xk, ik), (xl, il), (xj, ij)):
+        assert i.relres <= 1e-10
+        assert np.abs(x - xp).max() <= 1e-8 * np.abs(xp).max()
+    assert test_mse < 1.0       # better than predicting zero (targets have unit RMS)
+
+
+def test_learned_fallback_on_nan_network(gpulib):
+    sim, patches = poisson_model(nel=8)
+    sim.learn_setup(coarse_cells=2, hidden=32, capacity=500, seed=2, field_inputs=1)
+    sim.learn_collect(stride=1, rtol=1e-6)
+    sim.learn_train(epochs=2, batch=32)
+    theta, scale = sim.learn_get_weights()
+    theta[:] = np.nan
+    sim.learn_set_weights(theta, scale)
+    xp, ip = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10)
+    x, info = sim.solveSystem(method=G.FCG_LEARNED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    assert info.fallbacks >= 1
+    assert info.relres <= 1e-10
+    assert np.abs(x - xp).max() <= 1e-8 * np.abs(xp).max()
+
+
+def test_weight_checkpoint_roundtrip(gpulib):
+    sim, patches = poisson_model(nel=8)
+    sim.learn_setup(coarse_cells=2, hidden=32, capacity=500, seed=2, field_inputs=1)
+    sim.learn_collect(stride=1, rtol=1e-6)
+    sim.learn_train(epochs=5, batch=32)
+    theta, scale = sim.learn_get_weights()
+    x1, i1 = sim.solveSystem(method=G.FCG_LEARNED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    sim.learn_setup(coarse_cells=2, hidden=32, capacity=500, seed=99, field_inputs=1)
+    sim.learn_set_weights(theta, scale)
+    x2, i2 = sim.solveSystem(method=G.FCG_LEARNED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    assert i1.inner_iters == i2.inner_iters
+    assert np.array_equal(x1, x2)
+
+
+def test_learned_solve_needs_training(gpulib):
+    sim, _ = poisson_model(nel=4)
+    x = np.zeros(sim.sizes.neq)
+    info = G.SolveInfo()
+    o = G.SolverOptions(G.FCG_LEARNED, 1e-10, 20, 1000, 1e-4, 0)
+    assert sim.lib.ifemgpu_solve(sim.ctx, G.C.byref(o), G._ptr(x), G.C.byref(info)) == G.NOT_READY
