@@ -5,13 +5,18 @@ traction on w=1) -- the IFEM element-integration + assembly path on one GPU.
 
 One step = one full assembly of that model (basis tables, every element's
 stiffness and load, Neumann faces, scatter into the compressed-column
-system), inputs resident on the device.  `e2e` repeats the step through the
-C ABI with host buffers: the control net is uploaded from pinned memory and
-the assembled matrix values and right-hand side are copied back to pinned
-host memory inside the timed region.
+system), inputs resident on the device; `value` is elements/s of those
+steps.  `e2e` repeats the step through the C ABI with host buffers: the
+control net is uploaded from pinned memory and the assembled matrix values
+and right-hand side are copied back to pinned host memory inside the timed
+region.  The `solve` object holds the second half of the metric: wall time to
+the FP64 relative residual 1e-10 on the 64^3 p=3 log-normal Poisson system,
+plain Jacobi mixed-precision PCG against flexible CG with the Kronecker
+preconditioner and with the learned coarse correction (trained in the run,
+evaluated on a held-out field).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-                  [--precision split|fp64]
+                  [--precision split|fp64] [--solve-nel 64|0]
 
 --impl reference times the reference algorithm on the host cores: IFEM's
 ASMs3D::integrate + SAM/assemSparse scatter restated in C++ (oracle/), with
@@ -35,7 +40,7 @@ sys.path.insert(0, ROOT)
 
 NEL = 24
 WORKLOAD = "3D linear elasticity, 1 NURBS patch, p=2, 24^3 elements, 3x3x3 Gauss"
-METRIC = "elements/s assembled"
+METRIC = "elements/s assembled; time to 1e-10 residual, learned vs plain PCG, 1 GB300"
 
 
 def measured_peaks():
@@ -126,6 +131,80 @@ def cpu_baseline(patches, ng, threads, budget_s=20.0):
         orc.assemble(threads)
     dt = (time.perf_counter() - t0) / reps
     return s["nel"] / dt, dt, reps, s
+
+
+SOLVE_WORKLOAD = ("3D Poisson, 1 B-spline patch, p=3, 64^3 elements, 4x4x4 Gauss, "
+                  "log-normal conductivity (GRF sigma 1, correlation 0.1), u=0 on all faces")
+
+
+def run_solve(args, G, W):
+    """Time to the FP64 relative residual 1e-10 on the p=3 log-normal Poisson
+    system: plain Jacobi mixed-precision PCG, flexible CG with the Kronecker
+    preconditioner, and with the learned coarse correction on top (trained here
+    on pairs from seeded conductivity fields, evaluated on a held-out field).
+    Each solve is timed on the wall clock around the C-ABI call (device work,
+    the FP64 solution copied to host memory) and on device events."""
+    t0 = time.perf_counter()
+    patches, ng = W.config4(nel=args.solve_nel)
+    sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
+    W.load_into(sim, patches)
+    sz = sim.preprocess()
+    setup_s = time.perf_counter() - t0
+    pts = patches[0].coefs[:, :3]
+    # training: plain-PCG iterates of seeded fields
+    sim.learn_setup(coarse_cells=args.coarse_cells, hidden=256, capacity=20000, seed=2,
+                    field_inputs=1)
+    t0 = time.perf_counter()
+    for s in range(args.train_seeds):
+        sim.update_field(1, G.FIELD_LOG_KAPPA,
+                         W.gaussian_field_3d(np.random.default_rng(W.BASE_SEED + 500 + s), pts))
+        sim.assembleSystem()
+        pairs = sim.learn_collect(stride=1, rtol=1e-6)
+    collect_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = sim.learn_train(epochs=30, batch=128, lr=1e-3, seed=5)
+    train_s = time.perf_counter() - t0
+    mse_train = sim.learn_evaluate()
+    # held-out field: the configuration's own seed
+    sim.update_field(1, G.FIELD_LOG_KAPPA, patches[0].log_kappa)
+    sim.assembleSystem()
+    sim.learn_clear()
+    sim.learn_collect(stride=1, rtol=1e-6)
+    mse_held = sim.learn_evaluate()
+    out = {"workload": SOLVE_WORKLOAD, "neq": sz.neq, "nnz": sz.nnz, "rtol": 1e-10,
+           "inner": "FP32 with FP64 residual refinement (inner reduction 1e-4)",
+           "setup_s": setup_s}
+    xs = {}
+    for key, meth, pre in (("plain_pcg", G.PCG_MIXED, G.PRECOND_JACOBI),
+                           ("kronecker_fcg", G.PCG_MIXED, G.PRECOND_KRONECKER),
+                           ("learned_fcg", G.FCG_LEARNED, G.PRECOND_KRONECKER),
+                           ("learned_jacobi_fcg", G.FCG_LEARNED, G.PRECOND_JACOBI)):
+        for _ in range(2):                               # capture and warm up
+            sim.solveSystem(method=meth, rtol=1e-10, precond=pre, check=False)
+        walls, dev = [], []
+        for _ in range(args.solve_reps):
+            t0 = time.perf_counter()
+            x, info = sim.solveSystem(method=meth, rtol=1e-10, precond=pre, check=False)
+            walls.append((time.perf_counter() - t0) * 1e3)
+            dev.append(info.device_ms)
+        xs[key] = x
+        out[key] = {"wall_ms": float(np.median(walls)), "device_ms": float(np.median(dev)),
+                    "inner_iters": info.inner_iters, "outer_iters": info.outer_iters,
+                    "relres": info.relres, "fallbacks": info.fallbacks}
+    ref = xs["plain_pcg"]
+    for key in xs:
+        out[key]["max_rel_diff_vs_plain"] = float(np.abs(xs[key] - ref).max() / np.abs(ref).max())
+    out["learned_training"] = {"seeds": args.train_seeds, "pairs": pairs,
+                               "coarse_unknowns": args.coarse_cells and (args.coarse_cells + 1) ** 3,
+                               "hidden": 256, "epochs": 30, "final_batch_loss": loss,
+                               "mse_train": mse_train, "mse_held_out": mse_held,
+                               "collect_s": collect_s, "train_s": train_s}
+    p = out["plain_pcg"]["wall_ms"]
+    out["speedup_vs_plain_pcg"] = {k: p / out[k]["wall_ms"] for k in
+                                   ("kronecker_fcg", "learned_fcg", "learned_jacobi_fcg")}
+    out["learned_gain_over_kronecker"] = (out["kronecker_fcg"]["wall_ms"]
+                                          / out["learned_fcg"]["wall_ms"])
+    return out
 
 
 def run_reference(args):
@@ -244,6 +323,8 @@ def run_gpu(args):
         # and read its row index once, plus the right-hand side
         traffic_alg = nnz * 12 + 4 * (sz.neq + 1) + 8 * sz.neq
         achieved = traffic_alg / (vmax * 1e-3) / 1e9
+        nq, ndof_e, ns = 27, 81, 6     # p=2 elasticity: Gauss points, element DOFs, stresses
+        flops_el = 2 * nq * (ns * ndof_e ** 2 + ns ** 2 * ndof_e)
         value = world * sz.nel / (step_ms * 1e-3)
         cpu_v, cpu_dt, reps, _ = cpu_baseline(patches, ng, os.cpu_count() or 1,
                                               budget_s=args.cpu_budget)
@@ -265,6 +346,14 @@ def run_gpu(args):
                          "kernel": "volume integration + scatter passes",
                          "kernel_ms": vmax, "algorithmic_bytes": traffic_alg,
                          "peak_source": src},
+            "roofline_tensor": {
+                "bound": "tensor", "achieved": flops_el * sz.nel / (vmax * 1e-3) / 1e12,
+                "peak": bf16, "unit": "TFLOP/s",
+                "frac": flops_el * sz.nel / (vmax * 1e-3) / 1e12 / bf16,
+                "flops_per_element": flops_el,
+                "note": "element stiffness contraction 2 nq (ns ndof^2 + ns^2 ndof), ns = 6, "
+                        "counted once although 3xTF32 issues three MMAs per product; peak = "
+                        "measured dense bf16 rate (TF32 runs at half of it)"},
             "cpu_baseline": {"value": cpu_v, "unit": "elements/s", "cores": os.cpu_count(),
                              "kind": "port",
                              "sample": f"{reps} full assemblies of the same model "
@@ -273,6 +362,8 @@ def run_gpu(args):
             "clocks": clocks,
             "wall_s_timed_region": wall,
         }
+        if args.solve_nel > 0:
+            line["solve"] = run_solve(args, G, W)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -284,8 +375,13 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["split", "fp64"])
+    ap.add_argument("--precision", default="split", choices=["split", "fp64"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--solve-nel", type=int, default=64,
+                    help="elements per direction of the solve leg (0: skip it)")
+    ap.add_argument("--solve-reps", type=int, default=3)
+    ap.add_argument("--train-seeds", type=int, default=24)
+    ap.add_argument("--coarse-cells", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -195,9 +195,31 @@ struct SysView {
   const int* rowidx;
   double* K;
   double* b;
-  unsigned long long* counters;
+  unsigned long long* counters;  // [0] singular points [1] pattern misses [2] timeouts [3] work
   const int* F;  // free DOFs before each node
+  int* flags;    // per-element done flags of the persistent pass
 };
+
+constexpr uint32_t kGenFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wait
+
+// flags are polled with relaxed loads (served by L2); a thread that saw a
+// flag issues one acquire fence before the block's scatter
+__device__ __forceinline__ int genLoadRelaxed(const int* p)
+{
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void genFenceAcquire()
+{
+  asm volatile("fence.acq_rel.gpu;" : : : "memory");
+}
+
+__device__ __forceinline__ void genStoreRelease(int* p, int v)
+{
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
 
 // Generic element kernel, one CTA per element of one colour; T = double is
 // the exact-parity mode (FP64 arithmetic, plain adds: no two CTAs of a colour
@@ -207,18 +229,140 @@ struct SysView {
 //
 // Shared memory (T): Xn[nen*4] | N[nq*nen] | dX[3][nq*nen] | Jinv[nq*9]
 //                    | wq[nq] | kq[nq] | fq[nq]   then  eq[nd] (int)
-__device__ __forceinline__ void addEntry(double* p, double v) { *p += v; }
-__device__ __forceinline__ void addEntry(double* p, float v) { atomicAdd(p, tc::widenF32(v)); }
-
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ items,
-             SysView S)
+// FP64 values: plain adds within a colour pass (no two elements of a colour
+// share an entry), L2 reductions in the persistent pass (ordered by flags);
+// FP32 values: widened exactly and added by L2 reductions.
+__device__ __forceinline__ void addEntry(double* p, double v, bool red)
 {
-  extern __shared__ __align__(16) unsigned char smraw[];
+  if (red) atomicAdd(p, v);
+  else *p += v;
+}
+__device__ __forceinline__ void addEntry(double* p, float v, bool)
+{
+  atomicAdd(p, tc::widenF32(v));
+}
+
+template <typename V>
+__device__ __forceinline__ V warpAllSum(V v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// 1D basis tables in the element kernel's precision
+template <typename T> __device__ __forceinline__ const T* tableN(const DevPatch& P, int d);
+template <typename T> __device__ __forceinline__ const T* tableD(const DevPatch& P, int d);
+template <> __device__ __forceinline__ const double* tableN<double>(const DevPatch& P, int d) { return P.tabN[d]; }
+template <> __device__ __forceinline__ const double* tableD<double>(const DevPatch& P, int d) { return P.tabD[d]; }
+template <> __device__ __forceinline__ const float* tableN<float>(const DevPatch& P, int d) { return P.tabNf[d]; }
+template <> __device__ __forceinline__ const float* tableD<float>(const DevPatch& P, int d) { return P.tabDf[d]; }
+
+// Waits until every lower-colour neighbour of element e (the elements within
+// p spans in each direction share nodes with it) has published its flag.
+// Bounded: a wait that runs out counts in counters[2] and lets the element go
+// on (the host then reports IFEMGPU_DEVICE_TIMEOUT).
+__device__ void waitNeighbours(const DevPatch& P, int e, const SysView& S)
+{
+  const int q[3] = {P.p[0] + 1, P.p[1] + 1, P.dim == 3 ? P.p[2] + 1 : 1};
+  const int w[3] = {2 * P.p[0] + 1, 2 * P.p[1] + 1, P.dim == 3 ? 2 * P.p[2] + 1 : 1};
+  const int ee[3] = {e % P.nel[0], (e / P.nel[0]) % P.nel[1], e / (P.nel[0] * P.nel[1])};
+  const int myc = ee[0] % q[0] + q[0] * (ee[1] % q[1] + q[1] * (ee[2] % q[2]));
+  const int total = w[0] * w[1] * w[2];
+  bool waited = false;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int f[3] = {ee[0] + t % w[0] - P.p[0], ee[1] + (t / w[0]) % w[1] - P.p[1],
+                      ee[2] + (P.dim == 3 ? t / (w[0] * w[1]) - P.p[2] : 0)};
+    bool inside = true;
+    for (int d = 0; d < 3; d++) inside = inside && f[d] >= 0 && f[d] < P.nel[d];
+    if (!inside) continue;
+    const int nc = f[0] % q[0] + q[0] * (f[1] % q[1] + q[1] * (f[2] % q[2]));
+    if (nc >= myc) continue;  // the element itself and later colours
+    const int* flag = S.flags + P.flagBase + (f[2] * P.nel[1] + f[1]) * P.nel[0] + f[0];
+    uint32_t spin = 0;
+    waited = true;
+    while (genLoadRelaxed(flag) == 0) {
+      if (++spin > kGenFlagSpin) {
+        atomicAdd(S.counters + 2, 1ull);
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  if (waited) genFenceAcquire();
+}
+
+// FP32 Poisson element matrix in TS x TS register tiles of node pairs
+// (ta <= tb): Ke[a][b] = sum over (Gauss point, direction) of kq dX_a dX_b,
+// scattered as the (a, b) block and its transpose.
+template <int TS>
+__device__ void poissonTiles(const DevPatch& P, const SysView& S, const float* dX,
+                             const float* kq, const int* eq, const int* nodeA, const int* Fa)
+{
+  const int nen = P.nen, nq = P.nq, dim = P.dim;
+  const int q1 = P.p[0] + 1, q2 = P.p[1] + 1;
+  const int nt = (nen + TS - 1) / TS, ntp = nt * (nt + 1) / 2, K = nq * dim;
+  for (int t = threadIdx.x; t < ntp; t += blockDim.x) {
+    int tb = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+    while (tb * (tb + 1) / 2 > t) tb--;
+    while ((tb + 1) * (tb + 2) / 2 <= t) tb++;
+    const int ta = t - tb * (tb + 1) / 2;
+    float acc[TS][TS];
+#pragma unroll
+    for (int i = 0; i < TS; i++)
+#pragma unroll
+      for (int j = 0; j < TS; j++) acc[i][j] = 0.f;
+    for (int k = 0; k < K; k++) {
+      const int c = k / nq, q = k - c * nq;
+      const float* row = dX + c * nq * nen + q * nen;
+      const float s = kq[q];
+      float va[TS], vb[TS];
+#pragma unroll
+      for (int i = 0; i < TS; i++) {
+        const int a = TS * ta + i, b = TS * tb + i;
+        va[i] = a < nen ? row[a] * s : 0.f;
+        vb[i] = b < nen ? row[b] : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < TS; i++)
+#pragma unroll
+        for (int j = 0; j < TS; j++) acc[i][j] += va[i] * vb[j];
+    }
+#pragma unroll
+    for (int i = 0; i < TS; i++)
+#pragma unroll
+      for (int j = 0; j < TS; j++) {
+        const int a = TS * ta + i, bn = TS * tb + j;
+        if (a >= nen || bn >= nen || a > bn) continue;
+        for (int side = 0; side < (a == bn ? 1 : 2); side++) {
+          const int ra = side ? bn : a, cb = side ? a : bn;
+          const int r = eq[ra], ce = eq[cb];
+          if (r <= 0 || ce <= 0) continue;
+          int off;
+          if (P.lineOff) {
+            const int w1 = 2 * P.p[1] + 1, w2 = 2 * P.p[2] + 1;
+            const int dy = (ra / q1) % q2 - (cb / q1) % q2, dz = ra / (q1 * q2) - cb / (q1 * q2);
+            off = P.lineOff[(size_t)nodeA[cb] * w1 * w2 + (dz + P.p[2]) * w1 + dy + P.p[1]] +
+                  Fa[ra];
+          } else {
+            const int pos0 = findRow(S.colptr, S.rowidx, ce - 1, r - 1);
+            if (pos0 < 0) { atomicAdd(S.counters + 1, 1ull); continue; }
+            off = pos0 - S.colptr[ce - 1];
+          }
+          atomicAdd(S.K + S.colptr[ce - 1] + off, tc::widenF32(acc[i][j]));
+        }
+      }
+  }
+}
+
+// One element: basis, geometry, element matrix and load, scatter.  With
+// kFlow the element waits for its lower-colour neighbours before it
+// scatters and publishes its own done flag afterwards.
+template <typename T, bool kFlow>
+__device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S,
+                              unsigned char* smraw)
+{
   T* sm = reinterpret_cast<T*>(smraw);
-  const Item it = items[blockIdx.x];
-  const DevPatch& P = patches[it.patch];
   const int nen = P.nen, nq = P.nq, dim = P.dim, npv = P.npv, nd = nen * npv;
   const int e = it.elem;
   T* Xn = sm;
@@ -228,7 +372,10 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
   T* wq = Ji + nq * 9;
   T* kq = wq + nq;
   T* fq = kq + nq;
-  int* eq = reinterpret_cast<int*>(fq + nq);
+  double* gsum = reinterpret_cast<double*>(fq + nq);  // per point: log-kappa, noise sums
+  int* eq = reinterpret_cast<int*>(gsum + 2 * nq);
+  int* nodeA = eq + nd;     // patch-local node of each element function
+  int* Fa = nodeA + nen;    // free DOFs before that node
   const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
   const int q1 = P.p[0] + 1, q2 = P.p[1] + 1;
   const double* c00 = P.ctrl + (size_t)elemNode(P, e, 0) * 4;
@@ -241,31 +388,34 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
     const int g = P.firstNode + node;
     const int d0 = S.madof[g] - 1;
     for (int c = 0; c < npv; c++) eq[a * npv + c] = S.meqn[d0 + c];
+    nodeA[a] = node;
+    Fa[a] = S.F[g];
   }
   __syncthreads();
 
-  // tensor-product basis at every (Gauss point, function)
+  // tensor-product basis at every (Gauss point, function), from the 1D
+  // tables in the kernel's precision
   for (int t = threadIdx.x; t < nq * nen; t += blockDim.x) {
     const int q = t / nen, a = t % nen;
     const int gi = q % P.ng[0], gj = (q / P.ng[0]) % P.ng[1], gk = q / (P.ng[0] * P.ng[1]);
     const int i = a % q1, j = (a / q1) % q2, k = a / (q1 * q2);
-    const double* n0 = P.tabN[0] + ((size_t)e1 * P.ng[0] + gi) * q1;
-    const double* d0 = P.tabD[0] + ((size_t)e1 * P.ng[0] + gi) * q1;
-    const double* n1 = P.tabN[1] + ((size_t)e2 * P.ng[1] + gj) * q2;
-    const double* d1 = P.tabD[1] + ((size_t)e2 * P.ng[1] + gj) * q2;
+    const T* n0 = tableN<T>(P, 0) + ((size_t)e1 * P.ng[0] + gi) * q1;
+    const T* d0 = tableD<T>(P, 0) + ((size_t)e1 * P.ng[0] + gi) * q1;
+    const T* n1 = tableN<T>(P, 1) + ((size_t)e2 * P.ng[1] + gj) * q2;
+    const T* d1 = tableD<T>(P, 1) + ((size_t)e2 * P.ng[1] + gj) * q2;
     T N, du, dv, dw = 0;
     if (dim == 3) {
       const int q3 = P.p[2] + 1;
-      const double* n2 = P.tabN[2] + ((size_t)e3 * P.ng[2] + gk) * q3;
-      const double* d2 = P.tabD[2] + ((size_t)e3 * P.ng[2] + gk) * q3;
-      N = (T)(n0[i] * n1[j] * n2[k]);
-      du = (T)(d0[i] * n1[j] * n2[k]);
-      dv = (T)(n0[i] * d1[j] * n2[k]);
-      dw = (T)(n0[i] * n1[j] * d2[k]);
+      const T* n2 = tableN<T>(P, 2) + ((size_t)e3 * P.ng[2] + gk) * q3;
+      const T* d2 = tableD<T>(P, 2) + ((size_t)e3 * P.ng[2] + gk) * q3;
+      N = n0[i] * n1[j] * n2[k];
+      du = d0[i] * n1[j] * n2[k];
+      dv = n0[i] * d1[j] * n2[k];
+      dw = n0[i] * n1[j] * d2[k];
     } else {
-      N = (T)(n0[i] * n1[j]);
-      du = (T)(d0[i] * n1[j]);
-      dv = (T)(n0[i] * d1[j]);
+      N = n0[i] * n1[j];
+      du = d0[i] * n1[j];
+      dv = n0[i] * d1[j];
     }
     Nq[t] = N;
     dX[t] = du;
@@ -274,22 +424,29 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
   }
   __syncthreads();
 
-  // per Gauss point: rational weighting, Jacobian, FP64 determinant and inverse
-  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+  // per Gauss point, one warp each (lanes over the basis functions, sums by
+  // butterfly shuffles): rational weighting, Jacobian, material sums; lane 0
+  // forms the FP64 determinant and inverse
+  const int lane = threadIdx.x & 31;
+  for (int q = threadIdx.x >> 5; q < nq; q += blockDim.x >> 5) {
     T* Nr = Nq + q * nen;
     T* Du = dX + q * nen;
     T* Dv = dX + nq * nen + q * nen;
     T* Dw = dX + 2 * nq * nen + q * nen;
     if (P.rational) {
       T W = 0, Wu = 0, Wv = 0, Ww = 0;
-      for (int a = 0; a < nen; a++) {
+      for (int a = lane; a < nen; a += 32) {
         const T w = Xn[a * 4 + 3];
         W += w * Nr[a];
         Wu += w * Du[a];
         Wv += w * Dv[a];
         Ww += w * Dw[a];
       }
-      for (int a = 0; a < nen; a++) {
+      W = warpAllSum(W);
+      Wu = warpAllSum(Wu);
+      Wv = warpAllSum(Wv);
+      Ww = warpAllSum(Ww);
+      for (int a = lane; a < nen; a += 32) {
         const T w = Xn[a * 4 + 3];
         const T R = w * Nr[a] / W;
         Du[a] = (w * Du[a] - R * Wu) / W;
@@ -297,16 +454,45 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
         Dw[a] = (w * Dw[a] - R * Ww) / W;
         Nr[a] = R;
       }
+      __syncwarp();
     }
     T Jt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // column-major J(r,c) = dX_r/du_c
     T Xt[3] = {0, 0, 0};
-    for (int a = 0; a < nen; a++) {
+    double gk = 0.0, sn = 0.0;               // log-conductivity and noise sums
+    for (int a = lane; a < nen; a += 32) {
       const T x = Xn[a * 4], y = Xn[a * 4 + 1], z = Xn[a * 4 + 2];
       Jt[0] += x * Du[a]; Jt[1] += y * Du[a]; Jt[2] += z * Du[a];
       Jt[3] += x * Dv[a]; Jt[4] += y * Dv[a]; Jt[5] += z * Dv[a];
       Jt[6] += x * Dw[a]; Jt[7] += y * Dw[a]; Jt[8] += z * Dw[a];
       Xt[0] += x * Nr[a]; Xt[1] += y * Nr[a]; Xt[2] += z * Nr[a];
+      if (P.kind == IFEMGPU_POISSON && P.logk) gk += (double)Nr[a] * P.logk[nodeA[a]];
+      if (P.kind == IFEMGPU_POISSON && P.noise) sn += (double)Nr[a] * P.noise[nodeA[a]];
     }
+#pragma unroll
+    for (int c = 0; c < 9; c++) Jt[c] = warpAllSum(Jt[c]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) Xt[c] = warpAllSum(Xt[c]);
+    if (P.kind == IFEMGPU_POISSON && P.logk) gk = warpAllSum(gk);
+    if (P.kind == IFEMGPU_POISSON && P.noise) sn = warpAllSum(sn);
+    // park the sums (every lane holds them) for the thread-per-point FP64 stage
+#pragma unroll
+    for (int c = 0; c < 9; c++)
+      if (lane == c) Ji[q * 9 + c] = Jt[c];
+    if (lane == 9) wq[q] = Xt[0];
+    if (lane == 10) kq[q] = Xt[1];
+    if (lane == 11) fq[q] = Xt[2];
+    if (lane == 12) gsum[2 * q] = gk;
+    if (lane == 13) gsum[2 * q + 1] = sn;
+  }
+  __syncthreads();
+  // thread per Gauss point (FP64 instructions with every lane busy)
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    T Jt[9], Xt[3];
+    for (int c = 0; c < 9; c++) Jt[c] = Ji[q * 9 + c];
+    Xt[0] = wq[q];
+    Xt[1] = kq[q];
+    Xt[2] = fq[q];
+    const double gk = gsum[2 * q], sn = gsum[2 * q + 1];
     double J[9], X[3];
     for (int c = 0; c < 9; c++) J[c] = (double)Jt[c];
     for (int c = 0; c < 3; c++) X[c] = (double)Xt[c] + c00[c];
@@ -336,11 +522,11 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
     }
     double w = 0.0;
     if (det > kEpsZ || det < -kEpsZ) {
-      const int gi = q % P.ng[0], gj = (q / P.ng[0]) % P.ng[1], gk = q / (P.ng[0] * P.ng[1]);
+      const int gi = q % P.ng[0], gj = (q / P.ng[0]) % P.ng[1], gz = q / (P.ng[0] * P.ng[1]);
       double dV = (dim == 3 ? 0.125 : 0.25) * P.span[0][e1] * P.span[1][e2];
       if (dim == 3) dV *= P.span[2][e3];
       w = det * dV * P.gw[0][gi] * P.gw[1][gj];
-      if (dim == 3) w *= P.gw[2][gk];
+      if (dim == 3) w *= P.gw[2][gz];
     } else {
       atomicAdd(S.counters, 1ull);
     }
@@ -349,18 +535,10 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
     // material data at the point
     double kap = P.kappa, f = P.source;
     if (P.kind == IFEMGPU_POISSON) {
-      if (P.logk) {
-        double g = 0.0;
-        for (int a = 0; a < nen; a++) g += (double)Nr[a] * P.logk[elemNode(P, e, a)];
-        kap *= exp(g);
-      }
+      if (P.logk) kap *= exp(gk);
       if (P.source_shape == IFEMGPU_SOURCE_SINE)
         for (int c = 0; c < dim; c++) f *= sin(M_PI * X[c]);
-      if (P.noise) {
-        double s = 0.0;
-        for (int a = 0; a < nen; a++) s += (double)Nr[a] * P.noise[elemNode(P, e, a)];
-        f *= 1.0 + s;
-      }
+      if (P.noise) f *= 1.0 + sn;
     }
     kq[q] = (T)(kap * w);
     fq[q] = (T)f;
@@ -379,61 +557,16 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
   }
   __syncthreads();
 
-  // Poisson in split mode: 4x4 register tiles of node pairs (ta <= tb),
-  // Ke[a][b] = sum over (Gauss point, direction) of kq dX_a dX_b
-  if (sizeof(T) == sizeof(float) && P.kind == IFEMGPU_POISSON && S.c0 == nullptr) {
-    const int nt = (nen + 3) / 4, ntp = nt * (nt + 1) / 2, K = nq * dim;
-    for (int t = threadIdx.x; t < ntp; t += blockDim.x) {
-      int tb = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
-      while (tb * (tb + 1) / 2 > t) tb--;
-      while ((tb + 1) * (tb + 2) / 2 <= t) tb++;
-      const int ta = t - tb * (tb + 1) / 2;
-      T acc[4][4];
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = 0;
-      for (int k = 0; k < K; k++) {
-        const int c = k / nq, q = k - c * nq;
-        const T* row = dX + c * nq * nen + q * nen;
-        const T s = kq[q];
-        T va[4], vb[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const int a = 4 * ta + i, b = 4 * tb + i;
-          va[i] = a < nen ? row[a] * s : T(0);
-          vb[i] = b < nen ? row[b] : T(0);
-        }
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-          for (int j = 0; j < 4; j++) acc[i][j] += va[i] * vb[j];
-      }
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int a = 4 * ta + i, bn = 4 * tb + j;
-          if (a >= nen || bn >= nen || a > bn) continue;
-          for (int side = 0; side < (a == bn ? 1 : 2); side++) {
-            const int ra = side ? bn : a, cb = side ? a : bn;
-            const int r = eq[ra], ce = eq[cb];
-            if (r <= 0 || ce <= 0) continue;
-            int off;
-            if (P.lineOff) {
-              const int w1 = 2 * P.p[1] + 1, w2 = 2 * P.p[2] + 1;
-              const int dy = (ra / q1) % q2 - (cb / q1) % q2, dz = ra / (q1 * q2) - cb / (q1 * q2);
-              off = P.lineOff[(size_t)elemNode(P, e, cb) * w1 * w2 + (dz + P.p[2]) * w1 + dy +
-                              P.p[1]] +
-                    S.F[P.firstNode + elemNode(P, e, ra)];
-            } else {
-              const int pos0 = findRow(S.colptr, S.rowidx, ce - 1, r - 1);
-              if (pos0 < 0) { atomicAdd(S.counters + 1, 1ull); continue; }
-              off = pos0 - S.colptr[ce - 1];
-            }
-            addEntry(S.K + S.colptr[ce - 1] + off, acc[i][j]);
-          }
-        }
+  if (kFlow) {
+    waitNeighbours(P, e, S);
+    __syncthreads();
+  }
+
+  // Poisson in split mode: register tiles of node pairs, tile size per patch
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (P.kind == IFEMGPU_POISSON && S.c0 == nullptr) {
+      if (P.tile == 2) poissonTiles<2>(P, S, dX, kq, eq, nodeA, Fa);
+      else poissonTiles<4>(P, S, dX, kq, eq, nodeA, Fa);
     }
   }
 
@@ -491,8 +624,7 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
       if (P.lineOff) {  // structured patch: position from the line-offset table
         const int w1 = 2 * P.p[1] + 1, w2 = 2 * P.p[2] + 1;
         const int dy = (ra / q1) % q2 - (cb / q1) % q2, dz = ra / (q1 * q2) - cb / (q1 * q2);
-        off = P.lineOff[(size_t)elemNode(P, e, cb) * w1 * w2 + (dz + P.p[2]) * w1 + dy + P.p[1]] +
-              S.F[P.firstNode + elemNode(P, e, ra)];
+        off = P.lineOff[(size_t)nodeA[cb] * w1 * w2 + (dz + P.p[2]) * w1 + dy + P.p[1]] + Fa[ra];
       } else {
         const int pos0 = findRow(S.colptr, S.rowidx, firstCol, firstRow);
         if (pos0 < 0) { atomicAdd(S.counters + 1, 1ull); continue; }
@@ -505,7 +637,8 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
         for (int k = 0; k < npv; k++) {
           const int re = eq[ra * npv + k];
           if (re <= 0) continue;
-          addEntry(S.K + S.colptr[ce - 1] + off + rank, side ? Ke[l * npv + k] : Ke[k * npv + l]);
+          addEntry(S.K + S.colptr[ce - 1] + off + rank, side ? Ke[l * npv + k] : Ke[k * npv + l],
+                   kFlow);
           rank++;
         }
       }
@@ -552,8 +685,45 @@ k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ item
         acc -= S.c0[-ce - 1] * (double)kij;
       }
     }
-    if (sizeof(T) == sizeof(double)) S.b[r - 1] += acc;
+    if (sizeof(T) == sizeof(double) && !kFlow) S.b[r - 1] += acc;
     else atomicAdd(S.b + r - 1, acc);
+  }
+  if (kFlow) {  // publish: this element's contributions are all issued
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      genStoreRelease(S.flags + P.flagBase + e, 1);
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ items, SysView S)
+{
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const Item it = items[blockIdx.x];
+  volumeElement<T, false>(patches[it.patch], it, S, smraw);
+}
+
+// Persistent colour-major pass over many patches: blocks claim elements in
+// item order through counters[3], so an element only ever waits for elements
+// claimed before it by running blocks, whatever the grid size.
+template <typename T>
+__global__ void __launch_bounds__(256, 3)  // three blocks per SM, as the per-colour kernel
+k_volume_gen_flow(const DevPatch* __restrict__ patches, const Item* __restrict__ items, int count,
+                  SysView S)
+{
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int claimed;
+  for (;;) {
+    __syncthreads();  // the previous element is done with shared memory
+    if (threadIdx.x == 0) claimed = (int)atomicAdd(S.counters + 3, 1ull);
+    __syncthreads();
+    const int idx = claimed;
+    if (idx >= count) break;
+    const Item it = items[idx];
+    volumeElement<T, true>(patches[it.patch], it, S, smraw);
   }
 }
 
@@ -669,7 +839,7 @@ k_face_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ items
 size_t volumeSmem(const DevPatch& P, size_t real)
 {
   return real * ((size_t)P.nen * 4 + (size_t)P.nq * P.nen * 4 + (size_t)P.nq * 12) +
-         sizeof(int) * (size_t)P.nen * P.npv;
+         sizeof(double) * 2 * (size_t)P.nq + sizeof(int) * (size_t)P.nen * (P.npv + 2);
 }
 
 size_t faceSmem(const DevPatch& P, int nqf)
@@ -773,13 +943,21 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   // colour = (e1 mod q1) + q1 (e2 mod q2) + q1 q2 (e3 mod q3)
   std::vector<char> onTc(np, 0);
   int nflags = 0;
+  // the other patches share one persistent pass when every element has a
+  // volume (the done flags assume a full element grid)
+  bool flow = ctx->opts.colour_passes != 1;
   for (int pi = 0; pi < np; pi++) {
     DevPatch& D = ctx->h_devpatches[pi];
     onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) &&
                D.lineOff != nullptr && D.faceTables && ctx->patches[pi].neumann.size() <= 6;
+    if (!onTc[pi] && ctx->patches[pi].nelActive != ctx->patches[pi].nelAll) flow = false;
+  }
+  for (int pi = 0; pi < np; pi++) {
+    DevPatch& D = ctx->h_devpatches[pi];
     D.flagBase = nflags;
+    D.tile = 4;
+    if (onTc[pi] || flow) nflags += ctx->patches[pi].nelAll;
     if (onTc[pi]) {
-      nflags += ctx->patches[pi].nelAll;
       // the element kernel integrates this patch's Neumann faces itself
       D.nneu = (int)ctx->patches[pi].neumann.size();
       for (int f = 0; f < D.nneu; f++) {
@@ -800,7 +978,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
           if (pc.active[e]) out.push_back({pi, e, 0, 0});
         }
   };
-  if (nflags > 0) {
+  if (std::count(onTc.begin(), onTc.end(), 1) > 0) {
     Pass pass{(int)vol.size(), 0, 0, 81, tcVolumeSmem(), true};
     for (int c = 0; c < maxColours; c++)
       for (int pi = 0; pi < np; pi++)
@@ -808,17 +986,55 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     pass.count = (int)vol.size() - pass.first;
     ctx->passes.push_back(pass);
   }
-  for (int c = 0; c < maxColours; c++) {
+  ctx->onFlow.assign(np, 0);
+  for (int pi = 0; pi < np; pi++) ctx->onFlow[pi] = flow && !onTc[pi];
+  if (flow) {  // one colour-major launch over every other patch
     Pass pass{(int)vol.size(), 0, 0, 0, 0, false};
+    pass.persistent = true;
+    for (int c = 0; c < maxColours; c++)
+      for (int pi = 0; pi < np; pi++)
+        if (!onTc[pi]) colourItems(pi, c, vol);
     for (int pi = 0; pi < np; pi++) {
       if (onTc[pi]) continue;
-      const HostPatch& pc = ctx->patches[pi];
-      colourItems(pi, c, vol);
-      pass.maxNd = std::max(pass.maxNd, pc.nen() * pc.npv);
+      pass.maxNd = std::max(pass.maxNd, ctx->patches[pi].nen() * ctx->patches[pi].npv);
       pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi], realBytes));
     }
     pass.count = (int)vol.size() - pass.first;
-    if (pass.count) ctx->passes.push_back(pass);
+    if (pass.count) {
+      ctx->passes.push_back(pass);
+      // the same items as one launch per colour (the autotuner picks the faster)
+      int at = pass.first;
+      for (int c = 0; c < maxColours; c++) {
+        Pass cp{at, 0, 0, pass.maxNd, pass.smem, false};
+        cp.altColour = true;
+        for (int pi = 0; pi < np; pi++) {
+          if (onTc[pi]) continue;
+          const HostPatch& pc = ctx->patches[pi];
+          const int q1 = pc.p[0] + 1, q2 = pc.p[1] + 1, q3 = pc.dim == 3 ? pc.p[2] + 1 : 1;
+          if (c >= q1 * q2 * q3) continue;
+          const int c1 = c % q1, c2 = (c / q1) % q2, c3 = c / (q1 * q2);
+          cp.count += ((pc.nel[0] - c1 + q1 - 1) / q1) * ((pc.nel[1] - c2 + q2 - 1) / q2) *
+                      ((pc.nel[2] - c3 + q3 - 1) / q3);
+        }
+        at += cp.count;
+        if (cp.count) ctx->passes.push_back(cp);
+      }
+      if (at != pass.first + pass.count)
+        return setError(ctx, IFEMGPU_CUDA_ERROR, "internal: colour ranges of the persistent pass");
+    }
+  } else {
+    for (int c = 0; c < maxColours; c++) {
+      Pass pass{(int)vol.size(), 0, 0, 0, 0, false};
+      for (int pi = 0; pi < np; pi++) {
+        if (onTc[pi]) continue;
+        const HostPatch& pc = ctx->patches[pi];
+        colourItems(pi, c, vol);
+        pass.maxNd = std::max(pass.maxNd, pc.nen() * pc.npv);
+        pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi], realBytes));
+      }
+      pass.count = (int)vol.size() - pass.first;
+      if (pass.count) ctx->passes.push_back(pass);
+    }
   }
   ctx->nflags = nflags;
   if (nflags) IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_flags, sizeof(int) * nflags));
@@ -882,8 +1098,28 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
                                          (int)std::min<size_t>(maxSmem, 227 * 1024)));
   IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_face_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)std::min<size_t>(maxSmem, 227 * 1024)));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_gen_flow<double>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::min<size_t>(maxSmem, 227 * 1024)));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_gen_flow<float>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::min<size_t>(maxSmem, 227 * 1024)));
   IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&ctx->numSMs, cudaDevAttrMultiProcessorCount,
                                            ctx->opts.device));
+  // default grid of the persistent pass: as many blocks as fit at once
+  ctx->genGrid = 0;
+  ctx->tuned = false;
+  for (auto& p : ctx->passes)
+    if (p.persistent) {
+      int perSM = 0;
+      if (ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32)
+        IFEMGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                              &perSM, k_volume_gen_flow<float>, 256, p.smem));
+      else
+        IFEMGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                              &perSM, k_volume_gen_flow<double>, 256, p.smem));
+      ctx->genGrid = std::max(1, perSM) * ctx->numSMs;
+    }
   for (auto& p : ctx->passes)
     if (p.tc) {
       IFEMGPU_TRY(tcPrepare(ctx));
@@ -943,12 +1179,20 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
     return IFEMGPU_OK;
   }
   SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
-            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore};
+            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore, ctx->d_flags};
+  const bool split = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32;
   for (const Pass& p : ctx->passes) {
     if ((p.face != 0) != (seg == 2)) continue;
+    if ((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow)) continue;
     if (p.tc)
       IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
-    else if (!p.face && ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32)
+    else if (p.persistent && split)
+      k_volume_gen_flow<float><<<std::min(p.count, ctx->genGrid), 256, p.smem, s>>>(
+          ctx->d_patches, ctx->d_items + p.first, p.count, S);
+    else if (p.persistent)
+      k_volume_gen_flow<double><<<std::min(p.count, ctx->genGrid), 256, p.smem, s>>>(
+          ctx->d_patches, ctx->d_items + p.first, p.count, S);
+    else if (!p.face && split)
       k_volume_gen<float><<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
     else if (!p.face)
       k_volume_gen<double><<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
@@ -960,9 +1204,122 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
   return IFEMGPU_OK;
 }
 
+// Autotuner of the persistent pass, run once before the first assembly is
+// captured: for every (degree, dim) group of FP32 Poisson patches the register
+// tile of the element matrix (2 x 2 or 4 x 4 node pairs per thread), then the
+// grid (1 .. the occupancy limit of blocks per SM), each candidate timed with
+// device events on a full pass (prologue untimed); the fastest is kept.
+static ifemgpu_status autotune(ifemgpu_ctx* ctx)
+{
+  ctx->tuned = true;
+  ctx->tuneLog.clear();
+  const Pass* pp = nullptr;
+  for (const Pass& p : ctx->passes)
+    if (p.persistent) pp = &p;
+  if (!pp) return IFEMGPU_OK;
+  const bool split = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32;
+  cudaStream_t s = ctx->stream;
+  SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
+            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore, ctx->d_flags};
+  const int np = (int)ctx->h_devpatches.size();
+  // grid > 0: the persistent pass with that grid; grid = 0: its colour passes
+  auto timePass = [&](int grid, float* ms) -> ifemgpu_status {
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      IFEMGPU_TRY(enqueueSegment(ctx, 0));
+      IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+      if (grid > 0 && split)
+        k_volume_gen_flow<float><<<std::min(pp->count, grid), 256, pp->smem, s>>>(
+            ctx->d_patches, ctx->d_items + pp->first, pp->count, S);
+      else if (grid > 0)
+        k_volume_gen_flow<double><<<std::min(pp->count, grid), 256, pp->smem, s>>>(
+            ctx->d_patches, ctx->d_items + pp->first, pp->count, S);
+      else
+        for (const Pass& p : ctx->passes) {
+          if (!p.altColour) continue;
+          if (split)
+            k_volume_gen<float><<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
+          else
+            k_volume_gen<double><<<p.count, 256, p.smem, s>>>(ctx->d_patches, ctx->d_items + p.first, S);
+        }
+      IFEMGPU_CUDA(ctx, cudaGetLastError());
+      IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+      IFEMGPU_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]));
+      float t = 0.f;
+      IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
+      best = std::min(best, t);
+    }
+    *ms = best;
+    return IFEMGPU_OK;
+  };
+  auto pushPatches = [&]() -> ifemgpu_status {
+    IFEMGPU_CUDA(ctx, cudaMemcpy(ctx->d_patches, ctx->h_devpatches.data(),
+                                 sizeof(DevPatch) * np, cudaMemcpyHostToDevice));
+    return IFEMGPU_OK;
+  };
+  // groups of FP32 Poisson patches by (degree, dim)
+  std::vector<std::pair<int, int>> keys;
+  for (int pi = 0; pi < np; pi++) {
+    const DevPatch& D = ctx->h_devpatches[pi];
+    if (!split || !ctx->onFlow[pi] || D.kind != IFEMGPU_POISSON || ctx->nceq) continue;
+    const std::pair<int, int> k{std::max({D.p[0], D.p[1], D.p[2]}), D.dim};
+    if (std::find(keys.begin(), keys.end(), k) == keys.end()) keys.push_back(k);
+  }
+  for (const auto& k : keys) {
+    int bestTile = 4;
+    float bestMs = 1e30f;
+    for (int tile : {4, 2}) {
+      for (int pi = 0; pi < np; pi++) {
+        DevPatch& D = ctx->h_devpatches[pi];
+        if (ctx->onFlow[pi] && D.kind == IFEMGPU_POISSON &&
+            std::max({D.p[0], D.p[1], D.p[2]}) == k.first && D.dim == k.second)
+          D.tile = tile;
+      }
+      IFEMGPU_TRY(pushPatches());
+      float ms = 0.f;
+      IFEMGPU_TRY(timePass(ctx->genGrid, &ms));
+      if (ms < bestMs) { bestMs = ms; bestTile = tile; }
+    }
+    for (int pi = 0; pi < np; pi++) {
+      DevPatch& D = ctx->h_devpatches[pi];
+      if (ctx->onFlow[pi] && D.kind == IFEMGPU_POISSON &&
+          std::max({D.p[0], D.p[1], D.p[2]}) == k.first && D.dim == k.second)
+        D.tile = bestTile;
+    }
+    ctx->tuneLog.insert(ctx->tuneLog.end(), {k.first, k.second, bestTile});
+  }
+  IFEMGPU_TRY(pushPatches());
+  const int maxPerSM = std::max(1, ctx->genGrid / std::max(1, ctx->numSMs));
+  int bestGrid = ctx->genGrid;
+  float bestMs = 1e30f;
+  for (int perSM = 1; perSM <= maxPerSM; perSM++) {
+    float ms = 0.f;
+    IFEMGPU_TRY(timePass(perSM * ctx->numSMs, &ms));
+    if (ms < bestMs) { bestMs = ms; bestGrid = perSM * ctx->numSMs; }
+  }
+  ctx->genGrid = bestGrid;
+  ctx->tuneLog.insert(ctx->tuneLog.end(), {0, 0, bestGrid});
+  // persistent launch or one launch per colour (forced by the context option)
+  float colourMs = 0.f;
+  IFEMGPU_TRY(timePass(0, &colourMs));
+  ctx->useFlow = ctx->opts.colour_passes == 2 || (ctx->opts.colour_passes == 0 && bestMs <= colourMs);
+  ctx->tuneLog.insert(ctx->tuneLog.end(), {-1, (int)(bestMs * 1000.f), (int)(colourMs * 1000.f)});
+  if (ctx->opts.verbose) {
+    for (size_t i = 0; i + 2 < ctx->tuneLog.size(); i += 3) {
+      const int* t = ctx->tuneLog.data() + i;
+      if (t[0] > 0) std::printf("ifemgpu autotune: p=%d dim=%d tile %d\n", t[0], t[1], t[2]);
+      else if (t[0] == 0) std::printf("ifemgpu autotune: persistent grid %d\n", t[2]);
+      else std::printf("ifemgpu autotune: persistent %.3f ms, per colour %.3f ms -> %s\n",
+                       t[1] * 1e-3, t[2] * 1e-3, ctx->useFlow ? "persistent" : "per colour");
+    }
+  }
+  return IFEMGPU_OK;
+}
+
 ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
 {
   cudaStream_t s = ctx->stream;
+  if (!ctx->tuned) IFEMGPU_TRY(autotune(ctx));
   bool hasSeg[3] = {true, false, false};
   for (const Pass& p : ctx->passes) hasSeg[p.face ? 2 : 1] = true;
   for (int seg = 0; seg < 3; seg++) {
@@ -984,7 +1341,10 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
     if (hasSeg[seg]) IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[seg], s));
   }
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
-  ctx->launches_per_assembly = (int)ctx->h_devpatches.size() + (int)ctx->passes.size();
+  int used = 0;
+  for (const Pass& p : ctx->passes)
+    used += !((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow));
+  ctx->launches_per_assembly = (int)ctx->h_devpatches.size() + used;
   return IFEMGPU_OK;
 }
 

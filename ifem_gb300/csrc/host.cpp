@@ -657,6 +657,69 @@ ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
   return IFEMGPU_OK;
 }
 
+// Block-CSR copy of the assembled matrix: block rows of `block` consecutive
+// equations that are the DOFs of one node.  The pattern is symmetric, so the
+// block columns of block row I are the block rows listed in column I b; the
+// value of block (I, J)[k][l] = K(I b + k, J b + l) is read from column
+// J b + l at row I b + k (the values themselves are symmetric only up to
+// rounding).
+ifemgpu_status ifemgpu_copy_matrix_bsr(ifemgpu_ctx* ctx, int block, int* nbrows, int64_t* nnzb,
+                                       int* browptr, int* bcolind, double* bvals)
+{
+  if (!ctx || block < 1) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "copy_matrix_bsr before assemble");
+  const int b = block, neq = ctx->neq;
+  if (neq % b) return setError(ctx, IFEMGPU_UNSUPPORTED, "copy_matrix_bsr: equations not a multiple of the block");
+  // equation -> (node, component); blocks must be the DOFs 0..b-1 of one node
+  std::vector<int> eqNode(neq, -1), eqComp(neq, -1);
+  for (int n = 0; n < ctx->nnod; n++)
+    for (int d = ctx->madof[n] - 1; d < ctx->madof[n + 1] - 1; d++) {
+      const int e = ctx->meqn[d];
+      if (e > 0) { eqNode[e - 1] = n; eqComp[e - 1] = d - (ctx->madof[n] - 1); }
+    }
+  const int nb = neq / b;
+  for (int I = 0; I < nb; I++)
+    for (int k = 0; k < b; k++) {
+      const int e = I * b + k;
+      if (eqComp[e] != k || eqNode[e] != eqNode[I * b])
+        return setError(ctx, IFEMGPU_UNSUPPORTED, "copy_matrix_bsr: a node's DOFs are not one free block");
+      const int c0 = ctx->colptr[I * b], c = ctx->colptr[e];
+      const int len = ctx->colptr[I * b + 1] - c0;
+      if (ctx->colptr[e + 1] - c != len ||
+          !std::equal(ctx->rowidx.begin() + c0, ctx->rowidx.begin() + c0 + len, ctx->rowidx.begin() + c))
+        return setError(ctx, IFEMGPU_UNSUPPORTED, "copy_matrix_bsr: DOFs of a node couple differently");
+      if (len % b) return setError(ctx, IFEMGPU_UNSUPPORTED, "copy_matrix_bsr: partial blocks");
+    }
+  if (nbrows) *nbrows = nb;
+  if (nnzb) *nnzb = ctx->nnz / ((int64_t)b * b);
+  if (!browptr && !bcolind && !bvals) return IFEMGPU_OK;
+  std::vector<double> K;
+  if (bvals) {
+    K.resize(ctx->nnz);
+    ifemgpu_status st = ifemgpu_copy_matrix(ctx, K.data());
+    if (st != IFEMGPU_OK) return st;
+  }
+  int64_t blk = 0;
+  if (browptr) browptr[0] = 0;
+  for (int I = 0; I < nb; I++) {
+    const int c0 = ctx->colptr[I * b], len = ctx->colptr[I * b + 1] - c0;
+    for (int p = 0; p < len; p += b, blk++) {
+      const int J = ctx->rowidx[c0 + p] / b;
+      if (bcolind) bcolind[blk] = J;
+      if (!bvals) continue;
+      // position of row I b in column J b (same offset in columns J b + l)
+      const int* col = ctx->rowidx.data() + ctx->colptr[J * b];
+      const int clen = ctx->colptr[J * b + 1] - ctx->colptr[J * b];
+      const int q = (int)(std::lower_bound(col, col + clen, I * b) - col);
+      for (int k = 0; k < b; k++)
+        for (int l = 0; l < b; l++)
+          bvals[blk * b * b + k * b + l] = K[ctx->colptr[J * b + l] + q + k];
+    }
+    if (browptr) browptr[I + 1] = (int)blk;
+  }
+  return IFEMGPU_OK;
+}
+
 // ---- learned coarse correction (learned.cu, solver.cu) ----------------------
 
 static ifemgpu_status deviceReady(ifemgpu_ctx* ctx)

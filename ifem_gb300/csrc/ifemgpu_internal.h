@@ -46,6 +46,7 @@ struct DevPatch {
   float* tabNf[3];
   float* tabDf[3];
   int flagBase;       // first slot of this patch's elements in the done-flag array
+  int tile;           // register tile of the FP32 Poisson element matrix (2 or 4)
   // Neumann faces integrated inside the tensor-core element kernel
   int nneu;
   int neuFace[6];
@@ -120,6 +121,8 @@ struct Pass {
   int maxNd;   // largest element DOF count in the pass
   size_t smem; // dynamic shared memory of the pass' launch
   bool tc;     // volume pass on the tensor-core kernel
+  bool persistent = false;  // one colour-major launch ordered by done flags
+  bool altColour = false;   // colour pass over a part of the persistent pass' items
 };
 
 // tc_volume.cu
@@ -170,6 +173,12 @@ struct ifemgpu_ctx {
   unsigned long long last_singular = 0;
   int launches_per_assembly = 0;
   int numSMs = 1;
+  // persistent generic pass: grid (autotuned with the tile shapes at the first assembly)
+  int genGrid = 0;
+  bool tuned = false;
+  bool useFlow = true;           // persistent pass (true) or its colour passes
+  std::vector<int> tuneLog;      // (p, dim, tile) per tuned group, then (0, 0, grid)
+  std::vector<char> onFlow;      // per patch: element work in the persistent pass
   // solver workspace (allocated on first solve)
   float* d_K32 = nullptr;
   double* d_work = nullptr;

@@ -87,11 +87,18 @@ __device__ __forceinline__ void redAdd(double* p, double v)
   atomicAdd(p, v);  // result unused: compiles to an L2 reduction
 }
 
-__device__ __forceinline__ int loadAcquire(const int* p)
+// neighbour flags are polled with relaxed loads (served by L2); a thread that
+// saw one issues a single acquire fence before the block's scatter
+__device__ __forceinline__ int loadRelaxed(const int* p)
 {
   int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+
+__device__ __forceinline__ void fenceAcquire()
+{
+  asm volatile("fence.acq_rel.gpu;" : : : "memory");
 }
 
 __device__ __forceinline__ void storeRelease(int* p, int v)
@@ -456,13 +463,14 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
         if (nc < myc) {
           const int* flag = S.flags + P.flagBase + (f3 * P.nel[1] + f2) * P.nel[0] + f1;
           uint32_t spin = 0;
-          while (loadAcquire(flag) == 0) {
+          while (loadRelaxed(flag) == 0) {
             if (++spin > kFlagSpin) {
               atomicAdd(S.counters + 2, 1ull);
               break;
             }
             __nanosleep(64);
           }
+          fenceAcquire();
         }
       }
     }

@@ -20,7 +20,7 @@ from .build import LIB
 
 class Options(C.Structure):
     _fields_ = [("device", C.c_int), ("ke_precision", C.c_int), ("n_gauss", C.c_int),
-                ("verbose", C.c_int)]
+                ("verbose", C.c_int), ("colour_passes", C.c_int)]
 
 
 class Sizes(C.Structure):
@@ -73,7 +73,7 @@ EXPORTS = [
     "ifemgpu_learn_collect", "ifemgpu_learn_clear", "ifemgpu_learn_train",
     "ifemgpu_learn_evaluate", "ifemgpu_learn_gradients", "ifemgpu_learn_info",
     "ifemgpu_learn_get_weights", "ifemgpu_learn_set_weights", "ifemgpu_patch_update_field",
-    "ifemgpu_learn_get_pairs", "ifemgpu_apply_preconditioner",
+    "ifemgpu_learn_get_pairs", "ifemgpu_apply_preconditioner", "ifemgpu_copy_matrix_bsr",
 ]
 
 
@@ -129,6 +129,7 @@ def load_library(path: str | None = None):
         "ifemgpu_learn_clear": (I, [P]),
         "ifemgpu_learn_get_pairs": (I, [P, I, I, V, V]),
         "ifemgpu_apply_preconditioner": (I, [P, I, V, V]),
+        "ifemgpu_copy_matrix_bsr": (I, [P, I, C.POINTER(I), C.POINTER(C.c_int64), V, V, V]),
         "ifemgpu_learn_train": (I, [P, I, I, C.c_float, C.c_uint, C.POINTER(C.c_float)]),
         "ifemgpu_learn_evaluate": (I, [P, C.POINTER(C.c_float)]),
         "ifemgpu_learn_gradients": (I, [P, V, V, I, V, C.POINTER(C.c_float)]),
@@ -196,10 +197,10 @@ class SIM:
     """One GPU model: patches, numbering, system (mirrors SIMbase usage)."""
 
     def __init__(self, n_gauss: int = 4, ke_precision: int = KE_FP64, device: int = 0,
-                 verbose: int = 0):
+                 verbose: int = 0, colour_passes: int = 0):
         self.lib = load_library()
         self.ctx = C.c_void_p()
-        opts = Options(device, ke_precision, n_gauss, verbose)
+        opts = Options(device, ke_precision, n_gauss, verbose, colour_passes)
         st = self.lib.ifemgpu_ctx_create(C.byref(self.ctx), C.byref(opts))
         if st != OK:
             raise IfemGpuError(st, "ifemgpu_ctx_create failed (no CUDA device?)")
@@ -311,6 +312,18 @@ class SIM:
         out = np.zeros(self.sizes.neq, dtype=np.float64)
         self._check(self.lib.ifemgpu_copy_rhs(self.ctx, _ptr(out)))
         return out
+
+    def matrix_bsr(self, block: int):
+        """(browptr, bcolind, blocks[nnzb, block, block]) of the assembled matrix."""
+        nb, nnzb = C.c_int(), C.c_int64()
+        self._check(self.lib.ifemgpu_copy_matrix_bsr(self.ctx, block, C.byref(nb), C.byref(nnzb),
+                                                     None, None, None))
+        rp = np.zeros(nb.value + 1, dtype=np.int32)
+        ci = np.zeros(nnzb.value, dtype=np.int32)
+        vals = np.zeros((nnzb.value, block, block), dtype=np.float64)
+        self._check(self.lib.ifemgpu_copy_matrix_bsr(self.ctx, block, C.byref(nb), C.byref(nnzb),
+                                                     _ptr(rp), _ptr(ci), _ptr(vals)))
+        return rp, ci, vals
 
     def copy_matrix_into(self, out: np.ndarray):
         assert out.dtype == np.float64 and out.size >= self.sizes.nnz

@@ -66,6 +66,12 @@ typedef struct ifemgpu_options {
                         degree+1+k points (ASMbase::getNoGaussPt,
                         src/ASM/ASMbase.C:1788-1798)                          */
   int verbose;       /* 0 silent, 1 model summary on stdout                  */
+  int colour_passes; /* generic element kernel (patches off the tensor-core
+                        kernel): 0 the first assembly times one persistent
+                        colour-major launch ordered by per-element done flags
+                        (every element must have a volume) against one launch
+                        per colour and keeps the faster; 1 one launch per
+                        colour; 2 the persistent launch                     */
 } ifemgpu_options;
 
 typedef struct ifemgpu_sizes {
@@ -222,6 +228,17 @@ ifemgpu_status ifemgpu_last_assembly_stats(ifemgpu_ctx* ctx, double* total_ms,
                                            double* volume_ms,
                                            long long* singular_points,
                                            int* kernel_launches);
+
+/* Block-CSR copy of the assembled matrix for models whose free DOFs come in
+ * whole nodes of `block` DOFs (e.g. block 3 for elasticity with fully
+ * clamped faces): block rows in equation order, column indices ascending,
+ * blocks row-major (block (I, J)[k][l] = K(I*block + k, J*block + l)).
+ * Pass null arrays to get *nbrows and *nnzb only.  No IFEM counterpart in
+ * this form (IFEM's SparseMatrix is scalar CSC/CSR; PETSc's BAIJ matrices
+ * take this layout).                                                      */
+ifemgpu_status ifemgpu_copy_matrix_bsr(ifemgpu_ctx* ctx, int block, int* nbrows,
+                                       int64_t* nnzb, int* browptr, int* bcolind,
+                                       double* bvals);
 
 /* ---- solve ------------------------------------------------------------ */
 
