@@ -301,32 +301,40 @@ __device__ void poissonTiles(const DevPatch& P, const SysView& S, const float* d
 {
   const int nen = P.nen, nq = P.nq, dim = P.dim;
   const int q1 = P.p[0] + 1, q2 = P.p[1] + 1;
-  const int nt = (nen + TS - 1) / TS, ntp = nt * (nt + 1) / 2, K = nq * dim;
+  const int nt = (nen + TS - 1) / TS, ntp = nt * (nt + 1) / 2;
   for (int t = threadIdx.x; t < ntp; t += blockDim.x) {
     int tb = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
     while (tb * (tb + 1) / 2 > t) tb--;
     while ((tb + 1) * (tb + 2) / 2 <= t) tb++;
     const int ta = t - tb * (tb + 1) / 2;
+    // functions past nen are clamped to the last one; their sums are dropped
+    int ia[TS], ib[TS];
+#pragma unroll
+    for (int i = 0; i < TS; i++) {
+      ia[i] = min(TS * ta + i, nen - 1);
+      ib[i] = min(TS * tb + i, nen - 1);
+    }
     float acc[TS][TS];
 #pragma unroll
     for (int i = 0; i < TS; i++)
 #pragma unroll
       for (int j = 0; j < TS; j++) acc[i][j] = 0.f;
-    for (int k = 0; k < K; k++) {
-      const int c = k / nq, q = k - c * nq;
-      const float* row = dX + c * nq * nen + q * nen;
-      const float s = kq[q];
-      float va[TS], vb[TS];
+    for (int c = 0; c < dim; c++) {
+      const float* plane = dX + c * nq * nen;
+      for (int q = 0; q < nq; q++) {
+        const float* row = plane + q * nen;
+        const float s = kq[q];
+        float va[TS], vb[TS];
 #pragma unroll
-      for (int i = 0; i < TS; i++) {
-        const int a = TS * ta + i, b = TS * tb + i;
-        va[i] = a < nen ? row[a] * s : 0.f;
-        vb[i] = b < nen ? row[b] : 0.f;
+        for (int i = 0; i < TS; i++) {
+          va[i] = row[ia[i]] * s;
+          vb[i] = row[ib[i]];
+        }
+#pragma unroll
+        for (int i = 0; i < TS; i++)
+#pragma unroll
+          for (int j = 0; j < TS; j++) acc[i][j] = fmaf(va[i], vb[j], acc[i][j]);
       }
-#pragma unroll
-      for (int i = 0; i < TS; i++)
-#pragma unroll
-        for (int j = 0; j < TS; j++) acc[i][j] += va[i] * vb[j];
     }
 #pragma unroll
     for (int i = 0; i < TS; i++)
@@ -458,15 +466,15 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
     }
     T Jt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // column-major J(r,c) = dX_r/du_c
     T Xt[3] = {0, 0, 0};
-    double gk = 0.0, sn = 0.0;               // log-conductivity and noise sums
+    T gk = 0, sn = 0;                        // log-conductivity and noise sums
     for (int a = lane; a < nen; a += 32) {
       const T x = Xn[a * 4], y = Xn[a * 4 + 1], z = Xn[a * 4 + 2];
       Jt[0] += x * Du[a]; Jt[1] += y * Du[a]; Jt[2] += z * Du[a];
       Jt[3] += x * Dv[a]; Jt[4] += y * Dv[a]; Jt[5] += z * Dv[a];
       Jt[6] += x * Dw[a]; Jt[7] += y * Dw[a]; Jt[8] += z * Dw[a];
       Xt[0] += x * Nr[a]; Xt[1] += y * Nr[a]; Xt[2] += z * Nr[a];
-      if (P.kind == IFEMGPU_POISSON && P.logk) gk += (double)Nr[a] * P.logk[nodeA[a]];
-      if (P.kind == IFEMGPU_POISSON && P.noise) sn += (double)Nr[a] * P.noise[nodeA[a]];
+      if (P.kind == IFEMGPU_POISSON && P.logk) gk += Nr[a] * (T)P.logk[nodeA[a]];
+      if (P.kind == IFEMGPU_POISSON && P.noise) sn += Nr[a] * (T)P.noise[nodeA[a]];
     }
 #pragma unroll
     for (int c = 0; c < 9; c++) Jt[c] = warpAllSum(Jt[c]);
@@ -498,26 +506,29 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
     for (int c = 0; c < 3; c++) X[c] = (double)Xt[c] + c00[c];
     double det, B[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (dim == 3) {
-      // matrix<T>::det / inverse (src/LinAlg/matrix.h:790-850), T(i,j)=J[(j-1)*3+i-1]
+      // matrix<T>::det / inverse (src/LinAlg/matrix.h:790-850), T(i,j)=J[(j-1)*3+i-1];
+      // cofactors times one reciprocal of det (FP64 divisions are costly here)
       det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[3] * (J[1] * J[8] - J[2] * J[7]) +
             J[6] * (J[1] * J[5] - J[2] * J[4]);
       if (det > kEpsZ || det < -kEpsZ) {
-        B[0] = (J[4] * J[8] - J[5] * J[7]) / det;
-        B[1] = -(J[1] * J[8] - J[2] * J[7]) / det;
-        B[2] = (J[1] * J[5] - J[2] * J[4]) / det;
-        B[3] = -(J[3] * J[8] - J[5] * J[6]) / det;
-        B[4] = (J[0] * J[8] - J[2] * J[6]) / det;
-        B[5] = -(J[0] * J[5] - J[2] * J[3]) / det;
-        B[6] = (J[3] * J[7] - J[4] * J[6]) / det;
-        B[7] = -(J[0] * J[7] - J[1] * J[6]) / det;
-        B[8] = (J[0] * J[4] - J[1] * J[3]) / det;
+        const double id = 1.0 / det;
+        B[0] = (J[4] * J[8] - J[5] * J[7]) * id;
+        B[1] = -(J[1] * J[8] - J[2] * J[7]) * id;
+        B[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+        B[3] = -(J[3] * J[8] - J[5] * J[6]) * id;
+        B[4] = (J[0] * J[8] - J[2] * J[6]) * id;
+        B[5] = -(J[0] * J[5] - J[2] * J[3]) * id;
+        B[6] = (J[3] * J[7] - J[4] * J[6]) * id;
+        B[7] = -(J[0] * J[7] - J[1] * J[6]) * id;
+        B[8] = (J[0] * J[4] - J[1] * J[3]) * id;
       }
     } else {
       // 2x2: J(r,c) at J[c*3+r] in the 3x3 storage above
       det = J[0] * J[4] - J[1] * J[3];
       if (det > kEpsZ || det < -kEpsZ) {
-        B[0] = J[4] / det; B[1] = -J[1] / det;
-        B[3] = -J[3] / det; B[4] = J[0] / det;
+        const double id = 1.0 / det;
+        B[0] = J[4] * id; B[1] = -J[1] * id;
+        B[3] = -J[3] * id; B[4] = J[0] * id;
       }
     }
     double w = 0.0;
@@ -535,7 +546,7 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
     // material data at the point
     double kap = P.kappa, f = P.source;
     if (P.kind == IFEMGPU_POISSON) {
-      if (P.logk) kap *= exp(gk);
+      if (P.logk) kap *= sizeof(T) == sizeof(float) ? (double)expf((float)gk) : exp(gk);
       if (P.source_shape == IFEMGPU_SOURCE_SINE)
         for (int c = 0; c < dim; c++) f *= sin(M_PI * X[c]);
       if (P.noise) f *= 1.0 + sn;
@@ -698,7 +709,7 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 k_volume_gen(const DevPatch* __restrict__ patches, const Item* __restrict__ items, SysView S)
 {
   extern __shared__ __align__(16) unsigned char smraw[];

@@ -181,6 +181,8 @@ struct ifemgpu_ctx {
   std::vector<char> onFlow;      // per patch: element work in the persistent pass
   // solver workspace (allocated on first solve)
   float* d_K32 = nullptr;
+  short* d_off16 = nullptr;      // 16-bit column offsets of the FP32 SpMV (nullptr: 32-bit)
+  int off16State = 0;            // 0 not built, 1 in use, -1 bandwidth too large
   double* d_work = nullptr;
   size_t work_len = 0;
   double* h_pinned = nullptr;
@@ -229,7 +231,7 @@ double* learnXstar(ifemgpu_ctx* ctx);
 ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx);
 ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* q,
                           double* part, int nparts, unsigned* counter, double* dotOut,
-                          const double* guard);
+                          const double* pq, float* betaOut, const double* guard);
 ifemgpu_status learnTrain(ifemgpu_ctx* ctx, int epochs, int B, float lr, unsigned seed,
                           float* lossOut);
 ifemgpu_status learnEvaluate(ifemgpu_ctx* ctx, float* mse);

@@ -147,13 +147,14 @@ __global__ void __launch_bounds__(kT)
 k_prolong_add(const int* __restrict__ eqCell, const float4* __restrict__ eqFrac,
               const float* __restrict__ y, const float* __restrict__ nrm, int m, int npv,
               float* __restrict__ z, int n, const float* __restrict__ q, double* __restrict__ part,
-              unsigned* counter, double* dotOut, const double* guard)
+              unsigned* counter, double* dotOut, const double* pq, float* betaOut,
+              const double* guard)
 {
   if (stopped(guard)) return;
   __shared__ double sh[32];
   const float sc = nrm[0] * nrm[1];  // |rc| S
   const int m1 = m + 1;
-  double dot = 0.0;
+  float dot = 0.f;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     const int c = eqCell[e];
     const int ci = c % m, cj = (c / m) % m, ck = c / (m * m);
@@ -168,13 +169,16 @@ k_prolong_add(const int* __restrict__ eqCell, const float4* __restrict__ eqFrac,
     }
     const float zi = z[e] + sc * s;
     z[e] = zi;
-    if (q) dot += (double)zi * (double)q[e];
+    if (q) dot += zi * q[e];
   }
   if (!q) return;
-  const double t = blockReduceSum(dot, sh);
+  const double t = blockReduceSumF(dot, sh);
   if (lastBlockDone(part, t, counter)) {
     const double v = finalSum(part, gridDim.x, sh);
-    if (threadIdx.x == 0) *dotOut = v;
+    if (threadIdx.x == 0) {
+      *dotOut = v;
+      *betaOut = (float)(-v / *pq);  // flexible-CG beta
+    }
   }
 }
 
@@ -637,10 +641,11 @@ ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, dou
 
 // z += coarse correction of r with the BF16 network.  With q != 0 the
 // prolongation also forms (z, q) over its grid of nparts blocks and the last
-// block stores it in *dotOut.  Every kernel returns at once when *guard != 0.
+// block stores it in *dotOut and -(z, q) / *pq in *betaOut.  Every kernel
+// returns at once when *guard != 0.
 ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* q,
                           double* part, int nparts, unsigned* counter, double* dotOut,
-                          const double* guard)
+                          const double* pq, float* betaOut, const double* guard)
 {
   LearnState* L = ctx->learn;
   cudaStream_t s = ctx->stream;
@@ -654,7 +659,7 @@ ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const floa
   k_gemv_bf16<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW3, L->theta + L->ob3, L->h2,
                                                       nh, nullptr, 0, L->yc, nc, 0, nullptr, guard);
   k_prolong_add<<<nparts, kT, 0, s>>>(L->eqCell, L->eqFrac, L->yc, L->nrm, L->m, L->npv,
-                                      z, ctx->neq, q, part, counter, dotOut, guard);
+                                      z, ctx->neq, q, part, counter, dotOut, pq, betaOut, guard);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
   return IFEMGPU_OK;
 }

@@ -23,6 +23,24 @@ __device__ inline double blockReduceSum(double v, double* sh)
   return s;
 }
 
+// FP32 partials: warp and block sums in FP32, widened once per block (valid
+// in thread 0); the blocks' partials are then summed in FP64.  FP64
+// instructions issued by one lane cost the FP64 pipe a full warp on this GPU,
+// so per-element work stays in FP32.
+__device__ inline double blockReduceSumF(float v, double* sh)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float* shf = reinterpret_cast<float*>(sh);
+  if (lane == 0) shf[w] = v;
+  __syncthreads();
+  float s = 0.f;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += shf[i];
+  __syncthreads();
+  return (double)s;  // one widening per block
+}
+
 // after thread 0 has stored this block's partials: true in the block that
 // finishes last (every thread of it), which also resets the counter
 __device__ inline bool lastBlock(unsigned* counter)

@@ -246,6 +246,16 @@ constexpr double kStagFactor = 0.25; // required reduction of ||r||^2 per window
 __device__ inline unsigned* tickets(double* s) { return reinterpret_cast<unsigned*>(s + S_CNT); }
 __device__ inline bool loopStopped(const double* s) { return s[S_DONE] != 0.0; }
 
+// FP32 step ratios [0] alpha, [1] beta in scalar slot 16, formed once by the
+// last block of the kernel that finishes their numerator or denominator (an
+// FP64 division per thread or per block would keep the FP64 pipe busy)
+constexpr int S_RAT = 16;
+__device__ inline float* ratios(double* s) { return reinterpret_cast<float*>(s + S_RAT); }
+__device__ inline const float* ratios(const double* s)
+{
+  return reinterpret_cast<const float*>(s + S_RAT);
+}
+
 __global__ void k_loop_init(double* s, double tol2, double maxit, double stagnation)
 {
   s[S_DONE] = 0.0;
@@ -257,6 +267,7 @@ __global__ void k_loop_init(double* s, double tol2, double maxit, double stagnat
   s[S_STAG] = stagnation;
   s[S_RREF] = 1.0;  // the loops start from a unit right-hand side
   s[S_ITREF] = 0.0;
+  ratios(s)[0] = ratios(s)[1] = 0.f;
   unsigned* c = tickets(s);
   for (int i = 0; i < 8; i++) c[i] = 0u;
 }
@@ -291,7 +302,7 @@ g_pcg_start(const double* __restrict__ r64, double* s, T* __restrict__ r, T* __r
 {
   __shared__ double sh[32];
   const double inv = 1.0 / sqrt(s[9]);
-  double acc = 0.0;
+  float acc = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const T ri = (T)(r64[i] * inv);
     const T zi = dinv[i] * ri;
@@ -299,9 +310,9 @@ g_pcg_start(const double* __restrict__ r64, double* s, T* __restrict__ r, T* __r
     x[i] = 0;
     z[i] = zi;
     p[i] = zi;
-    acc += (double)ri * (double)zi;
+    acc += (float)(ri * zi);
   }
-  const double t = blockReduceSum(acc, sh);
+  const double t = blockReduceSumF(acc, sh);
   if (lastBlockDone(part, t, tickets(s) + 4)) {
     const double v = finalSum(part, gridDim.x, sh);
     if (threadIdx.x == 0) s[S_RZ] = s[S_RZN] = v;
@@ -319,7 +330,7 @@ g_spmv(const int* __restrict__ colptr, const int* __restrict__ rowidx, const T* 
   __shared__ double sh[32];
   const int lane = threadIdx.x & 31;
   const int warpsPerGrid = gridDim.x * (blockDim.x >> 5);
-  double dot = 0.0;
+  float dot = 0.f;
   for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += warpsPerGrid) {
     const int b = colptr[row], e = colptr[row + 1];
     T acc = 0;
@@ -327,17 +338,76 @@ g_spmv(const int* __restrict__ colptr, const int* __restrict__ rowidx, const T* 
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) {
       q[row] = acc;
-      dot += (double)acc * (double)p[row];
+      dot += (float)(acc * p[row]);
     }
   }
-  const double t = blockReduceSum(dot, sh);
+  const double t = blockReduceSumF(dot, sh);
   if (lastBlockDone(part, t, tickets(s) + 0)) {
     const double v = finalSum(part, gridDim.x, sh);
     if (threadIdx.x == 0) {
       s[S_PQ] = v;
       if (shift) s[S_RZ] = s[S_RZN];
+      ratios(s)[0] = (float)((shift ? s[S_RZ] : s[S_PR]) / v);  // alpha
     }
   }
+}
+
+// q = A p with 16-bit column offsets relative to the row (banded spline
+// patterns: 6 instead of 8 bytes per entry), four independent load chains per
+// lane; (p, q) -> S_PQ, alpha, with shift also S_RZ <- S_RZN
+__global__ void __launch_bounds__(kThreads)
+g_spmv16(const int* __restrict__ colptr, const short* __restrict__ off, const float* __restrict__ A,
+         const float* __restrict__ p, float* __restrict__ q, int n, double* __restrict__ part,
+         double* s, int shift)
+{
+  if (loopStopped(s)) return;
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31;
+  const int warpsPerGrid = gridDim.x * (blockDim.x >> 5);
+  float dot = 0.f;
+  for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += warpsPerGrid) {
+    const int b = colptr[row], e = colptr[row + 1];
+    float acc = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+    int k = b + lane;
+    for (; k + 96 < e; k += 128) {
+      const int o0 = off[k], o1 = off[k + 32], o2 = off[k + 64], o3 = off[k + 96];
+      const float a0 = A[k], a1 = A[k + 32], a2 = A[k + 64], a3 = A[k + 96];
+      acc += a0 * p[row + o0];
+      acc1 += a1 * p[row + o1];
+      acc2 += a2 * p[row + o2];
+      acc3 += a3 * p[row + o3];
+    }
+    for (; k < e; k += 32) acc += A[k] * p[row + off[k]];
+    acc += (acc1 + acc2) + acc3;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      q[row] = acc;
+      dot += acc * p[row];
+    }
+  }
+  const double t = blockReduceSumF(dot, sh);
+  if (lastBlockDone(part, t, tickets(s) + 0)) {
+    const double v = finalSum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      s[S_PQ] = v;
+      if (shift) s[S_RZ] = s[S_RZN];
+      ratios(s)[0] = (float)((shift ? s[S_RZ] : s[S_PR]) / v);  // alpha
+    }
+  }
+}
+
+// off[k] = rowidx[k] - row (warp per row); *bad = 1 when an offset needs more than 16 bits
+__global__ void k_make_off16(const int* __restrict__ colptr, const int* __restrict__ rowidx, int n,
+                             short* __restrict__ off, int* __restrict__ bad)
+{
+  const int lane = threadIdx.x & 31;
+  const int warpsPerGrid = gridDim.x * (blockDim.x >> 5);
+  for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += warpsPerGrid)
+    for (int k = colptr[row] + lane; k < colptr[row + 1]; k += 32) {
+      const int d = rowidx[k] - row;
+      if (d < -32768 || d > 32767) *bad = 1;
+      off[k] = (short)d;
+    }
 }
 
 // x += a p; r -= a q; z = Dinv r with a = rz / pq; (r, z) -> S_RZN, (r, r) -> check
@@ -349,25 +419,26 @@ g_pcg_update(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, const T* _
 {
   if (loopStopped(s)) return;
   __shared__ double sh[32];
-  const T alpha = (T)(s[S_RZ] / s[S_PQ]);
-  double a1 = 0.0, a2 = 0.0;
+  const T alpha = (T)ratios(s)[0];
+  float a1 = 0.f, a2 = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] += alpha * p[i];
     const T ri = r[i] - alpha * q[i];
     const T zi = dinv[i] * ri;
     r[i] = ri;
     z[i] = zi;
-    a1 += (double)ri * (double)zi;
-    a2 += (double)ri * (double)ri;
+    a1 += (float)(ri * zi);
+    a2 += (float)(ri * ri);
   }
-  const double t1 = blockReduceSum(a1, sh);
-  const double t2 = blockReduceSum(a2, sh);
+  const double t1 = blockReduceSumF(a1, sh);
+  const double t2 = blockReduceSumF(a2, sh);
   if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = t2;
   if (lastBlockDone(part, t1, tickets(s) + 1)) {
     const double rz = finalSum(part, gridDim.x, sh);
     const double rr = finalSum(part + gridDim.x, gridDim.x, sh);
     if (threadIdx.x == 0) {
       s[S_RZN] = rz;
+      ratios(s)[1] = (float)(rz / s[S_RZ]);  // beta of the PCG direction
       loopCheck(s, rr);
     }
   }
@@ -378,7 +449,7 @@ template <typename T>
 __global__ void g_pcg_dir(T* __restrict__ p, const T* __restrict__ z, const double* s, int n)
 {
   if (loopStopped(s)) return;
-  const T beta = (T)(s[S_RZN] / s[S_RZ]);
+  const T beta = (T)ratios(s)[1];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     p[i] = z[i] + beta * p[i];
 }
@@ -407,16 +478,16 @@ g_fcg_update(float* __restrict__ x, float* __restrict__ r, float* __restrict__ z
 {
   if (loopStopped(s)) return;
   __shared__ double sh[32];
-  const float alpha = (float)(s[S_PR] / s[S_PQ]);
-  double acc = 0.0;
+  const float alpha = ratios(s)[0];
+  float acc = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] += alpha * p[i];
     const float ri = r[i] - alpha * q[i];
     r[i] = ri;
     z[i] = dinv[i] * ri;
-    acc += (double)ri * (double)ri;
+    acc += ri * ri;
   }
-  const double t = blockReduceSum(acc, sh);
+  const double t = blockReduceSumF(acc, sh);
   if (lastBlockDone(part, t, tickets(s) + 1)) {
     const double rr = finalSum(part, gridDim.x, sh);
     if (threadIdx.x == 0) loopCheck(s, rr);
@@ -430,34 +501,37 @@ g_fcg_dir(float* __restrict__ p, const float* __restrict__ z, const float* __res
 {
   if (loopStopped(s)) return;
   __shared__ double sh[32];
-  const float beta = (float)(-s[S_ZQ] / s[S_PQ]);
-  double acc = 0.0;
+  const float beta = ratios(s)[1];
+  float acc = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float pi = z[i] + beta * p[i];
     p[i] = pi;
-    acc += (double)pi * (double)r[i];
+    acc += pi * r[i];
   }
-  const double t = blockReduceSum(acc, sh);
+  const double t = blockReduceSumF(acc, sh);
   if (lastBlockDone(part, t, tickets(s) + 3)) {
     const double v = finalSum(part, gridDim.x, sh);
     if (threadIdx.x == 0) s[S_PR] = v;
   }
 }
 
-// (a, b) -> *out
+// (z, q) -> S_ZQ and the flexible-CG beta = -(z, q) / (p, q)
 __global__ void __launch_bounds__(kThreads)
 g_dot(const float* __restrict__ a, const float* __restrict__ b, int n, double* __restrict__ part,
-      unsigned* counter, double* out, const double* s)
+      unsigned* counter, double* s)
 {
   if (loopStopped(s)) return;
   __shared__ double sh[32];
-  double acc = 0.0;
+  float acc = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    acc += (double)a[i] * (double)b[i];
-  const double t = blockReduceSum(acc, sh);
+    acc += a[i] * b[i];
+  const double t = blockReduceSumF(acc, sh);
   if (lastBlockDone(part, t, counter)) {
     const double v = finalSum(part, gridDim.x, sh);
-    if (threadIdx.x == 0) *out = v;
+    if (threadIdx.x == 0) {
+      s[S_ZQ] = v;
+      ratios(s)[1] = (float)(-v / s[S_PQ]);
+    }
   }
 }
 
@@ -515,8 +589,11 @@ void freeSolver(ifemgpu_ctx* ctx)
 {
   dropLoopGraphs(ctx);
   if (ctx->d_K32) cudaFree(ctx->d_K32);
+  if (ctx->d_off16) cudaFree(ctx->d_off16);
   if (ctx->d_work) cudaFree(ctx->d_work);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  ctx->d_off16 = nullptr;
+  ctx->off16State = 0;
   ctx->d_K32 = nullptr;
   ctx->d_work = nullptr;
   ctx->h_pinned = nullptr;
@@ -612,6 +689,8 @@ static inline unsigned* hostTickets(const Work& w)
   return reinterpret_cast<unsigned*>(w.scal + S_CNT);
 }
 
+static void spmv32(ifemgpu_ctx* ctx, const Work& w, const float* p, float* q, int shift);
+
 // FP32 Jacobi-PCG on rhs r64 / sqrt(scal[9]) from x = 0 (captured loop)
 static ifemgpu_status loopPCG32(ifemgpu_ctx* ctx, const Work& w, double rtol, int maxit,
                                 int* iters)
@@ -619,10 +698,8 @@ static ifemgpu_status loopPCG32(ifemgpu_ctx* ctx, const Work& w, double rtol, in
   cudaStream_t s = ctx->stream;
   const int n = ctx->neq;
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
-  const int sb = std::min(kRedBlocks, (n + 7) / 8);
   auto body = [&]() -> ifemgpu_status {
-    g_spmv<float><<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, w.p32, w.q32,
-                                          n, w.part, w.scal, 1);
+    spmv32(ctx, w, w.p32, w.q32, 1);
     g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32,
                                                 w.scal, n, w.part);
     g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
@@ -650,22 +727,21 @@ static ifemgpu_status loopFCG(ifemgpu_ctx* ctx, const Work& w, bool kron, bool l
   cudaStream_t s = ctx->stream;
   const int n = ctx->neq;
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
-  const int sb = std::min(kRedBlocks, (n + 7) / 8);
   unsigned* tk = hostTickets(w);
   const double* guard = w.scal + S_DONE;
-  // z = M r after the Jacobi step of the update kernel; (z, q) -> S_ZQ
+  // z = M r after the Jacobi step of the update kernel; (z, q) -> S_ZQ and beta
   auto precondition = [&](bool withDot) -> ifemgpu_status {
     ifemgpu_status st2;
     if (kron && (st2 = fdApply(ctx, w.r32, w.z32, guard)) != IFEMGPU_OK) return st2;
     if (learned)
       return learnApply(ctx, w.r32, w.z32, withDot ? w.q32 : nullptr, w.part, vb, tk + 2,
-                        w.scal + S_ZQ, guard);
-    if (withDot) g_dot<<<vb, kThreads, 0, s>>>(w.z32, w.q32, n, w.part, tk + 2, w.scal + S_ZQ, w.scal);
+                        w.scal + S_ZQ, w.scal + S_PQ,
+                        reinterpret_cast<float*>(w.scal + S_RAT) + 1, guard);
+    if (withDot) g_dot<<<vb, kThreads, 0, s>>>(w.z32, w.q32, n, w.part, tk + 2, w.scal);
     return IFEMGPU_OK;
   };
   auto body = [&]() -> ifemgpu_status {
-    g_spmv<float><<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, w.p32, w.q32,
-                                          n, w.part, w.scal, 0);
+    spmv32(ctx, w, w.p32, w.q32, 0);
     g_fcg_update<<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32, w.scal, n,
                                          w.part);
     ifemgpu_status st2 = precondition(true);
@@ -705,7 +781,42 @@ static ifemgpu_status ensureWork(ifemgpu_ctx* ctx, bool mixed)
   }
   if (!ctx->h_pinned) IFEMGPU_CUDA(ctx, cudaMallocHost(&ctx->h_pinned, 64));
   if (mixed && !ctx->d_K32) IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_K32, sizeof(float) * ctx->nnz));
+  if (mixed && ctx->off16State == 0) {  // 16-bit column offsets when the band allows
+    ctx->off16State = -1;
+    if (cudaMalloc(&ctx->d_off16, sizeof(short) * std::max<int64_t>(ctx->nnz, 1)) == cudaSuccess) {
+      int* d_bad = reinterpret_cast<int*>(carve(ctx).scal + 30);  // unused scalar slot
+      IFEMGPU_CUDA(ctx, cudaMemsetAsync(d_bad, 0, sizeof(int), ctx->stream));
+      k_make_off16<<<1024, kThreads, 0, ctx->stream>>>(ctx->d_colptr, ctx->d_rowidx, (int)n,
+                                                        ctx->d_off16, d_bad);
+      int bad = 1;
+      IFEMGPU_CUDA(ctx, cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (bad == 0) {
+        ctx->off16State = 1;
+      } else {
+        cudaFree(ctx->d_off16);
+        ctx->d_off16 = nullptr;
+      }
+      dropLoopGraphs(ctx);
+    } else {
+      cudaGetLastError();
+      ctx->d_off16 = nullptr;
+    }
+  }
   return IFEMGPU_OK;
+}
+
+// q = A p of the FP32 loops (16-bit offsets when available)
+static void spmv32(ifemgpu_ctx* ctx, const Work& w, const float* p, float* q, int shift)
+{
+  const int n = ctx->neq;
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  if (ctx->d_off16)
+    g_spmv16<<<sb, kThreads, 0, ctx->stream>>>(ctx->d_colptr, ctx->d_off16, ctx->d_K32, p, q, n,
+                                               w.part, w.scal, shift);
+  else
+    g_spmv<float><<<sb, kThreads, 0, ctx->stream>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, p, q,
+                                                    n, w.part, w.scal, shift);
 }
 
 // FP32 matrix copy, inverse diagonal, x64 = 0, r64 = b, ||b||^2 in scal[8]
@@ -913,8 +1024,7 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
   stride = std::max(1, stride);
   for (int l = 0; l <= maxit / stride; l++) {
     for (int k = 0; k < stride; k++) {
-      g_spmv<float><<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, w.p32, w.q32,
-                                            n, w.part, w.scal, 1);
+      spmv32(ctx, w, w.p32, w.q32, 1);
       g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32,
                                                   w.scal, n, w.part);
       g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
