@@ -740,7 +740,8 @@ ifemgpu_status ifemgpu_learn_setup(ifemgpu_ctx* ctx, const ifemgpu_learn_options
 }
 
 ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs, const double* xstar,
-                                     int stride, int max_iter, double rtol, int* pairs)
+                                     int stride, int max_iter, double rtol, int precond,
+                                     int* pairs)
 {
   ifemgpu_status st = deviceReady(ctx);
   if (st != IFEMGPU_OK) return st;
@@ -748,7 +749,7 @@ ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs, const 
   if (!rhs && !ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "learn_collect before assemble");
   if (stride < 1 || max_iter < 1 || !(rtol > 0))
     return setError(ctx, IFEMGPU_INVALID_ARG, "learn_collect: bad stride, cap or tolerance");
-  st = collectPairs(ctx, rhs, xstar, stride, max_iter, rtol);
+  st = collectPairs(ctx, rhs, xstar, stride, max_iter, rtol, precond);
   if (pairs) *pairs = learnCount(ctx);
   return st;
 }

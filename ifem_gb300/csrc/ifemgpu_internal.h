@@ -219,7 +219,7 @@ ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid);
 ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o,
                         double* x, ifemgpu_solve_info* info, const double* bdev = nullptr);
 ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* xstar,
-                            int stride, int maxit, double rtol);
+                            int stride, int maxit, double rtol, int precond);
 void freeSolver(ifemgpu_ctx* ctx);
 
 // learned.cu

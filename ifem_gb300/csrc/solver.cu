@@ -948,10 +948,6 @@ ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o, doubl
   return IFEMGPU_OK;
 }
 
-// Training pairs from one plain FP32 Jacobi-PCG solve of A x = rhs (the
-// assembled b when rhs is null) from x = 0: every stride-th iterate gives
-// (R r_k, Rn (x* - x_k)).  x* is the caller's reference solution, or the
-// FP64-refined mixed solve to 1e-12 when xstar is null.
 // z = M r for the FP32 preconditioner precond of the assembled matrix (host
 // vectors; diagnostic)
 ifemgpu_status applyPreconditioner(ifemgpu_ctx* ctx, int precond, const double* r, double* z)
@@ -983,9 +979,16 @@ ifemgpu_status applyPreconditioner(ifemgpu_ctx* ctx, int precond, const double* 
   return IFEMGPU_OK;
 }
 
+// Training pairs from one FP32 solve of A x = rhs (the assembled b when rhs
+// is null) from x = 0 -- Jacobi-PCG, or flexible CG with the Kronecker
+// preconditioner (the iteration the network will serve): every stride-th
+// iterate gives (R r_k, Rn (x* - x_k)).  x* is the caller's reference
+// solution, or the FP64-refined mixed solve to 1e-12 when xstar is null.
 ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* xstar, int stride,
-                            int maxit, double rtol)
+                            int maxit, double rtol, int precond)
 {
+  if (precond != IFEMGPU_PRECOND_JACOBI && precond != IFEMGPU_PRECOND_KRONECKER)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "learn_collect: unknown preconditioner");
   const int n = ctx->neq;
   cudaStream_t s = ctx->stream;
   double* xs = learnXstar(ctx);
@@ -1014,20 +1017,40 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
   double bn = 0.0;
   if ((st = solvePrologue(ctx, w, b, true, &bn)) != IFEMGPU_OK) return st;
   if (!(bn > 0)) return IFEMGPU_OK;
+  const bool kron = precond == IFEMGPU_PRECOND_KRONECKER;
+  if (kron) {
+    if ((st = fdSetup(ctx)) != IFEMGPU_OK) return st;
+    if ((st = fdRescale(ctx, w.d64)) != IFEMGPU_OK) return st;
+  }
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
-  const int sb = std::min(kRedBlocks, (n + 7) / 8);
   const double sx = 1.0 / bn;  // the loop solves the system scaled by 1/||b||
+  unsigned* tk = hostTickets(w);
   k_loop_init<<<1, 1, 0, s>>>(w.scal, rtol * rtol, (double)maxit, 0.0);
-  g_pcg_start<float><<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.dinv32,
-                                             n, w.part);
+  if (kron) {  // flexible CG with the Kronecker preconditioner
+    g_fcg_start<<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.q32, w.dinv32, n);
+    if ((st = fdApply(ctx, w.r32, w.z32, w.scal + S_DONE)) != IFEMGPU_OK) return st;
+    g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
+  } else {
+    g_pcg_start<float><<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.dinv32,
+                                               n, w.part);
+  }
   if ((st = learnRecord(ctx, w.r32, w.x32, sx)) != IFEMGPU_OK) return st;
   stride = std::max(1, stride);
   for (int l = 0; l <= maxit / stride; l++) {
     for (int k = 0; k < stride; k++) {
-      spmv32(ctx, w, w.p32, w.q32, 1);
-      g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32,
-                                                  w.scal, n, w.part);
-      g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
+      if (kron) {
+        spmv32(ctx, w, w.p32, w.q32, 0);
+        g_fcg_update<<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32, w.scal,
+                                             n, w.part);
+        if ((st = fdApply(ctx, w.r32, w.z32, w.scal + S_DONE)) != IFEMGPU_OK) return st;
+        g_dot<<<vb, kThreads, 0, s>>>(w.z32, w.q32, n, w.part, tk + 2, w.scal);
+        g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
+      } else {
+        spmv32(ctx, w, w.p32, w.q32, 1);
+        g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32,
+                                                    w.scal, n, w.part);
+        g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
+      }
     }
     IFEMGPU_CUDA(ctx, cudaGetLastError());
     IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + S_DONE, sizeof(double),

@@ -125,7 +125,7 @@ def load_library(path: str | None = None):
         "ifemgpu_selftest_tc_gemm": (I, [V, V, V]),
         "ifemgpu_solve_noalloc": (I, [P, D, I, V, C.POINTER(SolveInfo)]),
         "ifemgpu_learn_setup": (I, [P, C.POINTER(LearnOptions)]),
-        "ifemgpu_learn_collect": (I, [P, V, V, I, I, D, C.POINTER(I)]),
+        "ifemgpu_learn_collect": (I, [P, V, V, I, I, D, I, C.POINTER(I)]),
         "ifemgpu_learn_clear": (I, [P]),
         "ifemgpu_learn_get_pairs": (I, [P, I, I, V, V]),
         "ifemgpu_apply_preconditioner": (I, [P, I, V, V]),
@@ -382,7 +382,8 @@ class SIM:
         return {"coarse_unknowns": nc.value, "inputs": nin.value, "hidden": nh.value,
                 "nparam": npar.value, "pairs": pairs.value}
 
-    def learn_collect(self, rhs=None, xstar=None, stride=1, max_iter=20000, rtol=1e-6) -> int:
+    def learn_collect(self, rhs=None, xstar=None, stride=1, max_iter=20000, rtol=1e-6,
+                      precond=PRECOND_JACOBI) -> int:
         keep = []
         args = []
         for a in (rhs, xstar):
@@ -395,7 +396,7 @@ class SIM:
                 args.append(_ptr(v))
         n = C.c_int()
         self._check(self.lib.ifemgpu_learn_collect(self.ctx, args[0], args[1], stride, max_iter,
-                                                   rtol, C.byref(n)))
+                                                   rtol, precond, C.byref(n)))
         return n.value
 
     def learn_clear(self):

@@ -342,14 +342,17 @@ typedef struct ifemgpu_learn_options {
 ifemgpu_status ifemgpu_learn_setup(ifemgpu_ctx* ctx, const ifemgpu_learn_options* o);
 
 /* Solves A x = rhs (rhs: neq host values, or null for the assembled b)
- * with plain FP32 Jacobi-PCG from x = 0 to the relative residual rtol (at
- * most max_iter iterations) and stores one pair per stride-th iterate:
+ * from x = 0 to the relative residual rtol (at most max_iter iterations)
+ * with FP32 Jacobi-PCG (precond IFEMGPU_PRECOND_JACOBI) or flexible CG with
+ * the Kronecker preconditioner (IFEMGPU_PRECOND_KRONECKER: the iteration the
+ * network is added to) and stores one pair per stride-th iterate:
  * (R r_k / |R r_k|, Rn (x* - x_k) / |R r_k|), Rn the weight-normalised
  * restriction.  x* is xstar (neq host values) or, when null, the library's
  * FP64-refined solve to 1e-12.  *pairs receives the stored total.          */
 ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs,
                                      const double* xstar, int stride,
-                                     int max_iter, double rtol, int* pairs);
+                                     int max_iter, double rtol, int precond,
+                                     int* pairs);
 
 /* Forgets the stored pairs (the network is kept).                         */
 ifemgpu_status ifemgpu_learn_clear(ifemgpu_ctx* ctx);

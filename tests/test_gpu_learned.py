@@ -186,3 +186,19 @@ def test_learned_solve_needs_training(gpulib):
     info = G.SolveInfo()
     o = G.SolverOptions(G.FCG_LEARNED, 1e-10, 20, 1000, 1e-4, 0)
     assert sim.lib.ifemgpu_solve(sim.ctx, G.C.byref(o), G._ptr(x), G.C.byref(info)) == G.NOT_READY
+
+
+def test_pairs_from_kronecker_iterates(gpulib):
+    """Pairs collected along flexible CG with the Kronecker preconditioner:
+    iterate 0 is the same pair as along Jacobi-PCG (x = 0), the run stops
+    after far fewer iterates, and every pair is finite."""
+    sim, _ = poisson_model(nel=8)
+    sim.learn_setup(coarse_cells=3, hidden=16, capacity=2000, seed=1, field_inputs=1)
+    n_j = sim.learn_collect(stride=1, rtol=1e-6, precond=G.PRECOND_JACOBI)
+    Xj, Yj = sim.learn_pairs()
+    sim.learn_clear()
+    n_k = sim.learn_collect(stride=1, rtol=1e-6, precond=G.PRECOND_KRONECKER)
+    Xk, Yk = sim.learn_pairs()
+    assert 2 <= n_k < n_j
+    assert np.abs(Xk[0] - Xj[0]).max() <= 1e-6 and np.abs(Yk[0] - Yj[0]).max() <= 1e-6
+    assert np.isfinite(Xk).all() and np.isfinite(Yk).all()
