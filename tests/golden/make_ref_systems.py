@@ -1,0 +1,59 @@
+"""Write tests/golden/ref_systems.npz: global systems assembled by IFEM's own
+code (oracle/refmodel.py over oracle/_ref/libifem_ref.so, built from the IFEM
+sources).  Runs only where the IFEM sources are present:
+
+    python oracle/ref/build_ref.py && python tests/golden/make_ref_systems.py
+
+Cases (the seeded synthetic models of ifem_gb300/workloads.py):
+  c1_poisson2d_p2   2D Poisson p=2, 8x8 elements, all edges fixed, 3x3 Gauss
+  c4_poisson3d_p3   3D Poisson p=3, 3^3 elements, log-normal kappa, 4^3 Gauss
+  c3_poisson3d_nurbs 3D Poisson p=2 on a perturbed rational patch, 4^3 elements
+  c2_elast3d_p2     3D NURBS elasticity p=2, 2^3 elements, face 5 clamped
+Stored per case: IA, JA (0-based compressed columns), A, b (Poisson), MADOF, MEQN.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from ifem_gb300 import workloads as W  # noqa: E402
+
+
+def cases():
+    """name -> (patches, n_gauss); shared with the tests."""
+    rng = np.random.default_rng(W.BASE_SEED + 30)
+    nurbs = W.perturb(W.box_patch(3, 2, 4), rng, 0.1)
+    nurbs.kind = 1
+    nurbs.source = 1.0
+    nurbs.dirichlet = [(f, 1, 0.0) for f in range(1, 7)]
+    return {
+        "c1_poisson2d_p2": W.config1(nel=8),
+        "c4_poisson3d_p3": W.config4(nel=3, grid=16),
+        "c3_poisson3d_nurbs": ([nurbs], 3),
+        "c2_elast3d_p2": W.config2(nel=2),
+    }
+
+
+def main():
+    from oracle import refmodel
+    from oracle.ref import build_ref
+    if build_ref.build() is None:
+        sys.exit("IFEM sources not present: cannot build the reference")
+    out = {}
+    for name, (patches, ng) in cases().items():
+        ref = refmodel.reference_system(patches[0], ng)
+        for k, v in ref.items():
+            if v is not None:
+                out[f"{name}/{k}"] = v
+        print(f"{name}: neq {len(ref['IA']) - 1}, nnz {len(ref['A'])}")
+    np.savez_compressed(os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                                     "ref_systems.npz"), **out)
+
+
+if __name__ == "__main__":
+    main()
