@@ -575,7 +575,7 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
 
   // Poisson in split mode: register tiles of node pairs, tile size per patch
   if constexpr (sizeof(T) == sizeof(float)) {
-    if (P.kind == IFEMGPU_POISSON && S.c0 == nullptr) {
+    if (P.kind == IFEMGPU_POISSON && S.c0 == nullptr && P.mass == 0.0) {
       if (P.tile == 2) poissonTiles<2>(P, S, dX, kq, eq, nodeA, Fa);
       else poissonTiles<4>(P, S, dX, kq, eq, nodeA, Fa);
     }
@@ -583,9 +583,11 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
 
   // element matrix for node pairs a <= bn, scattered as the (a, bn) block and
   // its transpose (bn, a)
-  const T lam = (T)(P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu)));
-  const T mu = (T)(P.E / (2.0 * (1.0 + P.nu)));
-  const bool tiled = sizeof(T) == sizeof(float) && P.kind == IFEMGPU_POISSON && S.c0 == nullptr;
+  const T lam = sizeof(T) == sizeof(float) ? (T)P.lamf : (T)P.lam;
+  const T mu = sizeof(T) == sizeof(float) ? (T)P.muf : (T)P.mu;
+  const bool tiled =
+      sizeof(T) == sizeof(float) && P.kind == IFEMGPU_POISSON && S.c0 == nullptr && P.mass == 0.0;
+  const T ms = (T)P.mass;  // consistent mass: Ke += ms sum_q N_a N_b w_q per component
   const int npairs = tiled ? 0 : nen * (nen + 1) / 2;
   for (int t = threadIdx.x; t < npairs; t += blockDim.x) {
     int bn = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
@@ -621,6 +623,11 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
       for (int k = 0; k < 3; k++)
         for (int l = 0; l < 3; l++)
           Ke[k * 3 + l] = lam * G[k * 3 + l] + mu * G[l * 3 + k] + (k == l ? mu * tr : T(0));
+    }
+    if (ms != T(0)) {  // EqualOrderOperators::Weak::Mass
+      T m = 0;
+      for (int q = 0; q < nq; q++) m += Nq[q * nen + a] * Nq[q * nen + bn] * wq[q];
+      for (int k = 0; k < npv; k++) Ke[k * npv + k] += ms * m;
     }
     // scatter: block (rows of a, columns of bn), then (rows of bn, columns of a)
     for (int side = 0; side < (a == bn ? 1 : 2); side++) {
@@ -666,7 +673,7 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
       if (wq[q] == T(0)) continue;
       const T Na = Nq[q * nen + a];
       if (P.kind == IFEMGPU_POISSON) fe += Na * fq[q] * wq[q];
-      else fe += (T)P.body[k] * Na * wq[q];
+      else fe += (sizeof(T) == sizeof(float) ? (T)P.bodyf[k] : (T)P.body[k]) * Na * wq[q];
     }
     double acc = (double)fe;
     if (S.c0 != nullptr) {
@@ -692,6 +699,7 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
             kij += lam * ak * dX[l * nq * nen + q * nen + bn] +
                    mu * al * dX[k * nq * nen + q * nen + bn] + (k == l ? mu * g : T(0));
           }
+          if (k == l && ms != T(0)) kij += ms * Nq[q * nen + a] * Nq[q * nen + bn] * w;
         }
         acc -= S.c0[-ce - 1] * (double)kij;
       }
@@ -893,7 +901,15 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     D.source_shape = pc.mat.source_shape;
     D.E = pc.mat.E;
     D.nu = pc.mat.nu;
-    for (int c = 0; c < 3; c++) D.body[c] = pc.mat.body[c];
+    D.lam = D.E * D.nu / ((1.0 + D.nu) * (1.0 - 2.0 * D.nu));
+    D.mu = D.E / (2.0 * (1.0 + D.nu));
+    D.lamf = (float)D.lam;
+    D.muf = (float)D.mu;
+    D.mass = pc.mass;
+    for (int c = 0; c < 3; c++) {
+      D.body[c] = pc.mat.body[c];
+      D.bodyf[c] = (float)D.body[c];
+    }
     D.nq = 1;
     D.faceTables = 1;
     for (int d = 0; d < 3; d++) {
@@ -910,6 +926,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
         D.ngf[d] = ngf;
         gaussRule(ng, D.gx[d], D.gw[d]);
         gaussRule(ngf, D.fx[d], D.fw[d]);
+        for (int g = 0; g < ng; g++) D.gwf[d][g] = (float)D.gw[d][g];
         IFEMGPU_TRY(upload(ctx, &pc.d_knots[d], pc.knots[d].data(), pc.knots[d].size()));
         size_t tab = (size_t)pc.nel[d] * ng * (pc.p[d] + 1);
         IFEMGPU_CUDA(ctx, cudaMalloc(&pc.d_tabN[d], sizeof(double) * tab));
@@ -959,7 +976,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   bool flow = ctx->opts.colour_passes != 1;
   for (int pi = 0; pi < np; pi++) {
     DevPatch& D = ctx->h_devpatches[pi];
-    onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) &&
+    onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) && D.mass == 0.0 &&
                D.lineOff != nullptr && D.faceTables && ctx->patches[pi].neumann.size() <= 6;
     if (!onTc[pi] && ctx->patches[pi].nelActive != ctx->patches[pi].nelAll) flow = false;
   }

@@ -427,6 +427,15 @@ ifemgpu_status ifemgpu_patch_set_material(ifemgpu_ctx* ctx, int patch_id,
   return IFEMGPU_OK;
 }
 
+ifemgpu_status ifemgpu_patch_set_mass(ifemgpu_ctx* ctx, int patch_id, double scale)
+{
+  HostPatch* pc = getPatch(ctx, patch_id);
+  if (!pc || !std::isfinite(scale)) return setError(ctx, IFEMGPU_INVALID_ARG, "set_mass: bad patch or scale");
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "model already preprocessed");
+  pc->mass = scale;
+  return IFEMGPU_OK;
+}
+
 ifemgpu_status ifemgpu_patch_set_field(ifemgpu_ctx* ctx, int patch_id, int which,
                                        const double* values)
 {

@@ -30,6 +30,11 @@ struct DevPatch {
   int rational;
   int firstNode;      // global 0-based index of the patch's first node
   double kappa, source, E, nu, body[3];
+  // Lame constants and body force, formed once on the host (the FP64 pipe
+  // is slow on this GPU, so no per-element divisions)
+  double lam, mu;
+  float lamf, muf, bodyf[3];
+  double mass;        // scale of the consistent mass matrix added to K (0: none)
   int source_shape;
   const double* ctrl;     // nnod x 4: x, y, z, w (z = 0 in 2D, w = 1 if polynomial)
   const double* knots[3]; // n+p+1 per direction
@@ -61,6 +66,7 @@ struct DevPatch {
   const int* lineOff;
   // Gauss rules: volume (gx, gw) and face (fx, fw, ngf points)
   double gx[3][kMaxGauss], gw[3][kMaxGauss];
+  float gwf[3][kMaxGauss];
   double fx[3][kMaxGauss], fw[3][kMaxGauss];
   int ngf[3];
 };
@@ -85,6 +91,7 @@ struct HostPatch {
   bool rational = false;
   ifemgpu_material mat{};
   bool hasMat = false;
+  double mass = 0.0;          // scale of the consistent mass matrix added to K
   int npv = 1;
   std::vector<double> logk, noise;
   std::vector<HostBC> bcs;
@@ -183,6 +190,14 @@ struct ifemgpu_ctx {
   float* d_K32 = nullptr;
   short* d_off16 = nullptr;      // 16-bit column offsets of the FP32 SpMV (nullptr: 32-bit)
   int off16State = 0;            // 0 not built, 1 in use, -1 bandwidth too large
+  // row-pattern dictionary of the compressed rows: rows whose column offsets
+  // (col - row) form the same sequence share one int16 entry list; replaces
+  // the per-entry indices in the solver's SpMVs when it is small
+  int* d_rowPat = nullptr;       // neq: pattern of each row
+  int* d_patStart = nullptr;     // npat + 1: start of each pattern in d_patOff
+  short* d_patOff = nullptr;
+  int patState = 0;              // 0 not built, 1 in use, -1 not applicable
+  int numPatterns = 0;
   double* d_work = nullptr;
   size_t work_len = 0;
   double* h_pinned = nullptr;

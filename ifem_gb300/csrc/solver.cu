@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <unordered_map>
 #include <vector>
 
 #include "ifemgpu_internal.h"
@@ -113,11 +114,14 @@ k_spmv(const int* __restrict__ colptr, const int* __restrict__ rowidx, const T* 
   }
 }
 
-// r = b - A x in FP64, partial of ||r||^2
+// r = b - A x in FP64, partial of ||r||^2; column indices from rowidx, or
+// (rowPat != nullptr) from the row-pattern dictionary
 __global__ void __launch_bounds__(kThreads)
 k_residual(const int* __restrict__ colptr, const int* __restrict__ rowidx,
            const double* __restrict__ A, const double* __restrict__ x,
-           const double* __restrict__ b, double* __restrict__ r, int n, double* __restrict__ part)
+           const double* __restrict__ b, double* __restrict__ r, int n, double* __restrict__ part,
+           const int* __restrict__ rowPat = nullptr, const int* __restrict__ patStart = nullptr,
+           const short* __restrict__ patOff = nullptr)
 {
   __shared__ double sh[32];
   const int lane = threadIdx.x & 31;
@@ -126,7 +130,12 @@ k_residual(const int* __restrict__ colptr, const int* __restrict__ rowidx,
   for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += warpsPerGrid) {
     const int c0 = colptr[row], c1 = colptr[row + 1];
     double s = 0.0;
-    for (int k = c0 + lane; k < c1; k += 32) s += A[k] * x[rowidx[k]];
+    if (rowPat) {
+      const short* o = patOff + patStart[rowPat[row]];
+      for (int k = c0 + lane; k < c1; k += 32) s += A[k] * x[row + o[k - c0]];
+    } else {
+      for (int k = c0 + lane; k < c1; k += 32) s += A[k] * x[rowidx[k]];
+    }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) {
       const double v = b[row] - s;
@@ -353,12 +362,16 @@ g_spmv(const int* __restrict__ colptr, const int* __restrict__ rowidx, const T* 
 }
 
 // q = A p with 16-bit column offsets relative to the row (banded spline
-// patterns: 6 instead of 8 bytes per entry), four independent load chains per
-// lane; (p, q) -> S_PQ, alpha, with shift also S_RZ <- S_RZN
+// patterns), four independent load chains per lane; (p, q) -> S_PQ, alpha,
+// with shift also S_RZ <- S_RZN.  kPat: the offsets of row r are pattern
+// rowPat[r] of the row-pattern dictionary (4 bytes per entry from HBM, the
+// dictionary stays in L2); otherwise one offset per entry (6 bytes per entry).
+template <bool kPat>
 __global__ void __launch_bounds__(kThreads)
-g_spmv16(const int* __restrict__ colptr, const short* __restrict__ off, const float* __restrict__ A,
-         const float* __restrict__ p, float* __restrict__ q, int n, double* __restrict__ part,
-         double* s, int shift)
+g_spmvOff(const int* __restrict__ colptr, const int* __restrict__ rowPat,
+          const int* __restrict__ patStart, const short* __restrict__ off,
+          const float* __restrict__ A, const float* __restrict__ p, float* __restrict__ q, int n,
+          double* __restrict__ part, double* s, int shift)
 {
   if (loopStopped(s)) return;
   __shared__ double sh[32];
@@ -367,19 +380,20 @@ g_spmv16(const int* __restrict__ colptr, const short* __restrict__ off, const fl
   float dot = 0.f;
   for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += warpsPerGrid) {
     const int b = colptr[row], e = colptr[row + 1];
+    const int so = kPat ? patStart[rowPat[row]] - b : 0;  // offset of entry k: off[k + so]
     float acc = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
     int k = b + lane;
     for (; k + 96 < e; k += 128) {
-      const int o0 = off[k], o1 = off[k + 32], o2 = off[k + 64], o3 = off[k + 96];
+      const int o0 = off[k + so], o1 = off[k + so + 32], o2 = off[k + so + 64], o3 = off[k + so + 96];
       const float a0 = A[k], a1 = A[k + 32], a2 = A[k + 64], a3 = A[k + 96];
       acc += a0 * p[row + o0];
       acc1 += a1 * p[row + o1];
       acc2 += a2 * p[row + o2];
       acc3 += a3 * p[row + o3];
     }
-    for (; k < e; k += 32) acc += A[k] * p[row + off[k]];
+    for (; k < e; k += 32) acc += A[k] * p[row + off[k + so]];
     acc += (acc1 + acc2) + acc3;
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    for (int w = 16; w > 0; w >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, w);
     if (lane == 0) {
       q[row] = acc;
       dot += acc * p[row];
@@ -590,10 +604,17 @@ void freeSolver(ifemgpu_ctx* ctx)
   dropLoopGraphs(ctx);
   if (ctx->d_K32) cudaFree(ctx->d_K32);
   if (ctx->d_off16) cudaFree(ctx->d_off16);
+  if (ctx->d_rowPat) cudaFree(ctx->d_rowPat);
+  if (ctx->d_patStart) cudaFree(ctx->d_patStart);
+  if (ctx->d_patOff) cudaFree(ctx->d_patOff);
   if (ctx->d_work) cudaFree(ctx->d_work);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   ctx->d_off16 = nullptr;
   ctx->off16State = 0;
+  ctx->d_rowPat = ctx->d_patStart = nullptr;
+  ctx->d_patOff = nullptr;
+  ctx->patState = 0;
+  ctx->numPatterns = 0;
   ctx->d_K32 = nullptr;
   ctx->d_work = nullptr;
   ctx->h_pinned = nullptr;
@@ -766,6 +787,77 @@ static ifemgpu_status loopFCG(ifemgpu_ctx* ctx, const Work& w, bool kron, bool l
   return IFEMGPU_OK;
 }
 
+// SplitMix64 finaliser (Steele, Lea and Flood 2014) as the mixing step of a
+// hash over a row's column offsets
+static inline uint64_t mix64(uint64_t x)
+{
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+// Row-pattern dictionary of the compressed rows: rows whose column offsets
+// (col - row) are the same sequence share one entry.  A structured patch has
+// a few hundred distinct rows (interior, and each distance to each face), so
+// the dictionary is a few hundred KB against 2 bytes per stored entry for
+// per-entry offsets.  Returns false when an offset needs more than 16 bits,
+// the dictionary would exceed 1/16 of the entries, or two different rows
+// share a hash (then per-entry offsets are used).
+static bool buildRowPatterns(const ifemgpu_ctx* ctx, std::vector<int>& rowPat,
+                             std::vector<int>& patStart, std::vector<short>& patOff)
+{
+  const int n = ctx->neq;
+  const int* cp = ctx->colptr.data();
+  const int* ri = ctx->rowidx.data();
+  std::vector<uint64_t> h(n);
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int r = 0; r < n; r++) {
+    uint64_t x = mix64(0x9e3779b97f4a7c15ull + (uint64_t)(cp[r + 1] - cp[r]));
+    for (int k = cp[r]; k < cp[r + 1]; k++) {
+      const int d = ri[k] - r;
+      bad |= d < -32768 || d > 32767;
+      x = mix64(x ^ (uint32_t)d);
+    }
+    h[r] = x;
+  }
+  if (bad) return false;
+  std::unordered_map<uint64_t, int> ids;
+  std::vector<int> rep;
+  rowPat.resize(n);
+  for (int r = 0; r < n; r++) {
+    auto it = ids.find(h[r]);
+    if (it == ids.end()) {
+      it = ids.emplace(h[r], (int)rep.size()).first;
+      rep.push_back(r);
+    }
+    rowPat[r] = it->second;
+  }
+  patStart.assign(rep.size() + 1, 0);
+  for (size_t i = 0; i < rep.size(); i++)
+    patStart[i + 1] = patStart[i] + (cp[rep[i] + 1] - cp[rep[i]]);
+  if ((int64_t)patStart.back() * 16 > ctx->nnz) return false;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int r = 0; r < n; r++) {
+    const int q = rep[rowPat[r]];
+    if (cp[r + 1] - cp[r] != cp[q + 1] - cp[q]) {
+      bad = 1;
+      continue;
+    }
+    for (int k = 0; k < cp[r + 1] - cp[r]; k++)
+      bad |= ri[cp[r] + k] - r != ri[cp[q] + k] - q;
+  }
+  if (bad) return false;
+  patOff.resize(patStart.back());
+  for (size_t i = 0; i < rep.size(); i++) {
+    const int q = rep[i];
+    for (int k = cp[q]; k < cp[q + 1]; k++) patOff[patStart[i] + k - cp[q]] = (short)(ri[k] - q);
+  }
+  return true;
+}
+
 // workspace, pinned scalars and (mixed) the FP32 matrix copy
 static ifemgpu_status ensureWork(ifemgpu_ctx* ctx, bool mixed)
 {
@@ -781,7 +873,37 @@ static ifemgpu_status ensureWork(ifemgpu_ctx* ctx, bool mixed)
   }
   if (!ctx->h_pinned) IFEMGPU_CUDA(ctx, cudaMallocHost(&ctx->h_pinned, 64));
   if (mixed && !ctx->d_K32) IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_K32, sizeof(float) * ctx->nnz));
-  if (mixed && ctx->off16State == 0) {  // 16-bit column offsets when the band allows
+  if (ctx->patState == 0) {  // row-pattern dictionary when the rows repeat
+    ctx->patState = -1;
+    std::vector<int> rowPat, patStart;
+    std::vector<short> patOff;
+    if (buildRowPatterns(ctx, rowPat, patStart, patOff)) {
+      bool ok = cudaMalloc(&ctx->d_rowPat, sizeof(int) * rowPat.size()) == cudaSuccess &&
+                cudaMalloc(&ctx->d_patStart, sizeof(int) * patStart.size()) == cudaSuccess &&
+                cudaMalloc(&ctx->d_patOff, sizeof(short) * std::max<size_t>(patOff.size(), 1)) ==
+                    cudaSuccess;
+      ok = ok &&
+           cudaMemcpy(ctx->d_rowPat, rowPat.data(), sizeof(int) * rowPat.size(),
+                      cudaMemcpyHostToDevice) == cudaSuccess &&
+           cudaMemcpy(ctx->d_patStart, patStart.data(), sizeof(int) * patStart.size(),
+                      cudaMemcpyHostToDevice) == cudaSuccess &&
+           cudaMemcpy(ctx->d_patOff, patOff.data(), sizeof(short) * patOff.size(),
+                      cudaMemcpyHostToDevice) == cudaSuccess;
+      if (ok) {
+        ctx->patState = 1;
+        ctx->numPatterns = (int)patStart.size() - 1;
+      } else {
+        cudaGetLastError();
+        if (ctx->d_rowPat) cudaFree(ctx->d_rowPat);
+        if (ctx->d_patStart) cudaFree(ctx->d_patStart);
+        if (ctx->d_patOff) cudaFree(ctx->d_patOff);
+        ctx->d_rowPat = ctx->d_patStart = nullptr;
+        ctx->d_patOff = nullptr;
+      }
+      dropLoopGraphs(ctx);
+    }
+  }
+  if (mixed && ctx->off16State == 0 && ctx->patState != 1) {  // 16-bit column offsets when the band allows
     ctx->off16State = -1;
     if (cudaMalloc(&ctx->d_off16, sizeof(short) * std::max<int64_t>(ctx->nnz, 1)) == cudaSuccess) {
       int* d_bad = reinterpret_cast<int*>(carve(ctx).scal + 30);  // unused scalar slot
@@ -811,9 +933,14 @@ static void spmv32(ifemgpu_ctx* ctx, const Work& w, const float* p, float* q, in
 {
   const int n = ctx->neq;
   const int sb = std::min(kRedBlocks, (n + 7) / 8);
-  if (ctx->d_off16)
-    g_spmv16<<<sb, kThreads, 0, ctx->stream>>>(ctx->d_colptr, ctx->d_off16, ctx->d_K32, p, q, n,
-                                               w.part, w.scal, shift);
+  if (ctx->d_rowPat)
+    g_spmvOff<true><<<sb, kThreads, 0, ctx->stream>>>(ctx->d_colptr, ctx->d_rowPat, ctx->d_patStart,
+                                                      ctx->d_patOff, ctx->d_K32, p, q, n, w.part,
+                                                      w.scal, shift);
+  else if (ctx->d_off16)
+    g_spmvOff<false><<<sb, kThreads, 0, ctx->stream>>>(ctx->d_colptr, nullptr, nullptr,
+                                                       ctx->d_off16, ctx->d_K32, p, q, n, w.part,
+                                                       w.scal, shift);
   else
     g_spmv<float><<<sb, kThreads, 0, ctx->stream>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K32, p, q,
                                                     n, w.part, w.scal, shift);
@@ -848,7 +975,7 @@ static ifemgpu_status refineResidual(ifemgpu_ctx* ctx, const Work& w, const doub
   const int n = ctx->neq;
   const int sb = std::min(kRedBlocks, (n + 7) / 8);
   k_residual<<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K, w.x64, b, w.r64, n,
-                                     w.part);
+                                     w.part, ctx->d_rowPat, ctx->d_patStart, ctx->d_patOff);
   k_finish<<<1, kThreads, 0, s>>>(w.part, sb, 1, w.scal + 9);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + 9, sizeof(double), cudaMemcpyDeviceToHost, s));

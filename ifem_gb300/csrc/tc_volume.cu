@@ -41,10 +41,18 @@ constexpr int kM = 128;       // MMA M (rows 32k + a, k < 3, a < 27)
 constexpr int kN = 96;        // MMA N (columns 32l + b)
 constexpr int kGs = 81;       // row stride of the compact Gram matrix (conflict-free)
 constexpr uint32_t kFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wait
+constexpr int kTcPerSM = 4;   // CTAs per SM at most: 4 x 128 tensor-memory columns
+
+// The operand tile has 96 rows (32k + a for k < 3, a < 27, the rest zero);
+// the MMA's A operand reads M = 128 rows from the tile start, so the reads of
+// rows 96..127 run into the next 4 KB (Tlo after Thi, the basis/Gram union
+// after Tlo).  Those rows only feed accumulator lanes 96..127, which are
+// never read, and nothing writes shared memory while an MMA runs.
+constexpr int kRowsT = 96;
 
 struct TcSmem {
-  float Thi[kM * kK];      // operand tile, K-major core-matrix layout
-  float Tlo[kM * kK];
+  float Thi[kRowsT * kK];  // operand tile, K-major core-matrix layout
+  float Tlo[kRowsT * kK];
   union {
     struct {
       float N[kNq][kNen];   // weighted basis wN, then the rational basis R
@@ -59,14 +67,20 @@ struct TcSmem {
   float X[kNen][4];        // control points relative to the element's first, weight
   int eq[kNen * 3];
   int colStart[kNen * 3];  // colptr of the element's free columns
-  int Fa[kNen];            // F(a): free DOFs before node a
+  int rowBase[kNen * 3];   // F(a) + free DOFs of node a before component k, row r = 3a + k
   int lo[kNen][9];         // line offset of row node line (j + 3k) in column node b
   uint32_t dec[kNq * kNen];  // (q, a) decode: q | a<<5 | gi<<10 | gj<<12 | gk<<14 | i<<16 | j<<18 | k<<20
   unsigned long long mbar;
   uint32_t tmemSlot;
   int fail;
   int signs;               // bit 0: some w_q > 0, bit 1: some w_q < 0
+  float dVf;               // span volume / 8 of the element
 };
+
+static_assert(offsetof(TcSmem, Tlo) == offsetof(TcSmem, Thi) + sizeof(float) * kRowsT * kK &&
+                  offsetof(TcSmem, u) == offsetof(TcSmem, Tlo) + sizeof(float) * kRowsT * kK &&
+                  sizeof(TcSmem::u) >= sizeof(float) * (kM - kRowsT) * kK,
+              "A-operand reads of rows 96..127 must stay inside the tile and the union");
 
 // scratch views (dead before the epilogue writes G)
 struct Scratch {
@@ -133,9 +147,9 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     mbarInit(mbar, 1);
     sm.fail = 0;
   }
-  // the padding of the operand tile (rows >= 96, rows with a >= 27, q >= 27)
-  // is never written again
-  for (int i = tid; i < kM * kK; i += blockDim.x) {
+  // the padding of the operand tile (rows with a >= 27, q >= 27) is never
+  // written again
+  for (int i = tid; i < kRowsT * kK; i += blockDim.x) {
     sm.Thi[i] = 0.f;
     sm.Tlo[i] = 0.f;
   }
@@ -151,6 +165,11 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   const uint32_t tmem = sm.tmemSlot;
   const uint32_t tHi = smemAddr(sm.Thi), tLo = smemAddr(sm.Tlo);
   uint32_t phase = 0;
+  // done flag of this CTA's previous element, published (fence + release
+  // store by thread 0) when the next element reaches its neighbour wait: by
+  // then the previous element's reductions have long completed, so the fence
+  // costs little, and the delay is bounded by one element's front end
+  int* pending = nullptr;
 
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
     const Item item = items[it];
@@ -170,12 +189,17 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.X[a][2] = (float)(c[2] - c00[2]);
       sm.X[a][3] = (float)c[3];
       const int d0 = S.madof[P.firstNode + node] - 1;
-      sm.eq[3 * a] = S.meqn[d0];
-      sm.eq[3 * a + 1] = S.meqn[d0 + 1];
-      sm.eq[3 * a + 2] = S.meqn[d0 + 2];
-      sm.Fa[a] = S.F[P.firstNode + node];
+      const int q0 = S.meqn[d0], q1 = S.meqn[d0 + 1], q2 = S.meqn[d0 + 2];
+      sm.eq[3 * a] = q0;
+      sm.eq[3 * a + 1] = q1;
+      sm.eq[3 * a + 2] = q2;
+      const int Fa = S.F[P.firstNode + node];
+      sm.rowBase[3 * a] = Fa;
+      sm.rowBase[3 * a + 1] = Fa + (q0 > 0);
+      sm.rowBase[3 * a + 2] = Fa + (q0 > 0) + (q1 > 0);
     }
     if (tid == 0) sm.signs = 0;
+    if (tid == 32) sm.dVf = (float)(0.125 * P.span[0][e1] * P.span[1][e2] * P.span[2][e3]);
     for (int idx = tid; idx < kNen * 9; idx += blockDim.x) {
       const int bn = idx / 9, la = idx % 9;
       const int nodeb = n0 + ((bn / 9) * P.n[1] + (bn / 3) % 3) * P.n[0] + bn % 3;
@@ -231,29 +255,34 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       const int q = tid;
       const float* Pq = sc.P + q * 16;
       const float iW = 1.f / Pq[12];
-      double J[9];  // column-major: J[d*3 + r] = dX_r/du_d
+      // J[d*3 + r] = dX_r/du_d (column-major), formed in FP32 and widened
+      // exactly on the integer pipe; the cofactors, determinant and inverse
+      // are FP64 (each FP64 warp instruction costs tens of cycles here, so
+      // the count is kept to the cofactor expansion itself)
+      double J[9];
       for (int r = 0; r < 3; r++) {
         const float Xr = Pq[r * 4] * iW;
         for (int d = 0; d < 3; d++)
-          J[d * 3 + r] = (double)((Pq[r * 4 + 1 + d] - Xr * Pq[12 + 1 + d]) * iW);
+          J[d * 3 + r] = widenF32((Pq[r * 4 + 1 + d] - Xr * Pq[12 + 1 + d]) * iW);
       }
-      const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[3] * (J[1] * J[8] - J[2] * J[7]) +
-                         J[6] * (J[1] * J[5] - J[2] * J[4]);
+      const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[1] * J[8] - J[2] * J[7],
+                   c2 = J[1] * J[5] - J[2] * J[4];
+      const double det = J[0] * c0 - J[3] * c1 + J[6] * c2;
       float w = 0.f;
       float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if (det > kEpsZ || det < -kEpsZ) {
+      if (fabs(det) > kEpsZ) {
         const double id = 1.0 / det;
-        B[0] = (float)((J[4] * J[8] - J[5] * J[7]) * id);
-        B[1] = (float)(-(J[1] * J[8] - J[2] * J[7]) * id);
-        B[2] = (float)((J[1] * J[5] - J[2] * J[4]) * id);
+        B[0] = (float)(c0 * id);
+        B[1] = (float)(-c1 * id);
+        B[2] = (float)(c2 * id);
         B[3] = (float)(-(J[3] * J[8] - J[5] * J[6]) * id);
         B[4] = (float)((J[0] * J[8] - J[2] * J[6]) * id);
         B[5] = (float)(-(J[0] * J[5] - J[2] * J[3]) * id);
         B[6] = (float)((J[3] * J[7] - J[4] * J[6]) * id);
         B[7] = (float)(-(J[0] * J[7] - J[1] * J[6]) * id);
         B[8] = (float)((J[0] * J[4] - J[1] * J[3]) * id);
-        const double dV = 0.125 * P.span[0][e1] * P.span[1][e2] * P.span[2][e3];
-        w = (float)(det * dV * P.gw[0][q % 3] * P.gw[1][(q / 3) % 3] * P.gw[2][q / 9]);
+        // |J| dV w_i w_j w_k in FP32 (dV = span volume / 8)
+        w = (float)det * sm.dVf * P.gwf[0][q % 3] * P.gwf[1][(q / 3) % 3] * P.gwf[2][q / 9];
         atomicOr(&sm.signs, w > 0.f ? 1 : 2);
       } else {
         atomicAdd(S.counters, 1ull);
@@ -346,7 +375,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     float fe = 0.f;
     if (tid < kNen * 3) {
       const int a = tid / 3, k = tid % 3;
-      const float bk = (float)P.body[k];
+      const float bk = P.bodyf[k];
       if (bk != 0.f) {
         float acc = 0.f;
         for (int q = 0; q < kNq; q++) acc = fmaf(sm.u.b.N[q][a], sm.wq[q], acc);
@@ -452,7 +481,13 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     __syncthreads();
     if (sm.fail) break;
 
-    // ---- 8. wait for the lower-colour neighbours (they share nodes)
+    // ---- 8. publish the previous element, then wait for the lower-colour
+    //         neighbours of this one (they share nodes)
+    if (tid == 0 && pending) {
+      __threadfence();
+      storeRelease(pending, 1);
+      pending = nullptr;
+    }
     if (tid < 124) {
       const int t = tid < 62 ? tid : tid + 1;  // skip the element itself
       const int dx = t % 5 - 2, dy = (t / 5) % 5 - 2, dz = t / 25 - 2;
@@ -484,9 +519,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     // rows, so each reduction instruction touches contiguous column segments
     if (tid < kNen * 3 && sm.eq[tid] > 0) {
       const int a = tid / 3, k = tid - 3 * a;
-      int rank = 0;
-      for (int m = 0; m < k; m++) rank += sm.eq[3 * a + m] > 0;
-      const int base = sm.Fa[a] + rank;
+      const int base = sm.rowBase[tid];
       const int la = (a / 3) % 3 + 3 * (a / 9);
       const float* Grow = sm.u.Gc + tid * kGs;    // row (a, k)
       const float* Ga = sm.u.Gc + 3 * a * kGs;     // rows (a, 0..2)
@@ -526,12 +559,14 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       }
     }
 
-    // ---- 11. publish: all reductions of this element precede its flag
+    // ---- 11. this element's reductions are issued; its flag is published
+    //         at the next element's step 8 or after the loop
     __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      storeRelease(S.flags + P.flagBase + e, 1);
-    }
+    if (tid == 0) pending = S.flags + P.flagBase + e;
+  }
+  if (tid == 0 && pending) {
+    __threadfence();
+    storeRelease(pending, 1);
   }
 
   // release tensor memory (all tcgen05 traffic of this CTA has completed)
@@ -639,8 +674,7 @@ ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int)
                                            ctx->opts.device));
   const int bySmem = smemSM / (int)(tcVolumeSmem() + resv);
   const int byRegs = regsSM / (((fa.numRegs + 7) / 8) * 8 * 128);
-  const int perSM = std::min(std::min(bySmem, byRegs), 3);
-  if (perSM < 1) return setError(ctx, IFEMGPU_UNSUPPORTED, "tensor-core kernel does not fit an SM");
+  const int perSM = std::min(std::min(bySmem, byRegs), kTcPerSM);
   const int grid = std::min(p.count, perSM * ctx->numSMs);
   if (ctx->opts.verbose)
     std::printf("tensor-core volume kernel: %zu B shared memory, %d registers, %d blocks/SM, grid %d\n",

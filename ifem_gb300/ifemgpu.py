@@ -64,6 +64,7 @@ PRECOND_JACOBI, PRECOND_KRONECKER = 0, 1
 EXPORTS = [
     "ifemgpu_ctx_create", "ifemgpu_ctx_destroy", "ifemgpu_last_error", "ifemgpu_abi_version",
     "ifemgpu_patch_add", "ifemgpu_patch_set_material", "ifemgpu_patch_set_field",
+    "ifemgpu_patch_set_mass",
     "ifemgpu_patch_constrain_face", "ifemgpu_patch_add_neumann", "ifemgpu_preprocess",
     "ifemgpu_get_sizes", "ifemgpu_get_madof", "ifemgpu_get_meqn", "ifemgpu_get_mnpc",
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
@@ -104,6 +105,7 @@ def load_library(path: str | None = None):
         "ifemgpu_patch_add": (I, [P, I, V, V, V, V, I, C.POINTER(I)]),
         "ifemgpu_patch_set_material": (I, [P, I, C.POINTER(Material)]),
         "ifemgpu_patch_set_field": (I, [P, I, I, V]),
+        "ifemgpu_patch_set_mass": (I, [P, I, D]),
         "ifemgpu_patch_constrain_face": (I, [P, I, I, I, D]),
         "ifemgpu_patch_add_neumann": (I, [P, I, I, V]),
         "ifemgpu_preprocess": (I, [P]),
@@ -242,6 +244,10 @@ class SIM:
                      E=1.0, nu=0.3, body=(0.0, 0.0, 0.0)):
         m = Material(kind, kappa, source, source_shape, E, nu, (C.c_double * 3)(*body))
         self._check(self.lib.ifemgpu_patch_set_material(self.ctx, pid, C.byref(m)))
+
+    def set_mass(self, pid: int, scale: float):
+        """K_eff = K + scale * M (consistent mass, EqualOrderOperators::Weak::Mass)."""
+        self._check(self.lib.ifemgpu_patch_set_mass(self.ctx, pid, float(scale)))
 
     def set_field(self, pid: int, which: int, values):
         v = np.ascontiguousarray(values, dtype=np.float64)

@@ -41,6 +41,7 @@ class SplinePatch:
     E: float = 1.0
     nu: float = 0.3
     body: tuple = (0.0, 0.0, 0.0)
+    mass: float = 0.0          # scale of the consistent mass matrix added to K
     log_kappa: np.ndarray | None = None
     noise: np.ndarray | None = None
     dirichlet: list = field(default_factory=list)   # (face, dofs, value)
@@ -180,6 +181,8 @@ def load_into(sim, patches) -> list[int]:
         pid = sim.add_patch(pc)
         sim.set_material(pid, pc.kind, kappa=pc.kappa, source=pc.source,
                          source_shape=pc.source_shape, E=pc.E, nu=pc.nu, body=pc.body)
+        if pc.mass:
+            sim.set_mass(pid, pc.mass)
         if pc.log_kappa is not None:
             sim.set_field(pid, 1, pc.log_kappa)
         if pc.noise is not None:

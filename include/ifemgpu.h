@@ -139,6 +139,15 @@ ifemgpu_status ifemgpu_patch_add(ifemgpu_ctx* ctx, int dim, const int* degree,
 ifemgpu_status ifemgpu_patch_set_material(ifemgpu_ctx* ctx, int patch_id,
                                           const ifemgpu_material* mat);
 
+/* Adds scale x the consistent mass matrix to the patch's element matrices,
+ * K_eff = K + scale M with M_ab = integral N_a N_b (per solution component),
+ * the effective stiffness of implicit time stepping (Newmark: scale =
+ * density / (beta dt^2)).  M is EqualOrderOperators::Weak::Mass
+ * (Apps/Utils/EqualOrderOperators.C:214-227) as NewmarkMats combines it with
+ * K (src/ASM/NewmarkMats.C).  scale = 0 removes it.  Must precede
+ * ifemgpu_preprocess.                                                      */
+ifemgpu_status ifemgpu_patch_set_mass(ifemgpu_ctx* ctx, int patch_id, double scale);
+
 /* Per-control-point coefficient field (enum ifemgpu_field), nnod values.  */
 ifemgpu_status ifemgpu_patch_set_field(ifemgpu_ctx* ctx, int patch_id,
                                        int which, const double* values);

@@ -44,6 +44,7 @@ def lib():
             "ifo_add_patch": (I, [P, I, V, V, V, V, I]),
             "ifo_set_material": (I, [P, I, I, D, D, I, D, D, V]),
             "ifo_set_field": (I, [P, I, I, V]),
+            "ifo_set_mass": (I, [P, I, D]),
             "ifo_constrain_face": (I, [P, I, I, I, D]),
             "ifo_add_neumann": (I, [P, I, I, V]),
             "ifo_preprocess": (I, [P]), "ifo_sizes": (None, [P, V]),
@@ -105,6 +106,9 @@ class OracleModel:
                      body=(0.0, 0.0, 0.0)):
         b = np.ascontiguousarray(body, dtype=np.float64)
         self.L.ifo_set_material(self.h, pid, kind, kappa, source, source_shape, E, nu, _p(b))
+
+    def set_mass(self, pid, scale):
+        self.L.ifo_set_mass(self.h, pid, float(scale))
 
     def set_field(self, pid, which, values):
         v = np.ascontiguousarray(values, dtype=np.float64)

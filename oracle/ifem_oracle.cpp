@@ -146,6 +146,7 @@ struct Material {
   int source_shape = 0;
   double E = 1.0, nu = 0.3;
   double body[3] = {0, 0, 0};
+  double mass = 0.0;  // scale of the consistent mass matrix added to K
 };
 
 struct FaceBC { int face, dofs; double value; };
@@ -566,6 +567,10 @@ void evalPoisson(const Patch& pc, int nen, double detJxW, const std::vector<doub
       for (int c = 0; c < dim; c++) v += dNdX[(size_t)c * nen + i] * s * dNdX[(size_t)c * nen + j];
       eK[(size_t)j * nen + i] += v;
     }
+  // EqualOrderOperators::Weak::Mass (Apps/Utils/EqualOrderOperators.C:214-227)
+  if (pc.mat.mass != 0.0)
+    for (int j = 0; j < nen; j++)
+      for (int i = 0; i < nen; i++) eK[(size_t)j * nen + i] += N[i] * N[j] * pc.mat.mass * detJxW;
   if (pc.mat.source != 0.0) {
     double f = pc.mat.source;
     if (pc.mat.source_shape == 1)
@@ -618,6 +623,11 @@ void evalElasticity(const Patch& pc, int nen, double detJxW, const std::vector<d
       for (int k = 0; k < 6; k++) v += s.Bm[(size_t)i * 6 + k] * s.DB[(size_t)j * 6 + k];
       eK[(size_t)j * nd + i] += v;
     }
+  if (pc.mat.mass != 0.0)  // Weak::Mass per component (EqualOrderOperators.C:214-227)
+    for (int b = 0; b < nen; b++)
+      for (int a = 0; a < nen; a++)
+        for (int c = 0; c < 3; c++)
+          eK[(size_t)(3 * b + c) * nd + 3 * a + c] += N[a] * N[b] * pc.mat.mass * detJxW;
   for (int a = 0; a < nen; a++)
     for (int c = 0; c < 3; c++) eS[3 * a + c] += pc.mat.body[c] * N[a] * detJxW;
 }
@@ -832,6 +842,12 @@ int ifo_set_material(void* h, int pid, int kind, double kappa, double source,
   pc.mat.nu = nu;
   for (int c = 0; c < 3; c++) pc.mat.body[c] = body ? body[c] : 0.0;
   pc.npv = kind == 2 ? pc.dim : 1;
+  return 0;
+}
+
+int ifo_set_mass(void* h, int pid, double scale)
+{
+  static_cast<Model*>(h)->patches.at(pid - 1).mat.mass = scale;
   return 0;
 }
 

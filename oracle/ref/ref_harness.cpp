@@ -11,8 +11,8 @@
 //   * SparseMatrix(SUPERLU)::initAssembly(sam, 'F') (src/LinAlg/SparseMatrix.C:
 //     717-762) -> the locked compressed-column pattern of optimiseCols;
 //   * per Gauss point utl::Jacobian (src/Utility/CoordinateMapping.C:24-63),
-//     EqualOrderOperators::Weak::Laplacian / Source (Apps/Utils/
-//     EqualOrderOperators.C:158-174, :243-254) -- the loop body of
+//     EqualOrderOperators::Weak::Laplacian / Mass / Source (Apps/Utils/
+//     EqualOrderOperators.C:158-174, :214-227, :243-254) -- the loop body of
 //     ASMs3D::integrate (src/ASM/ASMs3D.C:2266-2312) restated here;
 //   * SAM::assembleSystem (src/LinAlg/SAM.C:430-543) into the SparseMatrix
 //     and a StdVector.
@@ -146,13 +146,14 @@ RH_API void rh_gauss(int n, double* xi, double* w)
 }
 
 // One Poisson element (1-based iel) from its nq Gauss points: N[q][a],
-// dNdu[q][d][a], wfac[q] = dV * w_i w_j (w_k), kappa[q], f[q], and the
-// element's control points X[a][3].  Forms eK, eS with IFEM's operators,
-// assembles them and returns them (eK column-major); the return value is the
-// number of points skipped for a singular Jacobian.
+// dNdu[q][d][a], wfac[q] = dV * w_i w_j (w_k), kappa[q], f[q]; the scale of
+// the mass matrix added to K (0: none) and the element's control points
+// X[a][3].  Forms eK, eS with IFEM's operators, assembles them and returns
+// them (eK column-major); the return value is the number of points skipped
+// for a singular Jacobian.
 RH_API int rh_poisson_element(void* p, int iel, int nq, const double* N, const double* dNdu,
                               const double* wfac, const double* kappa, const double* f,
-                              const double* X, double* eKout, double* eSout)
+                              double mass, const double* X, double* eKout, double* eSout)
 {
   Harness* h = static_cast<Harness*>(p);
   const int nen = h->nen, dim = h->dim;
@@ -176,6 +177,7 @@ RH_API int rh_poisson_element(void* p, int iel, int nq, const double* N, const d
     }
     fe.detJxW = detJ * wfac[q];
     EqualOrderOperators::Weak::Laplacian(eK, fe, kappa[q]);
+    if (mass != 0.0) EqualOrderOperators::Weak::Mass(eK, fe, mass);
     EqualOrderOperators::Weak::Source(eS, fe, f[q]);
   }
   h->sam.assembleSystem(h->K, h->b, eK, iel);

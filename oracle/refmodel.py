@@ -44,7 +44,7 @@ def lib():
             "rh_create": (P, [I, I, I, I, I, V]), "rh_destroy": (None, [P]),
             "rh_fix": (I, [P, I, I]), "rh_init": (I, [P, V]),
             "rh_gauss": (None, [I, V, V]),
-            "rh_poisson_element": (I, [P, I, I, V, V, V, V, V, V, V, V]),
+            "rh_poisson_element": (I, [P, I, I, V, V, V, V, V, C.c_double, V, V, V]),
             "rh_assemble": (I, [P, I, V, V]),
             "rh_get_sam": (None, [P, V, V]), "rh_get_system": (None, [P, V, V, V, V]),
         }
@@ -185,4 +185,4 @@ def _poisson_elements(L, h, orc, patch, n_gauss, mnpc, nen):
         Xe = np.ascontiguousarray(X[mnpc[e]])
         L.rh_poisson_element(h, e + 1, nq, _p(np.ascontiguousarray(Nq)),
                              _p(np.ascontiguousarray(dNq)), _p(wfac), _p(kap), _p(f),
-                             _p(Xe), _p(eK), _p(eS))
+                             float(patch.mass), _p(Xe), _p(eK), _p(eS))

@@ -9,6 +9,8 @@ Cases (the seeded synthetic models of ifem_gb300/workloads.py):
   c4_poisson3d_p3   3D Poisson p=3, 3^3 elements, log-normal kappa, 4^3 Gauss
   c3_poisson3d_nurbs 3D Poisson p=2 on a perturbed rational patch, 4^3 elements
   c2_elast3d_p2     3D NURBS elasticity p=2, 2^3 elements, face 5 clamped
+  c6_poisson3d_mass 3D NURBS Poisson p=2, 4^3 elements, K + 25 M, face 5 fixed
+  c7_elast3d_mass   c2 with K + 50 M (Newmark-type effective stiffness)
 Stored per case: IA, JA (0-based compressed columns), A, b (Poisson), MADOF, MEQN.
 """
 from __future__ import annotations
@@ -31,8 +33,17 @@ def cases():
     nurbs.kind = 1
     nurbs.source = 1.0
     nurbs.dirichlet = [(f, 1, 0.0) for f in range(1, 7)]
+    mass_p = W.perturb(W.box_patch(3, 2, 4), np.random.default_rng(W.BASE_SEED + 31), 0.1)
+    mass_p.kind = 1
+    mass_p.source = 1.0
+    mass_p.mass = 25.0
+    mass_p.dirichlet = [(5, 1, 0.0)]
+    elast_m, ng_m = W.config2(nel=2)
+    elast_m[0].mass = 50.0
     return {
         "c1_poisson2d_p2": W.config1(nel=8),
+        "c6_poisson3d_mass": ([mass_p], 3),
+        "c7_elast3d_mass": (elast_m, ng_m),
         "c4_poisson3d_p3": W.config4(nel=3, grid=16),
         "c3_poisson3d_nurbs": ([nurbs], 3),
         "c2_elast3d_p2": W.config2(nel=2),
