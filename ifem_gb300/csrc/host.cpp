@@ -9,6 +9,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <iomanip>
 #include <numeric>
 #include <string>
 
@@ -629,6 +631,106 @@ ifemgpu_status ifemgpu_copy_rhs(ifemgpu_ctx* ctx, double* rhs)
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(rhs, ctx->d_b, sizeof(double) * ctx->neq,
                                     cudaMemcpyDeviceToHost, ctx->stream));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return IFEMGPU_OK;
+}
+
+namespace {
+
+// Writer of the text formats of IFEM's SparseMatrix::dump (SuperLU layout)
+// and StdVector::dump; the character sequence follows those functions so
+// that dumps compare byte for byte.
+bool writeMatrix(std::ostream& os, int n, const int* IA, const int* JA, const double* A, int format)
+{
+  const int nnz = IA[n];
+  std::string end;
+  if (format == IFEMGPU_DUMP_MATRIX_MARKET) {
+    os << "%%MatrixMarket matrix coordinate real general\n% label = A\n";
+    os << n << ' ' << n << ' ' << nnz << '\n';
+    end = "\n";
+  } else if (format == IFEMGPU_DUMP_MATLAB) {
+    os << "A = [\n";
+    end = ";\n";
+  } else if (format == IFEMGPU_DUMP_FLAT) {  // SparseMatrix::write
+    os << "A = [\n";
+    os << n << ' ' << n << ' ' << nnz << '\n';
+    for (int i = 0; i < nnz; i++) os << A[i] << ' ';
+    os << '\n' << n + 1 << '\n';
+    for (int i = 0; i <= n; i++) os << IA[i] << ' ';
+    os << '\n' << nnz << '\n';
+    for (int i = 0; i < nnz; i++) os << JA[i] << ' ';
+    os << std::endl << "]\n";
+    return bool(os);
+  } else {
+    return false;
+  }
+  if (nnz > 0) {
+    os << JA[0] + 1 << " 1 " << A[0];
+    for (int j = 1; j <= n; j++)
+      for (int i = IA[j - 1]; i < IA[j]; i++)
+        if (j > 1 || i != IA[0]) os << end << JA[i] + 1 << ' ' << j << ' ' << A[i];
+  }
+  if (format == IFEMGPU_DUMP_MATLAB) os << "]";
+  os << end;
+  return bool(os);
+}
+
+bool writeVector(std::ostream& os, int n, const double* x, int format, double tol)
+{
+  auto trunc = [tol](double v) { return v > tol || v < -tol || std::isnan(v) ? v : 0.0; };
+  if (format == IFEMGPU_DUMP_MATLAB) {  // utl::writeMatlab
+    os << "b = [";
+    for (int i = 0; i < n; i++) os << ' ' << trunc(x[i]);
+    os << " ];" << std::endl;
+  } else if (format == IFEMGPU_DUMP_MATRIX_MARKET) {
+    os << "%%MatrixMarket matrix array real general\n" << n << " 1";
+    for (int i = 0; i < n; i++) os << '\n' << x[i];
+    os << std::endl;
+  } else if (format == IFEMGPU_DUMP_FLAT) {  // operator<< of utl::vector, 6 per line
+    os << "b =";
+    if (n < 1) os << " (empty)";
+    for (int i = 0; i < n; i++) os << ((i % 6) ? ' ' : '\n') << trunc(x[i]);
+    os << std::endl;
+  } else {
+    return false;
+  }
+  return bool(os);
+}
+
+}  // namespace
+
+ifemgpu_status ifemgpu_write_system(int n, const int* colptr, const int* rowidx,
+                                    const double* values, const double* rhs,
+                                    const char* matrix_path, const char* rhs_path,
+                                    int format, double zero_tol)
+{
+  if (n < 0 || (matrix_path && (!colptr || !rowidx || !values)) || (rhs_path && !rhs) ||
+      format < IFEMGPU_DUMP_FLAT || format > IFEMGPU_DUMP_MATRIX_MARKET)
+    return IFEMGPU_INVALID_ARG;
+  if (matrix_path) {
+    std::ofstream os(matrix_path);
+    os << std::setprecision(17);
+    if (!os || !writeMatrix(os, n, colptr, rowidx, values, format)) return IFEMGPU_INVALID_ARG;
+  }
+  if (rhs_path) {
+    std::ofstream os(rhs_path);
+    os << std::setprecision(17);
+    if (!os || !writeVector(os, n, rhs, format, zero_tol)) return IFEMGPU_INVALID_ARG;
+  }
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_dump_system(ifemgpu_ctx* ctx, const char* matrix_path,
+                                   const char* rhs_path, int format, double zero_tol)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
+  std::vector<double> A(matrix_path ? ctx->nnz : 0), b(rhs_path ? ctx->neq : 0);
+  ifemgpu_status st = IFEMGPU_OK;
+  if (matrix_path && (st = ifemgpu_copy_matrix(ctx, A.data())) != IFEMGPU_OK) return st;
+  if (rhs_path && (st = ifemgpu_copy_rhs(ctx, b.data())) != IFEMGPU_OK) return st;
+  st = ifemgpu_write_system(ctx->neq, ctx->colptr.data(), ctx->rowidx.data(), A.data(), b.data(),
+                            matrix_path, rhs_path, format, zero_tol);
+  if (st != IFEMGPU_OK) return setError(ctx, st, "dump_system: bad format or unwritable path");
   return IFEMGPU_OK;
 }
 

@@ -59,12 +59,13 @@ SOURCE_CONSTANT, SOURCE_SINE = 0, 1
 FIELD_LOG_KAPPA, FIELD_SOURCE_NOISE = 1, 2
 PCG_MIXED, PCG_FP64, FCG_LEARNED = 1, 2, 3
 PRECOND_JACOBI, PRECOND_KRONECKER = 0, 1
+DUMP_FLAT, DUMP_MATLAB, DUMP_MATRIX_MARKET = 1, 2, 3
 
 # Every symbol include/ifemgpu.h declares (checked by the CPU test suite).
 EXPORTS = [
     "ifemgpu_ctx_create", "ifemgpu_ctx_destroy", "ifemgpu_last_error", "ifemgpu_abi_version",
     "ifemgpu_patch_add", "ifemgpu_patch_set_material", "ifemgpu_patch_set_field",
-    "ifemgpu_patch_set_mass",
+    "ifemgpu_patch_set_mass", "ifemgpu_dump_system", "ifemgpu_write_system",
     "ifemgpu_patch_constrain_face", "ifemgpu_patch_add_neumann", "ifemgpu_preprocess",
     "ifemgpu_get_sizes", "ifemgpu_get_madof", "ifemgpu_get_meqn", "ifemgpu_get_mnpc",
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
@@ -106,6 +107,8 @@ def load_library(path: str | None = None):
         "ifemgpu_patch_set_material": (I, [P, I, C.POINTER(Material)]),
         "ifemgpu_patch_set_field": (I, [P, I, I, V]),
         "ifemgpu_patch_set_mass": (I, [P, I, D]),
+        "ifemgpu_dump_system": (I, [P, C.c_char_p, C.c_char_p, I, D]),
+        "ifemgpu_write_system": (I, [I, V, V, V, V, C.c_char_p, C.c_char_p, I, D]),
         "ifemgpu_patch_constrain_face": (I, [P, I, I, I, D]),
         "ifemgpu_patch_add_neumann": (I, [P, I, I, V]),
         "ifemgpu_preprocess": (I, [P]),
@@ -147,6 +150,21 @@ def load_library(path: str | None = None):
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def write_system(colptr, rowidx, values, rhs, matrix_path=None, rhs_path=None,
+                 fmt: int = DUMP_MATRIX_MARKET, zero_tol: float = 0.0, lib=None):
+    """IFEM's text formats for caller arrays (no context or GPU needed)."""
+    L = lib or load_library()
+    cp = np.ascontiguousarray(colptr, dtype=np.int32)
+    ri = np.ascontiguousarray(rowidx, dtype=np.int32)
+    va = np.ascontiguousarray(values, dtype=np.float64)
+    b = np.ascontiguousarray(rhs if rhs is not None else np.zeros(len(cp) - 1), dtype=np.float64)
+    enc = lambda p: None if p is None else os.fspath(p).encode()
+    st = L.ifemgpu_write_system(len(cp) - 1, _ptr(cp), _ptr(ri), _ptr(va), _ptr(b),
+                                enc(matrix_path), enc(rhs_path), fmt, float(zero_tol))
+    if st != OK:
+        raise IfemGpuError(st, "write_system failed")
 
 
 def _ptr(a: np.ndarray):
@@ -318,6 +336,14 @@ class SIM:
         out = np.zeros(self.sizes.neq, dtype=np.float64)
         self._check(self.lib.ifemgpu_copy_rhs(self.ctx, _ptr(out)))
         return out
+
+    def dump_system(self, matrix_path=None, rhs_path=None, fmt: int = DUMP_MATRIX_MARKET,
+                    zero_tol: float = 0.0):
+        """SIMbase::dumpEqSys: the matrix ("A") and right-hand side ("b") in
+        IFEM's text formats (DUMP_FLAT, DUMP_MATLAB, DUMP_MATRIX_MARKET)."""
+        enc = lambda p: None if p is None else os.fspath(p).encode()
+        self._check(self.lib.ifemgpu_dump_system(self.ctx, enc(matrix_path), enc(rhs_path), fmt,
+                                                 float(zero_tol)))
 
     def matrix_bsr(self, block: int):
         """(browptr, bcolind, blocks[nnzb, block, block]) of the assembled matrix."""

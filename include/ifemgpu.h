@@ -223,6 +223,27 @@ ifemgpu_status ifemgpu_assemble(ifemgpu_ctx* ctx, int sync);
 ifemgpu_status ifemgpu_copy_matrix(ifemgpu_ctx* ctx, double* values);
 ifemgpu_status ifemgpu_copy_rhs(ifemgpu_ctx* ctx, double* rhs);
 
+/* Text dumps of the system in the formats of SparseMatrix::dump and
+ * StdVector::dump (src/LinAlg/SparseMatrix.C:341-396, SystemMatrix.C:78-102)
+ * as SIMbase::dumpEqSys writes them (src/SIM/SIMbase.C:2863-2925): precision
+ * 17, matrix label "A" in IFEM's column-oriented (SuperLU) entry order,
+ * vector label "b", vector entries with |v| <= zero_tol printed as 0 where
+ * IFEM applies utl::trunc.  The format numbers are LinAlg::StorageFormat's
+ * (src/LinAlg/LinAlgenums.h:42-48).  Either path may be NULL.             */
+enum ifemgpu_dump_format {
+  IFEMGPU_DUMP_FLAT = 1,
+  IFEMGPU_DUMP_MATLAB = 2,
+  IFEMGPU_DUMP_MATRIX_MARKET = 3
+};
+ifemgpu_status ifemgpu_dump_system(ifemgpu_ctx* ctx, const char* matrix_path,
+                                   const char* rhs_path, int format, double zero_tol);
+/* The same writer on caller arrays (0-based compressed columns of an n x n
+ * matrix with nnz = colptr[n] entries); needs no context or GPU.          */
+ifemgpu_status ifemgpu_write_system(int n, const int* colptr, const int* rowidx,
+                                    const double* values, const double* rhs,
+                                    const char* matrix_path, const char* rhs_path,
+                                    int format, double zero_tol);
+
 /* Device pointers of the system, owned by the context (read-only use).   */
 ifemgpu_status ifemgpu_device_system(ifemgpu_ctx* ctx, const double** values,
                                      const int** colptr, const int** rowidx,

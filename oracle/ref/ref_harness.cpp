@@ -21,6 +21,8 @@
 // The library built from this file is the checker of the CPU oracle; nothing
 // of the product links it.
 #include <cstring>
+#include <fstream>
+#include <iomanip>
 #include <vector>
 
 #include "ASMbase.h"
@@ -28,6 +30,7 @@
 #include "EqualOrderOperators.h"
 #include "FiniteElement.h"
 #include "GaussQuadrature.h"
+#include "LinAlgenums.h"
 #include "MatVec.h"
 #include "SAMpatch.h"
 #include "SparseMatrix.h"
@@ -223,4 +226,27 @@ RH_API void rh_get_system(void* p, int* IA, int* JA, double* A, double* b)
   std::memcpy(JA, ja.data(), sizeof(int) * ja.size());
   std::memcpy(A, a.data(), sizeof(double) * a.size());
   for (size_t i = 0; i < h->b.size(); i++) b[i] = h->b[i];
+}
+
+// The system written by IFEM's own SparseMatrix::dump / StdVector::dump the
+// way SIMbase::dumpEqSys does (src/SIM/SIMbase.C:2863-2925): precision 17,
+// labels "A" and "b", utl::zero_print_tol = zero_tol.
+RH_API int rh_dump(void* p, const char* matrixPath, const char* rhsPath, int format,
+                   double zeroTol)
+{
+  Harness* h = static_cast<Harness*>(p);
+  const double old = utl::zero_print_tol;
+  utl::zero_print_tol = zeroTol;
+  if (matrixPath) {
+    std::ofstream os(matrixPath);
+    os << std::setprecision(17);
+    h->K.dump(os, static_cast<LinAlg::StorageFormat>(format), "A");
+  }
+  if (rhsPath) {
+    std::ofstream os(rhsPath);
+    os << std::setprecision(17);
+    h->b.dump(os, static_cast<LinAlg::StorageFormat>(format), "b");
+  }
+  utl::zero_print_tol = old;
+  return 0;
 }

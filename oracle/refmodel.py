@@ -47,6 +47,7 @@ def lib():
             "rh_poisson_element": (I, [P, I, I, V, V, V, V, V, C.c_double, V, V, V]),
             "rh_assemble": (I, [P, I, V, V]),
             "rh_get_sam": (None, [P, V, V]), "rh_get_system": (None, [P, V, V, V, V]),
+            "rh_dump": (I, [P, C.c_char_p, C.c_char_p, I, C.c_double]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -67,12 +68,14 @@ def gauss(n: int):
     return x, w
 
 
-def reference_system(patch, n_gauss: int):
+def reference_system(patch, n_gauss: int, dumps=None, zero_tol: float = 0.0):
     """K (CSC: IA, JA, A), b, MADOF, MEQN of one patch from IFEM's code.
 
     n_gauss follows ASMbase::getNoGaussPt: 1..10 points, 0 for p+1 per
     direction.  b is returned for Poisson patches only (elasticity tractions
-    are integrated on faces, outside this harness)."""
+    are integrated on faces, outside this harness).  dumps: optional list of
+    (format, matrix_path, rhs_path) written by IFEM's SparseMatrix::dump and
+    StdVector::dump (LinAlg::StorageFormat numbers)."""
     import oracle
     from ifem_gb300 import workloads as W
 
@@ -116,6 +119,9 @@ def reference_system(patch, n_gauss: int):
         madof = np.zeros(nnod + 1, dtype=np.int32)
         meqn = np.zeros(ndof, dtype=np.int32)
         L.rh_get_sam(h, _p(madof), _p(meqn))
+        for fmt, mpath, rpath in dumps or ():
+            L.rh_dump(h, mpath.encode() if mpath else None, rpath.encode() if rpath else None,
+                      fmt, zero_tol)
     finally:
         L.rh_destroy(h)
         orc.close()

@@ -12,6 +12,9 @@ Cases (the seeded synthetic models of ifem_gb300/workloads.py):
   c6_poisson3d_mass 3D NURBS Poisson p=2, 4^3 elements, K + 25 M, face 5 fixed
   c7_elast3d_mass   c2 with K + 50 M (Newmark-type effective stiffness)
 Stored per case: IA, JA (0-based compressed columns), A, b (Poisson), MADOF, MEQN.
+For c0_poisson2d_small (2D Poisson p=2, 4x4 elements) also the text dumps
+IFEM's SparseMatrix::dump / StdVector::dump write, in ref_dump/ (FLAT,
+MATLAB, MATRIX_MARKET; zero print tolerance 1e-12).
 """
 from __future__ import annotations
 
@@ -41,6 +44,7 @@ def cases():
     elast_m, ng_m = W.config2(nel=2)
     elast_m[0].mass = 50.0
     return {
+        "c0_poisson2d_small": W.config1(nel=4),
         "c1_poisson2d_p2": W.config1(nel=8),
         "c6_poisson3d_mass": ([mass_p], 3),
         "c7_elast3d_mass": (elast_m, ng_m),
@@ -55,9 +59,16 @@ def main():
     from oracle.ref import build_ref
     if build_ref.build() is None:
         sys.exit("IFEM sources not present: cannot build the reference")
+    here = os.path.dirname(os.path.abspath(__file__))
+    os.makedirs(os.path.join(here, "ref_dump"), exist_ok=True)
     out = {}
     for name, (patches, ng) in cases().items():
-        ref = refmodel.reference_system(patches[0], ng)
+        dumps = None
+        if name == "c0_poisson2d_small":
+            dumps = [(f, os.path.join(here, "ref_dump", f"A.{ext}"),
+                      os.path.join(here, "ref_dump", f"b.{ext}"))
+                     for f, ext in ((1, "flat"), (2, "m"), (3, "mtx"))]
+        ref = refmodel.reference_system(patches[0], ng, dumps=dumps, zero_tol=1e-12)
         for k, v in ref.items():
             if v is not None:
                 out[f"{name}/{k}"] = v

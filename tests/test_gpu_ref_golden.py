@@ -57,3 +57,25 @@ def test_gpu_matches_reference_system(gpulib, name, ke, tol):
     if "b" in ref:
         b = sim.rhs()
         assert np.abs(b - ref["b"]).max() <= tol * np.abs(ref["b"]).max()
+
+
+def test_gpu_dump_round_trip(gpulib, tmp_path):
+    """ifemgpu_dump_system of a GPU assembly reads back to the same values
+    (17 significant digits) and pattern, in IFEM's MatrixMarket layout."""
+    patches, ng = CASES["c1_poisson2d_p2"]
+    sim = G.SIM(n_gauss=ng, ke_precision=G.KE_FP64)
+    W.load_into(sim, patches)
+    sim.preprocess()
+    sim.assembleSystem()
+    sim.dump_system(tmp_path / "A.mtx", tmp_path / "b.mtx", G.DUMP_MATRIX_MARKET)
+    lines = (tmp_path / "A.mtx").read_text().splitlines()
+    assert lines[0].startswith("%%MatrixMarket matrix coordinate real general")
+    n, _, nnz = (int(v) for v in lines[2].split())
+    ent = np.array([[float(v) for v in ln.split()] for ln in lines[3:3 + nnz]])
+    sam = sim.getSAM()
+    cols = np.repeat(np.arange(n), np.diff(sam.colptr)) + 1
+    np.testing.assert_array_equal(ent[:, 0], sam.rowidx + 1)
+    np.testing.assert_array_equal(ent[:, 1], cols)
+    np.testing.assert_array_equal(ent[:, 2], sim.matrix_values())
+    b = np.array([float(v) for v in (tmp_path / "b.mtx").read_text().split()[7:]])
+    np.testing.assert_array_equal(b, sim.rhs())
