@@ -39,6 +39,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 NEL = 24
+TC_TRAFFIC_24 = 510.1e6  # bytes per launch of the tensor-core element kernel at 24^3 (ncu)
 WORKLOAD = "3D linear elasticity, 1 NURBS patch, p=2, 24^3 elements, 3x3x3 Gauss"
 METRIC = "elements/s assembled; time to 1e-10 residual, learned vs plain PCG, 1 GB300"
 
@@ -379,7 +380,12 @@ def run_gpu(args):
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
+                         "frac": achieved / hbm,
+                         # dram__bytes_read.sum + dram__bytes_write.sum of one
+                         # launch (one 24^3 assembly), ncu capture of this kernel
+                         # on this workload; None for other sizes
+                         "traffic": TC_TRAFFIC_24 if NEL == 24 and ke == G.KE_SPLIT_TF32
+                         else None,
                          "kernel": "volume integration + scatter passes",
                          "kernel_ms": vmax, "algorithmic_bytes": traffic_alg,
                          "peak_source": src},
