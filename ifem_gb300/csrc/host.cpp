@@ -74,6 +74,7 @@ void freeDevice(ifemgpu_ctx* ctx)
   ctx->d_neumann = nullptr;
   ctx->d_counters = nullptr;
   freeSolver(ctx);
+  freeNorms(ctx);
   destroyLearn(ctx);
   destroyFd(ctx);
   f(ctx->d_rhsAlt);

@@ -214,6 +214,13 @@ struct ifemgpu_ctx {
   int learnGen = 0;              // bumped by every setup
   int fieldVersion = 0;          // bumped by every field update
   double* d_rhsAlt = nullptr;    // right-hand side of a collecting solve (neq)
+  // solution norms and secondary solution (norms.cu): every active element
+  // in patch order, its output slot in Item::bc
+  ifemgpu::Item* d_normItems = nullptr;
+  int nNormItems = 0, nNormSlots = 0;
+  std::vector<int> normBase;     // per patch: first output slot (patch-local element e -> base + e)
+  double* d_normBuf = nullptr;   // ndof solution | 2 nNormSlots element values | 2 totals
+  size_t normBufLen = 0;
 };
 
 namespace ifemgpu {
@@ -236,6 +243,7 @@ ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o,
 ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* xstar,
                             int stride, int maxit, double rtol, int precond);
 void freeSolver(ifemgpu_ctx* ctx);
+void freeNorms(ifemgpu_ctx* ctx);
 
 // learned.cu
 ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigned seed,

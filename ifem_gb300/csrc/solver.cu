@@ -131,8 +131,8 @@ k_residual(const int* __restrict__ colptr, const int* __restrict__ rowidx,
     const int c0 = colptr[row], c1 = colptr[row + 1];
     double s = 0.0;
     if (rowPat) {
-      const short* o = patOff + patStart[rowPat[row]];
-      for (int k = c0 + lane; k < c1; k += 32) s += A[k] * x[row + o[k - c0]];
+      const int so = patStart[rowPat[row]] - c0;  // offset of entry k: patOff[k + so]
+      for (int k = c0 + lane; k < c1; k += 32) s += A[k] * x[row + patOff[k + so]];
     } else {
       for (int k = c0 + lane; k < c1; k += 32) s += A[k] * x[rowidx[k]];
     }

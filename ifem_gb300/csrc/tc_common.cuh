@@ -152,12 +152,14 @@ __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float* v)
 __device__ __forceinline__ double widenF32(float f)
 {
   const uint32_t b = __float_as_uint(f);
-  const uint32_t e = (b >> 23) & 0xFFu;
-  const uint64_t sign = static_cast<uint64_t>(b & 0x80000000u) << 32;
-  if (e == 0) return __longlong_as_double(static_cast<long long>(sign));
-  const uint64_t ed = e == 0xFFu ? 0x7FFull : static_cast<uint64_t>(e + 896u);
-  const uint64_t m = static_cast<uint64_t>(b & 0x7FFFFFu) << 29;
-  return __longlong_as_double(static_cast<long long>(sign | (ed << 52) | m));
+  const uint32_t mag = b & 0x7FFFFFFFu;
+  // normal numbers: exponent rebias by 896 and mantissa shift by 29; zero and
+  // subnormals to a signed zero; infinities and NaN keep their class
+  uint32_t hi = (b & 0x80000000u) | ((mag >> 3) + (896u << 20));
+  hi = mag < 0x00800000u ? (b & 0x80000000u) : hi;
+  hi = mag >= 0x7F800000u ? ((b & 0x80000000u) | 0x7FF00000u | (mag & 0x007FFFFFu ? 0x80000u : 0u)) : hi;
+  const uint32_t lo = mag < 0x00800000u ? 0u : (b << 29);
+  return __hiloint2double((int)hi, (int)lo);
 }
 
 // x = hi + lo with hi rounded to TF32 (10 explicit mantissa bits)

@@ -523,6 +523,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       const int la = (a / 3) % 3 + 3 * (a / 9);
       const float* Grow = sm.u.Gc + tid * kGs;    // row (a, k)
       const float* Ga = sm.u.Gc + 3 * a * kGs;     // rows (a, 0..2)
+#pragma unroll 3
       for (int bn = 0; bn < kNen; bn++) {
         const float trm =
             muf * (Ga[3 * bn] + Ga[kGs + 3 * bn + 1] + Ga[2 * kGs + 3 * bn + 2]);

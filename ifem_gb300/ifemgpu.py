@@ -66,6 +66,7 @@ EXPORTS = [
     "ifemgpu_ctx_create", "ifemgpu_ctx_destroy", "ifemgpu_last_error", "ifemgpu_abi_version",
     "ifemgpu_patch_add", "ifemgpu_patch_set_material", "ifemgpu_patch_set_field",
     "ifemgpu_patch_set_mass", "ifemgpu_dump_system", "ifemgpu_write_system",
+    "ifemgpu_solution_norms", "ifemgpu_secondary_solution",
     "ifemgpu_patch_constrain_face", "ifemgpu_patch_add_neumann", "ifemgpu_preprocess",
     "ifemgpu_get_sizes", "ifemgpu_get_madof", "ifemgpu_get_meqn", "ifemgpu_get_mnpc",
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
@@ -109,6 +110,8 @@ def load_library(path: str | None = None):
         "ifemgpu_patch_set_mass": (I, [P, I, D]),
         "ifemgpu_dump_system": (I, [P, C.c_char_p, C.c_char_p, I, D]),
         "ifemgpu_write_system": (I, [I, V, V, V, V, C.c_char_p, C.c_char_p, I, D]),
+        "ifemgpu_solution_norms": (I, [P, V, V, V]),
+        "ifemgpu_secondary_solution": (I, [P, I, V, V]),
         "ifemgpu_patch_constrain_face": (I, [P, I, I, I, D]),
         "ifemgpu_patch_add_neumann": (I, [P, I, I, V]),
         "ifemgpu_preprocess": (I, [P]),
@@ -335,6 +338,25 @@ class SIM:
     def rhs(self) -> np.ndarray:
         out = np.zeros(self.sizes.neq, dtype=np.float64)
         self._check(self.lib.ifemgpu_copy_rhs(self.ctx, _ptr(out)))
+        return out
+
+    def solution_norms(self, u_dof, per_element: bool = False):
+        """(a(u,u), int u.u) and optionally per-element values (nel x 2)."""
+        u = np.ascontiguousarray(u_dof, dtype=np.float64)
+        tot = np.zeros(2)
+        nel = sum(pc.nel for pc, _, _ in self._patches)
+        el = np.zeros((nel, 2)) if per_element else None
+        self._check(self.lib.ifemgpu_solution_norms(self.ctx, _ptr(u), _ptr(tot),
+                                                    _ptr(el) if per_element else None))
+        return (tot, el) if per_element else tot
+
+    def secondary_solution(self, pid: int, u_dof, nq: int, ncomp: int):
+        """Flux (Poisson) or stress (elasticity) at the Gauss points of patch
+        pid: array (nel, nq, ncomp)."""
+        u = np.ascontiguousarray(u_dof, dtype=np.float64)
+        nel = self._patches[pid - 1][0].nel
+        out = np.zeros((nel, nq, ncomp))
+        self._check(self.lib.ifemgpu_secondary_solution(self.ctx, pid, _ptr(u), _ptr(out)))
         return out
 
     def dump_system(self, matrix_path=None, rhs_path=None, fmt: int = DUMP_MATRIX_MARKET,

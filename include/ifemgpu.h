@@ -244,6 +244,25 @@ ifemgpu_status ifemgpu_write_system(int n, const int* colptr, const int* rowidx,
                                     const char* matrix_path, const char* rhs_path,
                                     int format, double zero_tol);
 
+/* Norms of a solution field u (DOF order, ndof values, e.g. from
+ * ifemgpu_expand_solution), integrated with the Gauss rules of the last
+ * assembly: totals[0] = a(u, u) (Poisson: int kappa grad u . grad u;
+ * elasticity: int sigma(u) : eps(u)), totals[1] = int u . u; element
+ * (optional, 2 values per element, patches in order, patch-local elements
+ * first index fastest) the same per element.  Replaces SIMbase::
+ * solutionNorms (src/SIM/SIMbase.C:1838-1967) with the applications'
+ * energy and L2 norm integrands.  Needs an assembly first.               */
+ifemgpu_status ifemgpu_solution_norms(ifemgpu_ctx* ctx, const double* u_dof,
+                                      double* totals, double* element);
+
+/* Secondary solution of u at every Gauss point of one patch: Poisson flux
+ * -kappa grad u (dim values), elasticity stress (6 values, Voigt order
+ * xx yy zz xy yz zx).  out: nel x nq x values, elements and points first
+ * index fastest; zero at singular points.  Replaces the integrand path of
+ * ASMs3D::evalSolution (src/ASM/ASMs3D.C:3179-3500) at the Gauss points. */
+ifemgpu_status ifemgpu_secondary_solution(ifemgpu_ctx* ctx, int patch_id,
+                                          const double* u_dof, double* out);
+
 /* Device pointers of the system, owned by the context (read-only use).   */
 ifemgpu_status ifemgpu_device_system(ifemgpu_ctx* ctx, const double** values,
                                      const int** colptr, const int** rowidx,

@@ -45,6 +45,8 @@ def lib():
             "ifo_set_material": (I, [P, I, I, D, D, I, D, D, V]),
             "ifo_set_field": (I, [P, I, I, V]),
             "ifo_set_mass": (I, [P, I, D]),
+            "ifo_norms": (None, [P, V, V, V]),
+            "ifo_secondary": (None, [P, I, V, V]),
             "ifo_constrain_face": (I, [P, I, I, I, D]),
             "ifo_add_neumann": (I, [P, I, I, V]),
             "ifo_preprocess": (I, [P]), "ifo_sizes": (None, [P, V]),
@@ -99,6 +101,7 @@ class OracleModel:
         karr = (C.c_void_p * 3)(*[_p(k) for k in kn] + [None] * (3 - patch.dim))
         coefs = np.ascontiguousarray(patch.coefs, dtype=np.float64)
         self._keep += [deg, nco, kn, coefs, karr]
+        self._nel_all = getattr(self, "_nel_all", 0) + patch.nel
         return self.L.ifo_add_patch(self.h, patch.dim, _p(deg), _p(nco), C.cast(karr, C.c_void_p),
                                     _p(coefs), int(patch.rational))
 
@@ -164,6 +167,19 @@ class OracleModel:
         eS = np.zeros(nd)
         n = self.L.ifo_element(self.h, pid, iel, _p(eK), _p(eS))
         return eK.reshape(nd, nd).T.copy(), eS, n  # row-major eK[i, j]
+
+    def norms(self, u_dof, per_element=False):
+        u = np.ascontiguousarray(u_dof, dtype=np.float64)
+        tot = np.zeros(2)
+        el = np.zeros((self._nel_all, 2)) if per_element else None
+        self.L.ifo_norms(self.h, _p(u), _p(tot), _p(el) if per_element else None)
+        return (tot, el) if per_element else tot
+
+    def secondary(self, pid, u_dof, nel, nq, ncomp):
+        u = np.ascontiguousarray(u_dof, dtype=np.float64)
+        out = np.zeros((nel, nq, ncomp))
+        self.L.ifo_secondary(self.h, pid, _p(u), _p(out))
+        return out
 
     def pcg(self, b, rtol=1e-10, maxit=100000, threads=1, x0=None):
         x = np.zeros(self.sizes["neq"]) if x0 is None else np.array(x0, dtype=np.float64)

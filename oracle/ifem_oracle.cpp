@@ -689,6 +689,87 @@ int integrateElement(Model& m, Patch& pc, int iel, const int ng[3],
   return singular;
 }
 
+// Energy and L2 norms of a DOF-order field u over one element, and the
+// secondary solution (Poisson flux -kappa grad u, elasticity stress in
+// Voigt order xx yy zz xy yz zx) at its Gauss points: the norm integrands
+// of the Poisson and elasticity applications as SIMbase::solutionNorms
+// (src/SIM/SIMbase.C:1838-1967) integrates them, and the point evaluation
+// of ASMs3D::evalSolution (src/ASM/ASMs3D.C:3179-3500) at the Gauss points.
+void elementNorms(const Model& m, Patch& pc, int iel, const double* u, double out[2],
+                  double* sec)
+{
+  out[0] = out[1] = 0.0;
+  const int dim = pc.dim, nen = pc.nen(), npv = pc.npv;
+  const auto& nodes = pc.mnpc[iel];
+  if (nodes.empty()) return;
+  int ng[3] = {1, 1, 1};
+  std::vector<double> xg[3], wg[3];
+  for (int d = 0; d < dim; d++) {
+    ng[d] = numGauss(m, pc.p[d] + 1, false);
+    xg[d].resize(ng[d]);
+    wg[d].resize(ng[d]);
+    gaussLegendre(ng[d], xg[d].data(), wg[d].data());
+  }
+  const int ee[3] = {iel % pc.nel_d[0], (iel / pc.nel_d[0]) % pc.nel_d[1],
+                     iel / (pc.nel_d[0] * pc.nel_d[1])};
+  double dV = dim == 3 ? 0.125 : 0.25;
+  for (int d = 0; d < dim; d++) dV *= pc.U[d][pc.p[d] + ee[d] + 1] - pc.U[d][pc.p[d] + ee[d]];
+  std::vector<double> Xn((size_t)nen * dim), Ue((size_t)nen * 3, 0.0);
+  for (int a = 0; a < nen; a++) {
+    for (int c = 0; c < dim; c++) Xn[(size_t)a * dim + c] = pc.X[(size_t)nodes[a] * dim + c];
+    const int d0 = m.madof[pc.firstNode + nodes[a]] - 1;
+    for (int c = 0; c < npv; c++) Ue[(size_t)a * 3 + c] = u[d0 + c];
+  }
+  const double E = pc.mat.E, nu = pc.mat.nu;
+  const double lam = E * nu / ((1 + nu) * (1 - 2 * nu)), mu = E / (2 * (1 + nu));
+  const int nc = pc.mat.kind == 1 ? dim : 6;
+  std::vector<double> N, dNdu, dNdX((size_t)nen * dim);
+  Basis1D b[3];
+  int q = 0;
+  for (int k = 0; k < (dim == 3 ? ng[2] : 1); k++)
+    for (int j = 0; j < ng[1]; j++)
+      for (int i = 0; i < ng[0]; i++, q++) {
+        const int gi[3] = {i, j, k};
+        for (int d = 0; d < dim; d++)
+          eval1D(pc, d, pc.p[d] + ee[d], gaussParam(pc, d, ee[d], xg[d][gi[d]]), b[d]);
+        tensorBasis(pc, b, nodes, N, dNdu);
+        const double det = jacobian(dim, nen, Xn.data(), dNdu.data(), nullptr, dNdX.data());
+        if (det == 0.0) continue;
+        const double w = det * dV * wg[0][i] * wg[1][j] * (dim == 3 ? wg[2][k] : 1.0);
+        double uh[3] = {0, 0, 0}, g[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, lk = 0.0;
+        for (int a = 0; a < nen; a++) {
+          for (int c = 0; c < npv; c++) {
+            uh[c] += N[a] * Ue[(size_t)a * 3 + c];
+            for (int r = 0; r < dim; r++) g[c][r] += dNdX[(size_t)r * nen + a] * Ue[(size_t)a * 3 + c];
+          }
+          if (!pc.logk.empty()) lk += N[a] * pc.logk[nodes[a]];
+        }
+        double energy, sv[6] = {0, 0, 0, 0, 0, 0};
+        if (pc.mat.kind == 1) {
+          const double kap = pc.mat.kappa * (pc.logk.empty() ? 1.0 : std::exp(lk));
+          energy = kap * (g[0][0] * g[0][0] + g[0][1] * g[0][1] + g[0][2] * g[0][2]);
+          for (int r = 0; r < dim; r++) sv[r] = -kap * g[0][r];
+        } else {
+          const double exx = g[0][0], eyy = g[1][1], ezz = g[2][2];
+          const double gxy = g[0][1] + g[1][0], gyz = g[1][2] + g[2][1], gzx = g[2][0] + g[0][2];
+          const double tr = exx + eyy + ezz;
+          sv[0] = lam * tr + 2 * mu * exx;
+          sv[1] = lam * tr + 2 * mu * eyy;
+          sv[2] = lam * tr + 2 * mu * ezz;
+          sv[3] = mu * gxy;
+          sv[4] = mu * gyz;
+          sv[5] = mu * gzx;
+          energy = sv[0] * exx + sv[1] * eyy + sv[2] * ezz + sv[3] * gxy + sv[4] * gyz + sv[5] * gzx;
+        }
+        double l2 = 0.0;
+        for (int c = 0; c < npv; c++) l2 += uh[c] * uh[c];
+        out[0] += w * energy;
+        out[1] += w * l2;
+        if (sec)
+          for (int c = 0; c < nc; c++) sec[(size_t)q * nc + c] = sv[c];
+      }
+}
+
 // Face overload of ASMs3D::integrate (src/ASM/ASMs3D.C:2547-2812) for
 // constant tractions (elasticity) or normal flux (Poisson).
 void integrateNeumann(Model& m, Patch& pc, const Neumann& nm)
@@ -994,6 +1075,39 @@ int ifo_element(void* h, int pid, int iel, double* eKout, double* eSout)
   std::memcpy(eKout, eK.data(), sizeof(double) * eK.size());
   std::memcpy(eSout, eS.data(), sizeof(double) * eS.size());
   return (int)eS.size();
+}
+
+// Norm totals and per-element norms (patches in order, all elements of a
+// patch first index fastest); the secondary solution of one patch.
+void ifo_norms(void* h, const double* u, double* totals, double* elem)
+{
+  Model& m = *static_cast<Model*>(h);
+  totals[0] = totals[1] = 0.0;
+  size_t slot = 0;
+  for (Patch& pc : m.patches)
+    for (int e = 0; e < pc.nelAll; e++, slot++) {
+      double o[2];
+      elementNorms(m, pc, e, u, o, nullptr);
+      totals[0] += o[0];
+      totals[1] += o[1];
+      if (elem) {
+        elem[2 * slot] = o[0];
+        elem[2 * slot + 1] = o[1];
+      }
+    }
+}
+
+void ifo_secondary(void* h, int pid, const double* u, double* out)
+{
+  Model& m = *static_cast<Model*>(h);
+  Patch& pc = m.patches.at(pid - 1);
+  int nq = 1;
+  for (int d = 0; d < pc.dim; d++) nq *= numGauss(m, pc.p[d] + 1, false);
+  const int nc = pc.mat.kind == 1 ? pc.dim : 6;
+  for (int e = 0; e < pc.nelAll; e++) {
+    double o[2];
+    elementNorms(m, pc, e, u, o, out + (size_t)e * nq * nc);
+  }
 }
 
 void ifo_get_system(void* h, double* A, double* b)
