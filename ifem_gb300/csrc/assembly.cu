@@ -393,7 +393,7 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
     const int node = elemNode(P, e, a);
     for (int c = 0; c < 3; c++) Xn[a * 4 + c] = (T)(P.ctrl[(size_t)node * 4 + c] - c00[c]);
     Xn[a * 4 + 3] = (T)P.ctrl[(size_t)node * 4 + 3];
-    const int g = P.firstNode + node;
+    const int g = globalNode(P, node);
     const int d0 = S.madof[g] - 1;
     for (int c = 0; c < npv; c++) eq[a * npv + c] = S.meqn[d0 + c];
     nodeA[a] = node;
@@ -773,7 +773,7 @@ k_face_fp64(const DevPatch* __restrict__ patches, const Item* __restrict__ items
   for (int a = threadIdx.x; a < nen; a += blockDim.x) {
     const int node = elemNode(P, e, a);
     for (int c = 0; c < 4; c++) Xn[a * 4 + c] = P.ctrl[(size_t)node * 4 + c];
-    const int d0 = S.madof[P.firstNode + node] - 1;
+    const int d0 = S.madof[globalNode(P, node)] - 1;
     for (int c = 0; c < npv; c++) eq[a * npv + c] = S.meqn[d0 + c];
   }
   __syncthreads();
@@ -896,6 +896,11 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     D.kind = pc.mat.kind;
     D.rational = pc.rational;
     D.firstNode = pc.firstNode;
+    D.mlgn = nullptr;
+    if (!ctx->conns.empty()) {  // connected model: global node table
+      IFEMGPU_TRY(upload(ctx, &pc.d_mlgn, pc.mlgn.data(), pc.mlgn.size()));
+      D.mlgn = pc.d_mlgn;
+    }
     D.kappa = pc.mat.kappa;
     D.source = pc.mat.source;
     D.source_shape = pc.mat.source_shape;
@@ -973,7 +978,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   int nflags = 0;
   // the other patches share one persistent pass when every element has a
   // volume (the done flags assume a full element grid)
-  bool flow = ctx->opts.colour_passes != 1;
+  bool flow = ctx->opts.colour_passes != 1 && ctx->conns.empty();
   for (int pi = 0; pi < np; pi++) {
     DevPatch& D = ctx->h_devpatches[pi];
     onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) && D.mass == 0.0 &&
@@ -1051,6 +1056,9 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
         return setError(ctx, IFEMGPU_CUDA_ERROR, "internal: colour ranges of the persistent pass");
     }
   } else {
+    // one launch per colour; in a connected model elements of two patches
+    // may share nodes, so there one launch per (colour, patch), in order
+    const bool perPatch = !ctx->conns.empty();
     for (int c = 0; c < maxColours; c++) {
       Pass pass{(int)vol.size(), 0, 0, 0, 0, false};
       for (int pi = 0; pi < np; pi++) {
@@ -1059,6 +1067,11 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
         colourItems(pi, c, vol);
         pass.maxNd = std::max(pass.maxNd, pc.nen() * pc.npv);
         pass.smem = std::max(pass.smem, volumeSmem(ctx->h_devpatches[pi], realBytes));
+        if (perPatch) {
+          pass.count = (int)vol.size() - pass.first;
+          if (pass.count) ctx->passes.push_back(pass);
+          pass = Pass{(int)vol.size(), 0, 0, 0, 0, false};
+        }
       }
       pass.count = (int)vol.size() - pass.first;
       if (pass.count) ctx->passes.push_back(pass);

@@ -480,7 +480,7 @@ ifemgpu_status fdSetup(ifemgpu_ctx* ctx)
     for (int comp = 0; comp < pc.npv; comp++) {
       auto eqOf = [&](int i, int j, int k) {
         const int node = (k * pc.n[1] + j) * pc.n[0] + i;
-        return ctx->meqn[ctx->madof[pc.firstNode + node] - 1 + comp];
+        return ctx->meqn[ctx->madof[pc.mlgn[node]] - 1 + comp];
       };
       int lo[3] = {pc.n[0], pc.n[1], pc.n[2]}, hi[3] = {-1, -1, -1};
       long nfree = 0;

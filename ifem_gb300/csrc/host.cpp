@@ -11,6 +11,7 @@
 #include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <map>
 #include <numeric>
 #include <string>
 
@@ -46,6 +47,7 @@ void freeDevice(ifemgpu_ctx* ctx)
     f(pc.d_lineOff); pc.d_lineOff = nullptr;
     f(pc.d_logk); pc.d_logk = nullptr;
     f(pc.d_noise); pc.d_noise = nullptr;
+    f(pc.d_mlgn); pc.d_mlgn = nullptr;
     for (int d = 0; d < 3; d++) {
       f(pc.d_knots[d]); f(pc.d_tabN[d]); f(pc.d_tabD[d]); f(pc.d_span[d]); f(pc.d_tabB[d]);
       f(pc.d_tabNf[d]); f(pc.d_tabDf[d]);
@@ -139,6 +141,122 @@ std::vector<int> faceNodes(const HostPatch& pc, int face)
 // prescribed ones and the first prescription of a DOF wins, as IFEM's
 // SAMpatch::initConstraintEqs ignores constraints on already fixed or
 // constrained DOFs (src/ASM/SAMpatch.C:300-310).
+// Face (3D) or edge (2D) size in IFEM's boundary-node order:
+// ASMs3D::getFaceSize (src/ASM/ASMs3D.C:3796-3810).
+void faceSize(const HostPatch& pc, int face, int& m1, int& m2)
+{
+  const int dir = (face + 1) / 2;
+  if (pc.dim == 2) {
+    m1 = dir == 1 ? pc.n[1] : pc.n[0];
+    m2 = 1;
+  } else if (dir == 1) {
+    m1 = pc.n[1];
+    m2 = pc.n[2];
+  } else if (dir == 2) {
+    m1 = pc.n[0];
+    m2 = pc.n[2];
+  } else {
+    m1 = pc.n[0];
+    m2 = pc.n[1];
+  }
+}
+
+// Global node numbers (1-based, IFEM's MLGN).  Patches first get
+// consecutive numbers (ASMs3D::generateFEMTopology); each connection then
+// identifies the slave face's nodes with the master face's in the order and
+// orientation of ASMs3D::connectBasis / ASMs2D::connectBasis
+// (src/ASM/ASMs3D.C:722-796, ASMs2D.C:697-749), keeping the smaller number of
+// a pair and passing the change on to the patches connected earlier
+// (ASMbase::collapseNodes / mergeNodes, src/ASM/ASMbase.C:1289-1331); last,
+// numbers are compacted in order of first appearance, patch by patch
+// (SIMbase::renumberNodes, src/SIM/SIMbase.C:535-565, with
+// ASMbase::renumberNodes and utl::renumber).  Returns the node count.
+int connectAndNumber(ifemgpu_ctx* ctx, std::vector<std::vector<int>>& mlgn, std::string& err)
+{
+  const int np = (int)ctx->patches.size();
+  std::vector<std::vector<int>> nbr(np);
+  auto merge = [&](int P, int inod, int num) {
+    const int old = mlgn[P][inod];
+    mlgn[P][inod] = num;
+    for (int Q : nbr[P])
+      for (int& g : mlgn[Q])
+        if (g == old) g = num;
+  };
+  auto collapse = [&](int M, int mnode, int S, int snode) {
+    const int a = mlgn[M][mnode], b = mlgn[S][snode];
+    if (a > b) merge(M, mnode, b);
+    else if (b > a) merge(S, snode, a);
+  };
+  auto coord = [&](int P, int node, int c) {
+    const HostPatch& pc = ctx->patches[P];
+    const double* x = pc.ctrl4.data() + (size_t)node * 4;
+    return c < pc.dim ? x[c] : 0.0;
+  };
+  for (const HostConnection& c : ctx->conns) {
+    const int M = c.master - 1, S = c.slave - 1;
+    const HostPatch &pm = ctx->patches[M], &ps = ctx->patches[S];
+    const std::vector<int> mn = faceNodes(pm, c.mface), sn = faceNodes(ps, c.sface);
+    int m1, m2, n1, n2;
+    faceSize(ps, c.sface, m1, m2);
+    faceSize(pm, c.mface, n1, n2);
+    if (pm.dim == 3 && c.orient > 3) std::swap(n1, n2);
+    if (n1 != m1 || n2 != m2 || mn.size() != sn.size()) {
+      err = "connect: faces of different sizes";
+      return -1;
+    }
+    if (pm.dim == 3 && c.orient > 3) std::swap(n1, n2);
+    auto check = [&](int mnode, int snode) {
+      for (int k = 0; k < 3; k++)
+        if (std::fabs(coord(M, mnode, k) - coord(S, snode, k)) > 1.0e-4) return false;
+      return true;
+    };
+    for (int j = 0, node = 0; j < n2; j++)
+      for (int i = 0; i < n1; i++, node++) {
+        int k = i, l = j;
+        if (pm.dim == 3) {
+          switch (c.orient) {
+            case 0: k = i; l = j; break;
+            case 1: k = i; l = n2 - j - 1; break;
+            case 2: k = n1 - i - 1; l = j; break;
+            case 3: k = n1 - i - 1; l = n2 - j - 1; break;
+            case 4: k = j; l = i; break;
+            case 5: k = j; l = m2 - i - 1; break;
+            case 6: k = m1 - j - 1; l = i; break;
+            case 7: k = m1 - j - 1; l = m2 - i - 1; break;
+          }
+        } else if (c.orient) {
+          k = n1 - i - 1;
+        }
+        const int snode = sn[(size_t)l * m1 + k], mnode = mn[node];
+        if (!check(mnode, snode)) {
+          err = "connect: non-matching nodes (face, orientation or geometry)";
+          return -1;
+        }
+        collapse(M, mnode, S, snode);
+      }
+    if (std::find(nbr[S].begin(), nbr[S].end(), M) == nbr[S].end()) {
+      nbr[S].push_back(M);
+      nbr[M].push_back(S);
+    }
+  }
+  std::map<int, int> old2new;
+  int runner = 0;
+  for (int P = 0; P < np; P++) {
+    int renum = 0;
+    for (int& g : mlgn[P]) {
+      auto it = old2new.find(g);
+      if (it == old2new.end()) it = old2new.emplace(g, ++runner).first;
+      if (g != it->second) {
+        g = it->second;
+        renum++;
+      }
+    }
+    if (renum == 0 && !mlgn[P].empty())
+      runner = std::max(runner, *std::max_element(mlgn[P].begin(), mlgn[P].end()));
+  }
+  return runner;
+}
+
 ifemgpu_status numbering(ifemgpu_ctx* ctx)
 {
   int gNod = 0, gEl = 0;
@@ -149,11 +267,32 @@ ifemgpu_status numbering(ifemgpu_ctx* ctx)
     gNod += pc.nnod;
     gEl += pc.nelActive;
   }
+  std::vector<std::vector<int>> mlgn(ctx->patches.size());
+  for (size_t pi = 0; pi < ctx->patches.size(); pi++) {
+    const HostPatch& pc = ctx->patches[pi];
+    mlgn[pi].resize(pc.nnod);
+    for (int i = 0; i < pc.nnod; i++) mlgn[pi][i] = pc.firstNode + i + 1;
+  }
+  if (!ctx->conns.empty()) {
+    std::string err;
+    gNod = connectAndNumber(ctx, mlgn, err);
+    if (gNod < 0) return setError(ctx, IFEMGPU_INVALID_ARG, err);
+  }
+  for (size_t pi = 0; pi < ctx->patches.size(); pi++) {
+    HostPatch& pc = ctx->patches[pi];
+    pc.mlgn.resize(pc.nnod);
+    for (int i = 0; i < pc.nnod; i++) pc.mlgn[i] = mlgn[pi][i] - 1;
+  }
   ctx->nnod = gNod;
   ctx->nel = gEl;
   ctx->madof.assign(ctx->nnod + 1, 0);
   for (auto& pc : ctx->patches)
-    for (int i = 0; i < pc.nnod; i++) ctx->madof[pc.firstNode + i + 1] = pc.npv;
+    for (int i = 0; i < pc.nnod; i++) {
+      int& m = ctx->madof[pc.mlgn[i] + 1];
+      if (m && m != pc.npv)
+        return setError(ctx, IFEMGPU_INVALID_ARG, "connected patches with different unknowns per node");
+      m = pc.npv;
+    }
   ctx->madof[0] = 1;
   for (int i = 0; i < ctx->nnod; i++) ctx->madof[i + 1] += ctx->madof[i];
   ctx->ndof = ctx->madof[ctx->nnod] - 1;
@@ -165,7 +304,7 @@ ifemgpu_status numbering(ifemgpu_ctx* ctx)
         for (char c : std::to_string(bc.dofs)) {
           int dof = c - '0';
           if (dof >= 1 && dof <= pc.npv)
-            msc[ctx->madof[pc.firstNode + node] - 1 + dof - 1] = 0;
+            msc[ctx->madof[pc.mlgn[node]] - 1 + dof - 1] = 0;
         }
     }
   ctx->c0.clear();
@@ -176,7 +315,7 @@ ifemgpu_status numbering(ifemgpu_ctx* ctx)
         for (char c : std::to_string(bc.dofs)) {
           int dof = c - '0';
           if (dof < 1 || dof > pc.npv) continue;
-          int idof = ctx->madof[pc.firstNode + node] - 1 + dof - 1;
+          int idof = ctx->madof[pc.mlgn[node]] - 1 + dof - 1;
           if (msc[idof] <= 0 || slave[idof]) continue;
           ctx->c0.push_back(bc.value);
           slave[idof] = (int)ctx->c0.size();
@@ -229,18 +368,55 @@ void coupledNodes(const HostPatch& pc, int node, std::vector<int>& out)
 ifemgpu_status pattern(ifemgpu_ctx* ctx)
 {
   const int neq = ctx->neq;
+  const bool connected = !ctx->conns.empty();
   // equation -> (patch, node, dof)
-  std::vector<int> eqPatch(neq), eqNode(neq);
+  std::vector<int> eqPatch(neq), eqNode(neq), eqGlobal(neq);
   for (int pi = 0; pi < (int)ctx->patches.size(); pi++) {
     auto& pc = ctx->patches[pi];
     for (int nd = 0; nd < pc.nnod; nd++) {
-      int g = pc.firstNode + nd;
+      int g = pc.mlgn[nd];
       for (int d = ctx->madof[g]; d < ctx->madof[g + 1]; d++) {
         int e = ctx->meqn[d - 1];
-        if (e > 0) { eqPatch[e - 1] = pi; eqNode[e - 1] = nd; }
+        if (e > 0) { eqPatch[e - 1] = pi; eqNode[e - 1] = nd; eqGlobal[e - 1] = g; }
       }
     }
   }
+  // connected models: coupled global nodes of every global node, from the
+  // elements of all patches (SAM::getDofCouplings, src/LinAlg/SAM.C:354-427)
+  std::vector<std::vector<int>> coupled;
+  if (connected) {
+    coupled.resize(ctx->nnod);
+    for (const auto& pc : ctx->patches) {
+      const int q1 = pc.p[0] + 1, q2 = pc.p[1] + 1, q3 = pc.dim == 3 ? pc.p[2] + 1 : 1;
+      std::vector<int> en;
+      for (int e = 0; e < pc.nelAll; e++) {
+        if (!pc.active[e]) continue;
+        const int e1 = e % pc.nel[0], e2 = (e / pc.nel[0]) % pc.nel[1],
+                  e3 = e / (pc.nel[0] * pc.nel[1]);
+        en.clear();
+        for (int c = 0; c < q3; c++)
+          for (int b = 0; b < q2; b++)
+            for (int a = 0; a < q1; a++)
+              en.push_back(pc.mlgn[((e3 + c) * pc.n[1] + e2 + b) * pc.n[0] + e1 + a]);
+        for (int g : en) coupled[g].insert(coupled[g].end(), en.begin(), en.end());
+      }
+    }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int g = 0; g < ctx->nnod; g++) {
+      std::sort(coupled[g].begin(), coupled[g].end());
+      coupled[g].erase(std::unique(coupled[g].begin(), coupled[g].end()), coupled[g].end());
+    }
+  }
+  // the coupled global nodes of the node of equation c, ascending
+  auto nodesOf = [&](int c, std::vector<int>& nb) {
+    if (connected) {
+      nb = coupled[eqGlobal[c]];
+      return;
+    }
+    const auto& pc = ctx->patches[eqPatch[c]];
+    coupledNodes(pc, eqNode[c], nb);
+    for (int& m : nb) m = pc.mlgn[m];
+  };
   // column counts (columns of one node share their row set)
   std::vector<int64_t> cnt(neq + 1, 0);
 #pragma omp parallel
@@ -248,13 +424,10 @@ ifemgpu_status pattern(ifemgpu_ctx* ctx)
     std::vector<int> nb;
 #pragma omp for schedule(dynamic, 256)
     for (int c = 0; c < neq; c++) {
-      const auto& pc = ctx->patches[eqPatch[c]];
-      coupledNodes(pc, eqNode[c], nb);
+      nodesOf(c, nb);
       int64_t s = 0;
-      for (int m : nb) {
-        int g = pc.firstNode + m;
+      for (int g : nb)
         for (int d = ctx->madof[g]; d < ctx->madof[g + 1]; d++) s += ctx->meqn[d - 1] > 0;
-      }
       cnt[c + 1] = s;
     }
   }
@@ -270,14 +443,11 @@ ifemgpu_status pattern(ifemgpu_ctx* ctx)
     std::vector<int> nb;
 #pragma omp for schedule(dynamic, 256)
     for (int c = 0; c < neq; c++) {
-      const auto& pc = ctx->patches[eqPatch[c]];
-      coupledNodes(pc, eqNode[c], nb);
+      nodesOf(c, nb);
       int64_t k = cnt[c];
-      for (int m : nb) {
-        int g = pc.firstNode + m;
+      for (int g : nb)
         for (int d = ctx->madof[g]; d < ctx->madof[g + 1]; d++)
           if (ctx->meqn[d - 1] > 0) ctx->rowidx[k++] = ctx->meqn[d - 1] - 1;
-      }
     }
   }
   // F(n), and the line-offset tables that give pattern positions without a
@@ -291,7 +461,7 @@ ifemgpu_status pattern(ifemgpu_ctx* ctx)
   const std::vector<int>& F = ctx->freeBefore;
   for (auto& pc : ctx->patches) {
     pc.lineOff.clear();
-    if (!boxCoupling(pc)) continue;
+    if (!boxCoupling(pc) || connected) continue;  // connected: positions by search
     const int w1 = 2 * pc.p[1] + 1, w2 = 2 * pc.p[2] + 1;
     pc.lineOff.assign((size_t)pc.nnod * w1 * w2, 0);
 #pragma omp parallel for schedule(static)
@@ -427,6 +597,22 @@ ifemgpu_status ifemgpu_patch_set_material(ifemgpu_ctx* ctx, int patch_id,
   pc->mat = *mat;
   pc->hasMat = true;
   pc->npv = mat->kind == IFEMGPU_ELASTICITY ? pc->dim : 1;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_patch_connect(ifemgpu_ctx* ctx, int master, int master_face, int slave,
+                                     int slave_face, int orient)
+{
+  HostPatch* pm = getPatch(ctx, master);
+  HostPatch* ps = getPatch(ctx, slave);
+  if (!pm || !ps || master == slave || pm->dim != ps->dim)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "connect: bad patches");
+  const int nf = 2 * pm->dim;
+  if (master_face < 1 || master_face > nf || slave_face < 1 || slave_face > nf || orient < 0 ||
+      orient > (pm->dim == 3 ? 7 : 1))
+    return setError(ctx, IFEMGPU_INVALID_ARG, "connect: bad face or orientation");
+  if (ctx->preprocessed) return setError(ctx, IFEMGPU_INVALID_ARG, "model already preprocessed");
+  ctx->conns.push_back({master, master_face, slave, slave_face, orient});
   return IFEMGPU_OK;
 }
 

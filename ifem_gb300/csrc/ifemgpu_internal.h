@@ -29,6 +29,8 @@ struct DevPatch {
   int kind;           // IFEMGPU_POISSON / IFEMGPU_ELASTICITY
   int rational;
   int firstNode;      // global 0-based index of the patch's first node
+  const int* mlgn;    // global 0-based node of each patch node (connected models;
+                      // nullptr: firstNode + node)
   double kappa, source, E, nu, body[3];
   // Lame constants and body force, formed once on the host (the FP64 pipe
   // is slow on this GPU, so no per-element divisions)
@@ -71,6 +73,12 @@ struct DevPatch {
   int ngf[3];
 };
 
+// Global 0-based node of patch-local node `node`.
+__host__ __device__ inline int globalNode(const DevPatch& P, int node)
+{
+  return P.mlgn ? P.mlgn[node] : P.firstNode + node;
+}
+
 // Work item of the volume and face passes.
 struct Item {
   int patch;    // index into the DevPatch array
@@ -80,6 +88,8 @@ struct Item {
 };
 
 struct HostBC { int face; int dofs; double value; };
+// face (3D) or edge (2D) of a slave patch identified with one of a master patch
+struct HostConnection { int master, mface, slave, sface, orient; };
 struct HostNeumann { int face; double t[3]; };
 
 struct HostPatch {
@@ -100,6 +110,8 @@ struct HostPatch {
   int nel[3] = {1, 1, 1};
   int nelAll = 0, nnod = 0, nelActive = 0;
   int firstNode = 0, firstElm = 0;
+  std::vector<int> mlgn;     // global 0-based node of each patch node (IFEM's MLGN - 1)
+  int* d_mlgn = nullptr;     // device copy for connected models
   std::vector<char> active;  // per element: non-zero parametric volume
   int nen() const {
     return (p[0] + 1) * (p[1] + 1) * (dim == 3 ? p[2] + 1 : 1);
@@ -147,6 +159,7 @@ struct ifemgpu_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<ifemgpu::HostPatch> patches;
+  std::vector<ifemgpu::HostConnection> conns;  // patch connections (topology)
   bool preprocessed = false;
   bool assembled = false;
   // SAM arrays

@@ -511,7 +511,7 @@ ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigne
                       (dk ? f[2] : 1.f - f[2]);
       flist[((c[2] + dk) * (m + 1) + c[1] + dj) * (m + 1) + c[0] + di].push_back({node, w});
     }
-    const int first = ctx->madof[pc.firstNode + node] - 1;
+    const int first = ctx->madof[pc.mlgn[node]] - 1;
     for (int comp = 0; comp < npv; comp++) {
       const int eq = ctx->meqn[first + comp];
       if (eq <= 0) continue;

@@ -58,7 +58,7 @@ k_norms(const DevPatch* __restrict__ patches, const Item* __restrict__ items,
     const int node = normElemNode(P, e, a);
     for (int c = 0; c < 3; c++) Xn[a * 4 + c] = (T)(P.ctrl[(size_t)node * 4 + c] - c00[c]);
     Xn[a * 4 + 3] = (T)P.ctrl[(size_t)node * 4 + 3];
-    const int d0 = madof[P.firstNode + node] - 1;
+    const int d0 = madof[globalNode(P, node)] - 1;
     for (int c = 0; c < 3; c++) U[a * 3 + c] = c < npv ? (T)u[d0 + c] : T(0);
     Gk[a] = P.logk ? (T)P.logk[node] : T(0);
   }

@@ -188,12 +188,12 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.X[a][1] = (float)(c[1] - c00[1]);
       sm.X[a][2] = (float)(c[2] - c00[2]);
       sm.X[a][3] = (float)c[3];
-      const int d0 = S.madof[P.firstNode + node] - 1;
+      const int d0 = S.madof[globalNode(P, node)] - 1;
       const int q0 = S.meqn[d0], q1 = S.meqn[d0 + 1], q2 = S.meqn[d0 + 2];
       sm.eq[3 * a] = q0;
       sm.eq[3 * a + 1] = q1;
       sm.eq[3 * a + 2] = q2;
-      const int Fa = S.F[P.firstNode + node];
+      const int Fa = S.F[globalNode(P, node)];
       sm.rowBase[3 * a] = Fa;
       sm.rowBase[3 * a + 1] = Fa + (q0 > 0);
       sm.rowBase[3 * a + 2] = Fa + (q0 > 0) + (q1 > 0);

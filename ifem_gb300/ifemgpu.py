@@ -65,7 +65,7 @@ DUMP_FLAT, DUMP_MATLAB, DUMP_MATRIX_MARKET = 1, 2, 3
 EXPORTS = [
     "ifemgpu_ctx_create", "ifemgpu_ctx_destroy", "ifemgpu_last_error", "ifemgpu_abi_version",
     "ifemgpu_patch_add", "ifemgpu_patch_set_material", "ifemgpu_patch_set_field",
-    "ifemgpu_patch_set_mass", "ifemgpu_dump_system", "ifemgpu_write_system",
+    "ifemgpu_patch_set_mass", "ifemgpu_dump_system", "ifemgpu_write_system", "ifemgpu_patch_connect",
     "ifemgpu_solution_norms", "ifemgpu_secondary_solution",
     "ifemgpu_patch_constrain_face", "ifemgpu_patch_add_neumann", "ifemgpu_preprocess",
     "ifemgpu_get_sizes", "ifemgpu_get_madof", "ifemgpu_get_meqn", "ifemgpu_get_mnpc",
@@ -108,6 +108,7 @@ def load_library(path: str | None = None):
         "ifemgpu_patch_set_material": (I, [P, I, C.POINTER(Material)]),
         "ifemgpu_patch_set_field": (I, [P, I, I, V]),
         "ifemgpu_patch_set_mass": (I, [P, I, D]),
+        "ifemgpu_patch_connect": (I, [P, I, I, I, I, I]),
         "ifemgpu_dump_system": (I, [P, C.c_char_p, C.c_char_p, I, D]),
         "ifemgpu_write_system": (I, [I, V, V, V, V, C.c_char_p, C.c_char_p, I, D]),
         "ifemgpu_solution_norms": (I, [P, V, V, V]),
@@ -265,6 +266,10 @@ class SIM:
                      E=1.0, nu=0.3, body=(0.0, 0.0, 0.0)):
         m = Material(kind, kappa, source, source_shape, E, nu, (C.c_double * 3)(*body))
         self._check(self.lib.ifemgpu_patch_set_material(self.ctx, pid, C.byref(m)))
+
+    def connect(self, master: int, mface: int, slave: int, sface: int, orient: int = 0):
+        """Conforming connection of two patches (SIM3D::connectPatches)."""
+        self._check(self.lib.ifemgpu_patch_connect(self.ctx, master, mface, slave, sface, orient))
 
     def set_mass(self, pid: int, scale: float):
         """K_eff = K + scale * M (consistent mass, EqualOrderOperators::Weak::Mass)."""

@@ -174,8 +174,45 @@ def config4(nel: int = 64, p: int = 3, seed: int | None = None, grid: int = 64):
     return [pc], 4
 
 
-def load_into(sim, patches) -> list[int]:
-    """Feed patches to an ifem_gb300.ifemgpu.SIM (or the oracle wrapper)."""
+def connected_boxes(kind: int = 1, p: int = 2, nel: int = 3, npatch: int = 2,
+                    rotated: bool = False):
+    """npatch unit cubes of nel^3 elements along x, conformingly connected
+    (patch i's +x face is patch i+1's -x face).  With rotated, the even
+    patches are parameterised (i, j, k) -> (x, z, 1 - y), so that the
+    connections onto them need face orientation 5 and those from them 6
+    (swapped and reversed parameter directions).  Poisson (kind 1: conductivity 1 + patch index, unit
+    source, u = 0 on the outer x faces) or elasticity (kind 2: clamped -x face
+    of the first patch, unit traction on the +x face of the last).
+    Returns (patches, n_gauss, connections)."""
+    patches, conns = [], []
+    for ip in range(npatch):
+        pc = box_patch(3, p, nel, origin=(float(ip), 0.0, 0.0))
+        if rotated and ip % 2 == 1:
+            g = greville(uniform_knots(p, nel), p)
+            n = len(g)
+            i, j, k = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+            order = lambda a: a.transpose(2, 1, 0).ravel()   # first index fastest
+            pc.coefs = np.stack([ip + g[order(i)], 1.0 - g[order(k)], g[order(j)]], axis=1)
+        pc.kind = kind
+        patches.append(pc)
+        if ip > 0:  # orientation 5 onto a rotated patch, 6 from one, else 0
+            orient = 0 if not rotated else (5 if ip % 2 == 1 else 6)
+            conns.append((ip, 2, ip + 1, 1, orient))
+    if kind == 1:
+        for ip, pc in enumerate(patches):
+            pc.kappa = 1.0 + ip
+            pc.source = 1.0
+        patches[0].dirichlet = [(1, 1, 0.0)]
+        patches[-1].dirichlet = [(2, 1, 0.0)]
+    else:
+        patches[0].dirichlet = [(1, 123, 0.0)]
+        patches[-1].neumann = [(2, (1.0, 0.0, 0.0))]
+    return patches, 3, conns
+
+
+def load_into(sim, patches, connections=()) -> list[int]:
+    """Feed patches to an ifem_gb300.ifemgpu.SIM (or the oracle wrapper);
+    connections: (master, mface, slave, sface, orient) tuples, 1-based."""
     ids = []
     for pc in patches:
         pid = sim.add_patch(pc)
@@ -192,4 +229,6 @@ def load_into(sim, patches) -> list[int]:
         for face, vals in pc.neumann:
             sim.add_neumann(pid, face, vals)
         ids.append(pid)
+    for c in connections:
+        sim.connect(*c)
     return ids

@@ -139,6 +139,20 @@ ifemgpu_status ifemgpu_patch_add(ifemgpu_ctx* ctx, int dim, const int* degree,
 ifemgpu_status ifemgpu_patch_set_material(ifemgpu_ctx* ctx, int patch_id,
                                           const ifemgpu_material* mat);
 
+/* Identifies face (3D, 1..6) or edge (2D, 1..4) slave_face of patch slave
+ * with face master_face of patch master: the slave's nodes there take the
+ * master's global node numbers, so the patches couple conformingly.
+ * orient: 0..7 in 3D as in ASMs3D::connectPatch (bit 2 swaps the face's
+ * parameter directions, then bits 1 and 0 reverse them), 0/1 in 2D
+ * (reversed edge).  Global nodes are numbered as SIMbase::renumberNodes
+ * does after connections (first appearance, patch by patch).  Replaces
+ * SIM3D/SIM2D::connectPatches -> ASMs3D::connectPatch (src/SIM/SIM3D.C:
+ * 44-95, src/ASM/ASMs3D.C:700-796).  Must precede ifemgpu_preprocess.
+ * Connected models assemble with per-patch colour passes; the Kronecker
+ * preconditioner needs unconnected patches.                              */
+ifemgpu_status ifemgpu_patch_connect(ifemgpu_ctx* ctx, int master, int master_face,
+                                     int slave, int slave_face, int orient);
+
 /* Adds scale x the consistent mass matrix to the patch's element matrices,
  * K_eff = K + scale M with M_ab = integral N_a N_b (per solution component),
  * the effective stiffness of implicit time stepping (Newmark: scale =

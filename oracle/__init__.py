@@ -45,6 +45,7 @@ def lib():
             "ifo_set_material": (I, [P, I, I, D, D, I, D, D, V]),
             "ifo_set_field": (I, [P, I, I, V]),
             "ifo_set_mass": (I, [P, I, D]),
+            "ifo_connect": (I, [P, I, I, I, I, I]),
             "ifo_norms": (None, [P, V, V, V]),
             "ifo_secondary": (None, [P, I, V, V]),
             "ifo_constrain_face": (I, [P, I, I, I, D]),
@@ -109,6 +110,9 @@ class OracleModel:
                      body=(0.0, 0.0, 0.0)):
         b = np.ascontiguousarray(body, dtype=np.float64)
         self.L.ifo_set_material(self.h, pid, kind, kappa, source, source_shape, E, nu, _p(b))
+
+    def connect(self, master, mface, slave, sface, orient=0):
+        self.L.ifo_connect(self.h, master, mface, slave, sface, orient)
 
     def set_mass(self, pid, scale):
         self.L.ifo_set_mass(self.h, pid, float(scale))

@@ -24,6 +24,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <set>
 #include <string>
 #include <vector>
@@ -150,6 +151,7 @@ struct Material {
 };
 
 struct FaceBC { int face, dofs; double value; };
+struct Connection { int master, mface, slave, sface, orient; };
 struct Neumann { int face; double t[3]; };
 
 struct Patch {
@@ -170,11 +172,13 @@ struct Patch {
   std::vector<std::vector<int>> mnpc;  // per element (empty: zero span)
   std::vector<int> mlge;               // 0 for zero-span elements
   int firstNode = 0;                   // global node offset (0-based)
+  std::vector<int> mlgn;               // global 0-based node per patch node
   int nen() const { return dim == 3 ? (p[0]+1)*(p[1]+1)*(p[2]+1) : (p[0]+1)*(p[1]+1); }
 };
 
 struct Model {
   std::vector<Patch> patches;
+  std::vector<Connection> conns;
   int nGauss = 4;
   int nnod = 0, nel = 0, ndof = 0, neq = 0, nceq = 0;
   std::vector<int> madof, msc, meqn;
@@ -258,6 +262,85 @@ std::vector<int> faceNodes(const Patch& pc, int face)
 // SAMpatch::init -> initNodeDofs / initElementConn / initConstraintEqs and
 // SAM::initSystemEquations (src/ASM/SAMpatch.C:21-360, src/LinAlg/SAM.C:225-336),
 // restricted to fixed and prescribed (master-less) constraints.
+// Patch connections: ASMs3D::connectPatch / connectBasis and
+// ASMs2D::connectBasis (src/ASM/ASMs3D.C:700-796, ASMs2D.C:697-749) with
+// ASMbase::collapseNodes / mergeNodes (src/ASM/ASMbase.C:1289-1331): the
+// slave face's nodes, in the master face's node order under orientation
+// `orient`, take the smaller of the two global numbers, a change reaching
+// the patches already connected to the changed one.  Then
+// SIMbase::renumberNodes (src/SIM/SIMbase.C:535-565): numbers compacted in
+// order of first appearance.  G holds 1-based numbers; returns the count,
+// or -1 when faces do not match.
+int connectPatches(Model& m, std::vector<std::vector<int>>& G)
+{
+  const size_t np = m.patches.size();
+  std::vector<std::vector<int>> nb(np);
+  auto faceDims = [](const Patch& pc, int face, int& a, int& b) {
+    const int dir = (face + 1) / 2;
+    if (pc.dim == 2) { a = dir == 1 ? pc.n[1] : pc.n[0]; b = 1; }
+    else if (dir == 1) { a = pc.n[1]; b = pc.n[2]; }
+    else if (dir == 2) { a = pc.n[0]; b = pc.n[2]; }
+    else { a = pc.n[0]; b = pc.n[1]; }
+  };
+  for (const Connection& c : m.conns) {
+    const int M = c.master - 1, S = c.slave - 1;
+    const Patch &pm = m.patches[M], &ps = m.patches[S];
+    const std::vector<int> mn = faceNodes(pm, c.mface), sn = faceNodes(ps, c.sface);
+    int m1, m2, n1, n2;
+    faceDims(ps, c.sface, m1, m2);
+    faceDims(pm, c.mface, n1, n2);
+    const bool swapped = pm.dim == 3 && c.orient > 3;
+    if ((swapped ? n2 : n1) != m1 || (swapped ? n1 : n2) != m2) return -1;
+    int node = 0;
+    for (int j = 0; j < n2; j++)
+      for (int i = 0; i < n1; i++, node++) {
+        int k = i, l = j;
+        if (pm.dim == 3) {
+          const int o = c.orient;
+          if (o & 4) { k = j; l = i; }
+          if (o == 1 || o == 3) l = n2 - 1 - j;
+          if (o == 2 || o == 3) k = n1 - 1 - i;
+          if (o == 5 || o == 7) l = m2 - 1 - i;
+          if (o == 6 || o == 7) k = m1 - 1 - j;
+        } else if (c.orient) {
+          k = n1 - 1 - i;
+        }
+        const int snode = sn[(size_t)l * m1 + k], mnode = mn[node];
+        for (int d = 0; d < pm.dim; d++)
+          if (std::fabs(pm.X[(size_t)mnode * pm.dim + d] - ps.X[(size_t)snode * ps.dim + d]) > 1e-4)
+            return -1;
+        int& gm = G[M][mnode];
+        int& gs = G[S][snode];
+        if (gm == gs) continue;
+        const int P = gm > gs ? M : S, inod = gm > gs ? mnode : snode;
+        const int oldNum = G[P][inod], newNum = std::min(gm, gs);
+        G[P][inod] = newNum;
+        for (int Q : nb[P])
+          for (int& g : G[Q])
+            if (g == oldNum) g = newNum;
+      }
+    if (std::find(nb[S].begin(), nb[S].end(), M) == nb[S].end()) {
+      nb[S].push_back(M);
+      nb[M].push_back(S);
+    }
+  }
+  std::map<int, int> renum;
+  int count = 0;
+  for (size_t P = 0; P < np; P++) {
+    bool changed = false;
+    for (int& g : G[P]) {
+      auto it = renum.find(g);
+      if (it == renum.end()) it = renum.emplace(g, ++count).first;
+      if (it->second != g) {
+        g = it->second;
+        changed = true;
+      }
+    }
+    if (!changed && !G[P].empty()) count = std::max(count, *std::max_element(G[P].begin(), G[P].end()));
+  }
+  return count;
+}
+
 bool initSAM(Model& m)
 {
   int gEl = 0, gNod = 0;
@@ -266,11 +349,22 @@ bool initSAM(Model& m)
     pc.firstNode = gNod;
     gNod += pc.nnod;
   }
+  std::vector<std::vector<int>> G(m.patches.size());
+  for (size_t p = 0; p < m.patches.size(); p++)
+    for (int i = 0; i < m.patches[p].nnod; i++) G[p].push_back(m.patches[p].firstNode + i + 1);
+  if (!m.conns.empty() && (gNod = connectPatches(m, G)) < 0) {
+    m.err = "non-matching patch connection";
+    return false;
+  }
+  for (size_t p = 0; p < m.patches.size(); p++) {
+    m.patches[p].mlgn = G[p];
+    for (int& g : m.patches[p].mlgn) g -= 1;
+  }
   m.nnod = gNod;
   m.nel = gEl;
   m.madof.assign(m.nnod + 1, 0);
   for (auto& pc : m.patches)
-    for (int i = 0; i < pc.nnod; i++) m.madof[pc.firstNode + i + 1] = pc.npv;
+    for (int i = 0; i < pc.nnod; i++) m.madof[pc.mlgn[i] + 1] = pc.npv;
   m.madof[0] = 1;
   for (int i = 0; i < m.nnod; i++) m.madof[i + 1] += m.madof[i];
   m.ndof = m.madof[m.nnod] - 1;
@@ -285,7 +379,7 @@ bool initSAM(Model& m)
         for (char c : std::to_string(bc.dofs)) {
           int dof = c - '0';
           if (dof < 1 || dof > pc.npv) continue;
-          m.msc[m.madof[pc.firstNode + node] - 1 + dof - 1] = 0;
+          m.msc[m.madof[pc.mlgn[node]] - 1 + dof - 1] = 0;
         }
     }
   // prescribed DOFs: one constraint equation each, first one wins, fixed wins
@@ -296,7 +390,7 @@ bool initSAM(Model& m)
         for (char c : std::to_string(bc.dofs)) {
           int dof = c - '0';
           if (dof < 1 || dof > pc.npv) continue;
-          int idof = m.madof[pc.firstNode + node] - 1 + dof - 1;
+          int idof = m.madof[pc.mlgn[node]] - 1 + dof - 1;
           if (m.msc[idof] <= 0 || slaveOf[idof]) continue;
           m.c0.push_back(bc.value);
           slaveOf[idof] = (int)m.c0.size();
@@ -316,7 +410,7 @@ bool initSAM(Model& m)
   for (auto& pc : m.patches)
     for (int e = 0; e < pc.nelAll; e++)
       if (pc.mlge[e] > 0) {
-        for (int nd : pc.mnpc[e]) m.mmnpc.push_back(pc.firstNode + nd + 1);
+        for (int nd : pc.mnpc[e]) m.mmnpc.push_back(pc.mlgn[nd] + 1);
         m.mpmnpc.push_back((int)m.mmnpc.size() + 1);
       }
   return true;
@@ -717,7 +811,7 @@ void elementNorms(const Model& m, Patch& pc, int iel, const double* u, double ou
   std::vector<double> Xn((size_t)nen * dim), Ue((size_t)nen * 3, 0.0);
   for (int a = 0; a < nen; a++) {
     for (int c = 0; c < dim; c++) Xn[(size_t)a * dim + c] = pc.X[(size_t)nodes[a] * dim + c];
-    const int d0 = m.madof[pc.firstNode + nodes[a]] - 1;
+    const int d0 = m.madof[pc.mlgn[nodes[a]]] - 1;
     for (int c = 0; c < npv; c++) Ue[(size_t)a * 3 + c] = u[d0 + c];
   }
   const double E = pc.mat.E, nu = pc.mat.nu;
@@ -926,6 +1020,12 @@ int ifo_set_material(void* h, int pid, int kind, double kappa, double source,
   return 0;
 }
 
+int ifo_connect(void* h, int master, int mface, int slave, int sface, int orient)
+{
+  static_cast<Model*>(h)->conns.push_back({master, mface, slave, sface, orient});
+  return 0;
+}
+
 int ifo_set_mass(void* h, int pid, double scale)
 {
   static_cast<Model*>(h)->patches.at(pid - 1).mat.mass = scale;
@@ -961,7 +1061,7 @@ int ifo_add_neumann(void* h, int pid, int face, const double* t)
 int ifo_preprocess(void* h)
 {
   Model& m = *static_cast<Model*>(h);
-  initSAM(m);
+  if (!initSAM(m)) return -1;
   buildPattern(m);
   return 0;
 }

@@ -23,6 +23,7 @@
 #include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <map>
 #include <vector>
 
 #include "ASMbase.h"
@@ -59,6 +60,18 @@ public:
   }
 
   int fixNode(size_t inod, int dirs) { return this->fix(inod, dirs); }
+  void setGlobal(int firstNode, int firstElm)
+  {
+    for (size_t i = 0; i < myMLGN.size(); i++) myMLGN[i] = firstNode + (int)i + 1;
+    for (size_t e = 0; e < myMLGE.size(); e++) myMLGE[e] = firstElm + (int)e + 1;
+  }
+  // ASMbase::collapseNodes and addNeighbor, as ASMs3D::connectBasis /
+  // connectPatch use them (protected in ASMbase)
+  static bool collapse(GridPatch& master, int mnode, GridPatch& slave, int snode)
+  {
+    return ASMbase::collapseNodes(master, mnode, slave, snode);
+  }
+  void neighbour(GridPatch* other) { this->addNeighbor(other); }
 
   bool empty() const override { return false; }
   bool read(std::istream&) override { return false; }
@@ -93,12 +106,19 @@ public:
 
 struct Harness
 {
-  GridPatch* patch = nullptr;
+  GridPatch* patch = nullptr;        // first patch (single-patch models)
+  std::vector<GridPatch*> patches;   // all patches, owned
+  std::vector<int> firstElm;         // global element offset per patch
+  int nnodGlobal = 0;
   SAMpatch sam;
   CscView K{SparseMatrix::SUPERLU};
   StdVector b;
   int dim = 3, nf = 1, nen = 0;
-  ~Harness() { delete patch; }
+  ~Harness()
+  {
+    if (patches.empty()) delete patch;
+    for (GridPatch* p : patches) delete p;
+  }
 };
 
 }  // namespace
@@ -123,12 +143,84 @@ RH_API int rh_fix(void* p, int inod, int dirs)
   return static_cast<Harness*>(p)->patch->fixNode(inod, dirs);
 }
 
+// Multi-patch model: npatch patches with nnod[i] nodes, nel[i] elements of
+// nen nodes each and MNPC (0-based patch nodes, patches one after the
+// other); global node and element numbers start consecutive per patch, as
+// ASMs3D::generateFEMTopology assigns them.
+RH_API void* rh_create_multi(int dim, int nf, int npatch, const int* nnod, const int* nel, int nen,
+                             const int* mnpc)
+{
+  Harness* h = new Harness;
+  h->dim = dim;
+  h->nf = nf;
+  h->nen = nen;
+  int gn = 0, ge = 0;
+  for (int i = 0; i < npatch; i++) {
+    GridPatch* g = new GridPatch(dim, nf, nnod[i], nel[i], nen, mnpc);
+    g->setGlobal(gn, ge);
+    h->firstElm.push_back(ge);
+    gn += nnod[i];
+    ge += nel[i];
+    mnpc += (size_t)nel[i] * nen;
+    h->patches.push_back(g);
+  }
+  h->patch = h->patches.front();
+  h->nnodGlobal = gn;
+  return h;
+}
+
+// One node pair of a connection (1-based patch-local nodes), then, after the
+// last pair of a connection, the neighbour registration of connectPatch.
+RH_API int rh_collapse(void* p, int master, int mnode, int slave, int snode)
+{
+  Harness* h = static_cast<Harness*>(p);
+  return GridPatch::collapse(*h->patches[master - 1], mnode, *h->patches[slave - 1], snode);
+}
+
+RH_API void rh_neighbours(void* p, int master, int slave)
+{
+  Harness* h = static_cast<Harness*>(p);
+  h->patches[slave - 1]->neighbour(h->patches[master - 1]);
+}
+
+// SIMbase::renumberNodes (src/SIM/SIMbase.C:535-565) with preserveNOrder
+// off: numbers compacted patch by patch in order of first appearance.
+RH_API int rh_renumber(void* p)
+{
+  Harness* h = static_cast<Harness*>(p);
+  std::map<int, int> old2new;
+  int nnod = 0;
+  for (GridPatch* g : h->patches) g->renumberNodes(old2new, nnod);
+  h->nnodGlobal = nnod;
+  return nnod;
+}
+
+// homogeneous Dirichlet code on 1-based patch-local node inod of patch pid
+RH_API int rh_fix_patch(void* p, int pid, int inod, int dirs)
+{
+  return static_cast<Harness*>(p)->patches[pid - 1]->fixNode(inod, dirs);
+}
+
+// the global node number (1-based) of patch-local node inod (1-based)
+RH_API int rh_node_id(void* p, int pid, int inod)
+{
+  return static_cast<Harness*>(p)->patches[pid - 1]->getNodeID(inod);
+}
+
+// global element number (1-based) of patch-local element iel (0-based)
+RH_API int rh_elm_id(void* p, int pid, int iel)
+{
+  return static_cast<Harness*>(p)->firstElm[pid - 1] + iel + 1;
+}
+
 // SAM numbering and the locked pattern; out = {nnod, ndof, neq, nnz}
 RH_API int rh_init(void* p, int* out)
 {
   Harness* h = static_cast<Harness*>(p);
-  std::vector<ASMbase*> model{h->patch};
-  if (!h->sam.init(model, 0, {})) return -1;
+  std::vector<ASMbase*> model;
+  if (h->patches.empty()) model.push_back(h->patch);
+  for (GridPatch* g : h->patches) model.push_back(g);
+  if (!h->sam.init(model, h->patches.empty() ? 0 : h->nnodGlobal, {})) return -1;
   h->K.initAssembly(h->sam, 'F');
   h->b.redim(h->sam.getNoEquations());
   out[0] = h->sam.getNoNodes();

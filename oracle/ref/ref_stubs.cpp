@@ -3,9 +3,11 @@
 // Definitions of the few symbols that the IFEM sources compiled for the
 // reference build (oracle/ref/build_ref.py) reference but that live in IFEM
 // translation units which cannot be built here (they need tinyxml2, CBLAS or
-// GoTools).  None of them is on the assembly path that the harness drives,
-// except utl::getDigits, which ASMbase::fix uses to split a DOF code such as
-// 123 into its digits and which is therefore implemented for real.
+// GoTools).  Three of them are on the path the harness drives and are
+// implemented from their documented behaviour (src/Utility/Utilities.h):
+// utl::getDigits (ASMbase::fix splits a DOF code such as 123 into digits)
+// and the two utl::renumber overloads (node merging and renumbering of
+// connected patches, ASMbase::mergeNodes / renumberNodes).
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
@@ -48,7 +50,26 @@ std::set<int> utl::getDigits(int value)
 }
 
 bool utl::parseIntegers(std::vector<int>&, const char*) { unavailable("utl::parseIntegers"); }
-bool utl::renumber(int&, int&, IntMap&) { unavailable("utl::renumber"); }
-bool utl::renumber(int&, const IntMap&, bool) { unavailable("utl::renumber"); }
+// A value not seen before becomes ++runner; returns whether num changed.
+bool utl::renumber(int& num, int& runner, IntMap& old2new)
+{
+  auto it = old2new.find(num);
+  if (it == old2new.end()) it = old2new.emplace(num, ++runner).first;
+  const bool changed = num != it->second;
+  num = it->second;
+  return changed;
+}
+
+// num mapped through old2new; returns whether num was in the mapping.
+bool utl::renumber(int& num, const IntMap& old2new, bool msg)
+{
+  auto it = old2new.find(num);
+  if (it == old2new.end()) {
+    if (msg) std::fprintf(stderr, "utl::renumber: %d not in the mapping\n", num);
+    return false;
+  }
+  num = it->second;
+  return true;
+}
 int utl::findKey(const IntMap&, int) { unavailable("utl::findKey"); }
 int utl::findIndex(const std::vector<int>&, int) { unavailable("utl::findIndex"); }

@@ -48,6 +48,10 @@ def lib():
             "rh_assemble": (I, [P, I, V, V]),
             "rh_get_sam": (None, [P, V, V]), "rh_get_system": (None, [P, V, V, V, V]),
             "rh_dump": (I, [P, C.c_char_p, C.c_char_p, I, C.c_double]),
+            "rh_create_multi": (P, [I, I, I, V, V, I, V]),
+            "rh_collapse": (I, [P, I, I, I, I]), "rh_neighbours": (None, [P, I, I]),
+            "rh_renumber": (I, [P]), "rh_fix_patch": (I, [P, I, I, I]),
+            "rh_node_id": (I, [P, I, I]), "rh_elm_id": (I, [P, I, I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -128,7 +132,114 @@ def reference_system(patch, n_gauss: int, dumps=None, zero_tol: float = 0.0):
     return dict(IA=IA, JA=JA, A=A, b=b if patch.kind == 1 else None, madof=madof, meqn=meqn)
 
 
-def _poisson_elements(L, h, orc, patch, n_gauss, mnpc, nen):
+def face_nodes(patch, face):
+    """0-based patch nodes of a face (3D) or edge (2D) in IFEM's order
+    (ASMs3D::getBoundaryNodes, src/ASM/ASMs3D.C:1770-1818)."""
+    n1, n2 = patch.ncoef[0], patch.ncoef[1]
+    n3 = patch.ncoef[2] if patch.dim == 3 else 1
+    d, hi = (face + 1) // 2, face % 2 == 0
+    idx = lambda i, j, k: (k * n2 + j) * n1 + i
+    if d == 1:
+        return [idx(n1 - 1 if hi else 0, j, k) for k in range(n3) for j in range(n2)]
+    if d == 2:
+        return [idx(i, n2 - 1 if hi else 0, k) for k in range(n3) for i in range(n1)]
+    return [idx(i, j, n3 - 1 if hi else 0) for j in range(n2) for i in range(n1)]
+
+
+def face_size(patch, face):
+    """ASMs3D::getFaceSize (src/ASM/ASMs3D.C:3796-3810); 2D: (edge nodes, 1)."""
+    n = list(patch.ncoef) + [1] * (3 - patch.dim)
+    d = (face + 1) // 2
+    if patch.dim == 2:
+        return (n[1] if d == 1 else n[0]), 1
+    return {1: (n[1], n[2]), 2: (n[0], n[2]), 3: (n[0], n[1])}[d]
+
+
+def connection_pairs(pm, mface, ps, sface, orient):
+    """(master node, slave node) pairs, 0-based, in the loop order of
+    ASMs3D::connectBasis / ASMs2D::connectBasis."""
+    mn, sn = face_nodes(pm, mface), face_nodes(ps, sface)
+    m1, m2 = face_size(ps, sface)
+    n1, n2 = face_size(pm, mface)
+    pairs, node = [], 0
+    for j in range(n2):
+        for i in range(n1):
+            if pm.dim == 3:
+                k, l = {0: (i, j), 1: (i, n2 - j - 1), 2: (n1 - i - 1, j), 3: (n1 - i - 1, n2 - j - 1),
+                        4: (j, i), 5: (j, m2 - i - 1), 6: (m1 - j - 1, i),
+                        7: (m1 - j - 1, m2 - i - 1)}[orient]
+            else:
+                k, l = (n1 - i - 1 if orient else i), 0
+            pairs.append((mn[node], sn[l * m1 + k]))
+            node += 1
+    return pairs
+
+
+def reference_system_multi(patches, connections, n_gauss: int):
+    """As reference_system for a model of several patches joined by
+    conforming connections (master, mface, slave, sface, orient): IFEM's
+    ASMbase::collapseNodes over the node pairs of each connection, its
+    neighbour registration, SIMbase::renumberNodes, SAMpatch::init over all
+    patches and SAM::assembleSystem with global element numbers.  Homogeneous
+    Dirichlet faces only."""
+    import oracle
+    from ifem_gb300 import workloads as W
+
+    orc = oracle.OracleModel(n_gauss)
+    W.load_into(orc, patches, connections)
+    orc.preprocess()
+    dim = patches[0].dim
+    nen = int(np.prod([q + 1 for q in patches[0].degree]))
+    nf = 1 if patches[0].kind == 1 else dim
+    mnpcs = [orc.mnpc(i + 1, pc.nel, nen).astype(np.int32) for i, pc in enumerate(patches)]
+    L = lib()
+    nn = np.array([pc.nnod for pc in patches], dtype=np.int32)
+    ne = np.array([pc.nel for pc in patches], dtype=np.int32)
+    allm = np.ascontiguousarray(np.concatenate([m.ravel() for m in mnpcs]))
+    h = L.rh_create_multi(dim, nf, len(patches), _p(nn), _p(ne), nen, _p(allm))
+    try:
+        for (m, mf, s, sf, o) in connections:
+            for a, b in connection_pairs(patches[m - 1], mf, patches[s - 1], sf, o):
+                L.rh_collapse(h, m, a + 1, s, b + 1)
+            L.rh_neighbours(h, m, s)
+        L.rh_renumber(h)
+        for i, pc in enumerate(patches):
+            for face, dofs, value in pc.dirichlet:
+                if value != 0.0:
+                    raise ValueError("homogeneous Dirichlet conditions only")
+                for node in face_nodes(pc, face):
+                    L.rh_fix_patch(h, i + 1, node + 1, dofs)
+        s = np.zeros(4, dtype=np.int32)
+        if L.rh_init(h, _p(s)) != 0:
+            raise RuntimeError("SAMpatch::init failed")
+        nnod, ndof, neq, nnz = (int(v) for v in s)
+        for i, pc in enumerate(patches):
+            iel = [L.rh_elm_id(h, i + 1, e) for e in range(pc.nel)]
+            if pc.kind == 1:
+                _poisson_elements(L, h, orc, pc, n_gauss, mnpcs[i], nen, pid=i + 1, iel=iel)
+            else:
+                nd = nf * nen
+                for e in range(pc.nel):
+                    eK, eS, _ = orc.element(i + 1, e, nd)
+                    if L.rh_assemble(h, iel[e], _p(np.ascontiguousarray(eK.ravel(order="F"))),
+                                     _p(np.ascontiguousarray(eS))) != 0:
+                        raise RuntimeError("SAM::assembleSystem failed")
+        IA = np.zeros(neq + 1, dtype=np.int32)
+        JA = np.zeros(nnz, dtype=np.int32)
+        A = np.zeros(nnz)
+        b = np.zeros(neq)
+        L.rh_get_system(h, _p(IA), _p(JA), _p(A), _p(b))
+        madof = np.zeros(nnod + 1, dtype=np.int32)
+        meqn = np.zeros(ndof, dtype=np.int32)
+        L.rh_get_sam(h, _p(madof), _p(meqn))
+    finally:
+        L.rh_destroy(h)
+        orc.close()
+    return dict(IA=IA, JA=JA, A=A, b=b if patches[0].kind == 1 else None, madof=madof,
+                meqn=meqn)
+
+
+def _poisson_elements(L, h, orc, patch, n_gauss, mnpc, nen, pid=1, iel=None):
     """The element loop of ASMs3D/ASMs2D::integrate with IFEM's operators."""
     dim, p = patch.dim, patch.degree
     ng = [n_gauss if n_gauss > 0 else p[d] + 1 for d in range(dim)]
@@ -169,7 +280,7 @@ def _poisson_elements(L, h, orc, patch, n_gauss, mnpc, nen):
                         b0, b1 = spans[d]
                         u[d] = 0.5 * ((b1 - b0) * xi[g[d]] + b1 + b0)
                         w *= wt[g[d]]
-                    orc.L.ifo_basis(orc.h, 1, _p(u), _p(Nb), _p(dNb), _p(nodes))
+                    orc.L.ifo_basis(orc.h, pid, _p(u), _p(Nb), _p(dNb), _p(nodes))
                     if not np.array_equal(nodes, mnpc[e]):
                         raise RuntimeError("basis node order differs from MNPC")
                     Nq[q] = Nb
@@ -189,6 +300,6 @@ def _poisson_elements(L, h, orc, patch, n_gauss, mnpc, nen):
                     f[q] = src
                     q += 1
         Xe = np.ascontiguousarray(X[mnpc[e]])
-        L.rh_poisson_element(h, e + 1, nq, _p(np.ascontiguousarray(Nq)),
+        L.rh_poisson_element(h, iel[e] if iel else e + 1, nq, _p(np.ascontiguousarray(Nq)),
                              _p(np.ascontiguousarray(dNq)), _p(wfac), _p(kap), _p(f),
                              float(patch.mass), _p(Xe), _p(eK), _p(eS))

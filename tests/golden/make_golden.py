@@ -53,9 +53,11 @@ def gauss_tables():
 
 
 def sam_refs():
-    out = {"source": "src/LinAlg/Test/TestSAM.C:62-96 + refdata", "cases": {}}
+    out = {"source": "src/LinAlg/Test/TestSAM.C:62-96, :133-176 + refdata", "cases": {}}
     for name, xinp in [("sam_2D_singlebasis_1P", "sam_2D_1P.xinp"),
-                       ("sam_2D_singlebasis_dir_1P", "sam_2D_dir_1P.xinp")]:
+                       ("sam_2D_singlebasis_dir_1P", "sam_2D_dir_1P.xinp"),
+                       ("sam_2D_singlebasis_2P", "sam_2D_2P.xinp"),
+                       ("sam_2D_singlebasis_dir_2P", "sam_2D_dir_2P.xinp")]:
         rel = f"src/LinAlg/Test/refdata/{name}.ref"
         vals = [int(x) for x in read(rel).split()]
         rows, k = [], 0
@@ -68,6 +70,15 @@ def sam_refs():
     # equation checks of TestSAM.SingleBasisDirichlet1P: nodes 3,6,9 prescribed
     out["cases"]["sam_2D_singlebasis_dir_1P"]["equations"] = {
         "node_eq": [[1, 1], [2, 2], [3, 0], [4, 3], [5, 4], [6, 0], [7, 5], [8, 6], [9, 0]]}
+    # two bilinear patches of square2.g2 ([0,0.5]x[0,1] and [0.5,1]x[0,1]),
+    # <connection master="1" medge="2" slave="2" sedge="1"/>; the Dirichlet
+    # variant prescribes edge 2 of patch 2 (TestSAM.SingleBasisDirichlet2P:
+    # equations 1..4 for nodes 1..4, none for nodes 5, 6)
+    for name in ("sam_2D_singlebasis_2P", "sam_2D_singlebasis_dir_2P"):
+        out["cases"][name]["geometry"] = "src/LinAlg/Test/refdata/square2.g2"
+        out["cases"][name]["connection"] = [1, 2, 2, 1, 0]
+    out["cases"]["sam_2D_singlebasis_dir_2P"]["equations"] = {
+        "node_eq": [[1, 1], [2, 2], [3, 3], [4, 4], [5, 0], [6, 0]]}
     return out
 
 

@@ -11,6 +11,10 @@ Cases (the seeded synthetic models of ifem_gb300/workloads.py):
   c2_elast3d_p2     3D NURBS elasticity p=2, 2^3 elements, face 5 clamped
   c6_poisson3d_mass 3D NURBS Poisson p=2, 4^3 elements, K + 25 M, face 5 fixed
   c7_elast3d_mass   c2 with K + 50 M (Newmark-type effective stiffness)
+  c8_connected_poisson   three connected p=2 Poisson cubes, 2^3 elements each, aligned faces
+  c9_connected_rotated   the same with every second patch re-parameterised (orientations 5, 6)
+  c10_connected_elast    three connected p=2 elasticity cubes, rotated, clamped at x=0
+Cases are (patches, n_gauss) or (patches, n_gauss, connections).
 Stored per case: IA, JA (0-based compressed columns), A, b (Poisson), MADOF, MEQN.
 For c0_poisson2d_small (2D Poisson p=2, 4x4 elements) also the text dumps
 IFEM's SparseMatrix::dump / StdVector::dump write, in ref_dump/ (FLAT,
@@ -48,6 +52,9 @@ def cases():
         "c1_poisson2d_p2": W.config1(nel=8),
         "c6_poisson3d_mass": ([mass_p], 3),
         "c7_elast3d_mass": (elast_m, ng_m),
+        "c8_connected_poisson": W.connected_boxes(1, 2, 2, 3, rotated=False),
+        "c9_connected_rotated": W.connected_boxes(1, 2, 2, 3, rotated=True),
+        "c10_connected_elast": W.connected_boxes(2, 2, 2, 3, rotated=True),
         "c4_poisson3d_p3": W.config4(nel=3, grid=16),
         "c3_poisson3d_nurbs": ([nurbs], 3),
         "c2_elast3d_p2": W.config2(nel=2),
@@ -62,13 +69,18 @@ def main():
     here = os.path.dirname(os.path.abspath(__file__))
     os.makedirs(os.path.join(here, "ref_dump"), exist_ok=True)
     out = {}
-    for name, (patches, ng) in cases().items():
+    for name, case in cases().items():
+        patches, ng = case[0], case[1]
+        conns = case[2] if len(case) > 2 else ()
         dumps = None
         if name == "c0_poisson2d_small":
             dumps = [(f, os.path.join(here, "ref_dump", f"A.{ext}"),
                       os.path.join(here, "ref_dump", f"b.{ext}"))
                      for f, ext in ((1, "flat"), (2, "m"), (3, "mtx"))]
-        ref = refmodel.reference_system(patches[0], ng, dumps=dumps, zero_tol=1e-12)
+        if conns:
+            ref = refmodel.reference_system_multi(patches, conns, ng)
+        else:
+            ref = refmodel.reference_system(patches[0], ng, dumps=dumps, zero_tol=1e-12)
         for k, v in ref.items():
             if v is not None:
                 out[f"{name}/{k}"] = v

@@ -116,6 +116,45 @@ def test_sam_golden_through_the_library(case, dirichlet, gpulib):
         assert sam.getEquation(node, 1) == eq
 
 
+def square2(dirichlet):
+    """src/LinAlg/Test/refdata/square2.g2: two bilinear one-element patches."""
+    p1 = W.box_patch(2, 1, 1, size=(0.5, 1.0))
+    p2 = W.box_patch(2, 1, 1, origin=(0.5, 0.0, 0.0), size=(0.5, 1.0))
+    for p in (p1, p2):
+        p.kind = G.POISSON
+    if dirichlet:
+        p2.dirichlet = [(2, 1, 1.0)]
+    return [p1, p2]
+
+
+@pytest.mark.parametrize("case,dirichlet", [("sam_2D_singlebasis_2P", False),
+                                            ("sam_2D_singlebasis_dir_2P", True)])
+def test_two_patch_sam_golden_through_the_library(case, dirichlet, gpulib):
+    with open(os.path.join(GOLD, "sam_refs.json")) as f:
+        g = json.load(f)["cases"][case]
+    sim = host_sim(2)
+    W.load_into(sim, square2(dirichlet), [tuple(g["connection"])])
+    sim.preprocess()
+    sam = sim.getSAM()
+    assert sam.getDofCouplings() == g["couplings"]
+    eqs = g.get("equations", {}).get("node_eq", [[n, n] for n in range(1, 7)])
+    for node, eq in eqs:
+        assert sam.getEquation(node, 1) == eq
+
+
+def test_connection_errors(gpulib):
+    sim = host_sim(2)
+    p1, p2 = square2(False)
+    W.load_into(sim, [p1, p2])
+    with pytest.raises(G.IfemGpuError):
+        sim.connect(1, 2, 1, 1, 0)                # a patch with itself
+    with pytest.raises(G.IfemGpuError):
+        sim.connect(1, 5, 2, 1, 0)                # no edge 5 in 2D
+    sim.connect(1, 1, 2, 1, 0)                    # edges that do not coincide
+    with pytest.raises(G.IfemGpuError):
+        sim.preprocess()
+
+
 def test_element_nodes_golden_through_the_library(gpulib):
     with open(os.path.join(GOLD, "elm_nodes.json")) as f:
         g = json.load(f)

@@ -41,10 +41,11 @@ def golden(name):
                          ids=["fp64", "split"])
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_gpu_matches_reference_system(gpulib, name, ke, tol):
-    patches, ng = CASES[name]
+    patches, ng = CASES[name][:2]
+    conns = CASES[name][2] if len(CASES[name]) > 2 else ()
     ref = golden(name)
     sim = G.SIM(n_gauss=ng, ke_precision=ke)
-    W.load_into(sim, patches)
+    W.load_into(sim, patches, conns)
     sim.preprocess()
     sim.assembleSystem()
     sam = sim.getSAM()
@@ -62,7 +63,7 @@ def test_gpu_matches_reference_system(gpulib, name, ke, tol):
 def test_gpu_dump_round_trip(gpulib, tmp_path):
     """ifemgpu_dump_system of a GPU assembly reads back to the same values
     (17 significant digits) and pattern, in IFEM's MatrixMarket layout."""
-    patches, ng = CASES["c1_poisson2d_p2"]
+    patches, ng = CASES["c1_poisson2d_p2"][:2]
     sim = G.SIM(n_gauss=ng, ke_precision=G.KE_FP64)
     W.load_into(sim, patches)
     sim.preprocess()

@@ -137,6 +137,27 @@ def test_sam_couplings(oracle_lib, case, dirichlet):
         assert list(meqn) == list(range(1, len(meqn) + 1))
 
 
+@pytest.mark.parametrize("case,dirichlet", [("sam_2D_singlebasis_2P", False),
+                                            ("sam_2D_singlebasis_dir_2P", True)])
+def test_two_patch_sam_couplings(oracle_lib, case, dirichlet):
+    g = gold("sam_refs.json")["cases"][case]
+    p1 = W.box_patch(2, 1, 1, size=(0.5, 1.0))
+    p2 = W.box_patch(2, 1, 1, origin=(0.5, 0.0, 0.0), size=(0.5, 1.0))
+    for p in (p1, p2):
+        p.kind = 1
+    if dirichlet:
+        p2.dirichlet = [(2, 1, 1.0)]
+    m = oracle_lib.OracleModel(2)
+    W.load_into(m, [p1, p2], [tuple(g["connection"])])
+    m.preprocess()
+    IA, JA = m.pattern()
+    assert [list(JA[IA[j]:IA[j + 1]] + 1) for j in range(len(IA) - 1)] == g["couplings"]
+    madof, meqn = m.sam()
+    eqs = g.get("equations", {}).get("node_eq", [[n, n] for n in range(1, 7)])
+    for node, eq in eqs:
+        assert max(int(meqn[madof[node - 1] - 1]), 0) == eq
+
+
 def test_oracle_poisson_converges_to_manufactured_solution(oracle_lib):
     """Global sanity of the restated assembly: -lap u = 2 pi^2 sin sin on the
     unit square; the spline solution converges at O(h^3) in the L2 sense."""

@@ -42,10 +42,11 @@ def golden(name):
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_matches_reference_system(oracle_lib, name):
     import oracle
-    patches, ng = CASES[name]
+    patches, ng = CASES[name][:2]
+    conns = CASES[name][2] if len(CASES[name]) > 2 else ()
     ref = golden(name)
     orc = oracle.OracleModel(ng)
-    W.load_into(orc, patches)
+    W.load_into(orc, patches, conns)
     orc.preprocess()
     orc.assemble(1)
     A, b = orc.system()
@@ -64,8 +65,11 @@ def test_reference_build_reproduces_fixture(oracle_lib):
     from oracle import refmodel
     if not refmodel.available():
         pytest.skip("reference build absent (IFEM sources not on this machine)")
-    for name, (patches, ng) in CASES.items():
+    for name, case in CASES.items():
         ref = golden(name)
-        new = refmodel.reference_system(patches[0], ng)
+        if len(case) > 2:
+            new = refmodel.reference_system_multi(case[0], case[2], case[1])
+        else:
+            new = refmodel.reference_system(case[0][0], case[1])
         for k, v in ref.items():
             np.testing.assert_array_equal(new[k], v, err_msg=f"{name}/{k}")
