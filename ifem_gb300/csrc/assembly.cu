@@ -983,6 +983,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     DevPatch& D = ctx->h_devpatches[pi];
     onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) && D.mass == 0.0 &&
                D.lineOff != nullptr && D.faceTables && ctx->patches[pi].neumann.size() <= 6;
+    if (onTc[pi]) onTc[pi] = tcUploadPatch(ctx, ctx->patches[pi], D);  // node tables, TMA maps
     if (!onTc[pi] && ctx->patches[pi].nelActive != ctx->patches[pi].nelAll) flow = false;
   }
   for (int pi = 0; pi < np; pi++) {

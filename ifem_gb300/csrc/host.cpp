@@ -48,6 +48,9 @@ void freeDevice(ifemgpu_ctx* ctx)
     f(pc.d_logk); pc.d_logk = nullptr;
     f(pc.d_noise); pc.d_noise = nullptr;
     f(pc.d_mlgn); pc.d_mlgn = nullptr;
+    f(pc.d_nodeTab); pc.d_nodeTab = nullptr;
+    f(pc.d_lineTab); pc.d_lineTab = nullptr;
+    f(pc.d_tmaps); pc.d_tmaps = nullptr;
     for (int d = 0; d < 3; d++) {
       f(pc.d_knots[d]); f(pc.d_tabN[d]); f(pc.d_tabD[d]); f(pc.d_span[d]); f(pc.d_tabB[d]);
       f(pc.d_tabNf[d]); f(pc.d_tabDf[d]);

@@ -66,6 +66,10 @@ struct DevPatch {
   // line), so that row (a, k) sits in column (b, l) at
   // colptr[c] + lineOff[...] + F(a) + rank of k among a's free DOFs.
   const int* lineOff;
+  // tensor-core patches: three TMA tensor maps (128 B each) over the control
+  // net, a per-node table (eq0..2, F, colptr of the free DOFs) and the
+  // line-offset rows padded to 28 values, each read as 3x3x3 node boxes
+  const void* tmaps;
   // Gauss rules: volume (gx, gw) and face (fx, fw, ngf points)
   double gx[3][kMaxGauss], gw[3][kMaxGauss];
   float gwf[3][kMaxGauss];
@@ -112,6 +116,9 @@ struct HostPatch {
   int firstNode = 0, firstElm = 0;
   std::vector<int> mlgn;     // global 0-based node of each patch node (IFEM's MLGN - 1)
   int* d_mlgn = nullptr;     // device copy for connected models
+  int* d_nodeTab = nullptr;  // tensor-core patches: node table and line-offset rows
+  int* d_lineTab = nullptr;
+  void* d_tmaps = nullptr;   // their TMA tensor maps
   std::vector<char> active;  // per element: non-zero parametric volume
   int nen() const {
     return (p[0] + 1) * (p[1] + 1) * (dim == 3 ? p[2] + 1 : 1);
@@ -248,6 +255,7 @@ ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs);
 
 // tc_volume.cu
 ifemgpu_status tcPrepare(ifemgpu_ctx* ctx);
+bool tcUploadPatch(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D);
 ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid);
 
 // solver.cu

@@ -94,6 +94,30 @@ __device__ __forceinline__ bool mbarWait(uint32_t mbar, uint32_t parity)
   return false;
 }
 
+// TMA: one tiled 4D box global -> shared (destination 128-byte aligned,
+// innermost coordinate 0), completing on an mbarrier that expects `bytes`.
+__device__ __forceinline__ void mbarExpectTx(uint32_t mbar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               : : "r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tmaLoad4d(uint32_t dst, const void* tmap, int c0, int c1, int c2,
+                                          int c3, uint32_t mbar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];"
+      : : "r"(dst), "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(mbar) : "memory");
+}
+
+// tensor maps written to global memory by copies before the launch: order
+// them before their first use by the tensor-map proxy
+__device__ __forceinline__ void tmapAcquire(const void* tmap)
+{
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" : : "l"(tmap) : "memory");
+}
+
 __device__ __forceinline__ void fenceProxyAsync()
 {
   asm volatile("fence.proxy.async.shared::cta;" : : : "memory");

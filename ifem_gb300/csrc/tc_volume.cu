@@ -6,6 +6,12 @@
 //
 // One persistent launch processes every element of the eligible patches.
 // Per element (one CTA of 128 threads, elements in colour-major order):
+//   0. the element's 3x3x3 node box -- control points, a node table (equation
+//      numbers, free DOFs before the node, column starts) and the rows of the
+//      pattern's line-offset table -- staged in shared memory by TMA, the
+//      control points requested as soon as the previous element has read its
+//      own, the tables once its scatter is done (they are first read at the
+//      scatter, so both copies overlap a whole front end);
 //   1. rational basis and Jacobian at the 27 Gauss points (FP32 sums of the
 //      homogeneous control net; determinant and inverse in FP64);
 //   2. operand tile T[(a,k), q] = sqrt|w_q| dN_a/dx_k (rows m = 32k + a), so
@@ -25,6 +31,9 @@
 //      its contributions in colour order, so the sums are deterministic.
 #include <algorithm>
 #include <cstdio>
+#include <vector>
+
+#include <cuda.h>  // CUtensorMap and its encoder's types (entry point fetched at run time)
 
 #include "ifemgpu_internal.h"
 #include "tc_common.cuh"
@@ -65,17 +74,22 @@ struct TcSmem {
   } u;
   float wq[kNq];           // signed integration weight (0 at skipped points)
   float X[kNen][4];        // control points relative to the element's first, weight
-  int eq[kNen * 3];
-  int colStart[kNen * 3];  // colptr of the element's free columns
-  int rowBase[kNen * 3];   // F(a) + free DOFs of node a before component k, row r = 3a + k
-  int lo[kNen][9];         // line offset of row node line (j + 3k) in column node b
-  uint32_t dec[kNq * kNen];  // (q, a) decode: q | a<<5 | gi<<10 | gj<<12 | gk<<14 | i<<16 | j<<18 | k<<20
+  // the element's node box, written by TMA (node a = i + 3 j + 9 k)
+  alignas(128) double ctrlT[kNen][4];  // control points x, y, z, w
+  alignas(128) int nodeT[kNen][8];     // eq of the 3 DOFs, F(node), colptr of the 3 DOFs, 0
+  alignas(128) int lineT[kNen][28];    // line-offset row of the node (25 values used)
   unsigned long long mbar;
+  unsigned long long ctrlbar;  // TMA completion of ctrlT
+  unsigned long long tabbar;   // TMA completion of nodeT and lineT
   uint32_t tmemSlot;
   int fail;
   int signs;               // bit 0: some w_q > 0, bit 1: some w_q < 0
   float dVf;               // span volume / 8 of the element
 };
+
+constexpr uint32_t kCtrlBytes = sizeof(double) * kNen * 4;
+constexpr uint32_t kTabBytes = sizeof(int) * kNen * (8 + 28);
+static_assert(sizeof(TcSmem) <= 56320, "4 CTAs per SM: 4 x (56 KB + 1 KB reserved) shared memory");
 
 static_assert(offsetof(TcSmem, Tlo) == offsetof(TcSmem, Thi) + sizeof(float) * kRowsT * kK &&
                   offsetof(TcSmem, u) == offsetof(TcSmem, Tlo) + sizeof(float) * kRowsT * kK &&
@@ -143,8 +157,11 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mbar = smemAddr(&sm.mbar);
   const Scratch sc = scratch(sm);
+  const uint32_t ctrlbar = smemAddr(&sm.ctrlbar), tabbar = smemAddr(&sm.tabbar);
   if (tid == 0) {
     mbarInit(mbar, 1);
+    mbarInit(ctrlbar, 1);
+    mbarInit(tabbar, 1);
     sm.fail = 0;
   }
   // the padding of the operand tile (rows with a >= 27, q >= 27) is never
@@ -152,11 +169,6 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   for (int i = tid; i < kRowsT * kK; i += blockDim.x) {
     sm.Thi[i] = 0.f;
     sm.Tlo[i] = 0.f;
-  }
-  for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
-    const uint32_t q = idx / kNen, a = idx % kNen;
-    sm.dec[idx] = q | (a << 5) | ((q % 3) << 10) | (((q / 3) % 3) << 12) | ((q / 9) << 14) |
-                  ((a % 3) << 16) | (((a / 3) % 3) << 18) | ((a / 9) << 20);
   }
   if (warp == 0) tmemAlloc(&sm.tmemSlot, 128);
   tcFenceBefore();
@@ -170,6 +182,48 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   // then the previous element's reductions have long completed, so the fence
   // costs little, and the delay is bounded by one element's front end
   int* pending = nullptr;
+  // thread 0: node boxes of item itn into the TMA buffers.  The control
+  // points of the next element are requested as soon as this element has
+  // read its own (step 1), the node and line tables once its scatter is
+  // done (step 11); each is waited for only where it is first read.
+  int mapPatch = -1;        // patch whose tensor maps were last acquired
+  bool ctrlOut = false, tabOut = false;  // copies in flight (thread 0)
+  auto nodeBox = [&](int itn, const char*& tm, int& f1, int& f2, int& f3) {
+    const Item nx = items[itn];
+    const DevPatch& Pn = patches[nx.patch];
+    f1 = nx.elem % Pn.nel[0];
+    f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
+    f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
+    tm = static_cast<const char*>(Pn.tmaps);
+    if (nx.patch != mapPatch) {
+      tmapAcquire(tm);
+      tmapAcquire(tm + 128);
+      tmapAcquire(tm + 256);
+      mapPatch = nx.patch;
+    }
+  };
+  auto stageCtrl = [&](int itn) {
+    const char* tm;
+    int f1, f2, f3;
+    nodeBox(itn, tm, f1, f2, f3);
+    mbarExpectTx(ctrlbar, kCtrlBytes);
+    tmaLoad4d(smemAddr(sm.ctrlT), tm, 0, f1, f2, f3, ctrlbar);
+    ctrlOut = true;
+  };
+  auto stageTab = [&](int itn) {
+    const char* tm;
+    int f1, f2, f3;
+    nodeBox(itn, tm, f1, f2, f3);
+    mbarExpectTx(tabbar, kTabBytes);
+    tmaLoad4d(smemAddr(sm.nodeT), tm + 128, 0, f1, f2, f3, tabbar);
+    tmaLoad4d(smemAddr(sm.lineT), tm + 256, 0, f1, f2, f3, tabbar);
+    tabOut = true;
+  };
+  if (tid == 0 && (int)blockIdx.x < count) {
+    stageCtrl(blockIdx.x);
+    stageTab(blockIdx.x);
+  }
+  uint32_t cphase = 0, tphase = 0;
 
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
     const Item item = items[it];
@@ -178,34 +232,24 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
     const int n0 = (e3 * P.n[1] + e2) * P.n[0] + e1;
 
-    // ---- 1. element nodes, equation numbers, pattern positions -----------
+    // ---- 1. element nodes from the TMA boxes: coordinates relative to the
+    //         first node, weights
+    if (mbarWait(ctrlbar, cphase)) {
+      cphase ^= 1u;
+      ctrlOut = false;
+    } else {
+      atomicAdd(S.counters + 2, 1ull);
+      sm.fail = 1;
+    }
     if (tid < kNen) {
       const int a = tid;
-      const int node = n0 + ((a / 9) * P.n[1] + (a / 3) % 3) * P.n[0] + a % 3;
-      const double* c = P.ctrl + (size_t)node * 4;
-      const double* c00 = P.ctrl + (size_t)n0 * 4;
-      sm.X[a][0] = (float)(c[0] - c00[0]);
-      sm.X[a][1] = (float)(c[1] - c00[1]);
-      sm.X[a][2] = (float)(c[2] - c00[2]);
-      sm.X[a][3] = (float)c[3];
-      const int d0 = S.madof[globalNode(P, node)] - 1;
-      const int q0 = S.meqn[d0], q1 = S.meqn[d0 + 1], q2 = S.meqn[d0 + 2];
-      sm.eq[3 * a] = q0;
-      sm.eq[3 * a + 1] = q1;
-      sm.eq[3 * a + 2] = q2;
-      const int Fa = S.F[globalNode(P, node)];
-      sm.rowBase[3 * a] = Fa;
-      sm.rowBase[3 * a + 1] = Fa + (q0 > 0);
-      sm.rowBase[3 * a + 2] = Fa + (q0 > 0) + (q1 > 0);
+      sm.X[a][0] = (float)(sm.ctrlT[a][0] - sm.ctrlT[0][0]);
+      sm.X[a][1] = (float)(sm.ctrlT[a][1] - sm.ctrlT[0][1]);
+      sm.X[a][2] = (float)(sm.ctrlT[a][2] - sm.ctrlT[0][2]);
+      sm.X[a][3] = (float)sm.ctrlT[a][3];
     }
     if (tid == 0) sm.signs = 0;
     if (tid == 32) sm.dVf = (float)(0.125 * P.span[0][e1] * P.span[1][e2] * P.span[2][e3]);
-    for (int idx = tid; idx < kNen * 9; idx += blockDim.x) {
-      const int bn = idx / 9, la = idx % 9;
-      const int nodeb = n0 + ((bn / 9) * P.n[1] + (bn / 3) % 3) * P.n[0] + bn % 3;
-      const int dy = la % 3 - (bn / 3) % 3, dz = la / 3 - bn / 9;
-      sm.lo[bn][la] = P.lineOff[(size_t)nodeb * 25 + (dz + 2) * 5 + dy + 2];
-    }
     // ---- 2. weighted tensor-product basis at every (Gauss point, function)
     const float* tn0 = P.tabNf[0] + e1 * 9;
     const float* tn1 = P.tabNf[1] + e2 * 9;
@@ -213,13 +257,14 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const float* td0 = P.tabDf[0] + e1 * 9;
     const float* td1 = P.tabDf[1] + e2 * 9;
     const float* td2 = P.tabDf[2] + e3 * 9;
-    __syncthreads();  // X, eq visible
+    __syncthreads();  // X visible, ctrlT read
+    if (sm.fail) break;
+    if (tid == 0 && it + (int)gridDim.x < count) stageCtrl(it + gridDim.x);
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
-      const uint32_t d = sm.dec[idx];
-      const int q = d & 31, a = (d >> 5) & 31;
-      const int g0 = ((d >> 10) & 3) * 3 + ((d >> 16) & 3);  // gi*3 + i
-      const int g1 = ((d >> 12) & 3) * 3 + ((d >> 18) & 3);
-      const int g2 = ((d >> 14) & 3) * 3 + ((d >> 20) & 3);
+      const int q = idx / kNen, a = idx - q * kNen;
+      const int g0 = (q % 3) * 3 + a % 3;  // gi*3 + i
+      const int g1 = ((q / 3) % 3) * 3 + (a / 3) % 3;
+      const int g2 = (q / 9) * 3 + a / 9;
       const float nx = tn0[g0], ny = tn1[g1], nz = tn2[g2];
       const float w = sm.X[a][3];
       sm.u.b.N[q][a] = w * nx * ny * nz;
@@ -228,7 +273,6 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.u.b.Dw[q][a] = w * nx * ny * td2[g2];
     }
     __syncthreads();
-    if (tid < kNen * 3) sm.colStart[tid] = sm.eq[tid] > 0 ? S.colptr[sm.eq[tid] - 1] : 0;
 
     // ---- 3. homogeneous sums per Gauss point: sum_a (wN)_a (X_a, 1) and derivatives
     if (tid < kNq * 4) {
@@ -298,8 +342,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
 
     // ---- 5. rational basis R and dR/du in place
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
-      const uint32_t d = sm.dec[idx];
-      const int q = d & 31, a = (d >> 5) & 31;
+      const int q = idx / kNen, a = idx - q * kNen;
       const float* Wq = sc.Wq + q * 4;
       const float R = sm.u.b.N[q][a] * Wq[0];
       sm.u.b.Du[q][a] = (sm.u.b.Du[q][a] - R * Wq[1]) * Wq[0];
@@ -509,7 +552,15 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
         }
       }
     }
+    if (mbarWait(tabbar, tphase)) {
+      tphase ^= 1u;
+      tabOut = false;
+    } else {
+      atomicAdd(S.counters + 2, 1ull);
+      sm.fail = 1;
+    }
     __syncthreads();
+    if (sm.fail) break;
 
     // ---- 9. element matrix and scatter, node pair by node pair (FP32
     //         arithmetic; the FP64 additions happen in the L2 reductions)
@@ -517,23 +568,26 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const float muf = (float)(P.E / (2.0 * (1.0 + P.nu)));
     // one matrix row (a, k) per thread: the lanes of a warp cover consecutive
     // rows, so each reduction instruction touches contiguous column segments
-    if (tid < kNen * 3 && sm.eq[tid] > 0) {
+    if (tid < kNen * 3 && sm.nodeT[tid / 3][tid % 3] > 0) {
       const int a = tid / 3, k = tid - 3 * a;
-      const int base = sm.rowBase[tid];
-      const int la = (a / 3) % 3 + 3 * (a / 9);
+      // F(a) plus the free DOFs of node a before component k
+      const int base = sm.nodeT[a][3] + (k > 0 && sm.nodeT[a][0] > 0) + (k > 1 && sm.nodeT[a][1] > 0);
+      // line-offset entry of row node a's line in column node bn: index
+      // (dz + 2) 5 + dy + 2 with dy, dz the line offsets of a relative to bn
+      const int rowLine = (a / 9) * 5 + (a / 3) % 3 + 12;
       const float* Grow = sm.u.Gc + tid * kGs;    // row (a, k)
       const float* Ga = sm.u.Gc + 3 * a * kGs;     // rows (a, 0..2)
 #pragma unroll 3
       for (int bn = 0; bn < kNen; bn++) {
         const float trm =
             muf * (Ga[3 * bn] + Ga[kGs + 3 * bn + 1] + Ga[2 * kGs + 3 * bn + 2]);
-        const int off = sm.lo[bn][la] + base;
+        const int off = sm.lineT[bn][rowLine - (bn / 9) * 5 - (bn / 3) % 3] + base;
 #pragma unroll
         for (int l = 0; l < 3; l++) {
-          if (sm.eq[3 * bn + l] <= 0) continue;
+          if (sm.nodeT[bn][l] <= 0) continue;
           const float ke = fmaf(lamf, Grow[3 * bn + l],
                                 fmaf(muf, Ga[l * kGs + 3 * bn + k], k == l ? trm : 0.f));
-          redAdd(S.K + sm.colStart[3 * bn + l] + off, widenF32(ke));
+          redAdd(S.K + sm.nodeT[bn][4 + l] + off, widenF32(ke));
         }
       }
     }
@@ -541,12 +595,12 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     // ---- 10. right-hand side: load vector minus prescribed-DOF terms
     if (tid < kNen * 3) {
       const int a = tid / 3, k = tid % 3;
-      const int r = sm.eq[tid];
+      const int r = sm.nodeT[a][k];
       if (r > 0) {
         double acc = widenF32(fe);
         if (S.c0) {
           for (int j = 0; j < kNen * 3; j++) {
-            const int ce = sm.eq[j];
+            const int ce = sm.nodeT[j / 3][j % 3];
             if (ce >= 0) continue;
             const int bn = j / 3, l = j % 3;
             const float* ga = sm.u.Gc + 3 * a * kGs + 3 * bn;
@@ -563,11 +617,19 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     // ---- 11. this element's reductions are issued; its flag is published
     //         at the next element's step 8 or after the loop
     __syncthreads();
-    if (tid == 0) pending = S.flags + P.flagBase + e;
+    if (tid == 0) {
+      pending = S.flags + P.flagBase + e;
+      if (it + (int)gridDim.x < count) stageTab(it + gridDim.x);  // node tables are free now
+    }
   }
-  if (tid == 0 && pending) {
-    __threadfence();
-    storeRelease(pending, 1);
+  if (tid == 0) {
+    if (pending) {
+      __threadfence();
+      storeRelease(pending, 1);
+    }
+    // after a timeout: copies still in flight land before the CTA exits
+    if (ctrlOut) mbarWait(ctrlbar, cphase);
+    if (tabOut) mbarWait(tabbar, tphase);
   }
 
   // release tensor memory (all tcgen05 traffic of this CTA has completed)
@@ -638,6 +700,82 @@ k_selftest_gemm(const float* __restrict__ A, const float* __restrict__ B, float*
 }
 
 size_t tcVolumeSmem() { return sizeof(TcSmem); }
+
+namespace {
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encodeTiled()
+{
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// Tensor map of a node-major array with `inner` values of `esize` bytes per
+// node of an n0 x n1 x n2 control net; boxes of inner x 3 x 3 x 3 (one
+// element's nodes for p = 2).  Row pitches are multiples of 16 bytes.
+bool nodeBoxMap(CUtensorMap* m, CUtensorMapDataType type, size_t esize, void* base, int inner,
+                const int n[3])
+{
+  const EncodeTiledFn enc = encodeTiled();
+  if (!enc || (esize * inner) % 16 != 0 || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)inner, (cuuint64_t)n[0], (cuuint64_t)n[1], (cuuint64_t)n[2]};
+  const cuuint64_t strides[3] = {esize * inner, esize * inner * n[0],
+                                 esize * inner * (cuuint64_t)n[0] * n[1]};
+  const cuuint32_t box[4] = {(cuuint32_t)inner, 3, 3, 3};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(m, type, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// Node table, padded line-offset rows and the three tensor maps of a
+// tensor-core patch; false leaves the patch to the generic kernel.
+bool tcUploadPatch(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D)
+{
+  if (pc.lineOff.size() != (size_t)pc.nnod * 25 || !pc.d_ctrl) return false;
+  std::vector<int> nodeT((size_t)pc.nnod * 8, 0), lineT((size_t)pc.nnod * 28, 0);
+  for (int n = 0; n < pc.nnod; n++) {
+    const int g = pc.mlgn[n], d0 = ctx->madof[g] - 1;
+    for (int k = 0; k < 3; k++) {
+      const int q = ctx->meqn[d0 + k];
+      nodeT[(size_t)n * 8 + k] = q;
+      nodeT[(size_t)n * 8 + 4 + k] = q > 0 ? ctx->colptr[q - 1] : 0;
+    }
+    nodeT[(size_t)n * 8 + 3] = ctx->freeBefore[g];
+    for (int t = 0; t < 25; t++) lineT[(size_t)n * 28 + t] = pc.lineOff[(size_t)n * 25 + t];
+  }
+  auto put = [&](auto** dst, const auto* src, size_t bytes) {
+    return cudaMalloc((void**)dst, bytes) == cudaSuccess &&
+           cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  CUtensorMap maps[3];
+  const bool ok = put(&pc.d_nodeTab, nodeT.data(), sizeof(int) * nodeT.size()) &&
+                  put(&pc.d_lineTab, lineT.data(), sizeof(int) * lineT.size()) &&
+                  nodeBoxMap(&maps[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, pc.d_ctrl, 4, pc.n) &&
+                  nodeBoxMap(&maps[1], CU_TENSOR_MAP_DATA_TYPE_INT32, 4, pc.d_nodeTab, 8, pc.n) &&
+                  nodeBoxMap(&maps[2], CU_TENSOR_MAP_DATA_TYPE_INT32, 4, pc.d_lineTab, 28, pc.n) &&
+                  put(&pc.d_tmaps, maps, sizeof(maps));
+  if (!ok) {
+    cudaGetLastError();
+    return false;
+  }
+  D.tmaps = pc.d_tmaps;
+  return true;
+}
 
 bool tcSupports(const DevPatch& P)
 {
