@@ -35,6 +35,7 @@ constexpr int kFdCols = 16;   // columns per block of the w-direction kernel
 struct FdBlock {
   int n[3];
   int* map = nullptr;         // box position (i fastest) -> equation (0-based)
+  int base = -1, stride = 0;  // map[o] = base + stride o when base >= 0 (no map reads)
   float* U[3] = {nullptr, nullptr, nullptr};    // n_d x n_d, row-major U[i][a]
   float* Ut[3] = {nullptr, nullptr, nullptr};   // transposes
   float* lam[3] = {nullptr, nullptr, nullptr};
@@ -55,41 +56,45 @@ constexpr int kT = 256;
 
 __device__ inline bool fdStopped(const double* guard) { return guard && guard[0] != 0.0; }
 
-// n floats global -> shared, eight loads in flight per thread
-__device__ inline void stage(float* __restrict__ dst, const float* __restrict__ src, int n)
+// Asynchronous staging (cp.async, 4-byte copies): every thread issues all of
+// its copies before waiting once, so a block's whole staging costs about one
+// L2 round trip instead of one per batch of loads.
+__device__ inline void cpAsync4(float* dst, const float* src)
 {
-  const int bd = blockDim.x;
-  int o = threadIdx.x;
-  for (; o + 7 * bd < n; o += 8 * bd) {
-    float v[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++) v[q] = src[o + q * bd];
-#pragma unroll
-    for (int q = 0; q < 8; q++) dst[o + q * bd] = v[q];
-  }
-  for (; o < n; o += bd) dst[o] = src[o];
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;"
+               :
+               : "r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))), "l"(src)
+               : "memory");
 }
 
-// S[o] = scale[map[o]] r[map[o]], eight gathers in flight per thread
-__device__ inline void stageGather(float* __restrict__ S, const int* __restrict__ map,
-                                   const float* __restrict__ scale, const float* __restrict__ r,
-                                   int n)
+__device__ inline void cpAsyncWaitAll()
 {
-  const int bd = blockDim.x;
-  int o = threadIdx.x;
-  for (; o + 7 * bd < n; o += 8 * bd) {
-    int e[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++) e[q] = map[o + q * bd];
-    float v[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++) v[q] = scale[e[q]] * r[e[q]];
-#pragma unroll
-    for (int q = 0; q < 8; q++) S[o + q * bd] = v[q];
-  }
-  for (; o < n; o += bd) {
-    const int e = map[o];
-    S[o] = scale[e] * r[e];
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" : : : "memory");
+}
+
+// n floats global -> shared (issued only)
+__device__ inline void stageAsync(float* __restrict__ dst, const float* __restrict__ src, int n)
+{
+  for (int o = threadIdx.x; o < n; o += blockDim.x) cpAsync4(dst + o, src + o);
+}
+
+// equation of box position o (affine maps need no map read)
+__device__ inline int boxEq(const int* __restrict__ map, int base, int stride, size_t o)
+{
+  return base >= 0 ? base + stride * (int)o : map[o];
+}
+
+// S[o] <- r[e(o)], X[o] <- scale[e(o)] for the positions [first, first + n) (issued only)
+__device__ inline void stageGatherAsync(float* __restrict__ S, float* __restrict__ X,
+                                        const int* __restrict__ map, int base, int stride,
+                                        size_t first, const float* __restrict__ scale,
+                                        const float* __restrict__ r, int n)
+{
+#pragma unroll 4
+  for (int o = threadIdx.x; o < n; o += blockDim.x) {
+    const int e = boxEq(map, base, stride, first + o);
+    cpAsync4(S + o, r + e);
+    cpAsync4(X + o, scale + e);
   }
 }
 
@@ -103,8 +108,8 @@ constexpr int kFdSplit = 4;   // blocks per w-slab in the slab kernels
 // and the block's share of the columns a
 __global__ void __launch_bounds__(kT)
 k_fd_fwd(const float* __restrict__ r, const float* __restrict__ scale, const int* __restrict__ map,
-         int n0, int n1, const float* __restrict__ U0, const float* __restrict__ U1,
-         float* __restrict__ out, const double* guard)
+         int base, int stride, int n0, int n1, const float* __restrict__ U0,
+         const float* __restrict__ U1, float* __restrict__ out, const double* guard)
 {
   if (fdStopped(guard)) return;
   extern __shared__ float sm[];
@@ -117,9 +122,13 @@ k_fd_fwd(const float* __restrict__ r, const float* __restrict__ scale, const int
   const int per = (n0 + gridDim.y - 1) / gridDim.y;
   const int a0 = blockIdx.y * per, na = min(n0, a0 + per) - a0;
   if (na <= 0) return;
-  stageGather(S, map + (size_t)k * ns, scale, r, ns);
-  stage(u0, U0, n0 * n0);
-  stage(u1, U1, n1 * n1);
+  // r and the scaling of the slab (the scaling into T, free until the first
+  // product), both eigenvector matrices; then S = scale r on own elements
+  stageGatherAsync(S, T, map, base, stride, (size_t)k * ns, scale, r, ns);
+  stageAsync(u0, U0, n0 * n0);
+  stageAsync(u1, U1, n1 * n1);
+  cpAsyncWaitAll();
+  for (int o = threadIdx.x; o < ns; o += blockDim.x) S[o] *= T[o];
   __syncthreads();
   const int nt = (n1 + kFdTile - 1) / kFdTile;
   for (int w = threadIdx.x; w < nt * na; w += blockDim.x) {
@@ -170,21 +179,13 @@ k_fd_mid(float* __restrict__ tmp, int n0, int n1, int n2, const float* __restric
   float* V = X + n2 * kFdCols;     // n2 x kFdCols
   float* u2 = V + n2 * kFdCols;    // n2 x n2
   const int ncol = n0 * n1, col0 = blockIdx.x * kFdCols;
-  {
-    const int n = n2 * kFdCols, bd = blockDim.x;
-    for (int o0 = threadIdx.x; o0 < n; o0 += 8 * bd) {  // eight loads in flight
-      float v[8];
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const int o = o0 + q * bd, k = o / kFdCols, t = o - k * kFdCols;
-        v[q] = (o < n && col0 + t < ncol) ? tmp[(size_t)k * ncol + col0 + t] : 0.f;
-      }
-#pragma unroll
-      for (int q = 0; q < 8; q++)
-        if (o0 + q * bd < n) X[o0 + q * bd] = v[q];
-    }
+  for (int o = threadIdx.x; o < n2 * kFdCols; o += blockDim.x) {
+    const int k = o / kFdCols, t = o - k * kFdCols;
+    if (col0 + t < ncol) cpAsync4(X + o, tmp + (size_t)k * ncol + col0 + t);
+    else X[o] = 0.f;
   }
-  stage(u2, U2, n2 * n2);
+  stageAsync(u2, U2, n2 * n2);
+  cpAsyncWaitAll();
   __syncthreads();
   const int nt = (n2 + kFdTile - 1) / kFdTile;
   for (int w = threadIdx.x; w < nt * kFdCols; w += blockDim.x) {
@@ -231,7 +232,8 @@ k_fd_mid(float* __restrict__ tmp, int n0, int n1, int n2, const float* __restric
 __global__ void __launch_bounds__(kT)
 k_fd_inv(const float* __restrict__ tmp, int n0, int n1, const float* __restrict__ U0t,
          const float* __restrict__ U1, const float* __restrict__ scale,
-         const int* __restrict__ map, float* __restrict__ z, const double* guard)
+         const int* __restrict__ map, int base, int stride, float* __restrict__ z, FdDot dot,
+         const double* guard)
 {
   if (fdStopped(guard)) return;
   extern __shared__ float sm[];
@@ -242,11 +244,11 @@ k_fd_inv(const float* __restrict__ tmp, int n0, int n1, const float* __restrict_
   float* u1 = u0t + n0 * n0;
   const int k = blockIdx.x;
   const int per = (n1 + gridDim.y - 1) / gridDim.y;
-  const int jb = blockIdx.y * per, nj = min(n1, jb + per) - jb;
-  if (nj <= 0) return;
-  stage(W, tmp + (size_t)k * ns, ns);
-  stage(u0t, U0t, n0 * n0);
-  stage(u1, U1, n1 * n1);
+  const int jb = blockIdx.y * per, nj = max(min(n1, jb + per) - jb, 0);
+  stageAsync(W, tmp + (size_t)k * ns, ns);
+  stageAsync(u0t, U0t, n0 * n0);
+  stageAsync(u1, U1, n1 * n1);
+  cpAsyncWaitAll();
   __syncthreads();
   const int nt = (nj + kFdTile - 1) / kFdTile, je = jb + nj;
   for (int w = threadIdx.x; w < nt * n0; w += blockDim.x) {
@@ -266,6 +268,7 @@ k_fd_inv(const float* __restrict__ tmp, int n0, int n1, const float* __restrict_
       if (j0 + q < je) T[(j0 + q) * n0 + a] = acc[q];
   }
   __syncthreads();
+  float zq = 0.f;
   for (int w = threadIdx.x; w < nt * n0; w += blockDim.x) {
     const int jt = w / n0, i = w - jt * n0, j0 = jb + jt * kFdTile;
     const float* trow[kFdTile];
@@ -282,8 +285,25 @@ k_fd_inv(const float* __restrict__ tmp, int n0, int n1, const float* __restrict_
     for (int q = 0; q < kFdTile; q++) {
       const int j = j0 + q;
       if (j >= je) continue;
-      const int e = map[(size_t)k * ns + j * n0 + i];
-      z[e] = scale[e] * acc[q];
+      const int e = boxEq(map, base, stride, (size_t)k * ns + j * n0 + i);
+      const float ze = scale[e] * acc[q];
+      z[e] = ze;
+      if (dot.q) zq = fmaf(ze, dot.q[e], zq);
+    }
+  }
+  // (z, q) of the flexible-CG step and beta = -(z, q) / (p, q), folded into
+  // this (single-box) product
+  if (dot.q) {
+    __shared__ double sh[32];
+    const double t = blockReduceSumF(zq, sh);
+    const unsigned nb = gridDim.x * gridDim.y;
+    if (threadIdx.x == 0) dot.part[blockIdx.y * gridDim.x + blockIdx.x] = t;
+    if (lastBlockOf(dot.counter, nb)) {
+      const double v = finalSum(dot.part, (int)nb, sh);
+      if (threadIdx.x == 0) {
+        *dot.out = v;
+        *dot.beta = (float)(-v / *dot.pq);
+      }
     }
   }
 }
@@ -555,6 +575,16 @@ ifemgpu_status fdSetup(ifemgpu_ctx* ctx)
   for (HostBlock& B : hb) {
     FdBlock D;
     for (int d = 0; d < 3; d++) D.n[d] = B.n[d];
+    // equations numbered in box order with a fixed stride (one component of a
+    // box-shaped free set): the kernels form them without reading the map
+    const int stride = B.map.size() > 1 ? B.map[1] - B.map[0] : 1;
+    bool affine = stride > 0;
+    for (size_t o = 0; affine && o < B.map.size(); o++)
+      affine = B.map[o] == B.map[0] + stride * (int)o;
+    if (affine) {
+      D.base = B.map[0];
+      D.stride = stride;
+    }
     bool ok = up(&D.map, B.map.data(), B.map.size());
     for (int d = 0; d < 3; d++) {
       ok = ok && up(&D.U[d], B.U[d].data(), B.U[d].size());
@@ -591,23 +621,33 @@ ifemgpu_status fdRescale(ifemgpu_ctx* ctx, const double* dinv)
   return IFEMGPU_OK;
 }
 
-// z = S P^-1 S r over every block; each kernel returns at once when *guard != 0
-ifemgpu_status fdApply(ifemgpu_ctx* ctx, const float* r, float* z, const double* guard)
+bool fdCanDot(const ifemgpu_ctx* ctx)
+{
+  return ctx->fd && ctx->fd->blocks.size() == 1 && ctx->fd->blocks[0].n[2] * kFdSplit <= 1024;
+}
+
+// z = S P^-1 S r over every block; each kernel returns at once when *guard != 0.
+// With dot (one box only, fdCanDot), the last kernel also forms (z, q) and beta.
+ifemgpu_status fdApply(ifemgpu_ctx* ctx, const float* r, float* z, const double* guard,
+                       const FdDot* dot)
 {
   FdState* F = ctx->fd;
   cudaStream_t s = ctx->stream;
+  if (dot && !fdCanDot(ctx))
+    return setError(ctx, IFEMGPU_INVALID_ARG, "internal: fused (z, q) needs a single box");
+  const FdDot none{};
   for (const FdBlock& B : F->blocks) {
     const size_t slab = sizeof(float) * (2 * (size_t)B.n[0] * B.n[1] + (size_t)B.n[0] * B.n[0] +
                                          (size_t)B.n[1] * B.n[1]);
     const size_t mid = sizeof(float) * (2 * (size_t)B.n[2] * kFdCols + (size_t)B.n[2] * B.n[2]);
     const int ncol = B.n[0] * B.n[1];
     const dim3 slabs(B.n[2], kFdSplit);
-    k_fd_fwd<<<slabs, kT, slab, s>>>(r, F->scale, B.map, B.n[0], B.n[1], B.U[0], B.U[1], F->tmp,
-                                     guard);
+    k_fd_fwd<<<slabs, kT, slab, s>>>(r, F->scale, B.map, B.base, B.stride, B.n[0], B.n[1], B.U[0],
+                                     B.U[1], F->tmp, guard);
     k_fd_mid<<<(ncol + kFdCols - 1) / kFdCols, kT, mid, s>>>(F->tmp, B.n[0], B.n[1], B.n[2], B.U[2],
                                                              B.lam[0], B.lam[1], B.lam[2], guard);
-    k_fd_inv<<<slabs, kT, slab, s>>>(F->tmp, B.n[0], B.n[1], B.Ut[0], B.U[1], F->scale, B.map, z,
-                                     guard);
+    k_fd_inv<<<slabs, kT, slab, s>>>(F->tmp, B.n[0], B.n[1], B.Ut[0], B.U[1], F->scale, B.map,
+                                     B.base, B.stride, z, dot ? *dot : none, guard);
   }
   IFEMGPU_CUDA(ctx, cudaGetLastError());
   return IFEMGPU_OK;

@@ -1062,6 +1062,14 @@ ifemgpu_status ifemgpu_learn_clear(ifemgpu_ctx* ctx)
   return IFEMGPU_OK;
 }
 
+ifemgpu_status ifemgpu_learn_set_target(ifemgpu_ctx* ctx, int mode)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (mode != IFEMGPU_LEARN_TARGET_ERROR && mode != IFEMGPU_LEARN_TARGET_COMPLEMENT)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "learn_set_target: unknown mode");
+  return learnSetTarget(ctx, mode);
+}
+
 ifemgpu_status ifemgpu_learn_train(ifemgpu_ctx* ctx, int epochs, int batch, float lr,
                                    unsigned seed, float* final_loss)
 {

@@ -272,7 +272,9 @@ ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigne
 ifemgpu_status learnPrepare(ifemgpu_ctx* ctx);
 void destroyLearn(ifemgpu_ctx* ctx);
 double* learnXstar(ifemgpu_ctx* ctx);
-ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx);
+// fine: the fine preconditioner's output for r (used by complement targets)
+ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx,
+                           const float* fine);
 ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* q,
                           double* part, int nparts, unsigned* counter, double* dotOut,
                           const double* pq, float* betaOut, const double* guard);
@@ -283,6 +285,8 @@ ifemgpu_status learnGradients(ifemgpu_ctx* ctx, const float* X, const float* Y, 
                               float* gradOut, float* lossOut);
 ifemgpu_status learnWeights(ifemgpu_ctx* ctx, float* theta, int* count, float* scale, int set);
 int learnCount(const ifemgpu_ctx* ctx);
+int learnTarget(const ifemgpu_ctx* ctx);
+ifemgpu_status learnSetTarget(ifemgpu_ctx* ctx, int mode);
 bool learnReady(const ifemgpu_ctx* ctx);
 void learnClear(ifemgpu_ctx* ctx);
 
@@ -290,7 +294,19 @@ void learnClear(ifemgpu_ctx* ctx);
 ifemgpu_status fdSetup(ifemgpu_ctx* ctx);
 void destroyFd(ifemgpu_ctx* ctx);
 ifemgpu_status fdRescale(ifemgpu_ctx* ctx, const double* dinv);
-ifemgpu_status fdApply(ifemgpu_ctx* ctx, const float* r, float* z, const double* guard);
+// (z, q) of a flexible-CG step folded into the preconditioner's last kernel:
+// partials in part (one per block), out = (z, q), beta = -(z, q) / *pq
+struct FdDot {
+  const float* q = nullptr;
+  double* part = nullptr;
+  unsigned* counter = nullptr;
+  double* out = nullptr;
+  const double* pq = nullptr;
+  float* beta = nullptr;
+};
+bool fdCanDot(const ifemgpu_ctx* ctx);
+ifemgpu_status fdApply(ifemgpu_ctx* ctx, const float* r, float* z, const double* guard,
+                       const FdDot* dot = nullptr);
 int fdLaunches(const ifemgpu_ctx* ctx);
 
 }  // namespace ifemgpu

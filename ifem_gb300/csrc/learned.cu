@@ -64,6 +64,7 @@ struct LearnState {
   float* Y = nullptr;
   int cap = 0, count = 0;
   double* xstar = nullptr;    // neq: reference solution of the collecting solve
+  int target = IFEMGPU_LEARN_TARGET_ERROR;
   // training scratch (batch B)
   int B = 0;
   float *Xb = nullptr, *Yb = nullptr, *H1 = nullptr, *H2 = nullptr, *Yp = nullptr;
@@ -99,15 +100,17 @@ __global__ void k_restrict(const int* __restrict__ vPtr, const int* __restrict__
 // ec = Rn (x* sx - x) for the error of an iterate
 __global__ void k_restrict_err(const int* __restrict__ vPtr, const int* __restrict__ vEq,
                                const float* __restrict__ vWn, const double* __restrict__ xs,
-                               double sx, const float* __restrict__ x, float* __restrict__ ec,
-                               int nc)
+                               double sx, const float* __restrict__ x,
+                               const float* __restrict__ fine, float* __restrict__ ec, int nc)
 {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= nc) return;
   float s = 0.f;
   for (int k = vPtr[warp] + lane; k < vPtr[warp + 1]; k += 32) {
     const int e = vEq[k];
-    s += vWn[k] * (float)(xs[e] * sx - (double)x[e]);
+    float d = (float)(xs[e] * sx - (double)x[e]);
+    if (fine) d -= fine[e];  // what the fine preconditioner already supplies
+    s += vWn[k] * d;
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) ec[warp] = s;
@@ -623,7 +626,8 @@ ifemgpu_status learnPrepare(ifemgpu_ctx* ctx)
 }
 
 // one plain-PCG iterate (r, x of the system scaled by sx) -> one pair
-ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx)
+ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx,
+                           const float* fine)
 {
   LearnState* L = ctx->learn;
   if (!L || L->count >= L->cap) return IFEMGPU_OK;
@@ -631,7 +635,9 @@ ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, dou
   const int nc = L->nc;
   const int blocks = (nc * 32 + kT - 1) / kT;
   k_restrict<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, L->rc, nc, nullptr);
-  k_restrict_err<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vWn, L->xstar, sx, x, L->yc, nc);
+  k_restrict_err<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vWn, L->xstar, sx, x,
+                                       L->target == IFEMGPU_LEARN_TARGET_COMPLEMENT ? fine : nullptr,
+                                       L->yc, nc);
   k_store_pair<<<1, kT, 0, s>>>(L->rc, L->yc, L->feat, L->X + (size_t)L->count * L->nin,
                                 L->Y + (size_t)L->count * nc, nc, L->nf);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
@@ -786,6 +792,17 @@ ifemgpu_status learnWeights(ifemgpu_ctx* ctx, float* theta, int* count, float* s
 }
 
 int learnCount(const ifemgpu_ctx* ctx) { return ctx->learn ? ctx->learn->count : 0; }
+int learnTarget(const ifemgpu_ctx* ctx)
+{
+  return ctx->learn ? ctx->learn->target : IFEMGPU_LEARN_TARGET_ERROR;
+}
+ifemgpu_status learnSetTarget(ifemgpu_ctx* ctx, int mode)
+{
+  if (!ctx->learn) return setError(ctx, IFEMGPU_NOT_READY, "learn_set_target before learn_setup");
+  if (ctx->learn->target != mode) ctx->learn->count = 0;
+  ctx->learn->target = mode;
+  return IFEMGPU_OK;
+}
 bool learnReady(const ifemgpu_ctx* ctx) { return ctx->learn && ctx->learn->trained; }
 void learnClear(ifemgpu_ctx* ctx)
 {

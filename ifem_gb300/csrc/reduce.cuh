@@ -42,21 +42,23 @@ __device__ inline double blockReduceSumF(float v, double* sh)
 }
 
 // after thread 0 has stored this block's partials: true in the block that
-// finishes last (every thread of it), which also resets the counter
-__device__ inline bool lastBlock(unsigned* counter)
+// finishes last of nblocks (every thread of it), which also resets the counter
+__device__ inline bool lastBlockOf(unsigned* counter, unsigned nblocks)
 {
   __shared__ unsigned ticket;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
   __syncthreads();
-  const bool last = ticket == gridDim.x - 1;
+  const bool last = ticket == nblocks - 1;
   if (last) {
     __threadfence();
     if (threadIdx.x == 0) *counter = 0u;
   }
   return last;
 }
+
+__device__ inline bool lastBlock(unsigned* counter) { return lastBlockOf(counter, gridDim.x); }
 
 // stores the partial t (thread 0's value) of this block in part[blockIdx.x]
 __device__ inline bool lastBlockDone(double* part, double t, unsigned* counter)

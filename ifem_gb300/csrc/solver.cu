@@ -498,7 +498,7 @@ g_fcg_update(float* __restrict__ x, float* __restrict__ r, float* __restrict__ z
     x[i] += alpha * p[i];
     const float ri = r[i] - alpha * q[i];
     r[i] = ri;
-    z[i] = dinv[i] * ri;
+    if (z) z[i] = dinv[i] * ri;  // Jacobi fine level (null when another preconditioner writes z)
     acc += ri * ri;
   }
   const double t = blockReduceSumF(acc, sh);
@@ -753,6 +753,16 @@ static ifemgpu_status loopFCG(ifemgpu_ctx* ctx, const Work& w, bool kron, bool l
   // z = M r after the Jacobi step of the update kernel; (z, q) -> S_ZQ and beta
   auto precondition = [&](bool withDot) -> ifemgpu_status {
     ifemgpu_status st2;
+    if (kron && !learned && withDot && fdCanDot(ctx)) {  // (z, q) inside the last FD kernel
+      FdDot dot;
+      dot.q = w.q32;
+      dot.part = w.part;
+      dot.counter = tk + 2;
+      dot.out = w.scal + S_ZQ;
+      dot.pq = w.scal + S_PQ;
+      dot.beta = reinterpret_cast<float*>(w.scal + S_RAT) + 1;
+      return fdApply(ctx, w.r32, w.z32, guard, &dot);
+    }
     if (kron && (st2 = fdApply(ctx, w.r32, w.z32, guard)) != IFEMGPU_OK) return st2;
     if (learned)
       return learnApply(ctx, w.r32, w.z32, withDot ? w.q32 : nullptr, w.part, vb, tk + 2,
@@ -763,8 +773,8 @@ static ifemgpu_status loopFCG(ifemgpu_ctx* ctx, const Work& w, bool kron, bool l
   };
   auto body = [&]() -> ifemgpu_status {
     spmv32(ctx, w, w.p32, w.q32, 0);
-    g_fcg_update<<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32, w.scal, n,
-                                         w.part);
+    g_fcg_update<<<vb, kThreads, 0, s>>>(w.x32, w.r32, kron ? nullptr : w.z32, w.p32, w.q32,
+                                         w.dinv32, w.scal, n, w.part);
     ifemgpu_status st2 = precondition(true);
     if (st2 != IFEMGPU_OK) return st2;
     g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
@@ -1145,12 +1155,25 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
   if ((st = solvePrologue(ctx, w, b, true, &bn)) != IFEMGPU_OK) return st;
   if (!(bn > 0)) return IFEMGPU_OK;
   const bool kron = precond == IFEMGPU_PRECOND_KRONECKER;
-  if (kron) {
+  // complement targets subtract the Kronecker preconditioner's output for r_k:
+  // z itself along flexible CG, a separate application into q (free between
+  // iterations) along Jacobi-PCG
+  const bool complement = learnTarget(ctx) == IFEMGPU_LEARN_TARGET_COMPLEMENT;
+  if (kron || complement) {
     if ((st = fdSetup(ctx)) != IFEMGPU_OK) return st;
     if ((st = fdRescale(ctx, w.d64)) != IFEMGPU_OK) return st;
   }
-  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
   const double sx = 1.0 / bn;  // the loop solves the system scaled by 1/||b||
+  auto record = [&]() -> ifemgpu_status {
+    const float* fine = nullptr;
+    if (complement) {
+      ifemgpu_status st2;
+      if (!kron && (st2 = fdApply(ctx, w.r32, w.q32, nullptr)) != IFEMGPU_OK) return st2;
+      fine = kron ? w.z32 : w.q32;
+    }
+    return learnRecord(ctx, w.r32, w.x32, sx, fine);
+  };
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
   unsigned* tk = hostTickets(w);
   k_loop_init<<<1, 1, 0, s>>>(w.scal, rtol * rtol, (double)maxit, 0.0);
   if (kron) {  // flexible CG with the Kronecker preconditioner
@@ -1161,7 +1184,7 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
     g_pcg_start<float><<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.dinv32,
                                                n, w.part);
   }
-  if ((st = learnRecord(ctx, w.r32, w.x32, sx)) != IFEMGPU_OK) return st;
+  if ((st = record()) != IFEMGPU_OK) return st;
   stride = std::max(1, stride);
   for (int l = 0; l <= maxit / stride; l++) {
     for (int k = 0; k < stride; k++) {
@@ -1184,7 +1207,7 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
                                       cudaMemcpyDeviceToHost, s));
     IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
     if (ctx->h_pinned[0] != 0.0) break;
-    if ((st = learnRecord(ctx, w.r32, w.x32, sx)) != IFEMGPU_OK) return st;
+    if ((st = record()) != IFEMGPU_OK) return st;
   }
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
   return IFEMGPU_OK;

@@ -59,6 +59,7 @@ SOURCE_CONSTANT, SOURCE_SINE = 0, 1
 FIELD_LOG_KAPPA, FIELD_SOURCE_NOISE = 1, 2
 PCG_MIXED, PCG_FP64, FCG_LEARNED = 1, 2, 3
 PRECOND_JACOBI, PRECOND_KRONECKER = 0, 1
+LEARN_TARGET_ERROR, LEARN_TARGET_COMPLEMENT = 0, 1
 DUMP_FLAT, DUMP_MATLAB, DUMP_MATRIX_MARKET = 1, 2, 3
 
 # Every symbol include/ifemgpu.h declares (checked by the CPU test suite).
@@ -73,7 +74,7 @@ EXPORTS = [
     "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_solve",
     "ifemgpu_expand_solution", "ifemgpu_patch_update_coefs", "ifemgpu_get_stream",
     "ifemgpu_selftest_tc_gemm", "ifemgpu_solve_noalloc", "ifemgpu_learn_setup",
-    "ifemgpu_learn_collect", "ifemgpu_learn_clear", "ifemgpu_learn_train",
+    "ifemgpu_learn_collect", "ifemgpu_learn_clear", "ifemgpu_learn_set_target", "ifemgpu_learn_train",
     "ifemgpu_learn_evaluate", "ifemgpu_learn_gradients", "ifemgpu_learn_info",
     "ifemgpu_learn_get_weights", "ifemgpu_learn_set_weights", "ifemgpu_patch_update_field",
     "ifemgpu_learn_get_pairs", "ifemgpu_apply_preconditioner", "ifemgpu_copy_matrix_bsr",
@@ -136,6 +137,7 @@ def load_library(path: str | None = None):
         "ifemgpu_learn_setup": (I, [P, C.POINTER(LearnOptions)]),
         "ifemgpu_learn_collect": (I, [P, V, V, I, I, D, I, C.POINTER(I)]),
         "ifemgpu_learn_clear": (I, [P]),
+        "ifemgpu_learn_set_target": (I, [P, I]),
         "ifemgpu_learn_get_pairs": (I, [P, I, I, V, V]),
         "ifemgpu_apply_preconditioner": (I, [P, I, V, V]),
         "ifemgpu_copy_matrix_bsr": (I, [P, I, C.POINTER(I), C.POINTER(C.c_int64), V, V, V]),
@@ -460,6 +462,12 @@ class SIM:
 
     def learn_clear(self):
         self._check(self.lib.ifemgpu_learn_clear(self.ctx))
+
+    def learn_set_target(self, mode):
+        """LEARN_TARGET_ERROR (whole coarse error) or LEARN_TARGET_COMPLEMENT
+        (the error minus the Kronecker preconditioner's output); forgets the
+        stored pairs when the mode changes."""
+        self._check(self.lib.ifemgpu_learn_set_target(self.ctx, mode))
 
     def learn_pairs(self, first=0, count=None):
         info = self.learn_info()

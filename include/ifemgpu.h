@@ -420,6 +420,20 @@ ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs,
 /* Forgets the stored pairs (the network is kept).                         */
 ifemgpu_status ifemgpu_learn_clear(ifemgpu_ctx* ctx);
 
+/* What the stored targets are (default IFEMGPU_LEARN_TARGET_ERROR):
+ *   ERROR       Rn (x* - x_k) / |R r_k|, the whole coarse error;
+ *   COMPLEMENT  Rn (x* - x_k - M r_k) / |R r_k| with M the Kronecker
+ *               preconditioner: the part of the error that the fine level
+ *               of flexible CG does not already supply, so that the added
+ *               correction does not count the coarse error twice.
+ * Changing the mode forgets the stored pairs; learn_setup restores the
+ * default.                                                                */
+enum ifemgpu_learn_target {
+  IFEMGPU_LEARN_TARGET_ERROR = 0,
+  IFEMGPU_LEARN_TARGET_COMPLEMENT = 1
+};
+ifemgpu_status ifemgpu_learn_set_target(ifemgpu_ctx* ctx, int mode);
+
 /* Copies stored pairs first .. first+count-1 to host rows X (`inputs`
  * floats each) and Y (`coarse_unknowns` floats each): the training set's
  * checkpoint, and the check of the restriction.                           */

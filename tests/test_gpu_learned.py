@@ -202,3 +202,32 @@ def test_pairs_from_kronecker_iterates(gpulib):
     assert 2 <= n_k < n_j
     assert np.abs(Xk[0] - Xj[0]).max() <= 1e-6 and np.abs(Yk[0] - Yj[0]).max() <= 1e-6
     assert np.isfinite(Xk).all() and np.isfinite(Yk).all()
+
+
+def test_complement_targets_subtract_the_kronecker_step(gpulib):
+    """Complement targets: the first pair's target is the whole-error target
+    minus the weight-normalised restriction of the Kronecker preconditioner's
+    output for the first residual, on the same scale."""
+    sim, patches = poisson_model(nel=8)
+    m = 3
+    sim.learn_setup(coarse_cells=m, hidden=16, capacity=64, seed=1, field_inputs=0)
+    x_ref, _ = sim.solveSystem(method=G.PCG_FP64, rtol=1e-12, max_inner=20000)
+    sim.learn_collect(xstar=x_ref, stride=4, rtol=1e-6)
+    Xe, Ye = sim.learn_pairs()
+    sim.learn_set_target(G.LEARN_TARGET_COMPLEMENT)
+    assert sim.learn_info()["pairs"] == 0          # changing the mode forgets the pairs
+    sim.learn_collect(xstar=x_ref, stride=4, rtol=1e-6)
+    Xc, Yc = sim.learn_pairs()
+    assert np.array_equal(Xc[0], Xe[0])
+    sam = sim.getSAM()
+    pc = patches[0]
+    R = mlp.restriction(pc.knots, pc.degree, pc.ncoef, sam.meqn, sam.madof, 1, m)
+    Rn = R / np.maximum(R.sum(1, keepdims=True), 1e-300)
+    b = sim.rhs()
+    r0 = b / np.linalg.norm(b)
+    z0 = sim.apply_preconditioner(r0, G.PRECOND_KRONECKER)
+    nrm = np.linalg.norm(R @ r0)
+    want = Ye[0] - (Rn @ z0) / nrm
+    assert np.abs(Yc[0] - want).max() <= 1e-4 * np.abs(Ye[0]).max()
+    with pytest.raises(G.IfemGpuError):
+        sim.learn_set_target(7)
