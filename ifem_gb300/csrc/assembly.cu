@@ -975,6 +975,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   // other patches: one FP64 launch per colour.
   // colour = (e1 mod q1) + q1 (e2 mod q2) + q1 q2 (e3 mod q3)
   std::vector<char> onTc(np, 0);
+  std::vector<int> tcDeg(np, 0);  // 0: elasticity p = 2 kernel; 2, 3: Poisson kernel
   int nflags = 0;
   // the other patches share one persistent pass when every element has a
   // volume (the done flags assume a full element grid)
@@ -984,6 +985,13 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) && D.mass == 0.0 &&
                D.lineOff != nullptr && D.faceTables && ctx->patches[pi].neumann.size() <= 6;
     if (onTc[pi]) onTc[pi] = tcUploadPatch(ctx, ctx->patches[pi], D);  // node tables, TMA maps
+    if (!onTc[pi] && ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32) {
+      const int deg = tcPoissonDegree(D, ctx->patches[pi]);
+      if (deg && tcPoissonUpload(ctx, ctx->patches[pi], D, deg)) {
+        onTc[pi] = 1;
+        tcDeg[pi] = deg;
+      }
+    }
     if (!onTc[pi] && ctx->patches[pi].nelActive != ctx->patches[pi].nelAll) flow = false;
   }
   for (int pi = 0; pi < np; pi++) {
@@ -991,7 +999,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     D.flagBase = nflags;
     D.tile = 4;
     if (onTc[pi] || flow) nflags += ctx->patches[pi].nelAll;
-    if (onTc[pi]) {
+    if (onTc[pi] && tcDeg[pi] == 0) {
       // the element kernel integrates this patch's Neumann faces itself
       D.nneu = (int)ctx->patches[pi].neumann.size();
       for (int f = 0; f < D.nneu; f++) {
@@ -1012,13 +1020,14 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
           if (pc.active[e]) out.push_back({pi, e, 0, 0});
         }
   };
-  if (std::count(onTc.begin(), onTc.end(), 1) > 0) {
-    Pass pass{(int)vol.size(), 0, 0, 81, tcVolumeSmem(), true};
+  for (int deg : {0, 2, 3}) {  // one persistent launch per tensor-core kernel
+    Pass pass{(int)vol.size(), 0, 0, deg ? 1 : 81, deg ? tcPoissonSmem(deg) : tcVolumeSmem(), true};
+    pass.tcDeg = deg;
     for (int c = 0; c < maxColours; c++)
       for (int pi = 0; pi < np; pi++)
-        if (onTc[pi]) colourItems(pi, c, vol);
+        if (onTc[pi] && tcDeg[pi] == deg) colourItems(pi, c, vol);
     pass.count = (int)vol.size() - pass.first;
-    ctx->passes.push_back(pass);
+    if (pass.count) ctx->passes.push_back(pass);
   }
   ctx->onFlow.assign(np, 0);
   for (int pi = 0; pi < np; pi++) ctx->onFlow[pi] = flow && !onTc[pi];
@@ -1165,6 +1174,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   for (auto& p : ctx->passes)
     if (p.tc) {
       IFEMGPU_TRY(tcPrepare(ctx));
+      IFEMGPU_TRY(tcPoissonPrepare(ctx));
       break;
     }
   return IFEMGPU_OK;
@@ -1226,7 +1236,9 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
   for (const Pass& p : ctx->passes) {
     if ((p.face != 0) != (seg == 2)) continue;
     if ((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow)) continue;
-    if (p.tc)
+    if (p.tc && p.tcDeg)
+      IFEMGPU_TRY(tcPoissonLaunch(ctx, p, p.tcDeg));
+    else if (p.tc)
       IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
     else if (p.persistent && split)
       k_volume_gen_flow<float><<<std::min(p.count, ctx->genGrid), 256, p.smem, s>>>(

@@ -146,7 +146,8 @@ struct Pass {
   int face;    // 0 volume, else face pass
   int maxNd;   // largest element DOF count in the pass
   size_t smem; // dynamic shared memory of the pass' launch
-  bool tc;     // volume pass on the tensor-core kernel
+  bool tc;     // volume pass on a tensor-core kernel
+  int tcDeg = 0;  // 0: elasticity p = 2 kernel; 2, 3: Poisson kernel of that degree
   bool persistent = false;  // one colour-major launch ordered by done flags
   bool altColour = false;   // colour pass over a part of the persistent pass' items
 };
@@ -256,6 +257,13 @@ ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs);
 // tc_volume.cu
 ifemgpu_status tcPrepare(ifemgpu_ctx* ctx);
 bool tcUploadPatch(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D);
+bool nodeBoxMap(void* out, size_t esize, void* base, int inner, const int n[3], int q);
+// tc_poisson.cu: tensor-core Poisson kernels (p = 2 and 3)
+int tcPoissonDegree(const DevPatch& P, const HostPatch& pc);  // 2, 3 or 0 (not eligible)
+bool tcPoissonUpload(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D, int deg);
+size_t tcPoissonSmem(int deg);
+ifemgpu_status tcPoissonPrepare(ifemgpu_ctx* ctx);
+ifemgpu_status tcPoissonLaunch(ifemgpu_ctx* ctx, const Pass& p, int deg);
 ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid);
 
 // solver.cu

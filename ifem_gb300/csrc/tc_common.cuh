@@ -186,6 +186,30 @@ __device__ __forceinline__ double widenF32(float f)
   return __hiloint2double((int)hi, (int)lo);
 }
 
+__device__ __forceinline__ void redAdd(double* p, double v)
+{
+  atomicAdd(p, v);  // result unused: compiles to an L2 reduction
+}
+
+// neighbour flags are polled with relaxed loads (served by L2); a thread that
+// saw one issues a single acquire fence before the block's scatter
+__device__ __forceinline__ int loadRelaxed(const int* p)
+{
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void fenceAcquire()
+{
+  asm volatile("fence.acq_rel.gpu;" : : : "memory");
+}
+
+__device__ __forceinline__ void storeRelease(int* p, int v)
+{
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
+
 // x = hi + lo with hi rounded to TF32 (10 explicit mantissa bits)
 __device__ __forceinline__ void splitTF32(float x, float& hi, float& lo)
 {

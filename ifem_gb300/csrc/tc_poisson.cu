@@ -1,0 +1,635 @@
+// tc_poisson.cu -- tensor-core (tcgen05, sm_103a) element kernels for the 3D
+// Poisson integrand with p = 2 and p = 3 spline patches (Gauss rule p + 1 per
+// direction): the hot loop of ASMs3D::integrate (src/ASM/ASMs3D.C:2266-2312)
+// with EqualOrderOperators::Weak::LaplacianCoeff and ::Source
+// (Apps/Utils/EqualOrderOperators.C:158-265), and the scatter of assemSparse
+// (src/LinAlg/SparseMatrix.C:614-688).
+//
+// One persistent launch per degree processes every element of its patches,
+// one CTA of 128 threads per element, elements in colour-major order (the
+// same done-flag ordering as the elasticity kernel, so the FP64 sums are
+// deterministic).  Per element:
+//   0. the (p+1)^3 node box -- control points, a node table (equation, free
+//      nodes before the node, column start) and the pattern's line-offset
+//      rows -- staged by TMA; the control points are requested as soon as the
+//      previous element has read its own, the tables after its scatter;
+//   1. geometry at the Gauss points by sum factorisation of the homogeneous
+//      control net (w x, w y, w z, w) and of w g, w n (log-conductivity and
+//      source noise at the nodes): three contractions of (p+1) terms, FP32;
+//      Jacobian determinant and inverse in FP64 from exactly widened sums;
+//   2. operand rows T[a, 3q + k] = sqrt|kappa_q w_q| dR_a/dx_k (functions a,
+//      Gauss points q, directions k) in chunks of 32 points, so that the
+//      element matrix is K = s T T^T with the sign s of kappa w; elements
+//      whose weights change sign run one pass per sign (negate-A bit);
+//   3. K on the tensor cores in 3xTF32 split precision (M = 128 over the
+//      function rows, N = 32 or 64, K = 96 per chunk), FP32 accumulation in
+//      tensor memory; the element load vector Fe_a = sum_q R_a f_q w_q on the
+//      CUDA cores while the operand rows are formed;
+//   4. K from tensor memory to shared memory, then FP64 L2 reductions into the
+//      compressed-column matrix once every lower-colour neighbour (sharing a
+//      node: within p elements in each direction) has published its flag.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "ifemgpu_internal.h"
+#include "tc_common.cuh"
+
+namespace ifemgpu {
+
+using namespace tc;
+
+namespace {
+
+constexpr uint32_t kPoisFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wait
+
+template <int P>
+struct PCfg {
+  static constexpr int Q = P + 1;                  // functions and Gauss points per direction
+  static constexpr int Q2 = Q * Q;
+  static constexpr int NEN = Q * Q * Q;            // 27, 64
+  static constexpr int NQ = NEN;
+  static constexpr int ROWS = P == 2 ? 32 : 64;    // operand rows = MMA N = TMEM columns
+  static constexpr int SPLIT = 128 / ROWS;         // thread groups per operand row (4, 2)
+  static constexpr int CHUNKS = (NQ + 31) / 32;    // 32 Gauss points per operand chunk
+  static constexpr int PTS = 32 / SPLIT;           // points per thread and chunk (8, 16)
+  static constexpr int TILE = ROWS * kK;           // floats per 32-wide K tile
+  static constexpr int TFL = 3 * TILE;             // floats per chunk and copy (K = 96)
+  static constexpr int W = 2 * P + 1;              // line-table width
+  static constexpr int LINES = W * W;              // 25, 49
+  static constexpr int LPAD = (LINES + 3) & ~3;    // 28, 52: 16-byte rows for TMA
+  static constexpr int GS = NEN % 2 ? NEN : NEN + 1;  // odd Gram row stride (conflict-free)
+  static constexpr int NB = W * W * W;             // neighbourhood incl. the element
+  static constexpr int OVER = (128 - ROWS) * kK;   // floats the A operand reads past Tlo
+  static constexpr int PER_SM = P == 2 ? 5 : 3;    // CTAs per SM (shared memory)
+};
+
+template <int P>
+struct PSmem {
+  using C = PCfg<P>;
+  alignas(128) double ctrlT[C::NEN][4];    // control points x, y, z, w (TMA)
+  alignas(128) int nodeT[C::NEN][4];       // eq, F(node), colptr(eq - 1), 0 (TMA)
+  alignas(128) int lineT[C::NEN][C::LPAD]; // line-offset row of the node (TMA)
+  float X[C::NEN][4];                      // relative control points, weight
+  float fv[2][C::NEN];                     // log-conductivity and noise at the nodes
+  float tb[3][2][C::Q2];                   // 1D tables [direction][N, dN/du][g (p+1) + i]
+  float fePart[C::SPLIT][C::ROWS];         // element load vector, per point group
+  double c00[3];                           // first control point of the element
+  unsigned long long mbar, ctrlbar, tabbar;
+  uint32_t tmemSlot;
+  int fail;
+  int signs;                               // bit 0: some kappa w > 0, bit 1: some < 0
+  float dVf;                               // span volume / 8
+  // operand chunk (K-major core matrices, three 32-wide K tiles); before the
+  // MMAs the sum-factorisation arrays live here, after them the element matrix
+  alignas(1024) float Thi[C::TFL];
+  float Tlo[C::TFL];
+  // the MMA's A operand reads 128 rows from each tile start: rows ROWS..127
+  // of the last Tlo tile fall into this union, only feeding accumulator lanes
+  // that are never read; nothing writes it while an MMA runs
+  union {
+    struct {
+      float Wq[C::NQ][4];   // 1/W and dW/du_d
+      float Ji[C::NQ][9];   // column-major inverse Jacobian
+      float Cq[C::NQ][9];   // sqrt(max(s kappa w, 0)) Jinv of the current sign pass
+      float kw[C::NQ];      // kappa |J| w, signed (0 at singular points)
+      float fw[C::NQ];      // f |J| w
+    } pt;
+    float over[C::OVER];
+  } t;
+};
+
+static_assert(sizeof(PSmem<3>) + 1024 <= 233472 / 3, "three p = 3 CTAs per SM");
+static_assert(sizeof(PSmem<2>) + 1024 <= 233472 / 5, "five p = 2 CTAs per SM");
+static_assert(6 * 2 * 64 + 6 * 3 * 64 + 64 * 24 <= PCfg<3>::TFL &&
+                  6 * 2 * 27 + 6 * 3 * 27 + 27 * 24 <= PCfg<2>::TFL,
+              "sum-factorisation arrays fit in the operand tile");
+static_assert(PCfg<3>::NEN * PCfg<3>::GS <= PCfg<3>::TFL &&
+                  PCfg<2>::NEN * PCfg<2>::GS <= PCfg<2>::TFL,
+              "element matrix fits in the operand tile");
+
+}  // namespace
+
+struct PoisSys {
+  const double* c0;
+  double* K;
+  double* b;
+  int* flags;
+  unsigned long long* counters;  // [0] singular points, [2] device timeouts
+};
+
+template <int P>
+__global__ void __launch_bounds__(128)
+k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict__ items,
+                    int count, PoisSys S)
+{
+  using C = PCfg<P>;
+  constexpr int Q = C::Q, Q2 = C::Q2, Q3 = C::NEN;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  PSmem<P>& sm = *reinterpret_cast<PSmem<P>*>(smraw);
+  static_assert(offsetof(PSmem<P>, Tlo) == offsetof(PSmem<P>, Thi) + sizeof(float) * C::TFL &&
+                    offsetof(PSmem<P>, t) == offsetof(PSmem<P>, Tlo) + sizeof(float) * C::TFL,
+                "A-operand reads past Tlo must stay inside the union");
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t mbar = smemAddr(&sm.mbar), ctrlbar = smemAddr(&sm.ctrlbar),
+                 tabbar = smemAddr(&sm.tabbar);
+  if (tid == 0) {
+    mbarInit(mbar, 1);
+    mbarInit(ctrlbar, 1);
+    mbarInit(tabbar, 1);
+    sm.fail = 0;
+  }
+  if (warp == 0) tmemAlloc(&sm.tmemSlot, C::ROWS);
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = sm.tmemSlot;
+  const uint32_t tHi = smemAddr(sm.Thi), tLo = smemAddr(sm.Tlo);
+  uint32_t phase = 0;
+  int* pending = nullptr;  // done flag of the previous element (published at step 4)
+  int mapPatch = -1;
+  bool ctrlOut = false, tabOut = false;  // copies in flight (thread 0)
+  auto nodeBox = [&](int itn, const char*& tm, int& f1, int& f2, int& f3) {
+    const Item nx = items[itn];
+    const DevPatch& Pn = patches[nx.patch];
+    f1 = nx.elem % Pn.nel[0];
+    f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
+    f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
+    tm = static_cast<const char*>(Pn.tmaps);
+    if (nx.patch != mapPatch) {
+      tmapAcquire(tm);
+      tmapAcquire(tm + 128);
+      tmapAcquire(tm + 256);
+      mapPatch = nx.patch;
+    }
+  };
+  auto stageCtrl = [&](int itn) {
+    const char* tm;
+    int f1, f2, f3;
+    nodeBox(itn, tm, f1, f2, f3);
+    mbarExpectTx(ctrlbar, sizeof(double) * C::NEN * 4);
+    tmaLoad4d(smemAddr(sm.ctrlT), tm, 0, f1, f2, f3, ctrlbar);
+    ctrlOut = true;
+  };
+  auto stageTab = [&](int itn) {
+    const char* tm;
+    int f1, f2, f3;
+    nodeBox(itn, tm, f1, f2, f3);
+    mbarExpectTx(tabbar, sizeof(int) * C::NEN * (4 + C::LPAD));
+    tmaLoad4d(smemAddr(sm.nodeT), tm + 128, 0, f1, f2, f3, tabbar);
+    tmaLoad4d(smemAddr(sm.lineT), tm + 256, 0, f1, f2, f3, tabbar);
+    tabOut = true;
+  };
+  if (tid == 0 && (int)blockIdx.x < count) {
+    stageCtrl(blockIdx.x);
+    stageTab(blockIdx.x);
+  }
+  uint32_t cphase = 0, tphase = 0;
+
+  for (int it = blockIdx.x; it < count; it += gridDim.x) {
+    const Item item = items[it];
+    const DevPatch& Pt = patches[item.patch];
+    const int e = item.elem;
+    const int e1 = e % Pt.nel[0], e2 = (e / Pt.nel[0]) % Pt.nel[1], e3 = e / (Pt.nel[0] * Pt.nel[1]);
+    const bool hasG = Pt.logk != nullptr, hasN = Pt.noise != nullptr;
+
+    // ---- 0. node data (control points by TMA), nodal fields, 1D tables
+    if (mbarWait(ctrlbar, cphase)) {
+      cphase ^= 1u;
+      ctrlOut = false;
+    } else {
+      atomicAdd(S.counters + 2, 1ull);
+      sm.fail = 1;
+    }
+    if (tid < C::NEN) {
+      const int a = tid;
+      sm.X[a][0] = (float)(sm.ctrlT[a][0] - sm.ctrlT[0][0]);
+      sm.X[a][1] = (float)(sm.ctrlT[a][1] - sm.ctrlT[0][1]);
+      sm.X[a][2] = (float)(sm.ctrlT[a][2] - sm.ctrlT[0][2]);
+      sm.X[a][3] = (float)sm.ctrlT[a][3];
+      const int node = ((e3 + a / Q2) * Pt.n[1] + e2 + (a / Q) % Q) * Pt.n[0] + e1 + a % Q;
+      sm.fv[0][a] = hasG ? (float)Pt.logk[node] : 0.f;
+      sm.fv[1][a] = hasN ? (float)Pt.noise[node] : 0.f;
+    }
+    if (tid >= 64 && tid < 67) sm.c00[tid - 64] = sm.ctrlT[0][tid - 64];
+    if (tid == 96) sm.signs = 0;
+    if (tid == 97) sm.dVf = (float)(0.125 * Pt.span[0][e1] * Pt.span[1][e2] * Pt.span[2][e3]);
+    for (int t = tid; t < 6 * Q2; t += blockDim.x) {
+      const int d = t / (2 * Q2), dd = (t / Q2) % 2, gi = t % Q2;
+      const int ed = d == 0 ? e1 : d == 1 ? e2 : e3;
+      sm.tb[d][dd][gi] = (dd ? Pt.tabDf[d] : Pt.tabNf[d])[ed * Q2 + gi];
+    }
+    __syncthreads();  // ctrlT read, node data visible
+    if (sm.fail) break;
+    if (tid == 0 && it + (int)gridDim.x < count) stageCtrl(it + gridDim.x);
+
+    // ---- 1. sums over the element's functions at every Gauss point by sum
+    //         factorisation; fields 0..2: w x_r, 3: w, 4: w g, 5: w n
+    float* sA = sm.Thi;            // [6][N, D][k][j][gi]
+    float* sB = sA + 6 * 2 * Q3;   // [6][NN, DN, ND][k][gj][gi]
+    float* sP = sB + 6 * 3 * Q3;   // [q][6][value, d/du, d/dv, d/dw]
+    for (int t = tid; t < 6 * 2 * Q3; t += blockDim.x) {
+      const int gi = t % Q, j = (t / Q) % Q, k = (t / Q2) % Q, d0 = (t / Q3) % 2, f = t / (2 * Q3);
+      float acc = 0.f;
+#pragma unroll
+      for (int i = 0; i < Q; i++) {
+        const int a = i + Q * j + Q2 * k;
+        const float w = sm.X[a][3];
+        const float v = f < 3 ? w * sm.X[a][f] : f == 3 ? w : w * sm.fv[f - 4][a];
+        acc = fmaf(sm.tb[0][d0][gi * Q + i], v, acc);
+      }
+      sA[t] = acc;
+    }
+    __syncthreads();
+    for (int t = tid; t < 6 * 3 * Q3; t += blockDim.x) {
+      const int gi = t % Q, gj = (t / Q) % Q, k = (t / Q2) % Q, c = (t / Q3) % 3, f = t / (3 * Q3);
+      const int d0 = c == 1, d1 = c == 2;
+      float acc = 0.f;
+#pragma unroll
+      for (int j = 0; j < Q; j++)
+        acc = fmaf(sm.tb[1][d1][gj * Q + j], sA[(((f * 2 + d0) * Q + k) * Q + j) * Q + gi], acc);
+      sB[t] = acc;
+    }
+    __syncthreads();
+    for (int t = tid; t < C::NQ * 24; t += blockDim.x) {
+      const int c4 = t % 4, f = (t / 4) % 6, q = t / 24;
+      const int gi = q % Q, gj = (q / Q) % Q, gk = q / Q2;
+      const int c3 = c4 == 1 ? 1 : c4 == 2 ? 2 : 0, d2 = c4 == 3;
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k < Q; k++)
+        acc = fmaf(sm.tb[2][d2][gk * Q + k], sB[(((f * 3 + c3) * Q + k) * Q + gj) * Q + gi], acc);
+      sP[t] = acc;
+    }
+    __syncthreads();
+
+    // ---- 2. per Gauss point: Jacobian (FP64 determinant and inverse),
+    //         weight, conductivity kappa = kappa0 exp(sum R g), source
+    if (tid < C::NQ) {
+      const int q = tid;
+      const float* Pq = sP + q * 24;
+      const float iW = 1.f / Pq[12];
+      double J[9];  // J[d*3 + r] = dX_r/du_d, formed in FP32 and widened exactly
+      for (int r = 0; r < 3; r++) {
+        const float Xr = Pq[r * 4] * iW;
+        for (int d = 0; d < 3; d++)
+          J[d * 3 + r] = widenF32((Pq[r * 4 + 1 + d] - Xr * Pq[12 + 1 + d]) * iW);
+      }
+      const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[1] * J[8] - J[2] * J[7],
+                   c2 = J[1] * J[5] - J[2] * J[4];
+      const double det = J[0] * c0 - J[3] * c1 + J[6] * c2;
+      float w = 0.f;
+      float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (fabs(det) > kEpsZ) {
+        const double id = 1.0 / det;
+        B[0] = (float)(c0 * id);
+        B[1] = (float)(-c1 * id);
+        B[2] = (float)(c2 * id);
+        B[3] = (float)(-(J[3] * J[8] - J[5] * J[6]) * id);
+        B[4] = (float)((J[0] * J[8] - J[2] * J[6]) * id);
+        B[5] = (float)(-(J[0] * J[5] - J[2] * J[3]) * id);
+        B[6] = (float)((J[3] * J[7] - J[4] * J[6]) * id);
+        B[7] = (float)(-(J[0] * J[7] - J[1] * J[6]) * id);
+        B[8] = (float)((J[0] * J[4] - J[1] * J[3]) * id);
+        w = (float)det * sm.dVf * Pt.gwf[0][q % Q] * Pt.gwf[1][(q / Q) % Q] * Pt.gwf[2][q / Q2];
+      } else {
+        atomicAdd(S.counters, 1ull);
+      }
+      float kap = (float)Pt.kappa;
+      if (hasG) kap *= expf(Pq[16] * iW);
+      float f = (float)Pt.source;
+      if (Pt.source_shape == IFEMGPU_SOURCE_SINE)
+        for (int c = 0; c < 3; c++) f *= sinpif((float)((double)(Pq[c * 4] * iW) + sm.c00[c]));
+      if (hasN) f *= 1.f + Pq[20] * iW;
+      const float kw = kap * w;
+      if (kw != 0.f) atomicOr(&sm.signs, kw > 0.f ? 1 : 2);
+      sm.t.pt.kw[q] = kw;
+      sm.t.pt.fw[q] = f * w;
+      sm.t.pt.Wq[q][0] = iW;
+      sm.t.pt.Wq[q][1] = Pq[13];
+      sm.t.pt.Wq[q][2] = Pq[14];
+      sm.t.pt.Wq[q][3] = Pq[15];
+      for (int c = 0; c < 9; c++) sm.t.pt.Ji[q][c] = B[c];
+    }
+    __syncthreads();
+
+    // ---- 3. operand rows and the tensor-core Gram matrix, one pass per sign
+    const int signs = sm.signs;
+    const int ra = tid % C::ROWS, hg = tid / C::ROWS;  // operand row, point group
+    bool first = true, ok = true;
+    float fe = 0.f;
+    bool feDone = false;
+    for (int pass = 0; pass < 2 && ok; pass++) {
+      if (!(signs & (1 << pass))) continue;
+      const float s = pass == 0 ? 1.f : -1.f;
+      if (tid < C::NQ) {
+        const float ws = s * sm.t.pt.kw[tid];
+        const float sw = ws > 0.f ? sqrtf(ws) : 0.f;
+#pragma unroll
+        for (int c = 0; c < 9; c++) sm.t.pt.Cq[tid][c] = sw * sm.t.pt.Ji[tid][c];
+      }
+      __syncthreads();
+      for (int ch = 0; ch < C::CHUNKS && ok; ch++) {
+        if (ch > 0) {  // the previous chunk's MMAs must have read the tiles
+          ok = mbarWait(mbar, phase);
+          phase ^= 1u;
+          tcFenceAfter();
+          if (!ok) break;
+        }
+        if (ra < C::NEN) {
+          const int i = ra % Q, j = (ra / Q) % Q, k = ra / Q2;
+          const float wa = sm.X[ra][3];
+#pragma unroll 1
+          for (int g4 = 0; g4 < C::PTS / 4; g4++) {
+            float hi[12], lo[12];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const int q = ch * 32 + hg * C::PTS + g4 * 4 + u;
+              float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+              if (q < C::NQ) {
+                const int gi = q % Q, gj = (q / Q) % Q, gk = q / Q2;
+                const float n0 = sm.tb[0][0][gi * Q + i], d0 = sm.tb[0][1][gi * Q + i];
+                const float n1 = sm.tb[1][0][gj * Q + j], d1 = sm.tb[1][1][gj * Q + j];
+                const float n2 = sm.tb[2][0][gk * Q + k], d2 = sm.tb[2][1][gk * Q + k];
+                const float* Wq = sm.t.pt.Wq[q];
+                const float w12 = wa * n1 * n2;
+                const float R = w12 * n0 * Wq[0];
+                const float du = (w12 * d0 - R * Wq[1]) * Wq[0];
+                const float dv = (wa * n0 * d1 * n2 - R * Wq[2]) * Wq[0];
+                const float dw = (wa * n0 * n1 * d2 - R * Wq[3]) * Wq[0];
+                const float* Cq = sm.t.pt.Cq[q];
+                t0 = du * Cq[0] + dv * Cq[1] + dw * Cq[2];
+                t1 = du * Cq[3] + dv * Cq[4] + dw * Cq[5];
+                t2 = du * Cq[6] + dv * Cq[7] + dw * Cq[8];
+                if (!feDone) fe = fmaf(R, sm.t.pt.fw[q], fe);
+              }
+              splitTF32(t0, hi[3 * u], lo[3 * u]);
+              splitTF32(t1, hi[3 * u + 1], lo[3 * u + 1]);
+              splitTF32(t2, hi[3 * u + 2], lo[3 * u + 2]);
+            }
+#pragma unroll
+            for (int v = 0; v < 3; v++) {
+              const int kk = 3 * (hg * C::PTS + 4 * g4) + 4 * v;  // K index within the chunk
+              const int o = (kk >> 5) * C::TILE + kmaj(ra, kk & 31);
+              *reinterpret_cast<float4*>(sm.Thi + o) =
+                  make_float4(hi[4 * v], hi[4 * v + 1], hi[4 * v + 2], hi[4 * v + 3]);
+              *reinterpret_cast<float4*>(sm.Tlo + o) =
+                  make_float4(lo[4 * v], lo[4 * v + 1], lo[4 * v + 2], lo[4 * v + 3]);
+            }
+          }
+        }
+        fenceProxyAsync();
+        __syncthreads();
+        if (tid == 0) {
+          tcFenceAfter();
+          const uint32_t idesc = instrDescTF32(128, C::ROWS) | (s < 0.f ? (1u << 13) : 0u);
+          for (int t3 = 0; t3 < 3; t3++)
+            for (int st = 0; st < kK / 8; st++) {
+              const uint32_t off = (uint32_t)(t3 * C::TILE) * 4u + st * 256u;
+              mmaTF32(tmem, smemDesc(tHi + off), smemDesc(tHi + off), idesc, first ? 0u : 1u);
+              mmaTF32(tmem, smemDesc(tHi + off), smemDesc(tLo + off), idesc, 1);
+              mmaTF32(tmem, smemDesc(tLo + off), smemDesc(tHi + off), idesc, 1);
+              first = false;
+            }
+          mmaCommit(mbar);
+        }
+        first = false;
+      }
+      feDone = true;
+      if (ok) {
+        ok = mbarWait(mbar, phase);
+        phase ^= 1u;
+        tcFenceAfter();
+      }
+    }
+    if (ra < C::NEN) sm.fePart[hg][ra] = fe;
+    if (!ok) sm.fail = 1;
+    __syncthreads();  // every MMA complete: the operand tile becomes the element matrix
+    if (sm.fail) {
+      if (tid == 0) atomicAdd(S.counters + 2, 1ull);
+      break;
+    }
+
+    // ---- 4. tensor memory -> element matrix G in shared memory
+    float* G = sm.Thi;
+    if (signs && warp < C::ROWS / 32) {
+      float v[16];
+      const int m = 32 * warp + lane;
+#pragma unroll
+      for (int c16 = 0; c16 < C::ROWS / 16; c16++) {
+        tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
+        if (m < C::NEN) {
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            const int n = 16 * c16 + i;
+            if (n < C::NEN) G[m * C::GS + n] = v[i];
+          }
+        }
+      }
+    } else if (!signs) {
+      for (int i = tid; i < C::NEN * C::GS; i += blockDim.x) G[i] = 0.f;
+    }
+    tcFenceBefore();
+
+    // publish the previous element, then wait for the lower-colour neighbours
+    if (tid == 0 && pending) {
+      __threadfence();
+      storeRelease(pending, 1);
+      pending = nullptr;
+    }
+    const int myc = e1 % Q + Q * (e2 % Q) + Q2 * (e3 % Q);
+    for (int t = tid; t < C::NB; t += blockDim.x) {
+      const int dx = t % C::W - P, dy = (t / C::W) % C::W - P, dz = t / (C::W * C::W) - P;
+      const int f1 = e1 + dx, f2 = e2 + dy, f3 = e3 + dz;
+      if ((dx | dy | dz) == 0 || f1 < 0 || f1 >= Pt.nel[0] || f2 < 0 || f2 >= Pt.nel[1] ||
+          f3 < 0 || f3 >= Pt.nel[2])
+        continue;
+      if (f1 % Q + Q * (f2 % Q) + Q2 * (f3 % Q) >= myc) continue;
+      const int* flag = S.flags + Pt.flagBase + (f3 * Pt.nel[1] + f2) * Pt.nel[0] + f1;
+      uint32_t spin = 0;
+      while (loadRelaxed(flag) == 0) {
+        if (++spin > kPoisFlagSpin) {
+          atomicAdd(S.counters + 2, 1ull);
+          break;
+        }
+        __nanosleep(64);
+      }
+      fenceAcquire();
+    }
+    if (mbarWait(tabbar, tphase)) {
+      tphase ^= 1u;
+      tabOut = false;
+    } else {
+      atomicAdd(S.counters + 2, 1ull);
+      sm.fail = 1;
+    }
+    __syncthreads();
+    if (sm.fail) break;
+
+    // ---- 5. FP64 reductions: row a per lane (consecutive rows of a column
+    //         are consecutive entries), a share of the columns per thread group
+    if (ra < C::NEN && sm.nodeT[ra][0] > 0) {
+      const int base = sm.nodeT[ra][1];
+      const int rowLine = (ra / Q2 + P) * C::W + (ra / Q) % Q + P;
+      const float* Grow = G + ra * C::GS;
+      const int b0 = hg * C::NEN / C::SPLIT, b1 = (hg + 1) * C::NEN / C::SPLIT;
+#pragma unroll 4
+      for (int bn = b0; bn < b1; bn++) {
+        if (sm.nodeT[bn][0] <= 0) continue;
+        const int off = sm.lineT[bn][rowLine - (bn / Q2) * C::W - (bn / Q) % Q] + base;
+        // the upper triangle for both halves: an exactly symmetric element
+        // matrix (the MMA's FP32 sums of G_ab and G_ba need not agree)
+        const float g = bn >= ra ? Grow[bn] : G[bn * C::GS + ra];
+        redAdd(S.K + sm.nodeT[bn][2] + off, widenF32(g));
+      }
+    }
+    // right-hand side: load vector minus prescribed-DOF terms
+    if (tid < C::NEN) {
+      const int r = sm.nodeT[tid][0];
+      if (r > 0) {
+        float fs = 0.f;
+#pragma unroll
+        for (int g = 0; g < C::SPLIT; g++) fs += sm.fePart[g][tid];
+        double acc = widenF32(fs);
+        if (S.c0) {
+          for (int bn = 0; bn < C::NEN; bn++) {
+            const int ce = sm.nodeT[bn][0];
+            if (ce < 0)
+              acc -= S.c0[-ce - 1] * widenF32(bn >= tid ? G[tid * C::GS + bn] : G[bn * C::GS + tid]);
+          }
+        }
+        if (acc != 0.0) redAdd(S.b + r - 1, acc);
+      }
+    }
+
+    // ---- 6. reductions issued; the flag is published at the next element
+    __syncthreads();
+    if (tid == 0) {
+      pending = S.flags + Pt.flagBase + e;
+      if (it + (int)gridDim.x < count) stageTab(it + gridDim.x);  // node tables are free now
+    }
+  }
+  if (tid == 0) {
+    if (pending) {
+      __threadfence();
+      storeRelease(pending, 1);
+    }
+    // after a timeout: copies still in flight land before the CTA exits
+    if (ctrlOut) mbarWait(ctrlbar, cphase);
+    if (tabOut) mbarWait(tabbar, tphase);
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (warp == 0) tmemDealloc(tmem, C::ROWS);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+int tcPoissonDegree(const DevPatch& D, const HostPatch& pc)
+{
+  if (D.dim != 3 || D.kind != IFEMGPU_POISSON || D.npv != 1 || D.mass != 0.0 || !D.lineOff ||
+      !pc.neumann.empty() || !D.tabNf[0] || !D.tabNf[1] || !D.tabNf[2])
+    return 0;
+  const int p = D.p[0];
+  if ((p != 2 && p != 3) || D.p[1] != p || D.p[2] != p) return 0;
+  for (int d = 0; d < 3; d++)
+    if (D.ng[d] != p + 1 || D.n[d] != D.nel[d] + p) return 0;
+  return p;
+}
+
+size_t tcPoissonSmem(int deg) { return deg == 2 ? sizeof(PSmem<2>) : sizeof(PSmem<3>); }
+
+// node table (eq, F, column start), padded line-offset rows and the three
+// tensor maps of a patch; false leaves the patch to the generic kernel
+bool tcPoissonUpload(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D, int deg)
+{
+  const int lines = (2 * deg + 1) * (2 * deg + 1), lpad = (lines + 3) & ~3;
+  if (pc.lineOff.size() != (size_t)pc.nnod * lines || !pc.d_ctrl) return false;
+  std::vector<int> nodeT((size_t)pc.nnod * 4, 0), lineT((size_t)pc.nnod * lpad, 0);
+  for (int n = 0; n < pc.nnod; n++) {
+    const int g = pc.mlgn[n];
+    const int q = ctx->meqn[ctx->madof[g] - 1];
+    nodeT[(size_t)n * 4] = q;
+    nodeT[(size_t)n * 4 + 1] = ctx->freeBefore[g];
+    nodeT[(size_t)n * 4 + 2] = q > 0 ? ctx->colptr[q - 1] : 0;
+    for (int t = 0; t < lines; t++) lineT[(size_t)n * lpad + t] = pc.lineOff[(size_t)n * lines + t];
+  }
+  auto put = [&](auto** dst, const auto* src, size_t bytes) {
+    return cudaMalloc((void**)dst, bytes) == cudaSuccess &&
+           cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  unsigned char maps[3][128];
+  const bool ok = put(&pc.d_nodeTab, nodeT.data(), sizeof(int) * nodeT.size()) &&
+                  put(&pc.d_lineTab, lineT.data(), sizeof(int) * lineT.size()) &&
+                  nodeBoxMap(maps[0], 8, (void*)pc.d_ctrl, 4, pc.n, deg + 1) &&
+                  nodeBoxMap(maps[1], 4, pc.d_nodeTab, 4, pc.n, deg + 1) &&
+                  nodeBoxMap(maps[2], 4, pc.d_lineTab, lpad, pc.n, deg + 1) &&
+                  put(&pc.d_tmaps, maps, sizeof(maps));
+  if (!ok) {
+    cudaGetLastError();
+    return false;
+  }
+  D.tmaps = pc.d_tmaps;
+  return true;
+}
+
+ifemgpu_status tcPoissonPrepare(ifemgpu_ctx* ctx)
+{
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_tc_poisson<2>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(PSmem<2>)));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_tc_poisson<3>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(PSmem<3>)));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_tc_poisson<2>,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_volume_tc_poisson<3>,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status tcPoissonLaunch(ifemgpu_ctx* ctx, const Pass& p, int deg)
+{
+  if (deg != 2 && deg != 3) return setError(ctx, IFEMGPU_INVALID_ARG, "internal: Poisson kernel degree");
+  PoisSys S{ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_K, ctx->d_b, ctx->d_flags, ctx->d_counters};
+  const void* fn = deg == 2 ? (const void*)k_volume_tc_poisson<2> : (const void*)k_volume_tc_poisson<3>;
+  const size_t smem = tcPoissonSmem(deg);
+  const int cap = deg == 2 ? PCfg<2>::PER_SM : PCfg<3>::PER_SM;
+  // every CTA must be resident (they wait on each other's done flags): the
+  // grid follows the SM's shared memory and registers; should residency ever
+  // fail, the bounded waits end with a reported device timeout
+  cudaFuncAttributes fa{};
+  IFEMGPU_CUDA(ctx, cudaFuncGetAttributes(&fa, fn));
+  int smemSM = 0, resv = 0, regsSM = 0;
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                           ctx->opts.device));
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock,
+                                           ctx->opts.device));
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&regsSM, cudaDevAttrMaxRegistersPerMultiprocessor,
+                                           ctx->opts.device));
+  const int bySmem = smemSM / (int)(smem + resv);
+  const int byRegs = regsSM / (((fa.numRegs + 7) / 8) * 8 * 128);
+  const int perSM = std::max(1, std::min(std::min(bySmem, byRegs), cap));
+  const int grid = std::min(p.count, perSM * ctx->numSMs);
+  if (ctx->opts.verbose)
+    std::printf("tensor-core Poisson kernel p=%d: %zu B shared memory, %d registers, %d blocks/SM, grid %d\n",
+                deg, smem, fa.numRegs, perSM, grid);
+  const DevPatch* patches = ctx->d_patches;
+  const Item* items = ctx->d_items + p.first;
+  int count = p.count;
+  void* args[] = {(void*)&patches, (void*)&items, (void*)&count, (void*)&S};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cfg.numAttrs = 0;
+  IFEMGPU_CUDA(ctx, cudaLaunchKernelExC(&cfg, fn, args));
+  return IFEMGPU_OK;
+}
+
+}  // namespace ifemgpu

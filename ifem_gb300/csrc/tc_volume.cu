@@ -110,30 +110,6 @@ __device__ __forceinline__ Scratch scratch(TcSmem& sm)
   return Scratch{b, b + 27 * 16, b + 27 * 16 + 27 * 9, b + 27 * 16 + 27 * 13};
 }
 
-__device__ __forceinline__ void redAdd(double* p, double v)
-{
-  atomicAdd(p, v);  // result unused: compiles to an L2 reduction
-}
-
-// neighbour flags are polled with relaxed loads (served by L2); a thread that
-// saw one issues a single acquire fence before the block's scatter
-__device__ __forceinline__ int loadRelaxed(const int* p)
-{
-  int v;
-  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void fenceAcquire()
-{
-  asm volatile("fence.acq_rel.gpu;" : : : "memory");
-}
-
-__device__ __forceinline__ void storeRelease(int* p, int v)
-{
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
-}
-
 }  // namespace
 
 struct TcSys {
@@ -504,16 +480,23 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
 
     // ---- 7. tensor memory -> compact Gram matrix in shared memory
     if (ok && warp < 3 && signs) {
+      // row r = 3a + k of G keeps its entries c >= r and mirrors them into
+      // column r: an exactly symmetric G (the MMA's FP32 sums of G_rc and
+      // G_cr need not agree), hence an exactly symmetric element matrix
       float v[16];
-      float* grow = sm.u.Gc + (3 * lane + warp) * kGs;
+      const int r = 3 * lane + warp;
+      float* grow = sm.u.Gc + r * kGs;
 #pragma unroll
       for (int c16 = 0; c16 < kN / 16; c16++) {
         tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
         if (lane < kNen) {
 #pragma unroll
           for (int i = 0; i < 16; i++) {
-            const int n = 16 * c16 + i, l = n >> 5, bcol = n & 31;
-            if (bcol < kNen) grow[3 * bcol + l] = v[i];
+            const int n = 16 * c16 + i, l = n >> 5, bcol = n & 31, c = 3 * bcol + l;
+            if (bcol < kNen && c >= r) {
+              grow[c] = v[i];
+              sm.u.Gc[c * kGs + r] = v[i];
+            }
           }
         }
       }
@@ -722,25 +705,29 @@ EncodeTiledFn encodeTiled()
   return fn;
 }
 
-// Tensor map of a node-major array with `inner` values of `esize` bytes per
-// node of an n0 x n1 x n2 control net; boxes of inner x 3 x 3 x 3 (one
-// element's nodes for p = 2).  Row pitches are multiples of 16 bytes.
-bool nodeBoxMap(CUtensorMap* m, CUtensorMapDataType type, size_t esize, void* base, int inner,
-                const int n[3])
+}  // namespace
+
+// Tensor map (128 bytes at out) of a node-major array with `inner` values of
+// `esize` bytes (4: INT32, 8: FLOAT64) per node of an n0 x n1 x n2 control
+// net; boxes of inner x q x q x q (one element's nodes for degree q - 1).
+// Row pitches and the inner extent are multiples of 16 bytes.
+bool nodeBoxMap(void* out, size_t esize, void* base, int inner, const int n[3], int q)
 {
   const EncodeTiledFn enc = encodeTiled();
-  if (!enc || (esize * inner) % 16 != 0 || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  if (!enc || (esize * inner) % 16 != 0 || reinterpret_cast<uintptr_t>(base) % 16 != 0 ||
+      (esize != 4 && esize != 8) || q < 1 || q > 8)
+    return false;
+  const CUtensorMapDataType type =
+      esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_INT32;
   const cuuint64_t dims[4] = {(cuuint64_t)inner, (cuuint64_t)n[0], (cuuint64_t)n[1], (cuuint64_t)n[2]};
   const cuuint64_t strides[3] = {esize * inner, esize * inner * n[0],
                                  esize * inner * (cuuint64_t)n[0] * n[1]};
-  const cuuint32_t box[4] = {(cuuint32_t)inner, 3, 3, 3};
+  const cuuint32_t box[4] = {(cuuint32_t)inner, (cuuint32_t)q, (cuuint32_t)q, (cuuint32_t)q};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
-  return enc(m, type, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return enc(static_cast<CUtensorMap*>(out), type, 4, base, dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
-
-}  // namespace
 
 // Node table, padded line-offset rows and the three tensor maps of a
 // tensor-core patch; false leaves the patch to the generic kernel.
@@ -765,9 +752,9 @@ bool tcUploadPatch(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D)
   CUtensorMap maps[3];
   const bool ok = put(&pc.d_nodeTab, nodeT.data(), sizeof(int) * nodeT.size()) &&
                   put(&pc.d_lineTab, lineT.data(), sizeof(int) * lineT.size()) &&
-                  nodeBoxMap(&maps[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, pc.d_ctrl, 4, pc.n) &&
-                  nodeBoxMap(&maps[1], CU_TENSOR_MAP_DATA_TYPE_INT32, 4, pc.d_nodeTab, 8, pc.n) &&
-                  nodeBoxMap(&maps[2], CU_TENSOR_MAP_DATA_TYPE_INT32, 4, pc.d_lineTab, 28, pc.n) &&
+                  nodeBoxMap(&maps[0], 8, (void*)pc.d_ctrl, 4, pc.n, 3) &&
+                  nodeBoxMap(&maps[1], 4, pc.d_nodeTab, 8, pc.n, 3) &&
+                  nodeBoxMap(&maps[2], 4, pc.d_lineTab, 28, pc.n, 3) &&
                   put(&pc.d_tmaps, maps, sizeof(maps));
   if (!ok) {
     cudaGetLastError();

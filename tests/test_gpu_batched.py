@@ -1,8 +1,9 @@
 """Batched multi-patch assembly (64 independent patches of uneven size and
 degree, Poisson and elasticity integrands): one system per integrand type,
 as two IFEM simulators would number them, each assembled by one persistent
-colour-major launch of the generic element kernel (plus the tensor-core
-launch for its p = 2 elasticity patches).
+colour-major launch of the generic element kernel, or in split precision one
+launch per tensor-core kernel (p = 2 elasticity, p = 2 and p = 3 Poisson)
+plus the generic launch for the rest.
 
 - FP64 mode against the oracle (relative 1e-12);
 - the persistent launch gives the same bits as one launch per colour (the
@@ -65,7 +66,10 @@ def test_persistent_launch_equals_colour_passes(gpulib, ke, kind):
     assert np.array_equal(s1.matrix_values(), K1) and np.array_equal(s1.rhs(), b1)
     s1.assembly_stats()
     s2.assembly_stats()
-    assert s1.kernel_launches < s2.kernel_launches
+    if ke == G.KE_SPLIT_TF32 and kind == 1:  # every patch on the tensor-core Poisson kernels
+        assert s1.kernel_launches == s2.kernel_launches
+    else:
+        assert s1.kernel_launches < s2.kernel_launches
 
 
 def test_block_csr_copy(gpulib):

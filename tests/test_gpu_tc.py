@@ -68,6 +68,7 @@ def test_split_elasticity_vs_oracle(gpulib, oracle_lib, nel):
     assert np.abs(b - bo).max() / np.abs(bo).max() < TC_TOL
     _, _, singular = sim.assembly_stats()
     assert singular == 0
+    assert_exactly_symmetric(sim, K)
 
 
 def test_split_assembly_deterministic(gpulib):
@@ -83,6 +84,15 @@ def test_split_assembly_solves_to_fp64_residual(gpulib):
     sim, K, b = assemble(patches, ng, G.KE_SPLIT_TF32)
     x, info = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10)
     assert info.relres <= 1e-10
+
+
+def assert_exactly_symmetric(sim, K):
+    """IFEM's element matrices are symmetric bit for bit, and the solvers
+    take the compressed-column arrays row-wise: so must ours be."""
+    import scipy.sparse as sp
+    sam = sim.getSAM()
+    A = sp.csc_matrix((K, sam.rowidx, sam.colptr), shape=(sim.sizes.neq,) * 2)
+    assert (A - A.T).count_nonzero() == 0 or abs(A - A.T).max() == 0.0
 
 
 def split_vs_oracle(patches, ng, tol=TC_TOL):
@@ -106,6 +116,43 @@ def test_split_poisson2d_config1(gpulib, oracle_lib):
 
 def test_split_poisson3d_p3_kappa_field(gpulib, oracle_lib):
     split_vs_oracle(*W.config4(nel=6, grid=16))
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_split_poisson3d_tensor_core_kernel(gpulib, oracle_lib, p):
+    """p = 2 and 3 Poisson patches run on the tensor-core Poisson kernel:
+    rational geometry, log-conductivity field, sine source with nodal noise
+    and a prescribed non-zero face value (right-hand side corrections), even
+    with colour passes forced for the generic kernel (one volume launch)."""
+    import oracle
+    rng = np.random.default_rng(77 + p)
+    pc = W.perturb(W.box_patch(3, p, 5), rng, 0.1)
+    pc.kind = 1
+    pc.source, pc.source_shape = 2.0, 1
+    pc.noise = 0.1 * rng.standard_normal(pc.nnod)
+    pc.log_kappa = W.gaussian_field_3d(rng, pc.coefs[:, :3], grid=16)
+    pc.dirichlet = [(1, 1, 0.5), (2, 1, 0.0), (5, 1, 0.0)]
+    sim = G.SIM(n_gauss=0, ke_precision=G.KE_SPLIT_TF32, colour_passes=1)
+    W.load_into(sim, [pc])
+    sim.preprocess()
+    sim.assembleSystem()
+    K, b = sim.matrix_values(), sim.rhs()
+    orc = oracle.OracleModel(0)
+    W.load_into(orc, [pc])
+    orc.preprocess()
+    orc.assemble(8)
+    Ko, bo = orc.system()
+    scale = np.abs(Ko).max()
+    assert np.abs(K - Ko).max() / scale < TC_TOL
+    big = np.abs(Ko) > 1e-3 * scale
+    assert (np.abs(K[big] - Ko[big]) / np.abs(Ko[big])).max() < 1e-4
+    assert np.abs(b - bo).max() / np.abs(bo).max() < TC_TOL
+    _, _, singular = sim.assembly_stats()
+    assert singular == 0
+    assert sim.kernel_launches <= 4     # basis tables + one element launch (not p^3 colours)
+    assert_exactly_symmetric(sim, K)
+    sim.assembleSystem()
+    assert np.array_equal(sim.matrix_values(), K) and np.array_equal(sim.rhs(), b)
 
 
 def test_split_multipatch_mixed(gpulib, oracle_lib):
