@@ -532,6 +532,14 @@ void ifemgpu_ctx_destroy(ifemgpu_ctx* ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     freeDevice(ctx);
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+    if (ctx->copyStream) {
+      cudaStreamSynchronize(ctx->copyStream);
+      cudaStreamDestroy(ctx->copyStream);
+    }
+    if (ctx->snapDone) cudaEventDestroy(ctx->snapDone);
+    if (ctx->copyDone) cudaEventDestroy(ctx->copyDone);
+    if (ctx->d_Ksnap) cudaFree(ctx->d_Ksnap);
+    if (ctx->d_bsnap) cudaFree(ctx->d_bsnap);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;
@@ -810,6 +818,44 @@ ifemgpu_status ifemgpu_copy_matrix(ifemgpu_ctx* ctx, double* values)
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(values, ctx->d_K, sizeof(double) * ctx->nnz,
                                     cudaMemcpyDeviceToHost, ctx->stream));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_copy_system_async(ifemgpu_ctx* ctx, double* values, double* rhs)
+{
+  if (!ctx || !values) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  if (!ctx->copyStream) {
+    IFEMGPU_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copyStream, cudaStreamNonBlocking));
+    IFEMGPU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->snapDone, cudaEventDisableTiming));
+    IFEMGPU_CUDA(ctx, cudaEventCreateWithFlags(&ctx->copyDone, cudaEventDisableTiming));
+    IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_Ksnap, sizeof(double) * std::max<int64_t>(ctx->nnz, 1)));
+    IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_bsnap, sizeof(double) * std::max(ctx->neq, 1)));
+    IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->copyDone, ctx->copyStream));
+  }
+  // the snapshot is overwritten only after the previous copy has drained it
+  IFEMGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copyDone, 0));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->d_Ksnap, ctx->d_K, sizeof(double) * ctx->nnz,
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+  if (rhs)
+    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->d_bsnap, ctx->d_b, sizeof(double) * ctx->neq,
+                                      cudaMemcpyDeviceToDevice, ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->snapDone, ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaStreamWaitEvent(ctx->copyStream, ctx->snapDone, 0));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(values, ctx->d_Ksnap, sizeof(double) * ctx->nnz,
+                                    cudaMemcpyDeviceToHost, ctx->copyStream));
+  if (rhs)
+    IFEMGPU_CUDA(ctx, cudaMemcpyAsync(rhs, ctx->d_bsnap, sizeof(double) * ctx->neq,
+                                      cudaMemcpyDeviceToHost, ctx->copyStream));
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->copyDone, ctx->copyStream));
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_copy_wait(ifemgpu_ctx* ctx)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (ctx->copyStream) IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->copyStream));
   return IFEMGPU_OK;
 }
 

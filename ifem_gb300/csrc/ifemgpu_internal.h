@@ -235,6 +235,11 @@ struct ifemgpu_ctx {
   int learnGen = 0;              // bumped by every setup
   int fieldVersion = 0;          // bumped by every field update
   double* d_rhsAlt = nullptr;    // right-hand side of a collecting solve (neq)
+  // asynchronous system copies: device snapshot, copy stream, events
+  double* d_Ksnap = nullptr;
+  double* d_bsnap = nullptr;
+  cudaStream_t copyStream = nullptr;
+  cudaEvent_t snapDone = nullptr, copyDone = nullptr;
   // solution norms and secondary solution (norms.cu): every active element
   // in patch order, its output slot in Item::bc
   ifemgpu::Item* d_normItems = nullptr;

@@ -72,6 +72,7 @@ EXPORTS = [
     "ifemgpu_get_sizes", "ifemgpu_get_madof", "ifemgpu_get_meqn", "ifemgpu_get_mnpc",
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
     "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_solve",
+    "ifemgpu_copy_system_async", "ifemgpu_copy_wait",
     "ifemgpu_expand_solution", "ifemgpu_patch_update_coefs", "ifemgpu_get_stream",
     "ifemgpu_selftest_tc_gemm", "ifemgpu_solve_noalloc", "ifemgpu_learn_setup",
     "ifemgpu_learn_collect", "ifemgpu_learn_clear", "ifemgpu_learn_set_target", "ifemgpu_learn_train",
@@ -138,6 +139,8 @@ def load_library(path: str | None = None):
         "ifemgpu_learn_collect": (I, [P, V, V, I, I, D, I, C.POINTER(I)]),
         "ifemgpu_learn_clear": (I, [P]),
         "ifemgpu_learn_set_target": (I, [P, I]),
+        "ifemgpu_copy_system_async": (I, [P, V, V]),
+        "ifemgpu_copy_wait": (I, [P]),
         "ifemgpu_learn_get_pairs": (I, [P, I, I, V, V]),
         "ifemgpu_apply_preconditioner": (I, [P, I, V, V]),
         "ifemgpu_copy_matrix_bsr": (I, [P, I, C.POINTER(I), C.POINTER(C.c_int64), V, V, V]),
@@ -393,6 +396,17 @@ class SIM:
     def copy_rhs_into(self, out: np.ndarray):
         assert out.dtype == np.float64 and out.size >= self.sizes.neq
         self._check(self.lib.ifemgpu_copy_rhs(self.ctx, _ptr(out)))
+
+    def copy_system_async(self, values: np.ndarray, rhs: np.ndarray | None = None):
+        """Snapshot K (and b) and copy them to the host buffers on the copy
+        stream; the buffers must stay alive and untouched until copy_wait()."""
+        assert values.dtype == np.float64 and values.size >= self.sizes.nnz
+        assert rhs is None or (rhs.dtype == np.float64 and rhs.size >= self.sizes.neq)
+        self._check(self.lib.ifemgpu_copy_system_async(self.ctx, _ptr(values),
+                                                       None if rhs is None else _ptr(rhs)))
+
+    def copy_wait(self):
+        self._check(self.lib.ifemgpu_copy_wait(self.ctx))
 
     def solveSystem(self, method=PCG_MIXED, rtol=1e-10, max_outer=20, max_inner=20000,
                     inner_rtol=1e-4, check=True, precond=PRECOND_JACOBI):

@@ -237,6 +237,17 @@ ifemgpu_status ifemgpu_assemble(ifemgpu_ctx* ctx, int sync);
 ifemgpu_status ifemgpu_copy_matrix(ifemgpu_ctx* ctx, double* values);
 ifemgpu_status ifemgpu_copy_rhs(ifemgpu_ctx* ctx, double* rhs);
 
+/* The same copies without waiting: the matrix values and the right-hand side
+ * (rhs may be null) are snapshotted on the device, stream-ordered after the
+ * last assembly, and copied to the host buffers on a copy stream, so the
+ * next ifemgpu_assemble runs while the copy proceeds (pinned host memory
+ * lets the two overlap).  The buffers must stay untouched until
+ * ifemgpu_copy_wait returns; copies complete in the order they were made.
+ * A time loop that hands every step's system to the host this way runs at
+ * the pace of the slower of assembly and copy instead of their sum.       */
+ifemgpu_status ifemgpu_copy_system_async(ifemgpu_ctx* ctx, double* values, double* rhs);
+ifemgpu_status ifemgpu_copy_wait(ifemgpu_ctx* ctx);
+
 /* Text dumps of the system in the formats of SparseMatrix::dump and
  * StdVector::dump (src/LinAlg/SparseMatrix.C:341-396, SystemMatrix.C:78-102)
  * as SIMbase::dumpEqSys writes them (src/SIM/SIMbase.C:2863-2925): precision

@@ -125,3 +125,54 @@ def test_singular_points_are_counted_and_skipped(gpulib, oracle_lib):
     _, _, singular = sim.assembly_stats()
     assert singular == 9 * 9
     assert not K.any() and not b.any() and not Ko.any()
+
+
+def test_matrix_copy_into_pinned_and_pageable_memory(gpulib):
+    """ifemgpu_copy_matrix into pinned and pageable host memory, aligned or
+    not: the same bits."""
+    torch = pytest.importorskip("torch")
+    patches, ng = W.config2(nel=6)
+    sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
+    W.load_into(sim, patches)
+    sim.preprocess()
+    sim.assembleSystem()
+    nnz = sim.sizes.nnz
+    pageable = np.empty(nnz + 1, dtype=np.float64)
+    sim.copy_matrix_into(pageable)
+    pinned = torch.empty(nnz + 1, dtype=torch.float64).pin_memory().numpy()
+    sim.copy_matrix_into(pinned)
+    assert np.array_equal(pinned[:nnz], pageable[:nnz])
+    odd = torch.empty(nnz + 1, dtype=torch.float64).pin_memory().numpy()[1:]   # 8-byte aligned only
+    sim.copy_matrix_into(odd)
+    assert np.array_equal(odd[:nnz], pageable[:nnz])
+
+
+def test_async_system_copies_overlap_the_next_assembly(gpulib):
+    """copy_system_async snapshots each assembled system before the next
+    assembly overwrites it: two assemblies with different control nets,
+    each copied asynchronously, equal the synchronous copies."""
+    torch = pytest.importorskip("torch")
+    patches, ng = W.config2(nel=6)
+    sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
+    W.load_into(sim, patches)
+    sim.preprocess()
+    coefs = [np.ascontiguousarray(patches[0].coefs, dtype=np.float64)]
+    moved = coefs[0].copy()
+    moved[:, :3] *= 1.1
+    coefs.append(moved)
+    want = []
+    for c in coefs:
+        sim.update_coefs(1, c)
+        sim.assembleSystem()
+        want.append((sim.matrix_values(), sim.rhs()))
+    nnz, neq = sim.sizes.nnz, sim.sizes.neq
+    K = [torch.empty(nnz, dtype=torch.float64).pin_memory().numpy() for _ in range(2)]
+    b = [torch.empty(neq, dtype=torch.float64).pin_memory().numpy() for _ in range(2)]
+    for i, c in enumerate(coefs):
+        sim.update_coefs(1, c)
+        sim.assembleSystem(sync=False)
+        sim.copy_system_async(K[i], b[i])
+    sim.copy_wait()
+    for i in range(2):
+        assert np.array_equal(K[i], want[i][0]) and np.array_equal(b[i], want[i][1])
+    assert not np.array_equal(want[0][0], want[1][0])
