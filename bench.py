@@ -300,6 +300,29 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def accuracy_vs_fp64(G, W, sim, patches, ng, device):
+    """The split-precision system of the benchmark against the FP64 assembly of
+    the same model (IFEMGPU_KE_FP64, equal to the oracle and to IFEM's own
+    assembly within 1e-12 in the tests): max-norm error relative to max|K|,
+    per-entry relative error of the entries above 1e-3 max|K|, right-hand
+    side error relative to max|b|."""
+    sim.assembleSystem()
+    K, b = sim.matrix_values(), sim.rhs()
+    ref = G.SIM(n_gauss=ng, ke_precision=G.KE_FP64, device=device)
+    W.load_into(ref, patches)
+    ref.preprocess()
+    ref.assembleSystem()
+    Kr, br = ref.matrix_values(), ref.rhs()
+    scale = np.abs(Kr).max()
+    big = np.abs(Kr) > 1e-3 * scale
+    per = np.abs(K[big] - Kr[big]) / np.abs(Kr[big])
+    return {"reference": "FP64 assembly of the same model",
+            "max_err_rel_to_max": float(np.abs(K - Kr).max() / scale),
+            "per_entry_rel_max": float(per.max()), "per_entry_rel_median": float(np.median(per)),
+            "entries_compared": int(big.sum()),
+            "rhs_err_rel_to_max": float(np.abs(b - br).max() / np.abs(br).max())}
+
+
 def run_gpu(args):
     import torch
     world, rank, local = dist_info()
@@ -427,6 +450,8 @@ def run_gpu(args):
             "clocks": clocks,
             "wall_s_timed_region": wall,
         }
+        if ke == G.KE_SPLIT_TF32:
+            line["accuracy"] = accuracy_vs_fp64(G, W, sim, patches, ng, local)
         if args.big:
             line["assembly_64"] = run_assembly_64(args, G, W)
             line["assembly_64"]["speedup_vs_cpu_port_at_24"] = \
