@@ -155,6 +155,42 @@ def test_split_poisson3d_tensor_core_kernel(gpulib, oracle_lib, p):
     assert np.array_equal(sim.matrix_values(), K) and np.array_equal(sim.rhs(), b)
 
 
+@pytest.mark.parametrize("kind,p", [(2, 2), (1, 2), (1, 3)])
+def test_split_folded_geometry(gpulib, oracle_lib, kind, p):
+    """An interior control point pushed past its neighbour folds the map: some
+    |J| w turn negative (IFEM integrates them with their sign), which the
+    tensor-core kernels integrate in a second pass with the MMA's negate-A
+    bit.  Entries partly cancel, so the comparison is in max norm only."""
+    import oracle
+    pc = W.box_patch(3, p, 4)
+    n0, n1, _ = pc.ncoef
+    node = (2 * n1 + 2) * n0 + 2
+    pc.coefs = pc.coefs.copy()
+    pc.coefs[node, 0] += 0.45       # past the next control point in x
+    pc.kind = kind
+    if kind == 1:
+        pc.source = 1.0
+        pc.dirichlet = [(1, 1, 0.0), (2, 1, 0.0)]
+    else:
+        pc.dirichlet = [(5, 123, 0.0)]
+        pc.neumann = [(6, (0.0, 0.0, 1.0))]
+    sim = G.SIM(n_gauss=0, ke_precision=G.KE_SPLIT_TF32, colour_passes=1)
+    W.load_into(sim, [pc])
+    sim.preprocess()
+    sim.assembleSystem()
+    K, b = sim.matrix_values(), sim.rhs()
+    sim.assembly_stats()
+    assert sim.kernel_launches <= 4              # the tensor-core kernel took the patch
+    orc = oracle.OracleModel(0)
+    W.load_into(orc, [pc])
+    orc.preprocess()
+    orc.assemble(8)
+    Ko, bo = orc.system()
+    assert np.abs(K - Ko).max() / np.abs(Ko).max() < TC_TOL
+    assert np.abs(b - bo).max() / np.abs(bo).max() < TC_TOL
+    assert_exactly_symmetric(sim, K)
+
+
 def test_split_multipatch_mixed(gpulib, oracle_lib):
     patches, ng = W.config3(npatch=6, nmin=2, nmax=5)
     split_vs_oracle(patches, ng)
