@@ -117,10 +117,8 @@ __device__ void bsplineDers(const double* __restrict__ U, int p, int k, double u
 }
 
 // 1D tables of one patch: thread per (direction, span, Gauss point).
-__global__ void k_basis_tables(DevPatch P)
+__device__ void basisItem(const DevPatch& P, int t)
 {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  int t = tid;
   for (int d = 0; d < P.dim; d++) {
     const int cnt = P.nel[d] * P.ng[d];
     if (t < cnt) {
@@ -158,6 +156,22 @@ __global__ void k_basis_tables(DevPatch P)
       tb[P.p[d] + 1 + r] = D[r];
     }
   }
+}
+
+// every patch's tables in one launch: item t of the concatenated work lists
+// belongs to the last patch whose start[] is <= t
+__global__ void k_basis_tables(const DevPatch* __restrict__ patches, const int* __restrict__ start,
+                               int np)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= start[np]) return;
+  int lo = 0, hi = np - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  basisItem(patches[lo], t - start[lo]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1129,6 +1143,19 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
   IFEMGPU_TRY(upload(ctx, &ctx->d_items, vol.data(), vol.size()));
   IFEMGPU_TRY(upload(ctx, &ctx->d_neumann, neuVals.data(), neuVals.size()));
   IFEMGPU_TRY(upload(ctx, &ctx->d_patches, ctx->h_devpatches.data(), np));
+  // work lists of the basis-table launch: per patch nel*ng points per
+  // direction plus the boundary tables
+  {
+    std::vector<int> start(np + 1, 0);
+    for (int pi = 0; pi < np; pi++) {
+      const DevPatch& D = ctx->h_devpatches[pi];
+      int work = 2 * D.dim;
+      for (int d = 0; d < D.dim; d++) work += D.nel[d] * D.ng[d];
+      start[pi + 1] = start[pi] + work;
+    }
+    ctx->basisWork = start[np];
+    IFEMGPU_TRY(upload(ctx, &ctx->d_basisStart, start.data(), start.size()));
+  }
   // system arrays
   IFEMGPU_TRY(upload(ctx, &ctx->d_madof, ctx->madof.data(), ctx->madof.size()));
   IFEMGPU_TRY(upload(ctx, &ctx->d_meqn, ctx->meqn.data(), ctx->meqn.size()));
@@ -1220,13 +1247,10 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
     IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4, s));
     if (ctx->nflags)
       IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * ctx->nflags, s));
-    for (int pi = 0; pi < (int)ctx->h_devpatches.size(); pi++) {
-      const DevPatch& D = ctx->h_devpatches[pi];
-      int work = 0;
-      for (int d = 0; d < D.dim; d++) work += D.nel[d] * D.ng[d];
-      work += 2 * D.dim;  // boundary tables
-      k_basis_tables<<<(work + 127) / 128, 128, 0, s>>>(D);
-    }
+    const int np = (int)ctx->h_devpatches.size();
+    if (np)
+      k_basis_tables<<<(ctx->basisWork + 127) / 128, 128, 0, s>>>(ctx->d_patches, ctx->d_basisStart,
+                                                                  np);
     IFEMGPU_CUDA(ctx, cudaGetLastError());
     return IFEMGPU_OK;
   }
@@ -1398,7 +1422,7 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
   int used = 0;
   for (const Pass& p : ctx->passes)
     used += !((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow));
-  ctx->launches_per_assembly = (int)ctx->h_devpatches.size() + used;
+  ctx->launches_per_assembly = (ctx->h_devpatches.empty() ? 0 : 1) + used;
   return IFEMGPU_OK;
 }
 

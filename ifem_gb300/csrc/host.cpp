@@ -62,8 +62,10 @@ void freeDevice(ifemgpu_ctx* ctx)
   f(ctx->d_rowidx); f(ctx->d_K); f(ctx->d_b); f(ctx->d_patches);
   f(ctx->d_items); f(ctx->d_neumann); f(ctx->d_counters); f(ctx->d_freeBefore);
   f(ctx->d_flags);
+  f(ctx->d_basisStart);
   ctx->d_freeBefore = nullptr;
   ctx->d_flags = nullptr;
+  ctx->d_basisStart = nullptr;
   for (int g = 0; g < 3; g++) {
     if (ctx->graphExec[g]) cudaGraphExecDestroy(ctx->graphExec[g]);
     if (ctx->graph[g]) cudaGraphDestroy(ctx->graph[g]);

@@ -236,6 +236,8 @@ struct ifemgpu_ctx {
   int fieldVersion = 0;          // bumped by every field update
   double* d_rhsAlt = nullptr;    // right-hand side of a collecting solve (neq)
   // asynchronous system copies: device snapshot, copy stream, events
+  int* d_basisStart = nullptr;   // per patch, first item of the basis-table launch (np + 1)
+  int basisWork = 0;
   double* d_Ksnap = nullptr;
   double* d_bsnap = nullptr;
   cudaStream_t copyStream = nullptr;
