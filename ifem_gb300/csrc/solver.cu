@@ -383,15 +383,29 @@ g_spmvOff(const int* __restrict__ colptr, const int* __restrict__ rowPat,
     const int so = kPat ? patStart[rowPat[row]] - b : 0;  // offset of entry k: off[k + so]
     float acc = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
     int k = b + lane;
+    // values stream (no L1 allocation: the offsets and p stay in L1)
     for (; k + 96 < e; k += 128) {
       const int o0 = off[k + so], o1 = off[k + so + 32], o2 = off[k + so + 64], o3 = off[k + so + 96];
-      const float a0 = A[k], a1 = A[k + 32], a2 = A[k + 64], a3 = A[k + 96];
+      const float a0 = __ldcs(A + k), a1 = __ldcs(A + k + 32), a2 = __ldcs(A + k + 64),
+                  a3 = __ldcs(A + k + 96);
       acc += a0 * p[row + o0];
       acc1 += a1 * p[row + o1];
       acc2 += a2 * p[row + o2];
       acc3 += a3 * p[row + o3];
     }
-    for (; k < e; k += 32) acc += A[k] * p[row + off[k + so]];
+    // the remainder (at most three 32-wide slices) in one round of loads
+    if (k < e) {
+      const bool h1 = k + 32 < e, h2 = k + 64 < e;
+      const int o0 = off[k + so];
+      const int o1 = h1 ? off[k + so + 32] : 0, o2 = h2 ? off[k + so + 64] : 0;
+      const float a0 = __ldcs(A + k);
+      const float a1 = h1 ? __ldcs(A + k + 32) : 0.f, a2 = h2 ? __ldcs(A + k + 64) : 0.f;
+      const float p0 = p[row + o0];
+      const float p1 = h1 ? p[row + o1] : 0.f, p2 = h2 ? p[row + o2] : 0.f;
+      acc += a0 * p0;
+      acc1 += a1 * p1;
+      acc2 += a2 * p2;
+    }
     acc += (acc1 + acc2) + acc3;
     for (int w = 16; w > 0; w >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, w);
     if (lane == 0) {
