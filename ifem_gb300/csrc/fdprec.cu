@@ -101,7 +101,7 @@ __device__ inline void stageGatherAsync(float* __restrict__ S, float* __restrict
 // Every thread of the three kernels below forms kFdTile outputs of one
 // column at once (independent FMA chains sharing each loaded coefficient);
 // rows past the end are clamped on load and dropped on store.
-constexpr int kFdTile = 4;
+constexpr int kFdTile = 8;
 constexpr int kFdSplit = 4;   // blocks per w-slab in the slab kernels
 
 // out[k][b][a] = sum_j U1[j][b] sum_i U0[i][a] scale_e r_e for one w-slab k
