@@ -101,8 +101,8 @@ struct PSmem {
 
 static_assert(sizeof(PSmem<3>) + 1024 <= 233472 / 3, "three p = 3 CTAs per SM");
 static_assert(sizeof(PSmem<2>) + 1024 <= 233472 / 5, "five p = 2 CTAs per SM");
-static_assert(6 * 2 * 64 + 6 * 3 * 64 + 64 * 24 <= PCfg<3>::TFL &&
-                  6 * 2 * 27 + 6 * 3 * 27 + 27 * 24 <= PCfg<2>::TFL,
+static_assert(6 * 64 + 10 * 64 + 14 * 64 + 64 * 24 <= PCfg<3>::TFL &&
+                  6 * 27 + 10 * 27 + 14 * 27 + 27 * 24 <= PCfg<2>::TFL,
               "sum-factorisation arrays fit in the operand tile");
 static_assert(PCfg<3>::NEN * PCfg<3>::GS <= PCfg<3>::TFL &&
                   PCfg<2>::NEN * PCfg<2>::GS <= PCfg<2>::TFL,
@@ -201,15 +201,27 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       atomicAdd(S.counters + 2, 1ull);
       sm.fail = 1;
     }
+    float* sFw = sm.Thi;  // weighted nodal fields [6][nen]: w x, w y, w z, w, w g, w n
     if (tid < C::NEN) {
       const int a = tid;
-      sm.X[a][0] = (float)(sm.ctrlT[a][0] - sm.ctrlT[0][0]);
-      sm.X[a][1] = (float)(sm.ctrlT[a][1] - sm.ctrlT[0][1]);
-      sm.X[a][2] = (float)(sm.ctrlT[a][2] - sm.ctrlT[0][2]);
-      sm.X[a][3] = (float)sm.ctrlT[a][3];
+      const float x0 = (float)(sm.ctrlT[a][0] - sm.ctrlT[0][0]);
+      const float x1 = (float)(sm.ctrlT[a][1] - sm.ctrlT[0][1]);
+      const float x2 = (float)(sm.ctrlT[a][2] - sm.ctrlT[0][2]);
+      const float w = (float)sm.ctrlT[a][3];
+      sm.X[a][0] = x0;
+      sm.X[a][1] = x1;
+      sm.X[a][2] = x2;
+      sm.X[a][3] = w;
       const int node = ((e3 + a / Q2) * Pt.n[1] + e2 + (a / Q) % Q) * Pt.n[0] + e1 + a % Q;
-      sm.fv[0][a] = hasG ? (float)Pt.logk[node] : 0.f;
-      sm.fv[1][a] = hasN ? (float)Pt.noise[node] : 0.f;
+      const float g = hasG ? (float)Pt.logk[node] : 0.f, nz = hasN ? (float)Pt.noise[node] : 0.f;
+      sm.fv[0][a] = g;
+      sm.fv[1][a] = nz;
+      sFw[a] = w * x0;
+      sFw[C::NEN + a] = w * x1;
+      sFw[2 * C::NEN + a] = w * x2;
+      sFw[3 * C::NEN + a] = w;
+      sFw[4 * C::NEN + a] = w * g;
+      sFw[5 * C::NEN + a] = w * nz;
     }
     if (tid >= 64 && tid < 67) sm.c00[tid - 64] = sm.ctrlT[0][tid - 64];
     if (tid == 96) sm.signs = 0;
@@ -224,42 +236,63 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     if (tid == 0 && it + (int)gridDim.x < count) stageCtrl(it + gridDim.x);
 
     // ---- 1. sums over the element's functions at every Gauss point by sum
-    //         factorisation; fields 0..2: w x_r, 3: w, 4: w g, 5: w n
-    float* sA = sm.Thi;            // [6][N, D][k][j][gi]
-    float* sB = sA + 6 * 2 * Q3;   // [6][NN, DN, ND][k][gj][gi]
-    float* sP = sB + 6 * 3 * Q3;   // [q][6][value, d/du, d/dv, d/dw]
-    for (int t = tid; t < 6 * 2 * Q3; t += blockDim.x) {
-      const int gi = t % Q, j = (t / Q) % Q, k = (t / Q2) % Q, d0 = (t / Q3) % 2, f = t / (2 * Q3);
+    //         factorisation.  Fields 0..3 (w x, w y, w z, w) with their
+    //         derivatives, fields 4, 5 (w g, w n) values only.
+    float* sA = sFw + 6 * C::NEN;  // blocks 2f + [N, D] (f < 4), 8 + (f - 4): [k][j][gi]
+    float* sB = sA + 10 * Q3;      // blocks 3f + [NN, DN, ND] (f < 4), 12 + (f - 4): [k][gj][gi]
+    float* sP = sB + 14 * Q3;      // [q][6][value, d/du, d/dv, d/dw]
+    for (int t = tid; t < 10 * Q3; t += blockDim.x) {
+      const int blk = t / Q3, r = t - blk * Q3;
+      const int gi = r % Q, j = (r / Q) % Q, k = r / Q2;
+      const int f = blk < 8 ? blk >> 1 : blk - 4, d0 = blk < 8 ? blk & 1 : 0;
+      const float* fw = sFw + f * C::NEN + Q * j + Q2 * k;
+      const float* tb = sm.tb[0][d0] + gi * Q;
       float acc = 0.f;
 #pragma unroll
-      for (int i = 0; i < Q; i++) {
-        const int a = i + Q * j + Q2 * k;
-        const float w = sm.X[a][3];
-        const float v = f < 3 ? w * sm.X[a][f] : f == 3 ? w : w * sm.fv[f - 4][a];
-        acc = fmaf(sm.tb[0][d0][gi * Q + i], v, acc);
-      }
+      for (int i = 0; i < Q; i++) acc = fmaf(tb[i], fw[i], acc);
       sA[t] = acc;
     }
     __syncthreads();
-    for (int t = tid; t < 6 * 3 * Q3; t += blockDim.x) {
-      const int gi = t % Q, gj = (t / Q) % Q, k = (t / Q2) % Q, c = (t / Q3) % 3, f = t / (3 * Q3);
-      const int d0 = c == 1, d1 = c == 2;
+    for (int t = tid; t < 14 * Q3; t += blockDim.x) {
+      const int blk = t / Q3, r = t - blk * Q3;
+      const int gi = r % Q, gj = (r / Q) % Q, k = r / Q2;
+      int src, d1;
+      if (blk < 12) {
+        const int f = blk / 3, c = blk - 3 * f;
+        src = 2 * f + (c == 1);
+        d1 = c == 2;
+      } else {
+        src = blk - 4;  // 12, 13 -> 8, 9
+        d1 = 0;
+      }
+      const float* a = sA + src * Q3 + k * Q2 + gi;
+      const float* tb = sm.tb[1][d1] + gj * Q;
       float acc = 0.f;
 #pragma unroll
-      for (int j = 0; j < Q; j++)
-        acc = fmaf(sm.tb[1][d1][gj * Q + j], sA[(((f * 2 + d0) * Q + k) * Q + j) * Q + gi], acc);
+      for (int jj = 0; jj < Q; jj++) acc = fmaf(tb[jj], a[jj * Q], acc);
       sB[t] = acc;
     }
     __syncthreads();
-    for (int t = tid; t < C::NQ * 24; t += blockDim.x) {
-      const int c4 = t % 4, f = (t / 4) % 6, q = t / 24;
+    for (int t = tid; t < C::NQ * 18; t += blockDim.x) {
+      const int q = t / 18, r = t - q * 18;
       const int gi = q % Q, gj = (q / Q) % Q, gk = q / Q2;
-      const int c3 = c4 == 1 ? 1 : c4 == 2 ? 2 : 0, d2 = c4 == 3;
+      int src, d2, slot;
+      if (r < 16) {
+        const int f = r >> 2, c4 = r & 3;
+        src = 3 * f + (c4 == 1 ? 1 : c4 == 2 ? 2 : 0);
+        d2 = c4 == 3;
+        slot = r;
+      } else {
+        src = r - 4;          // 16, 17 -> 12, 13
+        d2 = 0;
+        slot = (r - 12) * 4;  // 16, 20
+      }
+      const float* b = sB + src * Q3 + gj * Q + gi;
+      const float* tb = sm.tb[2][d2] + gk * Q;
       float acc = 0.f;
 #pragma unroll
-      for (int k = 0; k < Q; k++)
-        acc = fmaf(sm.tb[2][d2][gk * Q + k], sB[(((f * 3 + c3) * Q + k) * Q + gj) * Q + gi], acc);
-      sP[t] = acc;
+      for (int kk = 0; kk < Q; kk++) acc = fmaf(tb[kk], b[kk * Q2], acc);
+      sP[q * 24 + slot] = acc;
     }
     __syncthreads();
 
@@ -438,23 +471,43 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       pending = nullptr;
     }
     const int myc = e1 % Q + Q * (e2 % Q) + Q2 * (e3 % Q);
-    for (int t = tid; t < C::NB; t += blockDim.x) {
-      const int dx = t % C::W - P, dy = (t / C::W) % C::W - P, dz = t / (C::W * C::W) - P;
-      const int f1 = e1 + dx, f2 = e2 + dy, f3 = e3 + dz;
-      if ((dx | dy | dz) == 0 || f1 < 0 || f1 >= Pt.nel[0] || f2 < 0 || f2 >= Pt.nel[1] ||
-          f3 < 0 || f3 >= Pt.nel[2])
-        continue;
-      if (f1 % Q + Q * (f2 % Q) + Q2 * (f3 % Q) >= myc) continue;
-      const int* flag = S.flags + Pt.flagBase + (f3 * Pt.nel[1] + f2) * Pt.nel[0] + f1;
-      uint32_t spin = 0;
-      while (loadRelaxed(flag) == 0) {
-        if (++spin > kPoisFlagSpin) {
-          atomicAdd(S.counters + 2, 1ull);
-          break;
-        }
-        __nanosleep(64);
+    {
+      // this thread's lower-colour neighbours: every flag read issued before
+      // any spin, one acquire fence after the last
+      constexpr int R = (C::NB + 127) / 128;
+      const int* fl[R];
+      int seen[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int t = tid + 128 * r;
+        fl[r] = nullptr;
+        if (t >= C::NB) continue;
+        const int dx = t % C::W - P, dy = (t / C::W) % C::W - P, dz = t / (C::W * C::W) - P;
+        const int f1 = e1 + dx, f2 = e2 + dy, f3 = e3 + dz;
+        if ((dx | dy | dz) == 0 || f1 < 0 || f1 >= Pt.nel[0] || f2 < 0 || f2 >= Pt.nel[1] ||
+            f3 < 0 || f3 >= Pt.nel[2])
+          continue;
+        if (f1 % Q + Q * (f2 % Q) + Q2 * (f3 % Q) >= myc) continue;
+        fl[r] = S.flags + Pt.flagBase + (f3 * Pt.nel[1] + f2) * Pt.nel[0] + f1;
       }
-      fenceAcquire();
+#pragma unroll
+      for (int r = 0; r < R; r++) seen[r] = fl[r] ? loadRelaxed(fl[r]) : 1;
+      bool any = false;
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        if (!fl[r]) continue;
+        any = true;
+        uint32_t spin = 0;
+        while (seen[r] == 0) {
+          if (++spin > kPoisFlagSpin) {
+            atomicAdd(S.counters + 2, 1ull);
+            break;
+          }
+          __nanosleep(64);
+          seen[r] = loadRelaxed(fl[r]);
+        }
+      }
+      if (any) fenceAcquire();
     }
     if (mbarWait(tabbar, tphase)) {
       tphase ^= 1u;
