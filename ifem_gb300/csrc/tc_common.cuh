@@ -205,6 +205,16 @@ __device__ __forceinline__ void fenceAcquire()
   asm volatile("fence.acq_rel.gpu;" : : : "memory");
 }
 
+// acquire load of a flag already seen set: synchronises with the release
+// store that set it without draining this thread's own outstanding
+// reductions (which a full fence.acq_rel would wait for)
+__device__ __forceinline__ int loadAcquire(const int* p)
+{
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ void storeRelease(int* p, int v)
 {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");

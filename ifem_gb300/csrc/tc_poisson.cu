@@ -492,11 +492,9 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       }
 #pragma unroll
       for (int r = 0; r < R; r++) seen[r] = fl[r] ? loadRelaxed(fl[r]) : 1;
-      bool any = false;
 #pragma unroll
       for (int r = 0; r < R; r++) {
         if (!fl[r]) continue;
-        any = true;
         uint32_t spin = 0;
         while (seen[r] == 0) {
           if (++spin > kPoisFlagSpin) {
@@ -507,7 +505,11 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
           seen[r] = loadRelaxed(fl[r]);
         }
       }
-      if (any) fenceAcquire();
+      // acquire: the neighbours' reductions happen before this CTA's (the
+      // barrier below extends it to every thread)
+#pragma unroll
+      for (int r = 0; r < R; r++)
+        if (fl[r]) seen[r] = loadAcquire(fl[r]);
     }
     if (mbarWait(tabbar, tphase)) {
       tphase ^= 1u;

@@ -531,7 +531,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
             }
             __nanosleep(64);
           }
-          fenceAcquire();
+          loadAcquire(flag);  // synchronises with the release store (no fence)
         }
       }
     }
