@@ -193,7 +193,14 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     const int e1 = e % Pt.nel[0], e2 = (e / Pt.nel[0]) % Pt.nel[1], e3 = e / (Pt.nel[0] * Pt.nel[1]);
     const bool hasG = Pt.logk != nullptr, hasN = Pt.noise != nullptr;
 
-    // ---- 0. node data (control points by TMA), nodal fields, 1D tables
+    // ---- 0. node data (control points by TMA), nodal fields, 1D tables (read
+    //         from L2 while the control points arrive)
+    float tbv = 0.f;
+    if (tid < 6 * Q2) {
+      const int d = tid / (2 * Q2), dd = (tid / Q2) % 2, gi = tid % Q2;
+      const int ed = d == 0 ? e1 : d == 1 ? e2 : e3;
+      tbv = (dd ? Pt.tabDf[d] : Pt.tabNf[d])[ed * Q2 + gi];
+    }
     if (mbarWait(ctrlbar, cphase)) {
       cphase ^= 1u;
       ctrlOut = false;
@@ -226,11 +233,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     if (tid >= 64 && tid < 67) sm.c00[tid - 64] = sm.ctrlT[0][tid - 64];
     if (tid == 96) sm.signs = 0;
     if (tid == 97) sm.dVf = (float)(0.125 * Pt.span[0][e1] * Pt.span[1][e2] * Pt.span[2][e3]);
-    for (int t = tid; t < 6 * Q2; t += blockDim.x) {
-      const int d = t / (2 * Q2), dd = (t / Q2) % 2, gi = t % Q2;
-      const int ed = d == 0 ? e1 : d == 1 ? e2 : e3;
-      sm.tb[d][dd][gi] = (dd ? Pt.tabDf[d] : Pt.tabNf[d])[ed * Q2 + gi];
-    }
+    if (tid < 6 * Q2) sm.tb[tid / (2 * Q2)][(tid / Q2) % 2][tid % Q2] = tbv;
     __syncthreads();  // ctrlT read, node data visible
     if (sm.fail) break;
     if (tid == 0 && it + (int)gridDim.x < count) stageCtrl(it + gridDim.x);

@@ -209,7 +209,13 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const int n0 = (e3 * P.n[1] + e2) * P.n[0] + e1;
 
     // ---- 1. element nodes from the TMA boxes: coordinates relative to the
-    //         first node, weights
+    //         first node, weights; the 1D table rows of the element are read
+    //         from L2 while the control points arrive
+    float tbv = 0.f;
+    if (tid < 54) {
+      const int d = tid / 18, dd = (tid / 9) & 1, g = tid % 9;
+      tbv = (dd ? P.tabDf[d] : P.tabNf[d])[(d == 0 ? e1 : d == 1 ? e2 : e3) * 9 + g];
+    }
     if (mbarWait(ctrlbar, cphase)) {
       cphase ^= 1u;
       ctrlOut = false;
@@ -226,14 +232,18 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     }
     if (tid == 0) sm.signs = 0;
     if (tid == 32) sm.dVf = (float)(0.125 * P.span[0][e1] * P.span[1][e2] * P.span[2][e3]);
+    // the element's 1D tables [N0, D0, N1, D1, N2, D2][g 3 + i] in the per-point
+    // scratch, which step 3 overwrites only after step 2 has read them
+    float* const tbs = sm.u.b.scr;
+    if (tid < 54) tbs[tid] = tbv;
     // ---- 2. weighted tensor-product basis at every (Gauss point, function)
-    const float* tn0 = P.tabNf[0] + e1 * 9;
-    const float* tn1 = P.tabNf[1] + e2 * 9;
-    const float* tn2 = P.tabNf[2] + e3 * 9;
-    const float* td0 = P.tabDf[0] + e1 * 9;
-    const float* td1 = P.tabDf[1] + e2 * 9;
-    const float* td2 = P.tabDf[2] + e3 * 9;
-    __syncthreads();  // X visible, ctrlT read
+    const float* tn0 = tbs;
+    const float* td0 = tbs + 9;
+    const float* tn1 = tbs + 18;
+    const float* td1 = tbs + 27;
+    const float* tn2 = tbs + 36;
+    const float* td2 = tbs + 45;
+    __syncthreads();  // X and tables visible, ctrlT read
     if (sm.fail) break;
     if (tid == 0 && it + (int)gridDim.x < count) stageCtrl(it + gridDim.x);
     for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
