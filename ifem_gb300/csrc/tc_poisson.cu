@@ -186,8 +186,11 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
   }
   uint32_t cphase = 0, tphase = 0;
 
+  // the next element's item is read during the current element's scatter
+  Item nextItem{};
+  if ((int)blockIdx.x < count) nextItem = items[blockIdx.x];
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
-    const Item item = items[it];
+    const Item item = nextItem;
     const DevPatch& Pt = patches[item.patch];
     const int e = item.elem;
     const int e1 = e % Pt.nel[0], e2 = (e / Pt.nel[0]) % Pt.nel[1], e3 = e / (Pt.nel[0] * Pt.nel[1]);
@@ -523,6 +526,8 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     }
     __syncthreads();
     if (sm.fail) break;
+
+    if (it + (int)gridDim.x < count) nextItem = items[it + gridDim.x];
 
     // ---- 5. FP64 reductions: row a per lane (consecutive rows of a column
     //         are consecutive entries), a share of the columns per thread group

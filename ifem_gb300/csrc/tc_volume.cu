@@ -201,8 +201,11 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   }
   uint32_t cphase = 0, tphase = 0;
 
+  // the next element's item is read during the current element's scatter
+  Item nextItem{};
+  if ((int)blockIdx.x < count) nextItem = items[blockIdx.x];
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
-    const Item item = items[it];
+    const Item item = nextItem;
     const DevPatch& P = patches[item.patch];
     const int e = item.elem;
     const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
@@ -554,6 +557,8 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     }
     __syncthreads();
     if (sm.fail) break;
+
+    if (it + (int)gridDim.x < count) nextItem = items[it + gridDim.x];
 
     // ---- 9. element matrix and scatter, node pair by node pair (FP32
     //         arithmetic; the FP64 additions happen in the L2 reductions)
