@@ -204,6 +204,12 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       const int ed = d == 0 ? e1 : d == 1 ? e2 : e3;
       tbv = (dd ? Pt.tabDf[d] : Pt.tabNf[d])[ed * Q2 + gi];
     }
+    float gv = 0.f, nv = 0.f;  // nodal log-conductivity and noise, also read early
+    if (tid < C::NEN) {
+      const int node = ((e3 + tid / Q2) * Pt.n[1] + e2 + (tid / Q) % Q) * Pt.n[0] + e1 + tid % Q;
+      if (hasG) gv = (float)Pt.logk[node];
+      if (hasN) nv = (float)Pt.noise[node];
+    }
     if (mbarWait(ctrlbar, cphase)) {
       cphase ^= 1u;
       ctrlOut = false;
@@ -222,8 +228,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       sm.X[a][1] = x1;
       sm.X[a][2] = x2;
       sm.X[a][3] = w;
-      const int node = ((e3 + a / Q2) * Pt.n[1] + e2 + (a / Q) % Q) * Pt.n[0] + e1 + a % Q;
-      const float g = hasG ? (float)Pt.logk[node] : 0.f, nz = hasN ? (float)Pt.noise[node] : 0.f;
+      const float g = gv, nz = nv;
       sm.fv[0][a] = g;
       sm.fv[1][a] = nz;
       sFw[a] = w * x0;
