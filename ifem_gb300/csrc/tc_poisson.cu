@@ -204,6 +204,8 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       const int ed = d == 0 ? e1 : d == 1 ? e2 : e3;
       tbv = (dd ? Pt.tabDf[d] : Pt.tabNf[d])[ed * Q2 + gi];
     }
+    double dV = 0.0;  // span volume
+    if (tid == 97) dV = Pt.span[0][e1] * Pt.span[1][e2] * Pt.span[2][e3];
     float gv = 0.f, nv = 0.f;  // nodal log-conductivity and noise, also read early
     if (tid < C::NEN) {
       const int node = ((e3 + tid / Q2) * Pt.n[1] + e2 + (tid / Q) % Q) * Pt.n[0] + e1 + tid % Q;
@@ -240,7 +242,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     }
     if (tid >= 64 && tid < 67) sm.c00[tid - 64] = sm.ctrlT[0][tid - 64];
     if (tid == 96) sm.signs = 0;
-    if (tid == 97) sm.dVf = (float)(0.125 * Pt.span[0][e1] * Pt.span[1][e2] * Pt.span[2][e3]);
+    if (tid == 97) sm.dVf = (float)(0.125 * dV);
     if (tid < 6 * Q2) sm.tb[tid / (2 * Q2)][(tid / Q2) % 2][tid % Q2] = tbv;
     __syncthreads();  // ctrlT read, node data visible
     if (sm.fail) break;

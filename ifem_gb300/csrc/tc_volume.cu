@@ -214,6 +214,8 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     // ---- 1. element nodes from the TMA boxes: coordinates relative to the
     //         first node, weights; the 1D table rows of the element are read
     //         from L2 while the control points arrive
+    double dV = 0.0;  // span volume, read early as well
+    if (tid == 32) dV = P.span[0][e1] * P.span[1][e2] * P.span[2][e3];
     float tbv = 0.f;
     if (tid < 54) {
       const int d = tid / 18, dd = (tid / 9) & 1, g = tid % 9;
@@ -234,7 +236,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.X[a][3] = (float)sm.ctrlT[a][3];
     }
     if (tid == 0) sm.signs = 0;
-    if (tid == 32) sm.dVf = (float)(0.125 * P.span[0][e1] * P.span[1][e2] * P.span[2][e3]);
+    if (tid == 32) sm.dVf = (float)(0.125 * dV);
     // the element's 1D tables [N0, D0, N1, D1, N2, D2][g 3 + i] in the per-point
     // scratch, which step 3 overwrites only after step 2 has read them
     float* const tbs = sm.u.b.scr;
