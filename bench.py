@@ -1,29 +1,46 @@
 #!/usr/bin/env python
 """Benchmark: elements/s assembled for 3D linear elasticity on one NURBS patch,
-p=2, 24^3 elements, 3x3x3 Gauss points (E=1, nu=0.3, clamped w=0, unit
-traction on w=1) -- the IFEM element-integration + assembly path on one GPU.
+p=2, 64^3 elements (262,144 elements, 849,420 equations, 301 M matrix
+entries), 3x3x3 Gauss points, E=1, nu=0.3, clamped w=0, unit traction on w=1
+-- the IFEM element-integration + assembly path on one GPU.
 
 One step = one full assembly of that model (basis tables, every element's
 stiffness and load, Neumann faces, scatter into the compressed-column
 system), inputs resident on the device; `value` is elements/s of those
-steps.  `e2e` repeats the step through the C ABI with host buffers: the
-control net is uploaded from pinned memory and the assembled matrix values
-and right-hand side are copied back to pinned host memory inside the timed
-region (each step's copy overlaps the next step's assembly; the clock stops
-when the last copy has landed).  The `solve` object holds the second half of the metric: wall time to
-the FP64 relative residual 1e-10 on the 64^3 p=3 log-normal Poisson system,
-plain Jacobi mixed-precision PCG against flexible CG with the Kronecker
-preconditioner and with the learned coarse correction (trained in the run,
-evaluated on a held-out field).
+steps.  The matrix (2.4 GB of FP64 values) is larger than the 129 MB L2, so
+no flush is needed between steps.  `e2e` repeats the step through the C ABI
+with host buffers: the control net is uploaded from pinned memory and the
+assembled matrix values and right-hand side are copied back to pinned host
+memory inside the timed region (each step's copy overlaps the next step's
+assembly; the clock stops when the last copy has landed).
+
+Extra objects of the GPU line:
+  accuracy       the split-precision 64^3 system against the FP64 assembly of
+                 the oracle (IFEM's integrate + assemSparse restated on the
+                 host), per entry and in the max norm;
+  assembly_24    the same model at 24^3 (device-resident, L2 flushed);
+  elasticity_64  time to the FP64 relative residual 1e-10 on the 64^3 system
+                 (plain mixed PCG, Kronecker FCG), solutions against the
+                 oracle's FP64 PCG solution;
+  solve          the second half of the metric: wall time to 1e-10 on the
+                 64^3 p=3 log-normal Poisson system, plain Jacobi mixed PCG
+                 against flexible CG with the Kronecker preconditioner and with
+                 the learned coarse correction (trained in the run, evaluated
+                 on a held-out field), each solution against the oracle's FP64
+                 reference solution.
+  cpu_baseline   the oracle's assembly on the host cores (bounded sample of the
+                 same workload), and the CPU solve baselines (scipy SuperLU
+                 with IFEM's options on the 2D Poisson model, the oracle's FP64
+                 PCG on the 64^3 Poisson system).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-                  [--precision split|fp64] [--solve-nel 64|0]
 
 --impl reference times the reference algorithm on the host cores: IFEM's
 ASMs3D::integrate + SAM/assemSparse scatter restated in C++ (oracle/), with
-IFEM's OpenMP stripe colouring over all host threads.  Under torchrun every
-rank runs an independent replica (the path has no data exchange; replicas
-only) and rank 0 prints the line.
+IFEM's OpenMP stripe colouring over all host threads, each step the elements
+of the first SAMPLE_LAYERS element layers of the 64^3 model scattered into its
+full-size matrix.  Under torchrun every rank runs an independent replica (the
+path has no data exchange; replicas only) and rank 0 prints the line.
 """
 from __future__ import annotations
 
@@ -39,10 +56,21 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NEL = 24
-TC_TRAFFIC_24 = 504.0e6  # bytes per launch of the tensor-core element kernel at 24^3 (ncu)
-WORKLOAD = "3D linear elasticity, 1 NURBS patch, p=2, 24^3 elements, 3x3x3 Gauss"
+NEL = 64
+# element layers (of 64) in one step of the host baseline: 32,768 elements
+SAMPLE_LAYERS = 8
+WORKLOAD = "3D linear elasticity, 1 NURBS patch, p=2, 64^3 elements, 3x3x3 Gauss"
 METRIC = "elements/s assembled; time to 1e-10 residual, learned vs plain PCG, 1 GB300"
+DATA = "synthetic (seeded NURBS patch: Greville points + U(-0.1h, 0.1h), weights U[0.8, 1.2])"
+# dram__bytes_read.sum + dram__bytes_write.sum of the dominant kernel per
+# 64^3 assembly (ncu capture of a smaller case scaled by the element count)
+TRAFFIC_PER_ELEMENT = None
+
+
+def config_of(s):
+    """The `config` object of both arms (identical keys and values)."""
+    return {"workload": WORKLOAD, "nel": int(s["nel"]), "neq": int(s["neq"]),
+            "nnz": int(s["nnz"])}
 
 
 def measured_peaks():
@@ -70,8 +98,9 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -116,41 +145,134 @@ def dist_info():
     return world, rank, local
 
 
-def cpu_baseline(patches, ng, threads, budget_s=20.0):
-    """The reference algorithm (oracle/, IFEM's integrate + assemSparse restated)
-    on `threads` host threads: full assemblies of the model until ~budget_s."""
+def max_over_ranks(values, device):
+    """Element-wise maximum of per-rank timings (the slowest replica sets the
+    whole-job time); the values themselves on a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+# ---------------------------------------------------------------------------
+# host baseline (oracle: the reference algorithm restated; CPU legs only)
+
+def oracle_model(patches, ng):
     import oracle
-    orc = oracle.OracleModel(ng)
     from ifem_gb300 import workloads as W
+    orc = oracle.OracleModel(ng)
     W.load_into(orc, patches)
     s = orc.preprocess()
-    t0 = time.perf_counter()
-    orc.assemble(threads)
-    first = time.perf_counter() - t0
-    reps = max(1, min(5, int(budget_s / max(first, 1e-3))))
-    t0 = time.perf_counter()
+    return orc, s
+
+
+def sample_elements(s):
+    """Elements of one host sample: the first SAMPLE_LAYERS element layers."""
+    return min(s["nel"], NEL * NEL * SAMPLE_LAYERS)
+
+
+def cpu_sample_rate(orc, s, threads, reps):
+    """elements/s of `reps` bounded samples of the assembly on `threads` host
+    threads (IFEM's stripe colouring over the whole patch; every element of
+    the first element layers scattered into the full-size matrix)."""
+    n = sample_elements(s)
+    times = []
     for _ in range(reps):
-        orc.assemble(threads)
-    dt = (time.perf_counter() - t0) / reps
-    return s["nel"] / dt, dt, reps, s
+        t0 = time.perf_counter()
+        orc.assemble(threads, n)
+        times.append(time.perf_counter() - t0)
+    dt = float(np.mean(times))
+    return n / dt, dt, n
 
 
-# inner reduction of the FP32 iterations per FP64 refinement step for the
-# Poisson solve: 3e-6 needs two refinement steps to 1e-10 (1e-4 needs three
-# and restarts the Krylov space once more), the same for every method timed
-INNER_RTOL = 3e-6
+SAMPLE_TEXT = ("elements of the first {layers} of 64 element layers ({n} elements) per "
+               "sample, scattered into the full 64^3 matrix (IFEM integrate + assemSparse "
+               "restated in C++, IFEM's OpenMP stripe colouring over the whole patch)")
 
+
+def run_reference(args):
+    world, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from ifem_gb300 import workloads as W
+    patches, ng = W.config2(nel=NEL)
+    threads = os.cpu_count() or 1
+    orc, s = oracle_model(patches, ng)
+    n = sample_elements(s)
+    for _ in range(args.warmup):
+        orc.assemble(threads, n)
+    value, dt, n = cpu_sample_rate(orc, s, threads, args.steps)
+    sample = SAMPLE_TEXT.format(layers=SAMPLE_LAYERS, n=n)
+    line = {"metric": METRIC, "value": value, "unit": "elements/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": config_of(s),
+            "threads": threads,
+            "cpu_baseline": {"value": value, "unit": "elements/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def system_errors(K, b, Kr, br):
+    """Split-precision system against an FP64 reference of the same model."""
+    scale = float(np.abs(Kr).max())
+    big = np.abs(Kr) > 1e-3 * scale
+    per = np.abs(K[big] - Kr[big]) / np.abs(Kr[big])
+    return {"max_err_rel_to_max": float(np.abs(K - Kr).max() / scale),
+            "per_entry_rel_max": float(per.max()),
+            "per_entry_rel_median": float(np.median(per)),
+            "entries_compared": int(big.sum()),
+            "rhs_err_rel_to_max": float(np.abs(b - br).max() / np.abs(br).max())}
+
+
+def rel_err(x, xr):
+    return float(np.abs(x - xr).max() / np.abs(xr).max())
+
+
+# ---------------------------------------------------------------------------
+# extra legs of the GPU line
+
+INNER_RTOL = 3e-6  # inner FP32 reduction per FP64 refinement step of the solves
 SOLVE_WORKLOAD = ("3D Poisson, 1 B-spline patch, p=3, 64^3 elements, 4x4x4 Gauss, "
                   "log-normal conductivity (GRF sigma 1, correlation 0.1), u=0 on all faces")
 
 
-def run_solve(args, G, W):
+def timed_solves(sim, G, methods, reps):
+    out, xs = {}, {}
+    for key, meth, pre in methods:
+        for _ in range(2):                               # capture and warm up
+            sim.solveSystem(method=meth, rtol=1e-10, precond=pre, inner_rtol=INNER_RTOL,
+                            check=False)
+        walls, dev = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            x, info = sim.solveSystem(method=meth, rtol=1e-10, precond=pre,
+                                      inner_rtol=INNER_RTOL, check=False)
+            walls.append((time.perf_counter() - t0) * 1e3)
+            dev.append(info.device_ms)
+        xs[key] = x
+        out[key] = {"wall_ms": float(np.median(walls)), "device_ms": float(np.median(dev)),
+                    "inner_iters": info.inner_iters, "outer_iters": info.outer_iters,
+                    "relres": info.relres, "fallbacks": info.fallbacks}
+    return out, xs
+
+
+def run_solve(args, G, W, threads):
     """Time to the FP64 relative residual 1e-10 on the p=3 log-normal Poisson
     system: plain Jacobi mixed-precision PCG, flexible CG with the Kronecker
     preconditioner, and with the learned coarse correction on top (trained here
     on pairs from seeded conductivity fields, evaluated on a held-out field).
     Each solve is timed on the wall clock around the C-ABI call (device work,
-    the FP64 solution copied to host memory) and on device events."""
+    the FP64 solution copied to host memory) and on device events.  The FP64
+    reference solution is the oracle's FP64 Jacobi-PCG to 1e-13 on the oracle's
+    FP64 assembly of the same model; the oracle's PCG to 1e-10 on the host
+    cores is the CPU solve baseline."""
     t0 = time.perf_counter()
     patches, ng = W.config4(nel=args.solve_nel)
     sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
@@ -158,20 +280,46 @@ def run_solve(args, G, W):
     sz = sim.preprocess()
     setup_s = time.perf_counter() - t0
     pts = patches[0].coefs[:, :3]
-    # assembly of this system (tensor-core Poisson kernel, p = 3): device time
     asm_ms = []
     for _ in range(4):
         sim.assembleSystem()
         asm_ms.append(sim.assembly_stats()[0])
     asm_launches = sim.kernel_launches
+    out = {"workload": SOLVE_WORKLOAD, "neq": sz.neq, "nnz": sz.nnz, "rtol": 1e-10,
+           "inner": f"FP32 with FP64 residual refinement (inner reduction {INNER_RTOL:g})",
+           "setup_s": setup_s,
+           "assembly_ms": float(np.median(asm_ms[1:])), "assembly_launches": asm_launches,
+           "assembly_elements_per_s": sz.nel / (float(np.median(asm_ms[1:])) * 1e-3)}
+    K, b = sim.matrix_values(), sim.rhs()
+    # FP64 reference: the oracle's assembly of the same model and its PCG
+    ref = {}
+    if args.ref_solve:
+        orc, s = oracle_model(patches, ng)
+        t0 = time.perf_counter()
+        orc.assemble(threads)
+        ref_asm_s = time.perf_counter() - t0
+        Ko, bo = orc.system()
+        out["accuracy"] = dict(system_errors(K, b, Ko, bo),
+                               reference="oracle FP64 assembly of the same model")
+        del K
+        t0 = time.perf_counter()
+        x10, it10, rr10 = orc.pcg(bo, rtol=1e-10, threads=threads)
+        pcg_s = time.perf_counter() - t0
+        xref, itr, rrr = orc.pcg(bo, rtol=1e-13, threads=threads, x0=x10)
+        ref = {"x": xref, "cpu": {"assembly_s": ref_asm_s, "pcg_1e-10_s": pcg_s,
+                                   "pcg_iters": it10, "pcg_relres": rr10,
+                                   "threads": threads,
+                                   "what": "oracle FP64 Jacobi-PCG to 1e-10 on the host cores"},
+               "relres": rrr}
+        del orc, Ko
     # training: plain-PCG iterates of seeded fields, up to 20,000 pairs
     sim.learn_setup(coarse_cells=args.coarse_cells, hidden=256, capacity=20000, seed=2,
                     field_inputs=1)
     t0 = time.perf_counter()
-    seeds = 0
-    for s in range(args.train_seeds):
+    seeds, pairs = 0, 0
+    for s_ in range(args.train_seeds):
         sim.update_field(1, G.FIELD_LOG_KAPPA,
-                         W.gaussian_field_3d(np.random.default_rng(W.BASE_SEED + 500 + s), pts))
+                         W.gaussian_field_3d(np.random.default_rng(W.BASE_SEED + 500 + s_), pts))
         sim.assembleSystem()
         pairs = sim.learn_collect(stride=1, rtol=1e-6)
         seeds += 1
@@ -188,33 +336,20 @@ def run_solve(args, G, W):
     sim.learn_clear()
     sim.learn_collect(stride=1, rtol=1e-6)
     mse_held = sim.learn_evaluate()
-    out = {"workload": SOLVE_WORKLOAD, "neq": sz.neq, "nnz": sz.nnz, "rtol": 1e-10,
-           "inner": f"FP32 with FP64 residual refinement (inner reduction {INNER_RTOL:g})",
-           "setup_s": setup_s,
-           "assembly_ms": float(np.median(asm_ms[1:])), "assembly_launches": asm_launches,
-           "assembly_elements_per_s": sz.nel / (float(np.median(asm_ms[1:])) * 1e-3)}
-    xs = {}
-    for key, meth, pre in (("plain_pcg", G.PCG_MIXED, G.PRECOND_JACOBI),
-                           ("kronecker_fcg", G.PCG_MIXED, G.PRECOND_KRONECKER),
-                           ("learned_fcg", G.FCG_LEARNED, G.PRECOND_KRONECKER),
-                           ("learned_jacobi_fcg", G.FCG_LEARNED, G.PRECOND_JACOBI)):
-        for _ in range(2):                               # capture and warm up
-            sim.solveSystem(method=meth, rtol=1e-10, precond=pre, inner_rtol=INNER_RTOL,
-                            check=False)
-        walls, dev = [], []
-        for _ in range(args.solve_reps):
-            t0 = time.perf_counter()
-            x, info = sim.solveSystem(method=meth, rtol=1e-10, precond=pre,
-                                      inner_rtol=INNER_RTOL, check=False)
-            walls.append((time.perf_counter() - t0) * 1e3)
-            dev.append(info.device_ms)
-        xs[key] = x
-        out[key] = {"wall_ms": float(np.median(walls)), "device_ms": float(np.median(dev)),
-                    "inner_iters": info.inner_iters, "outer_iters": info.outer_iters,
-                    "relres": info.relres, "fallbacks": info.fallbacks}
-    ref = xs["plain_pcg"]
+    res, xs = timed_solves(sim, G, (("plain_pcg", G.PCG_MIXED, G.PRECOND_JACOBI),
+                                    ("kronecker_fcg", G.PCG_MIXED, G.PRECOND_KRONECKER),
+                                    ("learned_fcg", G.FCG_LEARNED, G.PRECOND_KRONECKER),
+                                    ("learned_jacobi_fcg", G.FCG_LEARNED, G.PRECOND_JACOBI)),
+                           args.solve_reps)
+    out.update(res)
     for key in xs:
-        out[key]["max_rel_diff_vs_plain"] = float(np.abs(xs[key] - ref).max() / np.abs(ref).max())
+        if ref:
+            out[key]["rel_err_vs_fp64_reference"] = rel_err(xs[key], ref["x"])
+    if ref:
+        out["fp64_reference"] = {"what": "oracle FP64 Jacobi-PCG on the oracle's FP64 "
+                                         "assembly, relative residual 1e-13",
+                                 "relres": ref["relres"]}
+        out["cpu_solve"] = ref["cpu"]
     out["learned_training"] = {"seeds": seeds, "pairs": pairs,
                                "coarse_unknowns": args.coarse_cells and (args.coarse_cells + 1) ** 3,
                                "hidden": 256, "epochs": 30, "final_batch_loss": loss,
@@ -228,100 +363,41 @@ def run_solve(args, G, W):
     return out
 
 
-def run_assembly_64(args, G, W):
-    """The elasticity model at 64^3 elements (262,144 elements, 849,420
-    equations, 301 M matrix entries): preprocessing time of the library (host
-    numbering and pattern), elements/s of device-resident assemblies (the
-    matrix alone, 2.4 GB, is larger than L2), and the time to the FP64
-    relative residual 1e-10 with plain mixed PCG and with Kronecker FCG."""
-    t0 = time.perf_counter()
-    patches, ng = W.config2(nel=64)
+def run_assembly_24(args, G, W):
+    """The headline model at 24^3 elements (13,824 elements; matrix 132 MB, about
+    the L2 size, so L2 is flushed between steps)."""
+    import torch
+    patches, ng = W.config2(nel=24)
     sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
     W.load_into(sim, patches)
     sz = sim.preprocess()
-    pre_s = time.perf_counter() - t0
-    for _ in range(2):
+    stream = torch.cuda.ExternalStream(sim.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
         sim.assembleSystem()
-    ts, vs = [], []
+    ts = []
     for _ in range(args.steps):
-        sim.assembleSystem()
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        sim.assembleSystem(sync=False)
         t, v, _ = sim.assembly_stats()
         ts.append(t)
-        vs.append(v)
     ms = float(np.median(ts))
-    out = {"workload": "3D linear elasticity, 1 NURBS patch, p=2, 64^3 elements, 3x3x3 Gauss",
-           "nel": sz.nel, "neq": sz.neq, "nnz": sz.nnz, "preprocess_s": pre_s,
-           "ms_per_assembly": ms, "volume_ms": float(np.median(vs)),
-           "elements_per_s": sz.nel / (ms * 1e-3), "steps": args.steps}
-    for key, pre in (("solve_plain_pcg", G.PRECOND_JACOBI),
-                     ("solve_kronecker_fcg", G.PRECOND_KRONECKER)):
-        sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10, precond=pre, check=False)
-        t0 = time.perf_counter()
-        x, info = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10, precond=pre, check=False)
-        out[key] = {"wall_ms": (time.perf_counter() - t0) * 1e3, "device_ms": info.device_ms,
-                    "inner_iters": info.inner_iters, "outer_iters": info.outer_iters,
-                    "relres": info.relres}
-    del sim
-    return out
+    return {"workload": WORKLOAD.replace("64^3", "24^3"), "nel": sz.nel, "neq": sz.neq,
+            "nnz": sz.nnz, "ms_per_assembly": ms, "elements_per_s": sz.nel / (ms * 1e-3),
+            "l2": "flushed between steps (256 MB write, untimed)"}
 
 
-def run_reference(args):
-    world, rank, _ = dist_info()
-    if rank != 0:
-        return
-    from ifem_gb300 import workloads as W
-    patches, ng = W.config2(nel=NEL)
-    threads = os.cpu_count() or 1
-    import oracle
-    orc = oracle.OracleModel(ng)
-    W.load_into(orc, patches)
-    s = orc.preprocess()
-    for _ in range(max(1, min(args.warmup, 1))):
-        orc.assemble(threads)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        orc.assemble(threads)
-        times.append(time.perf_counter() - t0)
-    dt = float(np.mean(times))
-    value = s["nel"] / dt
-    sample = (f"full assembly of the {s['nel']}-element model per step "
-              f"(IFEM integrate + assemSparse restated in C++, OpenMP stripe colouring)")
-    line = {"metric": METRIC, "value": value, "unit": "elements/s", "impl": "reference",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NURBS patch)",
-            "config": {"workload": WORKLOAD, "nel": s["nel"], "neq": s["neq"], "nnz": s["nnz"],
-                       "threads": threads},
-            "cpu_baseline": {"value": value, "unit": "elements/s", "cores": threads,
-                             "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+def run_elasticity_solves(args, G, sim, xref):
+    res, xs = timed_solves(sim, G, (("plain_pcg", G.PCG_MIXED, G.PRECOND_JACOBI),
+                                    ("kronecker_fcg", G.PCG_MIXED, G.PRECOND_KRONECKER)), 1)
+    if xref is not None:
+        for key in xs:
+            res[key]["rel_err_vs_fp64_reference"] = rel_err(xs[key], xref)
+    return res
 
 
-def accuracy_vs_fp64(G, W, sim, patches, ng, device):
-    """The split-precision system of the benchmark against the FP64 assembly of
-    the same model (IFEMGPU_KE_FP64, equal to the oracle and to IFEM's own
-    assembly within 1e-12 in the tests): max-norm error relative to max|K|,
-    per-entry relative error of the entries above 1e-3 max|K|, right-hand
-    side error relative to max|b|."""
-    sim.assembleSystem()
-    K, b = sim.matrix_values(), sim.rhs()
-    ref = G.SIM(n_gauss=ng, ke_precision=G.KE_FP64, device=device)
-    W.load_into(ref, patches)
-    ref.preprocess()
-    ref.assembleSystem()
-    Kr, br = ref.matrix_values(), ref.rhs()
-    scale = np.abs(Kr).max()
-    big = np.abs(Kr) > 1e-3 * scale
-    per = np.abs(K[big] - Kr[big]) / np.abs(Kr[big])
-    return {"reference": "FP64 assembly of the same model",
-            "max_err_rel_to_max": float(np.abs(K - Kr).max() / scale),
-            "per_entry_rel_max": float(per.max()), "per_entry_rel_median": float(np.median(per)),
-            "entries_compared": int(big.sum()),
-            "rhs_err_rel_to_max": float(np.abs(b - br).max() / np.abs(br).max())}
-
+# ---------------------------------------------------------------------------
 
 def run_gpu(args):
     import torch
@@ -334,13 +410,14 @@ def run_gpu(args):
     from ifem_gb300 import ifemgpu as G
     from ifem_gb300 import workloads as W
     gbuild.ensure_built()
-    ke = G.KE_SPLIT_TF32 if args.precision == "split" else G.KE_FP64
+    threads = os.cpu_count() or 1
     patches, ng = W.config2(nel=NEL)
-    sim = G.SIM(n_gauss=ng, ke_precision=ke, device=local)
+    sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32, device=local)
     W.load_into(sim, patches)
+    t0 = time.perf_counter()
     sz = sim.preprocess()
+    preprocess_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(sim.stream())
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # 256 MB > 129 MB L2
     for _ in range(args.warmup):
         sim.assembleSystem(sync=False)
     torch.cuda.synchronize()
@@ -350,7 +427,7 @@ def run_gpu(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-resident steps -------------------------------------------
+    # ---- device-resident steps (inputs larger than L2) ----------------------
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     vol_ms = []
@@ -359,7 +436,6 @@ def run_gpu(args):
         wall0 = time.perf_counter()
         for i in range(args.steps):
             with torch.cuda.stream(stream):
-                flush.zero_()                         # evict L2 between steps (untimed)
                 starts[i].record(stream)
             sim.assembleSystem(sync=False)
             with torch.cuda.stream(stream):
@@ -375,10 +451,12 @@ def run_gpu(args):
     # ---- end-to-end through the C ABI with host buffers -----------------------
     coefs_np = torch.from_numpy(np.ascontiguousarray(patches[0].coefs,
                                                      dtype=np.float64)).pin_memory().numpy()
-    # two pinned host buffers per result: step i's copy (device snapshot, then
-    # D2H on the copy stream) overlaps step i+1's assembly
     Kh = [torch.empty(sz.nnz, dtype=torch.float64).pin_memory().numpy() for _ in range(2)]
     bh = [torch.empty(sz.neq, dtype=torch.float64).pin_memory().numpy() for _ in range(2)]
+    for i in range(2):                                # touch the pinned pages once
+        sim.assembleSystem(sync=False)
+        sim.copy_system_async(Kh[i], bh[i])
+    sim.copy_wait()
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
@@ -390,14 +468,11 @@ def run_gpu(args):
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     h2d = coefs_np.nbytes
     d2h = 8 * (sz.nnz + sz.neq)
+    Ksplit, bsplit = Kh[(args.steps - 1) % 2].copy(), bh[(args.steps - 1) % 2].copy()
+    del Kh, bh
 
     # ---- max over ranks ----------------------------------------------------
-    if world > 1:
-        t = torch.tensor([step_ms, e2e_ms, float(np.mean(vol_ms))], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms, e2e_ms, vmax = t.tolist()
-    else:
-        vmax = float(np.mean(vol_ms))
+    step_ms, e2e_ms, vmax = max_over_ranks([step_ms, e2e_ms, float(np.mean(vol_ms))], "cuda")
 
     if rank == 0:
         hbm, bf16, src = measured_peaks()
@@ -409,28 +484,37 @@ def run_gpu(args):
         nq, ndof_e, ns = 27, 81, 6     # p=2 elasticity: Gauss points, element DOFs, stresses
         flops_el = 2 * nq * (ns * ndof_e ** 2 + ns ** 2 * ndof_e)
         value = world * sz.nel / (step_ms * 1e-3)
-        cpu_v, cpu_dt, reps, _ = cpu_baseline(patches, ng, os.cpu_count() or 1,
-                                              budget_s=args.cpu_budget)
+        # host baseline on the same workload (bounded sample), then the oracle's
+        # full FP64 assembly as the reference of the accuracy object
+        orc, s = oracle_model(patches, ng)
+        orc.assemble(threads, sample_elements(s))
+        cpu_v, cpu_dt, n_s = cpu_sample_rate(orc, s, threads, args.cpu_reps)
+        orc.assemble(threads)
+        Ko, bo = orc.system()
+        accuracy = dict(system_errors(Ksplit, bsplit, Ko, bo),
+                        reference="oracle FP64 assembly of the same model (IFEM's integrate "
+                                  "+ assemSparse restated on the host)")
+        del Ksplit, Ko
+        xref = None
+        if args.ref_solve:
+            xref, _, _ = orc.pcg(bo, rtol=1e-12, threads=threads)
+        del orc
         line = {
             "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32-split" if ke == G.KE_SPLIT_TF32 else "f64",
-            "data": "synthetic (seeded NURBS patch, BASE_SEED+2)",
-            "config": {"workload": WORKLOAD, "nel": sz.nel, "neq": sz.neq, "nnz": nnz,
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "flushed between steps (256 MB write, untimed)",
-                       "ke_precision": args.precision},
+            "dtype": "f32-split", "data": DATA,
+            "config": config_of({"nel": sz.nel, "neq": sz.neq, "nnz": nnz}),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (2.4 GB matrix), no flush",
+            "ke_precision": "3xTF32 tcgen05 element matrices, FP64 assembly sums",
             "e2e": {"value": world * sz.nel / (e2e_ms * 1e-3), "unit": "elements/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm,
-                         # dram__bytes_read.sum + dram__bytes_write.sum of one
-                         # launch (one 24^3 assembly), ncu capture of this kernel
-                         # on this workload; None for other sizes
-                         "traffic": TC_TRAFFIC_24 if NEL == 24 and ke == G.KE_SPLIT_TF32
-                         else None,
+                         "traffic": (TRAFFIC_PER_ELEMENT * sz.nel if TRAFFIC_PER_ELEMENT
+                                     else None),
                          "kernel": "volume integration + scatter passes",
                          "kernel_ms": vmax, "algorithmic_bytes": traffic_alg,
                          "peak_source": src},
@@ -442,25 +526,50 @@ def run_gpu(args):
                 "note": "element stiffness contraction 2 nq (ns ndof^2 + ns^2 ndof), ns = 6, "
                         "counted once although 3xTF32 issues three MMAs per product; peak = "
                         "measured dense bf16 rate (TF32 runs at half of it)"},
-            "cpu_baseline": {"value": cpu_v, "unit": "elements/s", "cores": os.cpu_count(),
+            "cpu_baseline": {"value": cpu_v, "unit": "elements/s", "cores": threads,
                              "kind": "port",
-                             "sample": f"{reps} full assemblies of the same model "
-                                       f"({cpu_dt * 1e3:.0f} ms each)"},
+                             "sample": f"{args.cpu_reps} samples: " +
+                                       SAMPLE_TEXT.format(layers=SAMPLE_LAYERS, n=n_s) +
+                                       f", {cpu_dt * 1e3:.0f} ms each"},
             "gpu_launches": launches,
             "clocks": clocks,
             "wall_s_timed_region": wall,
+            "preprocess_s": preprocess_s,
+            "accuracy": accuracy,
         }
-        if ke == G.KE_SPLIT_TF32:
-            line["accuracy"] = accuracy_vs_fp64(G, W, sim, patches, ng, local)
-        if args.big:
-            line["assembly_64"] = run_assembly_64(args, G, W)
-            line["assembly_64"]["speedup_vs_cpu_port_at_24"] = \
-                line["assembly_64"]["elements_per_s"] / cpu_v
+        line["elasticity_64"] = run_elasticity_solves(args, G, sim, xref)
+        del sim
+        line["assembly_24"] = run_assembly_24(args, G, W)
         if args.solve_nel > 0:
-            line["solve"] = run_solve(args, G, W)
+            line["solve"] = run_solve(args, G, W, threads)
+            if "cpu_solve" in line["solve"]:
+                line["cpu_baseline"]["solve"] = line["solve"]["cpu_solve"]
+        line["cpu_baseline"].setdefault("solve", {})
+        line["cpu_baseline"]["solve"]["superlu_2d_poisson"] = superlu_baseline(W)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def superlu_baseline(W):
+    """scipy's SuperLU with IFEM's options (MMD on A^T + A, diagonal pivot
+    threshold 0.001, symmetric mode; SparseMatrix.C:101-104) on the oracle's
+    FP64 system of the 2D Poisson model (p=2, 32^2 elements), one host thread."""
+    import scipy.sparse as sp
+    from scipy.sparse.linalg import splu
+    patches, ng = W.config1()
+    orc, s = oracle_model(patches, ng)
+    orc.assemble(1)
+    A, b = orc.system()
+    IA, JA = orc.pattern()
+    M = sp.csc_matrix((A, JA, IA), shape=(s["neq"], s["neq"]))
+    t0 = time.perf_counter()
+    lu = splu(M, permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.001,
+              options={"SymmetricMode": True})
+    x = lu.solve(b)
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "neq": s["neq"], "nnz": s["nnz"], "threads": 1,
+            "relres": float(np.linalg.norm(b - M @ x) / np.linalg.norm(b))}
 
 
 def main():
@@ -469,13 +578,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--precision", default="split", choices=["split", "fp64"])
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cpu-reps", type=int, default=3)
     ap.add_argument("--solve-nel", type=int, default=64,
-                    help="elements per direction of the solve leg (0: skip it)")
+                    help="elements per direction of the Poisson solve leg (0: skip it)")
     ap.add_argument("--solve-reps", type=int, default=3)
-    ap.add_argument("--big", type=int, default=1,
-                    help="1: also assemble and solve the 64^3 elasticity model (assembly_64)")
+    ap.add_argument("--ref-solve", type=int, default=1,
+                    help="1: FP64 reference solutions and CPU solve baselines by the oracle")
     ap.add_argument("--train-seeds", type=int, default=200)
     ap.add_argument("--coarse-cells", type=int, default=8)
     args = ap.parse_args()

@@ -1233,13 +1233,17 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
 // the vectors plus the reduction partials, about 5.8 MB, held by every GPU
 // that loads the library.  Host code reaches it through the address that
 // cudaGetSymbolAddress returns for the current device (the array's name in
-// host code is only a host-side stand-in).
+// host code is only a host-side stand-in).  The address is looked up at the
+// first call on a device and kept; the primary context of that device must
+// not be reset (cudaDeviceReset) while the library is in use.  The scalars
+// read back during a solve go through a stack variable of the call (a
+// pageable copy followed by a stream synchronisation allocates nothing), so
+// calls from several host threads share no host memory.
 constexpr int kNoAllocMaxEq = 65536;
 constexpr size_t kNoAllocWords = (size_t)kNoAllocMaxEq * 11 + 2 * kRedBlocks + 16;
 static __device__ __align__(256) double g_noallocWork[kNoAllocWords];
 constexpr int kMaxDevices = 64;
 static double* g_noallocAddr[kMaxDevices] = {};  // device address per device ordinal
-static double g_noallocScalar[2];                // pageable host copy of one reduced scalar
 
 static Work carveFrom(double* base, size_t n)
 {
@@ -1329,14 +1333,15 @@ ifemgpu_status solveNoAlloc(ifemgpu_ctx* ctx, double rtol, int maxit, double* xh
   k_finish<<<1, kThreads, 0, s>>>(w.part, vb, 1, w.scal + 8);
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.r64, ctx->d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(w.scal + 9, w.scal + 8, sizeof(double), cudaMemcpyDeviceToDevice, s));
-  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(g_noallocScalar, w.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
+  double hostScalar = 0.0;  // pageable, per call
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(&hostScalar, w.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
-  const double bn = std::sqrt(g_noallocScalar[0]);
+  const double bn = std::sqrt(hostScalar);
   int inner = 0, outer = 0;
   double relres = bn > 0 ? 1.0 : 0.0;
   ifemgpu_status st = IFEMGPU_OK;
   if (bn > 0) {
-    st = innerPCG64(ctx, w, rtol, maxit, g_noallocScalar, &inner);
+    st = innerPCG64(ctx, w, rtol, maxit, &hostScalar, &inner);
     outer = 1;
     if (st == IFEMGPU_OK) {
       k_accumulate<double><<<vb, kThreads, 0, s>>>(w.x64, w.xD, w.scal, 9, n);
@@ -1344,10 +1349,10 @@ ifemgpu_status solveNoAlloc(ifemgpu_ctx* ctx, double rtol, int maxit, double* xh
                                          w.r64, n, w.part);
       k_finish<<<1, kThreads, 0, s>>>(w.part, sb, 1, w.scal + 9);
       IFEMGPU_CUDA(ctx, cudaGetLastError());
-      IFEMGPU_CUDA(ctx, cudaMemcpyAsync(g_noallocScalar, w.scal + 9, sizeof(double),
+      IFEMGPU_CUDA(ctx, cudaMemcpyAsync(&hostScalar, w.scal + 9, sizeof(double),
                                         cudaMemcpyDeviceToHost, s));
       IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
-      relres = std::sqrt(g_noallocScalar[0]) / bn;
+      relres = std::sqrt(hostScalar) / bn;
     }
   }
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));

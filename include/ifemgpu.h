@@ -374,12 +374,14 @@ ifemgpu_status ifemgpu_solve(ifemgpu_ctx* ctx,
  *     5.8 MB, held by every GPU that loads the library until the process
  *     exits; it limits the system to 65,536 equations (larger systems are
  *     rejected with IFEMGPU_INVALID_ARG).
- *   - The first call on a device looks the array's device address up; make
- *     that first call before any stream capture.
+ *   - The first call on a device looks the array's device address up and
+ *     keeps it; make that first call before any stream capture, and do not
+ *     reset the device (cudaDeviceReset) while the library is in use.
  *   - All calls share the one array: calls that overlap on the GPU (two
  *     contexts of one device on different streams, or from several host
  *     threads) race and give wrong results.  Calls of one context are
- *     ordered on its stream and are safe.
+ *     ordered on its stream and are safe.  Calls on different GPUs use
+ *     different arrays and share no host memory.
  * rtol is the FP64 relative residual target, max_iter the PCG iteration cap,
  * x (neq, host) receives the solution; info is optional.                   */
 ifemgpu_status ifemgpu_solve_noalloc(ifemgpu_ctx* ctx, double rtol, int max_iter,

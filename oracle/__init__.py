@@ -50,7 +50,7 @@ def lib():
             "ifo_secondary": (None, [P, I, V, V]),
             "ifo_constrain_face": (I, [P, I, I, I, D]),
             "ifo_add_neumann": (I, [P, I, I, V]),
-            "ifo_preprocess": (I, [P]), "ifo_sizes": (None, [P, V]),
+            "ifo_preprocess": (I, [P, I]), "ifo_sizes": (None, [P, V]),
             "ifo_get_sam": (None, [P, V, V]), "ifo_get_pattern": (None, [P, V, V]),
             "ifo_get_mnpc": (I, [P, I, V]),
             "ifo_assemble": (C.c_long, [P, I, C.c_long]),
@@ -129,8 +129,10 @@ class OracleModel:
         v[:len(values)] = values
         self.L.ifo_add_neumann(self.h, pid, face, _p(v))
 
-    def preprocess(self):
-        self.L.ifo_preprocess(self.h)
+    def preprocess(self, pattern: int = -1):
+        """pattern: 0 IFEM's std::set couplings, 1 the parallel node-neighbour
+        construction, -1 the latter only for large models (same arrays)."""
+        self.L.ifo_preprocess(self.h, pattern)
         s = np.zeros(6, dtype=np.int32)
         self.L.ifo_sizes(self.h, _p(s))
         self.sizes = dict(nnod=int(s[0]), nel=int(s[1]), ndof=int(s[2]), neq=int(s[3]),

@@ -470,6 +470,81 @@ void buildPattern(Model& m)
   m.b.assign(m.neq, 0.0);
 }
 
+// The same compressed-column pattern as buildPattern for large models (the
+// std::set couplings of SAM::getDofCouplings take minutes and tens of GB at
+// 3e8 entries): all DOFs of a node couple with the same equations -- the free
+// DOFs of every node that shares an element with it -- and equations grow
+// with the global node number (node-major DOFs, free DOFs numbered in DOF
+// order), so a node's sorted, de-duplicated neighbour nodes give each of its
+// columns in ascending row order.  Nodes are processed in parallel.
+void buildPatternFast(Model& m)
+{
+  // elements around each global node (0-based nodes, 1-based elements)
+  std::vector<int> start(m.nnod + 1, 0);
+  for (int iel = 1; iel <= m.nel; iel++)
+    for (int ip = m.mpmnpc[iel - 1]; ip < m.mpmnpc[iel]; ip++) start[m.mmnpc[ip - 1]]++;
+  for (int n = 0; n < m.nnod; n++) start[n + 1] += start[n];
+  std::vector<int> elms(start[m.nnod]);
+  {
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int iel = 1; iel <= m.nel; iel++)
+      for (int ip = m.mpmnpc[iel - 1]; ip < m.mpmnpc[iel]; ip++)
+        elms[fill[m.mmnpc[ip - 1] - 1]++] = iel;
+  }
+  auto freeEqs = [&](int node, std::vector<int>& out) {  // node 0-based
+    for (int d = m.madof[node]; d < m.madof[node + 1]; d++)
+      if (m.meqn[d - 1] > 0) out.push_back(m.meqn[d - 1]);
+  };
+  auto neighbours = [&](int node, std::vector<int>& nb) {
+    nb.clear();
+    for (int k = start[node]; k < start[node + 1]; k++) {
+      const int iel = elms[k];
+      for (int ip = m.mpmnpc[iel - 1]; ip < m.mpmnpc[iel]; ip++) nb.push_back(m.mmnpc[ip - 1] - 1);
+    }
+    std::sort(nb.begin(), nb.end());
+    nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+  };
+  // column lengths, then the row indices
+  std::vector<long long> len(m.nnod, 0);
+#pragma omp parallel
+  {
+    std::vector<int> nb, eqs;
+#pragma omp for schedule(dynamic, 256)
+    for (int n = 0; n < m.nnod; n++) {
+      neighbours(n, nb);
+      eqs.clear();
+      for (int b : nb) freeEqs(b, eqs);
+      len[n] = (long long)eqs.size();
+    }
+  }
+  m.IA.assign(m.neq + 1, 0);
+  std::vector<int> own;
+  for (int n = 0; n < m.nnod; n++) {
+    own.clear();
+    freeEqs(n, own);
+    for (int q : own) m.IA[q] = (int)len[n];
+  }
+  for (int j = 0; j < m.neq; j++) m.IA[j + 1] += m.IA[j];
+  m.JA.assign(m.IA[m.neq], 0);
+#pragma omp parallel
+  {
+    std::vector<int> nb, eqs, mine;
+#pragma omp for schedule(dynamic, 256)
+    for (int n = 0; n < m.nnod; n++) {
+      mine.clear();
+      freeEqs(n, mine);
+      if (mine.empty()) continue;
+      neighbours(n, nb);
+      eqs.clear();
+      for (int b : nb) freeEqs(b, eqs);
+      for (int q : mine)
+        for (size_t i = 0; i < eqs.size(); i++) m.JA[m.IA[q - 1] + i] = eqs[i] - 1;
+    }
+  }
+  m.A.assign(m.JA.size(), 0.0);
+  m.b.assign(m.neq, 0.0);
+}
+
 // SparseMatrix::operator() compressed-column branch, SparseMatrix.C:283-289
 inline double& entry(Model& m, int r, int c)
 {
@@ -1058,11 +1133,26 @@ int ifo_add_neumann(void* h, int pid, int face, const double* t)
   return 0;
 }
 
-int ifo_preprocess(void* h)
+// mode 0: IFEM's std::set couplings (buildPattern), mode 1: the parallel
+// node-neighbour construction (buildPatternFast), -1: the latter for models
+// with more than 5e7 element-matrix entries.  Both give the same arrays.
+int ifo_preprocess(void* h, int mode)
 {
   Model& m = *static_cast<Model*>(h);
   if (!initSAM(m)) return -1;
-  buildPattern(m);
+  long long work = 0;
+  for (int iel = 1; iel <= m.nel; iel++) {
+    long long nd = 0;
+    for (int ip = m.mpmnpc[iel - 1]; ip < m.mpmnpc[iel]; ip++) {
+      const int node = m.mmnpc[ip - 1];
+      nd += m.madof[node] - m.madof[node - 1];
+    }
+    work += nd * nd;
+  }
+  if (mode == 1 || (mode < 0 && work > 50000000LL))
+    buildPatternFast(m);
+  else
+    buildPattern(m);
   return 0;
 }
 
@@ -1106,7 +1196,10 @@ int ifo_get_mnpc(void* h, int pid, int* out)
 long ifo_assemble(void* h, int threads, long max_elements)
 {
   Model& m = *static_cast<Model*>(h);
-  std::fill(m.A.begin(), m.A.end(), 0.0);
+  // SystemMatrix::init / SystemVector::init (zeroing), on every thread
+  const long long nA = (long long)m.A.size();
+#pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1)
+  for (long long i = 0; i < nA; i++) m.A[i] = 0.0;
   std::fill(m.b.begin(), m.b.end(), 0.0);
   long singular = 0;
   for (auto& pc : m.patches) {
@@ -1296,14 +1389,16 @@ int ifo_pcg(void* h, const double* b, double* x, double rtol, int maxit,
 {
   Model& m = *static_cast<Model*>(h);
   const int n = m.neq;
+  const int nt = threads > 0 ? threads : 1;
   std::vector<double> r(n), z(n), p(n), q(n), dinv(n);
+#pragma omp parallel for schedule(static) num_threads(nt)
   for (int j = 0; j < n; j++) {
     dinv[j] = 1.0;
     for (int k = m.IA[j]; k < m.IA[j + 1]; k++)
       if (m.JA[k] == j) dinv[j] = 1.0 / m.A[k];
   }
   auto spmv = [&](const std::vector<double>& v, std::vector<double>& out) {
-#pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1)
+#pragma omp parallel for schedule(static) num_threads(nt)
     for (int j = 0; j < n; j++) {
       double s = 0.0;
       for (int k = m.IA[j]; k < m.IA[j + 1]; k++) s += m.A[k] * v[m.JA[k]];
@@ -1313,6 +1408,7 @@ int ifo_pcg(void* h, const double* b, double* x, double rtol, int maxit,
   std::vector<double> xv(x, x + n);
   spmv(xv, q);
   double bn = 0.0, rz = 0.0;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+:bn, rz)
   for (int i = 0; i < n; i++) {
     r[i] = b[i] - q[i];
     bn += b[i] * b[i];
@@ -1326,12 +1422,15 @@ int ifo_pcg(void* h, const double* b, double* x, double rtol, int maxit,
   double rn = 0.0;
   for (; it < maxit; it++) {
     rn = 0.0;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+:rn)
     for (int i = 0; i < n; i++) rn += r[i] * r[i];
     if (std::sqrt(rn) / bn <= rtol) break;
     spmv(p, q);
     double pq = 0.0;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+:pq)
     for (int i = 0; i < n; i++) pq += p[i] * q[i];
     double alpha = rz / pq, rz1 = 0.0;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+:rz1)
     for (int i = 0; i < n; i++) {
       xv[i] += alpha * p[i];
       r[i] -= alpha * q[i];
@@ -1340,11 +1439,13 @@ int ifo_pcg(void* h, const double* b, double* x, double rtol, int maxit,
     }
     double beta = rz1 / rz;
     rz = rz1;
+#pragma omp parallel for schedule(static) num_threads(nt)
     for (int i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
   }
   // true residual
   spmv(xv, q);
   rn = 0.0;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+:rn)
   for (int i = 0; i < n; i++) rn += (b[i] - q[i]) * (b[i] - q[i]);
   *relres = std::sqrt(rn) / bn;
   std::memcpy(x, xv.data(), sizeof(double) * n);

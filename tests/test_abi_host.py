@@ -194,3 +194,25 @@ def test_errors_are_reported_not_fallen_back(gpulib):
     with pytest.raises(G.IfemGpuError) as e:
         host_sim().add_patch(bad)
     assert e.value.status == G.UNSUPPORTED
+
+
+FAST_CASES = dict(CASES, connected=lambda: W.connected_boxes(kind=2, nel=3, npatch=3,
+                                                                rotated=True))
+
+
+@pytest.mark.parametrize("name", sorted(FAST_CASES))
+def test_oracle_parallel_pattern_equals_set_couplings(oracle_lib, name):
+    """The oracle's parallel pattern construction (used for the large models of
+    the benchmark) gives the arrays of IFEM's std::set couplings."""
+    import oracle
+    made = FAST_CASES[name]()
+    patches, ng = made[0], made[1]
+    conns = made[2] if len(made) > 2 else ()
+    pats = []
+    for mode in (0, 1):
+        orc = oracle.OracleModel(ng)
+        W.load_into(orc, patches, conns)
+        orc.preprocess(pattern=mode)
+        pats.append(orc.pattern())
+    np.testing.assert_array_equal(pats[0][0], pats[1][0])
+    np.testing.assert_array_equal(pats[0][1], pats[1][1])

@@ -43,6 +43,27 @@ def test_noalloc_solve_matches_allocating_solve(gpulib, ke):
         assert np.abs(x - ref).max() <= TOL * np.abs(ref).max()
 
 
+def test_noalloc_first_solve_allocates_no_device_memory(gpulib):
+    """On a freshly assembled model the first solve is the allocation-free one:
+    the device's free memory is the same before and after it (the context has
+    no solver workspace yet, so an allocation would show), and its solution
+    equals the allocating solve's."""
+    torch = pytest.importorskip("torch")
+    warm = model(G.KE_FP64, nel=4)           # loads the solver kernels once
+    warm.solve_noalloc(rtol=1e-10, max_iter=20000)
+    sim = model(G.KE_FP64)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    x, info, st = sim.solve_noalloc(rtol=1e-10, max_iter=20000)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert st == G.OK and info.relres <= 1e-10
+    assert free1 == free0, (free0, free1)
+    ref, rinfo = sim.solveSystem(method=G.PCG_FP64, rtol=1e-10, max_inner=20000)
+    assert info.inner_iters == rinfo.inner_iters
+    assert np.abs(x - ref).max() <= TOL * np.abs(ref).max()
+
+
 def test_noalloc_rejects_systems_above_its_limit(gpulib):
     sim = model(G.KE_SPLIT_TF32, nel=20)     # 3 * 22 * 22 * 21 = 30,492 equations: fits
     assert sim.sizes.neq <= 65536
