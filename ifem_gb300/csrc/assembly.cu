@@ -1008,11 +1008,56 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     }
     if (!onTc[pi] && ctx->patches[pi].nelActive != ctx->patches[pi].nelAll) flow = false;
   }
+  // element scratch of the tensor-core patches (one block per element, read
+  // back by the node-wise gather) and the gather launches per (degree, npv)
+  ctx->elmFloats = 0;
+  for (int pi = 0; pi < np; pi++)
+    if (onTc[pi])
+      ctx->elmFloats += (size_t)ctx->patches[pi].nelAll *
+                        elementBlockFloats(ctx->h_devpatches[pi].p[0], ctx->h_devpatches[pi].npv);
+  if (ctx->elmFloats)
+    IFEMGPU_CUDA(ctx, cudaMalloc(&ctx->d_elm, sizeof(float) * ctx->elmFloats));
+  {
+    size_t at = 0;
+    for (int pi = 0; pi < np; pi++) {
+      DevPatch& D = ctx->h_devpatches[pi];
+      D.elm = nullptr;
+      D.elmStride = 0;
+      if (!onTc[pi]) continue;
+      D.elmStride = (int)elementBlockFloats(D.p[0], D.npv);
+      D.elm = ctx->d_elm + at;
+      at += (size_t)ctx->patches[pi].nelAll * D.elmStride;
+    }
+  }
+  ctx->gathers.clear();
+  ctx->zeroSystem = false;
+  for (int pi = 0; pi < np; pi++) ctx->zeroSystem |= !onTc[pi];
+  for (const auto& cls : {std::make_pair(2, 3), std::make_pair(3, 3), std::make_pair(2, 1),
+                          std::make_pair(3, 1)}) {
+    std::vector<int> start, pidx;
+    int total = 0;
+    for (int pi = 0; pi < np; pi++) {
+      const DevPatch& D = ctx->h_devpatches[pi];
+      if (!onTc[pi] || D.p[0] != cls.first || D.npv != cls.second) continue;
+      start.push_back(total);
+      pidx.push_back(pi);
+      total += ctx->patches[pi].nnod;
+    }
+    if (!total) continue;
+    GatherList g;
+    g.p = cls.first;
+    g.npv = cls.second;
+    g.nranges = (int)start.size();
+    g.total = total;
+    IFEMGPU_TRY(upload(ctx, &g.d_start, start.data(), start.size()));
+    IFEMGPU_TRY(upload(ctx, &g.d_pidx, pidx.data(), pidx.size()));
+    ctx->gathers.push_back(g);
+  }
   for (int pi = 0; pi < np; pi++) {
     DevPatch& D = ctx->h_devpatches[pi];
     D.flagBase = nflags;
     D.tile = 4;
-    if (onTc[pi] || flow) nflags += ctx->patches[pi].nelAll;
+    if (!onTc[pi] && flow) nflags += ctx->patches[pi].nelAll;
     if (onTc[pi] && tcDeg[pi] == 0) {
       // the element kernel integrates this patch's Neumann faces itself
       D.nneu = (int)ctx->patches[pi].neumann.size();
@@ -1034,12 +1079,12 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
           if (pc.active[e]) out.push_back({pi, e, 0, 0});
         }
   };
-  for (int deg : {0, 2, 3}) {  // one persistent launch per tensor-core kernel
+  for (int deg : {0, 2, 3}) {  // one persistent launch per tensor-core kernel, elements in order
     Pass pass{(int)vol.size(), 0, 0, deg ? 1 : 81, deg ? tcPoissonSmem(deg) : tcVolumeSmem(), true};
     pass.tcDeg = deg;
-    for (int c = 0; c < maxColours; c++)
-      for (int pi = 0; pi < np; pi++)
-        if (onTc[pi] && tcDeg[pi] == deg) colourItems(pi, c, vol);
+    for (int pi = 0; pi < np; pi++)
+      if (onTc[pi] && tcDeg[pi] == deg)
+        for (int e = 0; e < ctx->patches[pi].nelAll; e++) vol.push_back({pi, e, 0, 0});
     pass.count = (int)vol.size() - pass.first;
     if (pass.count) ctx->passes.push_back(pass);
   }
@@ -1204,6 +1249,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
       IFEMGPU_TRY(tcPoissonPrepare(ctx));
       break;
     }
+  for (auto& g : ctx->gathers) IFEMGPU_TRY(gatherPrepare(ctx, g));
   return IFEMGPU_OK;
 }
 
@@ -1242,8 +1288,12 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
 {
   cudaStream_t s = ctx->stream;
   if (seg == 0) {
-    IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_K, 0, sizeof(double) * ctx->nnz, s));
-    IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_b, 0, sizeof(double) * ctx->neq, s));
+    // the gather writes every entry of the tensor-core patches' columns; the
+    // generic kernels add into a zeroed system
+    if (ctx->zeroSystem) {
+      IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_K, 0, sizeof(double) * ctx->nnz, s));
+      IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_b, 0, sizeof(double) * ctx->neq, s));
+    }
     IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * 4, s));
     if (ctx->nflags)
       IFEMGPU_CUDA(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(int) * ctx->nflags, s));
@@ -1257,14 +1307,19 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
   SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
             ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore, ctx->d_flags};
   const bool split = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32;
+  if (seg == 1) {  // element kernels of the tensor-core patches, then their gathers
+    for (const Pass& p : ctx->passes) {
+      if (!p.tc) continue;
+      if (p.tcDeg) IFEMGPU_TRY(tcPoissonLaunch(ctx, p, p.tcDeg));
+      else IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
+    }
+    for (const GatherList& g : ctx->gathers) IFEMGPU_TRY(gatherLaunch(ctx, g));
+  }
   for (const Pass& p : ctx->passes) {
+    if (p.tc) continue;
     if ((p.face != 0) != (seg == 2)) continue;
     if ((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow)) continue;
-    if (p.tc && p.tcDeg)
-      IFEMGPU_TRY(tcPoissonLaunch(ctx, p, p.tcDeg));
-    else if (p.tc)
-      IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
-    else if (p.persistent && split)
+    if (p.persistent && split)
       k_volume_gen_flow<float><<<std::min(p.count, ctx->genGrid), 256, p.smem, s>>>(
           ctx->d_patches, ctx->d_items + p.first, p.count, S);
     else if (p.persistent)
@@ -1422,7 +1477,7 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
   int used = 0;
   for (const Pass& p : ctx->passes)
     used += !((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow));
-  ctx->launches_per_assembly = (ctx->h_devpatches.empty() ? 0 : 1) + used;
+  ctx->launches_per_assembly = (ctx->h_devpatches.empty() ? 0 : 1) + used + (int)ctx->gathers.size();
   return IFEMGPU_OK;
 }
 

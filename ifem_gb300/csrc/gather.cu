@@ -1,0 +1,261 @@
+// gather.cu -- deterministic assembly of the tensor-core element matrices:
+// the second half of the tensor-core assembly.  The element kernels
+// (tc_volume.cu, tc_poisson.cu) write each element's matrix (FP32, exactly
+// symmetric) and load vector to a block of an element scratch array; here one
+// warp per node sums, in ascending element order, the contributions of the
+// elements around the node to the node's columns of the compressed-column
+// matrix and to its right-hand side entries, and writes every matrix entry
+// once.  Together they replace the scatter of assemSparse
+// (src/LinAlg/SparseMatrix.C:614-688) driven by SAM::assembleSystem
+// (src/LinAlg/SAM.C:430-543), including the right-hand side corrections of
+// prescribed DOFs (-c0 K(i, j), SparseMatrix.C:639-687).
+//
+// Why a gather: every entry is written by one warp, with its contributions
+// added in a fixed order (the order of the elements' indices), so the result
+// is bitwise reproducible without colouring, flags or atomics, every element
+// kernel runs without waiting for its neighbours, and the matrix needs no
+// zeroing.  The entry (a, k; b, l) and its mirror (b, l; a, k) are summed by
+// different warps from the same exactly symmetric element values in the same
+// element order, so the assembled matrix is exactly symmetric.
+//
+// Element scratch block (floats, per element, `stride` apart):
+//   G[a][k][l][b]  element matrix entry of rows (a, k), column (b, l)
+//                  (a, b element functions, k, l < npv), at
+//                  ((a npv + k) npv + l) nen + b;
+//                  elasticity stores the gradient Gram matrix
+//                  G_kl(a, b) = sum_q w_q dN_a/dx_k dN_b/dx_l and the entry is
+//                  formed here: lambda G_kl + mu G_lk + delta_kl mu tr G;
+//   F[a][k]        element load vector, at npv^2 nen^2 + a npv + k.
+// Sums are double-float (an FP32 value and its FP32 rounding error, Knuth's
+// TwoSum per addition), widened exactly and added once in FP64 at the end:
+// the FP32 element values are summed with an error far below their own.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "ifemgpu_internal.h"
+#include "tc_common.cuh"
+
+namespace ifemgpu {
+
+namespace {
+
+template <int P, int NPV>
+struct GCfg {
+  static constexpr int Q = P + 1;
+  static constexpr int NEN = Q * Q * Q;
+  static constexpr int W = 2 * P + 1;
+  static constexpr int NS = W * W * W;           // neighbour slots of a node
+  static constexpr int KL = NPV * NPV;
+  static constexpr int WARPS = (P == 3 && NPV == 3) ? 4 : 8;
+  static constexpr size_t SMEM = sizeof(float) * 2 * KL * NS * WARPS;
+};
+
+// hi + lo += x (TwoSum: the rounding error of hi + x goes to lo)
+__device__ __forceinline__ void dfAdd(float& hi, float& lo, float x)
+{
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+}  // namespace
+
+size_t elementBlockFloats(int p, int npv)
+{
+  const size_t nen = (size_t)(p + 1) * (p + 1) * (p + 1);
+  const size_t f = (size_t)npv * npv * nen * nen + nen * npv;
+  return (f + 3) & ~(size_t)3;  // 16-byte blocks
+}
+
+struct GatherSys {
+  const int* madof;
+  const int* meqn;
+  const int* F;        // free DOFs of the nodes before each global node
+  const double* c0;    // prescribed values (null: none)
+  const int* colptr;
+  double* K;
+  double* b;
+};
+
+// One warp per node of the patches of one (degree, npv) class; node item t
+// belongs to the last range whose start is <= t.
+template <int P, int NPV>
+__global__ void __launch_bounds__(GCfg<P, NPV>::WARPS * 32)
+k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
+         const int* __restrict__ pidx, int nranges, int total, GatherSys S)
+{
+  using C = GCfg<P, NPV>;
+  constexpr int Q = C::Q, NEN = C::NEN, W = C::W, NS = C::NS, KL = C::KL;
+  extern __shared__ float gsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* accHi = gsm + warp * 2 * KL * NS;  // [kl][slot]
+  float* accLo = accHi + KL * NS;
+  for (int t = blockIdx.x * C::WARPS + warp; t < total; t += gridDim.x * C::WARPS) {
+    int r0 = 0, r1 = nranges - 1;
+    while (r0 < r1) {
+      const int mid = (r0 + r1 + 1) >> 1;
+      if (start[mid] <= t) r0 = mid;
+      else r1 = mid - 1;
+    }
+    const DevPatch& Pt = patches[pidx[r0]];
+    const int a = t - start[r0];
+    const int n0 = Pt.n[0], n1 = Pt.n[1];
+    const int ax = a % n0, ay = (a / n0) % n1, az = a / (n0 * n1);
+    const int ga = Pt.firstNode + a;
+    const int da = S.madof[ga] - 1;
+    int eqa[NPV], cpa[NPV];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < NPV; k++) {
+      eqa[k] = S.meqn[da + k];
+      any |= eqa[k] > 0;
+      cpa[k] = eqa[k] > 0 ? S.colptr[eqa[k] - 1] : 0;
+    }
+    if (!any) continue;  // no column: fixed or prescribed DOFs only
+    for (int i = lane; i < KL * NS; i += 32) {
+      accHi[i] = 0.f;
+      accLo[i] = 0.f;
+    }
+    float feHi = 0.f, feLo = 0.f;  // lane k < NPV: load vector of DOF k
+    const float lamf = Pt.lamf, muf = Pt.muf;
+    const int ex0 = max(0, ax - P), ex1 = min(ax, Pt.nel[0] - 1);
+    const int ey0 = max(0, ay - P), ey1 = min(ay, Pt.nel[1] - 1);
+    const int ez0 = max(0, az - P), ez1 = min(az, Pt.nel[2] - 1);
+    __syncwarp();
+    for (int ez = ez0; ez <= ez1; ez++)
+      for (int ey = ey0; ey <= ey1; ey++)
+        for (int ex = ex0; ex <= ex1; ex++) {
+          const size_t e = ((size_t)ez * Pt.nel[1] + ey) * Pt.nel[0] + ex;
+          const int alx = ax - ex, aly = ay - ey, alz = az - ez;
+          const int al = alx + Q * (aly + Q * alz);
+          const float* blk = Pt.elm + e * (size_t)Pt.elmStride;
+          const float* row = blk + (size_t)al * KL * NEN;
+#pragma unroll
+          for (int bb = 0; bb < (NEN + 31) / 32; bb++) {
+            const int bl = lane + 32 * bb;
+            if (bl < NEN) {
+              const int blx = bl % Q, bly = (bl / Q) % Q, blz = bl / (Q * Q);
+              const int s = (blx - alx + P) + W * ((bly - aly + P) + W * (blz - alz + P));
+              float g[KL];
+#pragma unroll
+              for (int kl = 0; kl < KL; kl++) g[kl] = __ldcs(row + kl * NEN + bl);
+              if (NPV == 3) {
+                const float tr = muf * (g[0] + g[4] + g[8]);
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                  for (int l = 0; l < 3; l++) {
+                    const float ke = fmaf(lamf, g[3 * k + l], fmaf(muf, g[3 * l + k], k == l ? tr : 0.f));
+                    dfAdd(accHi[(3 * k + l) * NS + s], accLo[(3 * k + l) * NS + s], ke);
+                  }
+              } else {
+                dfAdd(accHi[s], accLo[s], g[0]);
+              }
+            }
+          }
+          if (lane < NPV) dfAdd(feHi, feLo, __ldcs(blk + (size_t)KL * NEN * NEN + al * NPV + lane));
+          __syncwarp();
+        }
+    // write the node's columns; prescribed neighbours feed the right-hand side
+    double corr[NPV];
+#pragma unroll
+    for (int k = 0; k < NPV; k++) corr[k] = 0.0;
+    const int* lineOff = Pt.lineOff + (size_t)a * W * W;
+    for (int s = lane; s < NS; s += 32) {
+      const int dx = s % W - P, dy = (s / W) % W - P, dz = s / (W * W) - P;
+      const int bx = ax + dx, by = ay + dy, bz = az + dz;
+      if (bx < 0 || bx >= n0 || by < 0 || by >= n1 || bz < 0 || bz >= Pt.n[2]) continue;
+      const int gb = Pt.firstNode + (bz * n1 + by) * n0 + bx;
+      const int db = S.madof[gb] - 1;
+      const int pos = lineOff[(dz + P) * W + dy + P] + S.F[gb];
+      int rank = 0;
+#pragma unroll
+      for (int l = 0; l < NPV; l++) {
+        const int eqb = S.meqn[db + l];
+        if (eqb == 0) continue;
+#pragma unroll
+        for (int k = 0; k < NPV; k++) {
+          if (eqa[k] <= 0) continue;
+          const int kl = k * NPV + l;
+          const double v = tc::widenF32(accHi[kl * NS + s]) + tc::widenF32(accLo[kl * NS + s]);
+          if (eqb > 0)
+            S.K[cpa[k] + pos + rank] = v;
+          else if (S.c0)
+            corr[k] = fma(S.c0[-eqb - 1], v, corr[k]);
+        }
+        rank += eqb > 0;
+      }
+    }
+    // right-hand side: load vector minus the prescribed-DOF terms, the lanes'
+    // parts added in a fixed order
+#pragma unroll
+    for (int k = 0; k < NPV; k++) {
+      double c = corr[k];
+      if (S.c0)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+      const float fh = __shfl_sync(0xffffffffu, feHi, k), fl = __shfl_sync(0xffffffffu, feLo, k);
+      if (lane == 0 && eqa[k] > 0) S.b[eqa[k] - 1] = (tc::widenF32(fh) + tc::widenF32(fl)) - c;
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+namespace {
+
+template <int P, int NPV>
+ifemgpu_status prepareOne(ifemgpu_ctx* ctx, GatherList& g)
+{
+  using C = GCfg<P, NPV>;
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_gather<P, NPV>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)C::SMEM));
+  int perSM = 0;
+  IFEMGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_gather<P, NPV>,
+                                                                  C::WARPS * 32, C::SMEM));
+  const int need = (g.total + C::WARPS - 1) / C::WARPS;
+  g.grid = std::max(1, std::min(need, std::max(1, perSM) * ctx->numSMs));
+  return IFEMGPU_OK;
+}
+
+template <int P, int NPV>
+ifemgpu_status launchOne(ifemgpu_ctx* ctx, const GatherList& g)
+{
+  using C = GCfg<P, NPV>;
+  GatherSys S{ctx->d_madof, ctx->d_meqn, ctx->d_freeBefore, ctx->nceq ? ctx->d_c0 : nullptr,
+              ctx->d_colptr, ctx->d_K, ctx->d_b};
+  k_gather<P, NPV><<<g.grid, C::WARPS * 32, C::SMEM, ctx->stream>>>(
+      ctx->d_patches, g.d_start, g.d_pidx, g.nranges, g.total, S);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  return IFEMGPU_OK;
+}
+
+}  // namespace
+
+// kernel attributes and grid of a gather launch (before any capture)
+ifemgpu_status gatherPrepare(ifemgpu_ctx* ctx, GatherList& g)
+{
+  if (g.p == 2 && g.npv == 3) return prepareOne<2, 3>(ctx, g);
+  if (g.p == 2 && g.npv == 1) return prepareOne<2, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 1) return prepareOne<3, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 3) return prepareOne<3, 3>(ctx, g);
+  return setError(ctx, IFEMGPU_INVALID_ARG, "internal: gather class");
+}
+
+ifemgpu_status gatherLaunch(ifemgpu_ctx* ctx, const GatherList& g)
+{
+  if (g.total == 0) return IFEMGPU_OK;
+  if (g.p == 2 && g.npv == 3) return launchOne<2, 3>(ctx, g);
+  if (g.p == 2 && g.npv == 1) return launchOne<2, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 1) return launchOne<3, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 3) return launchOne<3, 3>(ctx, g);
+  return setError(ctx, IFEMGPU_INVALID_ARG, "internal: gather class");
+}
+
+}  // namespace ifemgpu

@@ -48,8 +48,6 @@ void freeDevice(ifemgpu_ctx* ctx)
     f(pc.d_logk); pc.d_logk = nullptr;
     f(pc.d_noise); pc.d_noise = nullptr;
     f(pc.d_mlgn); pc.d_mlgn = nullptr;
-    f(pc.d_nodeTab); pc.d_nodeTab = nullptr;
-    f(pc.d_lineTab); pc.d_lineTab = nullptr;
     f(pc.d_tmaps); pc.d_tmaps = nullptr;
     for (int d = 0; d < 3; d++) {
       f(pc.d_knots[d]); f(pc.d_tabN[d]); f(pc.d_tabD[d]); f(pc.d_span[d]); f(pc.d_tabB[d]);
@@ -63,6 +61,14 @@ void freeDevice(ifemgpu_ctx* ctx)
   f(ctx->d_items); f(ctx->d_neumann); f(ctx->d_counters); f(ctx->d_freeBefore);
   f(ctx->d_flags);
   f(ctx->d_basisStart);
+  f(ctx->d_elm);
+  for (auto& g : ctx->gathers) {
+    f(g.d_start);
+    f(g.d_pidx);
+  }
+  ctx->gathers.clear();
+  ctx->d_elm = nullptr;
+  ctx->elmFloats = 0;
   ctx->d_freeBefore = nullptr;
   ctx->d_flags = nullptr;
   ctx->d_basisStart = nullptr;

@@ -66,10 +66,13 @@ struct DevPatch {
   // line), so that row (a, k) sits in column (b, l) at
   // colptr[c] + lineOff[...] + F(a) + rank of k among a's free DOFs.
   const int* lineOff;
-  // tensor-core patches: three TMA tensor maps (128 B each) over the control
-  // net, a per-node table (eq0..2, F, colptr of the free DOFs) and the
-  // line-offset rows padded to 28 values, each read as 3x3x3 node boxes
+  // tensor-core patches: TMA tensor map (128 B) of the control net, read as
+  // (p+1)^3 node boxes
   const void* tmaps;
+  // tensor-core patches: element scratch (one block of elmStride floats per
+  // element: element matrix and load vector, see gather.cu)
+  float* elm;
+  int elmStride;
   // Gauss rules: volume (gx, gw) and face (fx, fw, ngf points)
   double gx[3][kMaxGauss], gw[3][kMaxGauss];
   float gwf[3][kMaxGauss];
@@ -116,9 +119,7 @@ struct HostPatch {
   int firstNode = 0, firstElm = 0;
   std::vector<int> mlgn;     // global 0-based node of each patch node (IFEM's MLGN - 1)
   int* d_mlgn = nullptr;     // device copy for connected models
-  int* d_nodeTab = nullptr;  // tensor-core patches: node table and line-offset rows
-  int* d_lineTab = nullptr;
-  void* d_tmaps = nullptr;   // their TMA tensor maps
+  void* d_tmaps = nullptr;   // tensor-core patches: TMA tensor map of the control net
   std::vector<char> active;  // per element: non-zero parametric volume
   int nen() const {
     return (p[0] + 1) * (p[1] + 1) * (dim == 3 ? p[2] + 1 : 1);
@@ -150,6 +151,17 @@ struct Pass {
   int tcDeg = 0;  // 0: elasticity p = 2 kernel; 2, 3: Poisson kernel of that degree
   bool persistent = false;  // one colour-major launch ordered by done flags
   bool altColour = false;   // colour pass over a part of the persistent pass' items
+};
+
+// Node-wise gather launch of one (degree, npv) class of tensor-core patches:
+// node item t belongs to patch pidx[r] for the last range r with start[r] <= t.
+struct GatherList {
+  int p = 0, npv = 0;
+  int* d_start = nullptr;
+  int* d_pidx = nullptr;
+  int nranges = 0;
+  int total = 0;
+  int grid = 0;
 };
 
 // tc_volume.cu
@@ -194,8 +206,13 @@ struct ifemgpu_ctx {
   double* d_neumann = nullptr;  // Neumann values, 3 per face condition
   std::vector<ifemgpu::Pass> passes;
   unsigned long long* d_counters = nullptr;  // [0] singular points
-  int* d_flags = nullptr;        // per-element done flags of the tensor-core pass
+  int* d_flags = nullptr;        // per-element done flags of the persistent generic pass
   int nflags = 0;
+  // tensor-core patches: element scratch and the node-wise gather launches
+  float* d_elm = nullptr;
+  size_t elmFloats = 0;
+  std::vector<ifemgpu::GatherList> gathers;
+  bool zeroSystem = true;        // some patch adds into the system (generic kernels)
   // statistics of the last assembly
   double last_total_ms = 0.0, last_volume_ms = 0.0;
   unsigned long long last_singular = 0;
@@ -272,6 +289,11 @@ size_t tcPoissonSmem(int deg);
 ifemgpu_status tcPoissonPrepare(ifemgpu_ctx* ctx);
 ifemgpu_status tcPoissonLaunch(ifemgpu_ctx* ctx, const Pass& p, int deg);
 ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid);
+
+// gather.cu
+size_t elementBlockFloats(int p, int npv);
+ifemgpu_status gatherPrepare(ifemgpu_ctx* ctx, GatherList& g);
+ifemgpu_status gatherLaunch(ifemgpu_ctx* ctx, const GatherList& g);
 
 // solver.cu
 ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o,

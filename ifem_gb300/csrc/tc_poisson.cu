@@ -2,17 +2,16 @@
 // Poisson integrand with p = 2 and p = 3 spline patches (Gauss rule p + 1 per
 // direction): the hot loop of ASMs3D::integrate (src/ASM/ASMs3D.C:2266-2312)
 // with EqualOrderOperators::Weak::LaplacianCoeff and ::Source
-// (Apps/Utils/EqualOrderOperators.C:158-265), and the scatter of assemSparse
-// (src/LinAlg/SparseMatrix.C:614-688).
+// (Apps/Utils/EqualOrderOperators.C:158-265).  The element matrices go to the
+// element scratch, which the node-wise gather (gather.cu) sums into the
+// compressed-column matrix (the scatter of assemSparse,
+// src/LinAlg/SparseMatrix.C:614-688).
 //
 // One persistent launch per degree processes every element of its patches,
-// one CTA of 128 threads per element, elements in colour-major order (the
-// same done-flag ordering as the elasticity kernel, so the FP64 sums are
-// deterministic).  Per element:
-//   0. the (p+1)^3 node box -- control points, a node table (equation, free
-//      nodes before the node, column start) and the pattern's line-offset
-//      rows -- staged by TMA; the control points are requested as soon as the
-//      previous element has read its own, the tables after its scatter;
+// one CTA of 128 threads per element, elements in index order (no element
+// waits for another).  Per element:
+//   0. the (p+1)^3 control points staged by TMA, requested as soon as the
+//      previous element has read its own;
 //   1. geometry at the Gauss points by sum factorisation of the homogeneous
 //      control net (w x, w y, w z, w) and of w g, w n (log-conductivity and
 //      source noise at the nodes): three contractions of (p+1) terms, FP32;
@@ -25,9 +24,9 @@
 //      function rows, N = 32 or 64, K = 96 per chunk), FP32 accumulation in
 //      tensor memory; the element load vector Fe_a = sum_q R_a f_q w_q on the
 //      CUDA cores while the operand rows are formed;
-//   4. K from tensor memory to shared memory, then FP64 L2 reductions into the
-//      compressed-column matrix once every lower-colour neighbour (sharing a
-//      node: within p elements in each direction) has published its flag.
+//   4. K from tensor memory to shared memory, exactly symmetric (the upper
+//      triangle mirrored), and with Fe to the element's scratch block
+//      K[a][b], F[a].
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -41,8 +40,6 @@ using namespace tc;
 
 namespace {
 
-constexpr uint32_t kPoisFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wait
-
 template <int P>
 struct PCfg {
   static constexpr int Q = P + 1;                  // functions and Gauss points per direction
@@ -55,27 +52,22 @@ struct PCfg {
   static constexpr int PTS = 32 / SPLIT;           // points per thread and chunk (8, 16)
   static constexpr int TILE = ROWS * kK;           // floats per 32-wide K tile
   static constexpr int TFL = 3 * TILE;             // floats per chunk and copy (K = 96)
-  static constexpr int W = 2 * P + 1;              // line-table width
-  static constexpr int LINES = W * W;              // 25, 49
-  static constexpr int LPAD = (LINES + 3) & ~3;    // 28, 52: 16-byte rows for TMA
   static constexpr int GS = NEN % 2 ? NEN : NEN + 1;  // odd Gram row stride (conflict-free)
-  static constexpr int NB = W * W * W;             // neighbourhood incl. the element
   static constexpr int OVER = (128 - ROWS) * kK;   // floats the A operand reads past Tlo
   static constexpr int PER_SM = P == 2 ? 5 : 3;    // CTAs per SM (shared memory)
+  static constexpr int BLOCK = NEN * NEN + NEN;    // element block: K[a][b], F[a] (16-byte multiple)
 };
 
 template <int P>
 struct PSmem {
   using C = PCfg<P>;
   alignas(128) double ctrlT[C::NEN][4];    // control points x, y, z, w (TMA)
-  alignas(128) int nodeT[C::NEN][4];       // eq, F(node), colptr(eq - 1), 0 (TMA)
-  alignas(128) int lineT[C::NEN][C::LPAD]; // line-offset row of the node (TMA)
   float X[C::NEN][4];                      // relative control points, weight
   float fv[2][C::NEN];                     // log-conductivity and noise at the nodes
   float tb[3][2][C::Q2];                   // 1D tables [direction][N, dN/du][g (p+1) + i]
   float fePart[C::SPLIT][C::ROWS];         // element load vector, per point group
   double c00[3];                           // first control point of the element
-  unsigned long long mbar, ctrlbar, tabbar;
+  unsigned long long mbar, ctrlbar;
   uint32_t tmemSlot;
   int fail;
   int signs;                               // bit 0: some kappa w > 0, bit 1: some < 0
@@ -104,17 +96,14 @@ static_assert(sizeof(PSmem<2>) + 1024 <= 233472 / 5, "five p = 2 CTAs per SM");
 static_assert(6 * 64 + 10 * 64 + 14 * 64 + 64 * 24 <= PCfg<3>::TFL &&
                   6 * 27 + 10 * 27 + 14 * 27 + 27 * 24 <= PCfg<2>::TFL,
               "sum-factorisation arrays fit in the operand tile");
-static_assert(PCfg<3>::NEN * PCfg<3>::GS <= PCfg<3>::TFL &&
-                  PCfg<2>::NEN * PCfg<2>::GS <= PCfg<2>::TFL,
-              "element matrix fits in the operand tile");
+static_assert(PCfg<3>::NEN * (PCfg<3>::GS + 1) <= PCfg<3>::TFL &&
+                  PCfg<2>::NEN * (PCfg<2>::GS + 1) <= PCfg<2>::TFL,
+              "element matrix and load vector fit in the operand tile");
+static_assert(PCfg<3>::BLOCK % 4 == 0 && PCfg<2>::BLOCK % 4 == 0, "16-byte element blocks");
 
 }  // namespace
 
 struct PoisSys {
-  const double* c0;
-  double* K;
-  double* b;
-  int* flags;
   unsigned long long* counters;  // [0] singular points, [2] device timeouts
 };
 
@@ -131,12 +120,10 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
                     offsetof(PSmem<P>, t) == offsetof(PSmem<P>, Tlo) + sizeof(float) * C::TFL,
                 "A-operand reads past Tlo must stay inside the union");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t mbar = smemAddr(&sm.mbar), ctrlbar = smemAddr(&sm.ctrlbar),
-                 tabbar = smemAddr(&sm.tabbar);
+  const uint32_t mbar = smemAddr(&sm.mbar), ctrlbar = smemAddr(&sm.ctrlbar);
   if (tid == 0) {
     mbarInit(mbar, 1);
     mbarInit(ctrlbar, 1);
-    mbarInit(tabbar, 1);
     sm.fail = 0;
   }
   if (warp == 0) tmemAlloc(&sm.tmemSlot, C::ROWS);
@@ -146,47 +133,27 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
   const uint32_t tmem = sm.tmemSlot;
   const uint32_t tHi = smemAddr(sm.Thi), tLo = smemAddr(sm.Tlo);
   uint32_t phase = 0;
-  int* pending = nullptr;  // done flag of the previous element (published at step 4)
   int mapPatch = -1;
-  bool ctrlOut = false, tabOut = false;  // copies in flight (thread 0)
-  auto nodeBox = [&](int itn, const char*& tm, int& f1, int& f2, int& f3) {
+  bool ctrlOut = false;  // copy in flight (thread 0)
+  auto stageCtrl = [&](int itn) {
     const Item nx = items[itn];
     const DevPatch& Pn = patches[nx.patch];
-    f1 = nx.elem % Pn.nel[0];
-    f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
-    f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
-    tm = static_cast<const char*>(Pn.tmaps);
+    const int f1 = nx.elem % Pn.nel[0];
+    const int f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
+    const int f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
+    const char* tm = static_cast<const char*>(Pn.tmaps);
     if (nx.patch != mapPatch) {
       tmapAcquire(tm);
-      tmapAcquire(tm + 128);
-      tmapAcquire(tm + 256);
       mapPatch = nx.patch;
     }
-  };
-  auto stageCtrl = [&](int itn) {
-    const char* tm;
-    int f1, f2, f3;
-    nodeBox(itn, tm, f1, f2, f3);
     mbarExpectTx(ctrlbar, sizeof(double) * C::NEN * 4);
     tmaLoad4d(smemAddr(sm.ctrlT), tm, 0, f1, f2, f3, ctrlbar);
     ctrlOut = true;
   };
-  auto stageTab = [&](int itn) {
-    const char* tm;
-    int f1, f2, f3;
-    nodeBox(itn, tm, f1, f2, f3);
-    mbarExpectTx(tabbar, sizeof(int) * C::NEN * (4 + C::LPAD));
-    tmaLoad4d(smemAddr(sm.nodeT), tm + 128, 0, f1, f2, f3, tabbar);
-    tmaLoad4d(smemAddr(sm.lineT), tm + 256, 0, f1, f2, f3, tabbar);
-    tabOut = true;
-  };
-  if (tid == 0 && (int)blockIdx.x < count) {
-    stageCtrl(blockIdx.x);
-    stageTab(blockIdx.x);
-  }
-  uint32_t cphase = 0, tphase = 0;
+  if (tid == 0 && (int)blockIdx.x < count) stageCtrl(blockIdx.x);
+  uint32_t cphase = 0;
 
-  // the next element's item is read during the current element's scatter
+  // the next element's item is read during the current element's store
   Item nextItem{};
   if ((int)blockIdx.x < count) nextItem = items[blockIdx.x];
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
@@ -456,7 +423,10 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       break;
     }
 
-    // ---- 4. tensor memory -> element matrix G in shared memory
+    // ---- 4. tensor memory -> element matrix G in shared memory (row stride
+    //         GS), exactly symmetric: row m keeps its entries at and right of
+    //         the diagonal and mirrors them (the MMA's FP32 sums of G_ab and
+    //         G_ba need not agree); the load vector after it
     float* G = sm.Thi;
     if (signs && warp < C::ROWS / 32) {
       float v[16];
@@ -468,126 +438,44 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
 #pragma unroll
           for (int i = 0; i < 16; i++) {
             const int n = 16 * c16 + i;
-            if (n < C::NEN) G[m * C::GS + n] = v[i];
+            if (n < C::NEN && n >= m) {
+              G[m * C::GS + n] = v[i];
+              G[n * C::GS + m] = v[i];
+            }
           }
         }
       }
     } else if (!signs) {
       for (int i = tid; i < C::NEN * C::GS; i += blockDim.x) G[i] = 0.f;
     }
+    if (tid < C::NEN) {
+      float fs = 0.f;
+#pragma unroll
+      for (int g = 0; g < C::SPLIT; g++) fs += sm.fePart[g][tid];
+      G[C::NEN * C::GS + tid] = fs;
+    }
     tcFenceBefore();
-
-    // publish the previous element, then wait for the lower-colour neighbours
-    if (tid == 0 && pending) {
-      __threadfence();
-      storeRelease(pending, 1);
-      pending = nullptr;
-    }
-    const int myc = e1 % Q + Q * (e2 % Q) + Q2 * (e3 % Q);
-    {
-      // this thread's lower-colour neighbours: every flag read issued before
-      // any spin, one acquire fence after the last
-      constexpr int R = (C::NB + 127) / 128;
-      const int* fl[R];
-      int seen[R];
-#pragma unroll
-      for (int r = 0; r < R; r++) {
-        const int t = tid + 128 * r;
-        fl[r] = nullptr;
-        if (t >= C::NB) continue;
-        const int dx = t % C::W - P, dy = (t / C::W) % C::W - P, dz = t / (C::W * C::W) - P;
-        const int f1 = e1 + dx, f2 = e2 + dy, f3 = e3 + dz;
-        if ((dx | dy | dz) == 0 || f1 < 0 || f1 >= Pt.nel[0] || f2 < 0 || f2 >= Pt.nel[1] ||
-            f3 < 0 || f3 >= Pt.nel[2])
-          continue;
-        if (f1 % Q + Q * (f2 % Q) + Q2 * (f3 % Q) >= myc) continue;
-        fl[r] = S.flags + Pt.flagBase + (f3 * Pt.nel[1] + f2) * Pt.nel[0] + f1;
-      }
-#pragma unroll
-      for (int r = 0; r < R; r++) seen[r] = fl[r] ? loadRelaxed(fl[r]) : 1;
-#pragma unroll
-      for (int r = 0; r < R; r++) {
-        if (!fl[r]) continue;
-        uint32_t spin = 0;
-        while (seen[r] == 0) {
-          if (++spin > kPoisFlagSpin) {
-            atomicAdd(S.counters + 2, 1ull);
-            break;
-          }
-          __nanosleep(64);
-          seen[r] = loadRelaxed(fl[r]);
-        }
-      }
-      // acquire: the neighbours' reductions happen before this CTA's (the
-      // barrier below extends it to every thread)
-#pragma unroll
-      for (int r = 0; r < R; r++)
-        if (fl[r]) seen[r] = loadAcquire(fl[r]);
-    }
-    if (mbarWait(tabbar, tphase)) {
-      tphase ^= 1u;
-      tabOut = false;
-    } else {
-      atomicAdd(S.counters + 2, 1ull);
-      sm.fail = 1;
-    }
     __syncthreads();
-    if (sm.fail) break;
-
     if (it + (int)gridDim.x < count) nextItem = items[it + gridDim.x];
 
-    // ---- 5. FP64 reductions: row a per lane (consecutive rows of a column
-    //         are consecutive entries), a share of the columns per thread group
-    if (ra < C::NEN && sm.nodeT[ra][0] > 0) {
-      const int base = sm.nodeT[ra][1];
-      const int rowLine = (ra / Q2 + P) * C::W + (ra / Q) % Q + P;
-      const float* Grow = G + ra * C::GS;
-      const int b0 = hg * C::NEN / C::SPLIT, b1 = (hg + 1) * C::NEN / C::SPLIT;
-#pragma unroll 4
-      for (int bn = b0; bn < b1; bn++) {
-        if (sm.nodeT[bn][0] <= 0) continue;
-        const int off = sm.lineT[bn][rowLine - (bn / Q2) * C::W - (bn / Q) % Q] + base;
-        // the upper triangle for both halves: an exactly symmetric element
-        // matrix (the MMA's FP32 sums of G_ab and G_ba need not agree)
-        const float g = bn >= ra ? Grow[bn] : G[bn * C::GS + ra];
-        redAdd(S.K + sm.nodeT[bn][2] + off, widenF32(g));
-      }
-    }
-    // right-hand side: load vector minus prescribed-DOF terms
-    if (tid < C::NEN) {
-      const int r = sm.nodeT[tid][0];
-      if (r > 0) {
-        float fs = 0.f;
+    // ---- 5. the element block to the scratch: K[a][b] (row stride nen), F[a]
+    {
+      float4* dst = reinterpret_cast<float4*>(Pt.elm + (size_t)e * Pt.elmStride);
+      for (int i4 = tid; i4 < C::BLOCK / 4; i4 += blockDim.x) {
+        float v4[4];
 #pragma unroll
-        for (int g = 0; g < C::SPLIT; g++) fs += sm.fePart[g][tid];
-        double acc = widenF32(fs);
-        if (S.c0) {
-          for (int bn = 0; bn < C::NEN; bn++) {
-            const int ce = sm.nodeT[bn][0];
-            if (ce < 0)
-              acc -= S.c0[-ce - 1] * widenF32(bn >= tid ? G[tid * C::GS + bn] : G[bn * C::GS + tid]);
-          }
+        for (int u = 0; u < 4; u++) {
+          const int i = 4 * i4 + u;
+          const int a = i / C::NEN, b = i - a * C::NEN;
+          v4[u] = a < C::NEN ? G[a * C::GS + b] : G[C::NEN * C::GS + b];
         }
-        if (acc != 0.0) redAdd(S.b + r - 1, acc);
+        dst[i4] = make_float4(v4[0], v4[1], v4[2], v4[3]);
       }
     }
-
-    // ---- 6. reductions issued; the flag is published at the next element
-    __syncthreads();
-    if (tid == 0) {
-      pending = S.flags + Pt.flagBase + e;
-      if (it + (int)gridDim.x < count) stageTab(it + gridDim.x);  // node tables are free now
-    }
+    __syncthreads();  // the next element's node data overwrite the tile
   }
-  if (tid == 0) {
-    if (pending) {
-      __threadfence();
-      storeRelease(pending, 1);
-    }
-    // after a timeout: copies still in flight land before the CTA exits
-    if (ctrlOut) mbarWait(ctrlbar, cphase);
-    if (tabOut) mbarWait(tabbar, tphase);
-  }
+  // after a timeout: a copy still in flight lands before the CTA exits
+  if (tid == 0 && ctrlOut) mbarWait(ctrlbar, cphase);
   tcFenceBefore();
   __syncthreads();
   tcFenceAfter();
@@ -611,32 +499,16 @@ int tcPoissonDegree(const DevPatch& D, const HostPatch& pc)
 
 size_t tcPoissonSmem(int deg) { return deg == 2 ? sizeof(PSmem<2>) : sizeof(PSmem<3>); }
 
-// node table (eq, F, column start), padded line-offset rows and the three
-// tensor maps of a patch; false leaves the patch to the generic kernel
+// the tensor map of the control net ((p+1)^3 node boxes); false leaves the
+// patch to the generic kernel
 bool tcPoissonUpload(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D, int deg)
 {
-  const int lines = (2 * deg + 1) * (2 * deg + 1), lpad = (lines + 3) & ~3;
-  if (pc.lineOff.size() != (size_t)pc.nnod * lines || !pc.d_ctrl) return false;
-  std::vector<int> nodeT((size_t)pc.nnod * 4, 0), lineT((size_t)pc.nnod * lpad, 0);
-  for (int n = 0; n < pc.nnod; n++) {
-    const int g = pc.mlgn[n];
-    const int q = ctx->meqn[ctx->madof[g] - 1];
-    nodeT[(size_t)n * 4] = q;
-    nodeT[(size_t)n * 4 + 1] = ctx->freeBefore[g];
-    nodeT[(size_t)n * 4 + 2] = q > 0 ? ctx->colptr[q - 1] : 0;
-    for (int t = 0; t < lines; t++) lineT[(size_t)n * lpad + t] = pc.lineOff[(size_t)n * lines + t];
-  }
-  auto put = [&](auto** dst, const auto* src, size_t bytes) {
-    return cudaMalloc((void**)dst, bytes) == cudaSuccess &&
-           cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
-  };
-  unsigned char maps[3][128];
-  const bool ok = put(&pc.d_nodeTab, nodeT.data(), sizeof(int) * nodeT.size()) &&
-                  put(&pc.d_lineTab, lineT.data(), sizeof(int) * lineT.size()) &&
-                  nodeBoxMap(maps[0], 8, (void*)pc.d_ctrl, 4, pc.n, deg + 1) &&
-                  nodeBoxMap(maps[1], 4, pc.d_nodeTab, 4, pc.n, deg + 1) &&
-                  nodeBoxMap(maps[2], 4, pc.d_lineTab, lpad, pc.n, deg + 1) &&
-                  put(&pc.d_tmaps, maps, sizeof(maps));
+  (void)ctx;
+  if (!pc.d_ctrl) return false;
+  alignas(64) unsigned char map[128];
+  const bool ok = nodeBoxMap(map, 8, (void*)pc.d_ctrl, 4, pc.n, deg + 1) &&
+                  cudaMalloc(&pc.d_tmaps, sizeof(map)) == cudaSuccess &&
+                  cudaMemcpy(pc.d_tmaps, map, sizeof(map), cudaMemcpyHostToDevice) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     return false;
@@ -665,13 +537,12 @@ ifemgpu_status tcPoissonPrepare(ifemgpu_ctx* ctx)
 ifemgpu_status tcPoissonLaunch(ifemgpu_ctx* ctx, const Pass& p, int deg)
 {
   if (deg != 2 && deg != 3) return setError(ctx, IFEMGPU_INVALID_ARG, "internal: Poisson kernel degree");
-  PoisSys S{ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_K, ctx->d_b, ctx->d_flags, ctx->d_counters};
+  PoisSys S{ctx->d_counters};
   const void* fn = deg == 2 ? (const void*)k_volume_tc_poisson<2> : (const void*)k_volume_tc_poisson<3>;
   const size_t smem = tcPoissonSmem(deg);
   const int cap = deg == 2 ? PCfg<2>::PER_SM : PCfg<3>::PER_SM;
-  // every CTA must be resident (they wait on each other's done flags): the
-  // grid follows the SM's shared memory and registers; should residency ever
-  // fail, the bounded waits end with a reported device timeout
+  // as many CTAs as fit at once (shared memory, registers); no CTA waits
+  // for another
   cudaFuncAttributes fa{};
   IFEMGPU_CUDA(ctx, cudaFuncGetAttributes(&fa, fn));
   int smemSM = 0, resv = 0, regsSM = 0;

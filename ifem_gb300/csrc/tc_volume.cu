@@ -1,17 +1,17 @@
 // tc_volume.cu -- tensor-core (tcgen05, sm_103a) element kernel for 3D
 // isotropic linear elasticity with quadratic (p=2) spline patches and 3x3x3
 // Gauss points: the hot loop of ASMs3D::integrate (src/ASM/ASMs3D.C:2266-2312)
-// with the linear-elasticity integrand, and the scatter of assemSparse
-// (src/LinAlg/SparseMatrix.C:614-688).
+// with the linear-elasticity integrand.  Its element matrices go to the
+// element scratch, which the node-wise gather (gather.cu) sums into the
+// compressed-column matrix (the scatter of assemSparse,
+// src/LinAlg/SparseMatrix.C:614-688).
 //
 // One persistent launch processes every element of the eligible patches.
-// Per element (one CTA of 128 threads, elements in colour-major order):
-//   0. the element's 3x3x3 node box -- control points, a node table (equation
-//      numbers, free DOFs before the node, column starts) and the rows of the
-//      pattern's line-offset table -- staged in shared memory by TMA, the
-//      control points requested as soon as the previous element has read its
-//      own, the tables once its scatter is done (they are first read at the
-//      scatter, so both copies overlap a whole front end);
+// Per element (one CTA of 128 threads; elements in index order, no element
+// waits for another):
+//   0. the element's 3x3x3 control points staged in shared memory by TMA,
+//      the next element's requested as soon as the current one has read its
+//      own;
 //   1. rational basis and Jacobian at the 27 Gauss points (FP32 sums of the
 //      homogeneous control net; determinant and inverse in FP64);
 //   2. operand tile T[(a,k), q] = sqrt|w_q| dN_a/dx_k (rows m = 32k + a), so
@@ -20,15 +20,12 @@
 //      one pass per sign, the negative one with the negate-A bit of the MMA;
 //   3. G on the tensor cores in 3xTF32 split precision,
 //      G = Thi^T Thi + Thi^T Tlo + Tlo^T Thi, FP32 accumulation in tensor memory;
-//   4. Ke[(a,k),(b,l)] = lambda G[(a,k),(b,l)] + mu G[(a,l),(b,k)]
-//                        + mu delta_kl sum_m G[(a,m),(b,m)]
+//   4. G made exactly symmetric in shared memory (the upper triangle mirrored)
+//      and written, with the element load vector (body force, Neumann
+//      traction), as the element's scratch block G[a][k][l][b], F[a][k]; the
+//      gather forms Ke[(a,k),(b,l)] = lambda G_kl + mu G_lk + delta_kl mu tr G
 //      -- B^T D B of isotropic elasticity regrouped so the tensor cores
-//      contract over the Gauss points once;
-//   5. FP64 reductions of Ke into the compressed-column matrix in L2
-//      (red.global.add.f64).  An element reduces only after every
-//      lower-colour neighbour (sharing a node) has published its done flag,
-//      and elements of one colour share no node: every matrix entry receives
-//      its contributions in colour order, so the sums are deterministic.
+//      contract over the Gauss points once.
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -48,8 +45,8 @@ constexpr int kNen = 27;      // p = 2: 3x3x3 functions
 constexpr int kNq = 27;       // 3x3x3 Gauss points
 constexpr int kM = 128;       // MMA M (rows 32k + a, k < 3, a < 27)
 constexpr int kN = 96;        // MMA N (columns 32l + b)
-constexpr int kGs = 81;       // row stride of the compact Gram matrix (conflict-free)
-constexpr uint32_t kFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wait
+constexpr int kGs = 81;       // row stride of the Gram matrix in the element block
+constexpr int kBlock = 81 * 81 + 81 + 2;  // element block: G, F, padding to 16 bytes
 constexpr int kTcPerSM = 4;   // CTAs per SM at most: 4 x 128 tensor-memory columns
 
 // The operand tile has 96 rows (32k + a for k < 3, a < 27, the rest zero);
@@ -70,17 +67,16 @@ struct TcSmem {
       float Dw[kNq][kNen];
       float scr[1026];      // per-point scratch (see Scratch)
     } b;
-    float Gc[81 * kGs];     // G[(3a+k)][(3b+l)], written once the basis data is dead
+    // the element's scratch block, written once the basis data is dead:
+    // G[a][k][l][b] at (3a + k) 81 + 27 l + b, then F[a][k], 2 floats padding
+    float Gc[kBlock];
   } u;
   float wq[kNq];           // signed integration weight (0 at skipped points)
   float X[kNen][4];        // control points relative to the element's first, weight
   // the element's node box, written by TMA (node a = i + 3 j + 9 k)
   alignas(128) double ctrlT[kNen][4];  // control points x, y, z, w
-  alignas(128) int nodeT[kNen][8];     // eq of the 3 DOFs, F(node), colptr of the 3 DOFs, 0
-  alignas(128) int lineT[kNen][28];    // line-offset row of the node (25 values used)
   unsigned long long mbar;
   unsigned long long ctrlbar;  // TMA completion of ctrlT
-  unsigned long long tabbar;   // TMA completion of nodeT and lineT
   uint32_t tmemSlot;
   int fail;
   int signs;               // bit 0: some w_q > 0, bit 1: some w_q < 0
@@ -88,8 +84,9 @@ struct TcSmem {
 };
 
 constexpr uint32_t kCtrlBytes = sizeof(double) * kNen * 4;
-constexpr uint32_t kTabBytes = sizeof(int) * kNen * (8 + 28);
 static_assert(sizeof(TcSmem) <= 56320, "4 CTAs per SM: 4 x (56 KB + 1 KB reserved) shared memory");
+static_assert(offsetof(TcSmem, u) % 16 == 0 && (kBlock * sizeof(float)) % 16 == 0,
+              "element blocks are copied in 16-byte pieces");
 
 static_assert(offsetof(TcSmem, Tlo) == offsetof(TcSmem, Thi) + sizeof(float) * kRowsT * kK &&
                   offsetof(TcSmem, u) == offsetof(TcSmem, Tlo) + sizeof(float) * kRowsT * kK &&
@@ -113,14 +110,6 @@ __device__ __forceinline__ Scratch scratch(TcSmem& sm)
 }  // namespace
 
 struct TcSys {
-  const int* madof;
-  const int* meqn;
-  const int* F;
-  const double* c0;
-  double* K;
-  double* b;
-  const int* colptr;
-  int* flags;
   unsigned long long* counters;  // [0] singular points, [2] device timeouts
 };
 
@@ -133,11 +122,10 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mbar = smemAddr(&sm.mbar);
   const Scratch sc = scratch(sm);
-  const uint32_t ctrlbar = smemAddr(&sm.ctrlbar), tabbar = smemAddr(&sm.tabbar);
+  const uint32_t ctrlbar = smemAddr(&sm.ctrlbar);
   if (tid == 0) {
     mbarInit(mbar, 1);
     mbarInit(ctrlbar, 1);
-    mbarInit(tabbar, 1);
     sm.fail = 0;
   }
   // the padding of the operand tile (rows with a >= 27, q >= 27) is never
@@ -153,55 +141,30 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
   const uint32_t tmem = sm.tmemSlot;
   const uint32_t tHi = smemAddr(sm.Thi), tLo = smemAddr(sm.Tlo);
   uint32_t phase = 0;
-  // done flag of this CTA's previous element, published (fence + release
-  // store by thread 0) when the next element reaches its neighbour wait: by
-  // then the previous element's reductions have long completed, so the fence
-  // costs little, and the delay is bounded by one element's front end
-  int* pending = nullptr;
-  // thread 0: node boxes of item itn into the TMA buffers.  The control
-  // points of the next element are requested as soon as this element has
-  // read its own (step 1), the node and line tables once its scatter is
-  // done (step 11); each is waited for only where it is first read.
-  int mapPatch = -1;        // patch whose tensor maps were last acquired
-  bool ctrlOut = false, tabOut = false;  // copies in flight (thread 0)
-  auto nodeBox = [&](int itn, const char*& tm, int& f1, int& f2, int& f3) {
+  // thread 0: control points of item itn into the TMA buffer, requested as
+  // soon as the current element has read its own (step 1) and waited for
+  // only where they are first read
+  int mapPatch = -1;        // patch whose tensor map was last acquired
+  bool ctrlOut = false;     // copy in flight (thread 0)
+  auto stageCtrl = [&](int itn) {
     const Item nx = items[itn];
     const DevPatch& Pn = patches[nx.patch];
-    f1 = nx.elem % Pn.nel[0];
-    f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
-    f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
-    tm = static_cast<const char*>(Pn.tmaps);
+    const int f1 = nx.elem % Pn.nel[0];
+    const int f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
+    const int f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
+    const char* tm = static_cast<const char*>(Pn.tmaps);
     if (nx.patch != mapPatch) {
       tmapAcquire(tm);
-      tmapAcquire(tm + 128);
-      tmapAcquire(tm + 256);
       mapPatch = nx.patch;
     }
-  };
-  auto stageCtrl = [&](int itn) {
-    const char* tm;
-    int f1, f2, f3;
-    nodeBox(itn, tm, f1, f2, f3);
     mbarExpectTx(ctrlbar, kCtrlBytes);
     tmaLoad4d(smemAddr(sm.ctrlT), tm, 0, f1, f2, f3, ctrlbar);
     ctrlOut = true;
   };
-  auto stageTab = [&](int itn) {
-    const char* tm;
-    int f1, f2, f3;
-    nodeBox(itn, tm, f1, f2, f3);
-    mbarExpectTx(tabbar, kTabBytes);
-    tmaLoad4d(smemAddr(sm.nodeT), tm + 128, 0, f1, f2, f3, tabbar);
-    tmaLoad4d(smemAddr(sm.lineT), tm + 256, 0, f1, f2, f3, tabbar);
-    tabOut = true;
-  };
-  if (tid == 0 && (int)blockIdx.x < count) {
-    stageCtrl(blockIdx.x);
-    stageTab(blockIdx.x);
-  }
-  uint32_t cphase = 0, tphase = 0;
+  if (tid == 0 && (int)blockIdx.x < count) stageCtrl(blockIdx.x);
+  uint32_t cphase = 0;
 
-  // the next element's item is read during the current element's scatter
+  // the next element's item is read during the current element's store
   Item nextItem{};
   if ((int)blockIdx.x < count) nextItem = items[blockIdx.x];
   for (int it = blockIdx.x; it < count; it += gridDim.x) {
@@ -209,7 +172,6 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const DevPatch& P = patches[item.patch];
     const int e = item.elem;
     const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
-    const int n0 = (e3 * P.n[1] + e2) * P.n[0] + e1;
 
     // ---- 1. element nodes from the TMA boxes: coordinates relative to the
     //         first node, weights; the 1D table rows of the element are read
@@ -493,14 +455,15 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     }
     __syncthreads();  // the Gram stage below overlays the basis arrays
 
-    // ---- 7. tensor memory -> compact Gram matrix in shared memory
+    // ---- 7. tensor memory -> exactly symmetric Gram matrix in the element
+    //         block layout: row r = 3a + k keeps its entries at and right of
+    //         the diagonal (c = 3b + l >= r) and mirrors them (the MMA's FP32
+    //         sums of G_rc and G_cr need not agree), so the element matrix and
+    //         the assembled matrix are exactly symmetric
+    float* Gc = sm.u.Gc;
     if (ok && warp < 3 && signs) {
-      // row r = 3a + k of G keeps its entries c >= r and mirrors them into
-      // column r: an exactly symmetric G (the MMA's FP32 sums of G_rc and
-      // G_cr need not agree), hence an exactly symmetric element matrix
       float v[16];
-      const int r = 3 * lane + warp;
-      float* grow = sm.u.Gc + r * kGs;
+      const int a = lane, k = warp, r = 3 * lane + warp;
 #pragma unroll
       for (int c16 = 0; c16 < kN / 16; c16++) {
         tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
@@ -509,128 +472,32 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
           for (int i = 0; i < 16; i++) {
             const int n = 16 * c16 + i, l = n >> 5, bcol = n & 31, c = 3 * bcol + l;
             if (bcol < kNen && c >= r) {
-              grow[c] = v[i];
-              sm.u.Gc[c * kGs + r] = v[i];
+              Gc[r * kGs + 27 * l + bcol] = v[i];
+              Gc[c * kGs + 27 * k + a] = v[i];
             }
           }
         }
       }
     } else if (!signs) {
-      for (int i = tid; i < 81 * kGs; i += blockDim.x) sm.u.Gc[i] = 0.f;
+      for (int i = tid; i < 81 * kGs; i += blockDim.x) Gc[i] = 0.f;
     }
+    if (tid < kNen * 3) Gc[81 * kGs + tid] = fe;  // F[a][k] at 3a + k = tid
+    if (tid < kBlock - 82 * 81) Gc[82 * 81 + tid] = 0.f;
     tcFenceBefore();
     __syncthreads();
     if (sm.fail) break;
-
-    // ---- 8. publish the previous element, then wait for the lower-colour
-    //         neighbours of this one (they share nodes)
-    if (tid == 0 && pending) {
-      __threadfence();
-      storeRelease(pending, 1);
-      pending = nullptr;
-    }
-    if (tid < 124) {
-      const int t = tid < 62 ? tid : tid + 1;  // skip the element itself
-      const int dx = t % 5 - 2, dy = (t / 5) % 5 - 2, dz = t / 25 - 2;
-      const int f1 = e1 + dx, f2 = e2 + dy, f3 = e3 + dz;
-      if (f1 >= 0 && f1 < P.nel[0] && f2 >= 0 && f2 < P.nel[1] && f3 >= 0 && f3 < P.nel[2]) {
-        const int myc = e1 % 3 + 3 * (e2 % 3) + 9 * (e3 % 3);
-        const int nc = f1 % 3 + 3 * (f2 % 3) + 9 * (f3 % 3);
-        if (nc < myc) {
-          const int* flag = S.flags + P.flagBase + (f3 * P.nel[1] + f2) * P.nel[0] + f1;
-          uint32_t spin = 0;
-          while (loadRelaxed(flag) == 0) {
-            if (++spin > kFlagSpin) {
-              atomicAdd(S.counters + 2, 1ull);
-              break;
-            }
-            __nanosleep(64);
-          }
-          loadAcquire(flag);  // synchronises with the release store (no fence)
-        }
-      }
-    }
-    if (mbarWait(tabbar, tphase)) {
-      tphase ^= 1u;
-      tabOut = false;
-    } else {
-      atomicAdd(S.counters + 2, 1ull);
-      sm.fail = 1;
-    }
-    __syncthreads();
-    if (sm.fail) break;
-
     if (it + (int)gridDim.x < count) nextItem = items[it + gridDim.x];
 
-    // ---- 9. element matrix and scatter, node pair by node pair (FP32
-    //         arithmetic; the FP64 additions happen in the L2 reductions)
-    const float lamf = (float)(P.E * P.nu / ((1.0 + P.nu) * (1.0 - 2.0 * P.nu)));
-    const float muf = (float)(P.E / (2.0 * (1.0 + P.nu)));
-    // one matrix row (a, k) per thread: the lanes of a warp cover consecutive
-    // rows, so each reduction instruction touches contiguous column segments
-    if (tid < kNen * 3 && sm.nodeT[tid / 3][tid % 3] > 0) {
-      const int a = tid / 3, k = tid - 3 * a;
-      // F(a) plus the free DOFs of node a before component k
-      const int base = sm.nodeT[a][3] + (k > 0 && sm.nodeT[a][0] > 0) + (k > 1 && sm.nodeT[a][1] > 0);
-      // line-offset entry of row node a's line in column node bn: index
-      // (dz + 2) 5 + dy + 2 with dy, dz the line offsets of a relative to bn
-      const int rowLine = (a / 9) * 5 + (a / 3) % 3 + 12;
-      const float* Grow = sm.u.Gc + tid * kGs;    // row (a, k)
-      const float* Ga = sm.u.Gc + 3 * a * kGs;     // rows (a, 0..2)
-#pragma unroll 3
-      for (int bn = 0; bn < kNen; bn++) {
-        const float trm =
-            muf * (Ga[3 * bn] + Ga[kGs + 3 * bn + 1] + Ga[2 * kGs + 3 * bn + 2]);
-        const int off = sm.lineT[bn][rowLine - (bn / 9) * 5 - (bn / 3) % 3] + base;
-#pragma unroll
-        for (int l = 0; l < 3; l++) {
-          if (sm.nodeT[bn][l] <= 0) continue;
-          const float ke = fmaf(lamf, Grow[3 * bn + l],
-                                fmaf(muf, Ga[l * kGs + 3 * bn + k], k == l ? trm : 0.f));
-          redAdd(S.K + sm.nodeT[bn][4 + l] + off, widenF32(ke));
-        }
-      }
+    // ---- 8. the element block to the scratch (16-byte stores)
+    {
+      float4* dst = reinterpret_cast<float4*>(P.elm + (size_t)e * P.elmStride);
+      const float4* src = reinterpret_cast<const float4*>(Gc);
+      for (int i = tid; i < kBlock / 4; i += blockDim.x) dst[i] = src[i];
     }
-
-    // ---- 10. right-hand side: load vector minus prescribed-DOF terms
-    if (tid < kNen * 3) {
-      const int a = tid / 3, k = tid % 3;
-      const int r = sm.nodeT[a][k];
-      if (r > 0) {
-        double acc = widenF32(fe);
-        if (S.c0) {
-          for (int j = 0; j < kNen * 3; j++) {
-            const int ce = sm.nodeT[j / 3][j % 3];
-            if (ce >= 0) continue;
-            const int bn = j / 3, l = j % 3;
-            const float* ga = sm.u.Gc + 3 * a * kGs + 3 * bn;
-            const double tr = (double)ga[0] + ga[kGs + 1] + ga[2 * kGs + 2];
-            const double ke = lamf * (double)ga[k * kGs + l] + muf * (double)ga[l * kGs + k] +
-                              (k == l ? muf * tr : 0.0);
-            acc -= S.c0[-ce - 1] * ke;
-          }
-        }
-        if (acc != 0.0) redAdd(S.b + r - 1, acc);
-      }
-    }
-
-    // ---- 11. this element's reductions are issued; its flag is published
-    //         at the next element's step 8 or after the loop
-    __syncthreads();
-    if (tid == 0) {
-      pending = S.flags + P.flagBase + e;
-      if (it + (int)gridDim.x < count) stageTab(it + gridDim.x);  // node tables are free now
-    }
+    __syncthreads();  // the next element's step 1 overwrites the block
   }
-  if (tid == 0) {
-    if (pending) {
-      __threadfence();
-      storeRelease(pending, 1);
-    }
-    // after a timeout: copies still in flight land before the CTA exits
-    if (ctrlOut) mbarWait(ctrlbar, cphase);
-    if (tabOut) mbarWait(tabbar, tphase);
-  }
+  // after a timeout: a copy still in flight lands before the CTA exits
+  if (tid == 0 && ctrlOut) mbarWait(ctrlbar, cphase);
 
   // release tensor memory (all tcgen05 traffic of this CTA has completed)
   tcFenceBefore();
@@ -746,33 +613,16 @@ bool nodeBoxMap(void* out, size_t esize, void* base, int inner, const int n[3], 
              CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Node table, padded line-offset rows and the three tensor maps of a
-// tensor-core patch; false leaves the patch to the generic kernel.
+// The tensor map of the control net of a tensor-core patch (3x3x3 node
+// boxes); false leaves the patch to the generic kernel.
 bool tcUploadPatch(ifemgpu_ctx* ctx, HostPatch& pc, DevPatch& D)
 {
-  if (pc.lineOff.size() != (size_t)pc.nnod * 25 || !pc.d_ctrl) return false;
-  std::vector<int> nodeT((size_t)pc.nnod * 8, 0), lineT((size_t)pc.nnod * 28, 0);
-  for (int n = 0; n < pc.nnod; n++) {
-    const int g = pc.mlgn[n], d0 = ctx->madof[g] - 1;
-    for (int k = 0; k < 3; k++) {
-      const int q = ctx->meqn[d0 + k];
-      nodeT[(size_t)n * 8 + k] = q;
-      nodeT[(size_t)n * 8 + 4 + k] = q > 0 ? ctx->colptr[q - 1] : 0;
-    }
-    nodeT[(size_t)n * 8 + 3] = ctx->freeBefore[g];
-    for (int t = 0; t < 25; t++) lineT[(size_t)n * 28 + t] = pc.lineOff[(size_t)n * 25 + t];
-  }
-  auto put = [&](auto** dst, const auto* src, size_t bytes) {
-    return cudaMalloc((void**)dst, bytes) == cudaSuccess &&
-           cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
-  };
-  CUtensorMap maps[3];
-  const bool ok = put(&pc.d_nodeTab, nodeT.data(), sizeof(int) * nodeT.size()) &&
-                  put(&pc.d_lineTab, lineT.data(), sizeof(int) * lineT.size()) &&
-                  nodeBoxMap(&maps[0], 8, (void*)pc.d_ctrl, 4, pc.n, 3) &&
-                  nodeBoxMap(&maps[1], 4, pc.d_nodeTab, 8, pc.n, 3) &&
-                  nodeBoxMap(&maps[2], 4, pc.d_lineTab, 28, pc.n, 3) &&
-                  put(&pc.d_tmaps, maps, sizeof(maps));
+  (void)ctx;
+  if (!pc.d_ctrl) return false;
+  CUtensorMap map;
+  const bool ok = nodeBoxMap(&map, 8, (void*)pc.d_ctrl, 4, pc.n, 3) &&
+                  cudaMalloc(&pc.d_tmaps, sizeof(map)) == cudaSuccess &&
+                  cudaMemcpy(pc.d_tmaps, &map, sizeof(map), cudaMemcpyHostToDevice) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     return false;
@@ -800,12 +650,9 @@ ifemgpu_status tcPrepare(ifemgpu_ctx* ctx)
 
 ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int)
 {
-  TcSys S{ctx->d_madof, ctx->d_meqn, ctx->d_freeBefore, ctx->nceq ? ctx->d_c0 : nullptr,
-          ctx->d_K, ctx->d_b, ctx->d_colptr, ctx->d_flags, ctx->d_counters};
-  // every CTA must be resident (CTAs wait on each other's done flags): the
-  // grid is sized from the SM's shared memory, registers and tensor memory
-  // (4 x 128 columns).  Should residency ever fail, the bounded flag waits
-  // end with a reported device timeout instead of a hang.
+  TcSys S{ctx->d_counters};
+  // as many CTAs as fit at once (shared memory, registers and the 4 x 128
+  // tensor-memory columns of an SM); no CTA waits for another
   cudaFuncAttributes fa{};
   IFEMGPU_CUDA(ctx, cudaFuncGetAttributes(&fa, k_volume_tc_elast_p2));
   int smemSM = 0, resv = 0, regsSM = 0;
