@@ -48,7 +48,10 @@ struct GCfg {
   static constexpr int NS = W * W * W;           // neighbour slots of a node
   static constexpr int KL = NPV * NPV;
   static constexpr int WARPS = (P == 3 && NPV == 3) ? 4 : 8;
+  static constexpr int NB = (NEN + 31) / 32;           // element functions per lane
+  static constexpr int U = NPV == 3 ? 3 : (P == 3 ? 4 : 6);  // elements in flight per warp
   static constexpr size_t SMEM = sizeof(float) * 2 * KL * NS * WARPS;
+  static constexpr int MINB = (P == 3 && NPV == 3) ? 2 : (NPV == 3 ? 3 : 4);  // CTAs per SM
 };
 
 // hi + lo += x (TwoSum: the rounding error of hi + x goes to lo)
@@ -83,7 +86,7 @@ struct GatherSys {
 // One warp per node of the patches of one (degree, npv) class; node item t
 // belongs to the last range whose start is <= t.
 template <int P, int NPV>
-__global__ void __launch_bounds__(GCfg<P, NPV>::WARPS * 32)
+__global__ void __launch_bounds__(GCfg<P, NPV>::WARPS * 32, GCfg<P, NPV>::MINB)
 k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
          const int* __restrict__ pidx, int nranges, int total, GatherSys S)
 {
@@ -121,44 +124,75 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
     }
     float feHi = 0.f, feLo = 0.f;  // lane k < NPV: load vector of DOF k
     const float lamf = Pt.lamf, muf = Pt.muf;
-    const int ex0 = max(0, ax - P), ex1 = min(ax, Pt.nel[0] - 1);
-    const int ey0 = max(0, ay - P), ey1 = min(ay, Pt.nel[1] - 1);
-    const int ez0 = max(0, az - P), ez1 = min(az, Pt.nel[2] - 1);
+    const int ex0 = max(0, ax - P), cx = min(ax, Pt.nel[0] - 1) - ex0 + 1;
+    const int ey0 = max(0, ay - P), cy = min(ay, Pt.nel[1] - 1) - ey0 + 1;
+    const int ez0 = max(0, az - P), cz = min(az, Pt.nel[2] - 1) - ez0 + 1;
+    const int ne = cx * cy * cz;
     __syncwarp();
-    for (int ez = ez0; ez <= ez1; ez++)
-      for (int ey = ey0; ey <= ey1; ey++)
-        for (int ex = ex0; ex <= ex1; ex++) {
-          const size_t e = ((size_t)ez * Pt.nel[1] + ey) * Pt.nel[0] + ex;
-          const int alx = ax - ex, aly = ay - ey, alz = az - ez;
-          const int al = alx + Q * (aly + Q * alz);
-          const float* blk = Pt.elm + e * (size_t)Pt.elmStride;
-          const float* row = blk + (size_t)al * KL * NEN;
+    // elements around the node in ascending index order, U at a time: the
+    // loads of U elements are issued before any of them is added, so that
+    // each warp keeps U row blocks in flight
+    int jx = 0, jy = 0, jz = 0;  // next element, offsets from (ex0, ey0, ez0)
+    for (int j0 = 0; j0 < ne; j0 += C::U) {
+      float g[C::U][C::NB][KL];
+      int alU[C::U];
+      const float* blkU[C::U];
 #pragma unroll
-          for (int bb = 0; bb < (NEN + 31) / 32; bb++) {
-            const int bl = lane + 32 * bb;
-            if (bl < NEN) {
-              const int blx = bl % Q, bly = (bl / Q) % Q, blz = bl / (Q * Q);
-              const int s = (blx - alx + P) + W * ((bly - aly + P) + W * (blz - alz + P));
-              float g[KL];
-#pragma unroll
-              for (int kl = 0; kl < KL; kl++) g[kl] = __ldcs(row + kl * NEN + bl);
-              if (NPV == 3) {
-                const float tr = muf * (g[0] + g[4] + g[8]);
-#pragma unroll
-                for (int k = 0; k < 3; k++)
-#pragma unroll
-                  for (int l = 0; l < 3; l++) {
-                    const float ke = fmaf(lamf, g[3 * k + l], fmaf(muf, g[3 * l + k], k == l ? tr : 0.f));
-                    dfAdd(accHi[(3 * k + l) * NS + s], accLo[(3 * k + l) * NS + s], ke);
-                  }
-              } else {
-                dfAdd(accHi[s], accLo[s], g[0]);
-              }
+      for (int u = 0; u < C::U; u++) {
+        const int j = j0 + u;
+        alU[u] = -1;
+        blkU[u] = nullptr;
+        if (j < ne) {
+          const int ex = ex0 + jx, ey = ey0 + jy, ez = ez0 + jz;
+          if (++jx == cx) {
+            jx = 0;
+            if (++jy == cy) {
+              jy = 0;
+              ++jz;
             }
           }
-          if (lane < NPV) dfAdd(feHi, feLo, __ldcs(blk + (size_t)KL * NEN * NEN + al * NPV + lane));
-          __syncwarp();
+          const size_t e = ((size_t)ez * Pt.nel[1] + ey) * Pt.nel[0] + ex;
+          alU[u] = (ax - ex) + Q * ((ay - ey) + Q * (az - ez));
+          blkU[u] = Pt.elm + e * (size_t)Pt.elmStride;
+          const float* row = blkU[u] + (size_t)alU[u] * KL * NEN;
+#pragma unroll
+          for (int bb = 0; bb < C::NB; bb++) {
+            const int bl = lane + 32 * bb;
+#pragma unroll
+            for (int kl = 0; kl < KL; kl++) g[u][bb][kl] = bl < NEN ? __ldcs(row + kl * NEN + bl) : 0.f;
+          }
         }
+      }
+#pragma unroll
+      for (int u = 0; u < C::U; u++) {
+        if (alU[u] < 0) break;
+        const int al = alU[u];
+        const int alx = al % Q, aly = (al / Q) % Q, alz = al / (Q * Q);  // constant divisors
+#pragma unroll
+        for (int bb = 0; bb < C::NB; bb++) {
+          const int bl = lane + 32 * bb;
+          if (bl < NEN) {
+            const int blx = bl % Q, bly = (bl / Q) % Q, blz = bl / (Q * Q);
+            const int s = (blx - alx + P) + W * ((bly - aly + P) + W * (blz - alz + P));
+            const float* gg = g[u][bb];
+            if (NPV == 3) {
+              const float tr = muf * (gg[0] + gg[4] + gg[8]);
+#pragma unroll
+              for (int k = 0; k < 3; k++)
+#pragma unroll
+                for (int l = 0; l < 3; l++) {
+                  const float ke = fmaf(lamf, gg[3 * k + l], fmaf(muf, gg[3 * l + k], k == l ? tr : 0.f));
+                  dfAdd(accHi[(3 * k + l) * NS + s], accLo[(3 * k + l) * NS + s], ke);
+                }
+            } else {
+              dfAdd(accHi[s], accLo[s], gg[0]);
+            }
+          }
+        }
+        if (lane < NPV) dfAdd(feHi, feLo, __ldcs(blkU[u] + (size_t)KL * NEN * NEN + al * NPV + lane));
+        __syncwarp();
+      }
+    }
     // write the node's columns; prescribed neighbours feed the right-hand side
     double corr[NPV];
 #pragma unroll

@@ -186,6 +186,26 @@ __device__ __forceinline__ double widenF32(float f)
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// Double -> float narrowing on the integer pipe, rounded to nearest even (the
+// conversion instruction runs on the FP64 units, which are scarce on this
+// GPU).  Results below the smallest normal float flush to a signed zero,
+// results beyond the largest finite float become infinity, NaN stays NaN.
+__device__ __forceinline__ float narrowF64(double d)
+{
+  const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu);
+  const int ef = e - 1023 + 127;
+  const uint32_t m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // top 23 mantissa bits
+  const uint32_t rest = lo & 0x1FFFFFFFu;                  // the 29 bits rounded away
+  uint32_t bits = ((uint32_t)(ef & 0xFF) << 23) | m;
+  bits += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  bits = ef <= 0 ? 0u : bits;
+  bits = ef >= 255 ? 0x7F800000u : bits;
+  bits = (e == 0x7FF && (((hi & 0xFFFFFu) | lo) != 0u)) ? 0x7FC00000u : bits;
+  return __uint_as_float(sign | bits);
+}
+
 __device__ __forceinline__ void redAdd(double* p, double v)
 {
   atomicAdd(p, v);  // result unused: compiles to an L2 reduction

@@ -51,26 +51,33 @@ constexpr int kTcPerSM = 4;   // CTAs per SM at most: 4 x 128 tensor-memory colu
 
 // The operand tile has 96 rows (32k + a for k < 3, a < 27, the rest zero);
 // the MMA's A operand reads M = 128 rows from the tile start, so the reads of
-// rows 96..127 run into the next 4 KB (Tlo after Thi, the basis/Gram union
-// after Tlo).  Those rows only feed accumulator lanes 96..127, which are
-// never read, and nothing writes shared memory while an MMA runs.
+// rows 96..127 run into the next 4 KB (Tlo after Thi, the union after Tlo).
+// Those rows only feed accumulator lanes 96..127, which are never read, and
+// nothing writes shared memory while an MMA runs.
 constexpr int kRowsT = 96;
+
+// per-element front-end arrays (dead before the element block is formed)
+struct Front {
+  float wX[4][kNen];          // weighted control net: w x, w y, w z, w (x relative)
+  float A[2][4][3][9];        // x contracted: [N/D][field][gx][j + 3k]
+  float B[3][4][9][3];        // y contracted: [NN/DN/ND][field][gx + 3gy][k]
+  float S[kNq][4][4];         // [q][field][value, d/du, d/dv, d/dw]: homogeneous sums
+  float E[kNq][12];           // du_d/dx_k / W at [k 3 + d], then e_k = sum_d dW_d/W E_kd
+  float Es[kNq][12];          // E scaled by sqrt(max(s w_q, 0)) for the current sign pass
+  float iW[kNq];              // 1 / W
+  float face[9 * 27 + 9];     // Neumann face points: rational basis, dS weights
+};
 
 struct TcSmem {
   float Thi[kRowsT * kK];  // operand tile, K-major core-matrix layout
   float Tlo[kRowsT * kK];
   union {
-    struct {
-      float N[kNq][kNen];   // weighted basis wN, then the rational basis R
-      float Du[kNq][kNen];  // weighted parametric derivatives, then dR/du_d
-      float Dv[kNq][kNen];
-      float Dw[kNq][kNen];
-      float scr[1026];      // per-point scratch (see Scratch)
-    } b;
-    // the element's scratch block, written once the basis data is dead:
+    Front f;
+    // the element's scratch block, written once the front-end data is dead:
     // G[a][k][l][b] at (3a + k) 81 + 27 l + b, then F[a][k], 2 floats padding
     float Gc[kBlock];
   } u;
+  float tb[3][2][9];       // 1D tables of the element: [direction][N, dN/du][g 3 + i]
   float wq[kNq];           // signed integration weight (0 at skipped points)
   float X[kNen][4];        // control points relative to the element's first, weight
   // the element's node box, written by TMA (node a = i + 3 j + 9 k)
@@ -87,25 +94,10 @@ constexpr uint32_t kCtrlBytes = sizeof(double) * kNen * 4;
 static_assert(sizeof(TcSmem) <= 56320, "4 CTAs per SM: 4 x (56 KB + 1 KB reserved) shared memory");
 static_assert(offsetof(TcSmem, u) % 16 == 0 && (kBlock * sizeof(float)) % 16 == 0,
               "element blocks are copied in 16-byte pieces");
-
 static_assert(offsetof(TcSmem, Tlo) == offsetof(TcSmem, Thi) + sizeof(float) * kRowsT * kK &&
                   offsetof(TcSmem, u) == offsetof(TcSmem, Tlo) + sizeof(float) * kRowsT * kK &&
                   sizeof(TcSmem::u) >= sizeof(float) * (kM - kRowsT) * kK,
               "A-operand reads of rows 96..127 must stay inside the tile and the union");
-
-// scratch views (dead before the epilogue writes G)
-struct Scratch {
-  float* P;     // [27][4][4] homogeneous sums
-  float* Jinv;  // [27][9] column-major inverse Jacobian
-  float* Wq;    // [27][4] 1/W and dW/du_d
-  float* C;     // [27][9] sqrt(max(s w_q, 0)) * Jinv of the current sign pass
-};
-
-__device__ __forceinline__ Scratch scratch(TcSmem& sm)
-{
-  float* b = sm.u.b.scr;
-  return Scratch{b, b + 27 * 16, b + 27 * 16 + 27 * 9, b + 27 * 16 + 27 * 13};
-}
 
 }  // namespace
 
@@ -119,17 +111,17 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
 {
   extern __shared__ __align__(1024) unsigned char smraw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(smraw);
+  Front& F = sm.u.f;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t mbar = smemAddr(&sm.mbar);
-  const Scratch sc = scratch(sm);
   const uint32_t ctrlbar = smemAddr(&sm.ctrlbar);
   if (tid == 0) {
     mbarInit(mbar, 1);
     mbarInit(ctrlbar, 1);
     sm.fail = 0;
   }
-  // the padding of the operand tile (rows with a >= 27, q >= 27) is never
-  // written again
+  // the padding of the operand tile (rows with a >= 27, q >= 27) is written
+  // with zeros only
   for (int i = tid; i < kRowsT * kK; i += blockDim.x) {
     sm.Thi[i] = 0.f;
     sm.Tlo[i] = 0.f;
@@ -173,11 +165,11 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const int e = item.elem;
     const int e1 = e % P.nel[0], e2 = (e / P.nel[0]) % P.nel[1], e3 = e / (P.nel[0] * P.nel[1]);
 
-    // ---- 1. element nodes from the TMA boxes: coordinates relative to the
-    //         first node, weights; the 1D table rows of the element are read
-    //         from L2 while the control points arrive
-    double dV = 0.0;  // span volume, read early as well
-    if (tid == 32) dV = P.span[0][e1] * P.span[1][e2] * P.span[2][e3];
+    // ---- 1. element nodes from the TMA box: coordinates relative to the
+    //         first node, weights, the weighted net; the 1D table rows and
+    //         the span volume are read from L2 while the control points arrive
+    double dV = 0.0;
+    if (tid == 96) dV = P.span[0][e1] * P.span[1][e2] * P.span[2][e3];
     float tbv = 0.f;
     if (tid < 54) {
       const int d = tid / 18, dd = (tid / 9) & 1, g = tid % 9;
@@ -192,155 +184,157 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     }
     if (tid < kNen) {
       const int a = tid;
-      sm.X[a][0] = (float)(sm.ctrlT[a][0] - sm.ctrlT[0][0]);
-      sm.X[a][1] = (float)(sm.ctrlT[a][1] - sm.ctrlT[0][1]);
-      sm.X[a][2] = (float)(sm.ctrlT[a][2] - sm.ctrlT[0][2]);
-      sm.X[a][3] = (float)sm.ctrlT[a][3];
+      const float x0 = (float)(sm.ctrlT[a][0] - sm.ctrlT[0][0]);
+      const float x1 = (float)(sm.ctrlT[a][1] - sm.ctrlT[0][1]);
+      const float x2 = (float)(sm.ctrlT[a][2] - sm.ctrlT[0][2]);
+      const float w = (float)sm.ctrlT[a][3];
+      sm.X[a][0] = x0;
+      sm.X[a][1] = x1;
+      sm.X[a][2] = x2;
+      sm.X[a][3] = w;
+      F.wX[0][a] = w * x0;
+      F.wX[1][a] = w * x1;
+      F.wX[2][a] = w * x2;
+      F.wX[3][a] = w;
     }
-    if (tid == 0) sm.signs = 0;
-    if (tid == 32) sm.dVf = (float)(0.125 * dV);
-    // the element's 1D tables [N0, D0, N1, D1, N2, D2][g 3 + i] in the per-point
-    // scratch, which step 3 overwrites only after step 2 has read them
-    float* const tbs = sm.u.b.scr;
-    if (tid < 54) tbs[tid] = tbv;
-    // ---- 2. weighted tensor-product basis at every (Gauss point, function)
-    const float* tn0 = tbs;
-    const float* td0 = tbs + 9;
-    const float* tn1 = tbs + 18;
-    const float* td1 = tbs + 27;
-    const float* tn2 = tbs + 36;
-    const float* td2 = tbs + 45;
-    __syncthreads();  // X and tables visible, ctrlT read
+    if (tid < 54) sm.tb[tid / 18][(tid / 9) & 1][tid % 9] = tbv;
+    if (tid == 96) {
+      sm.signs = 0;
+      sm.dVf = (float)(0.125 * dV);
+    }
+    __syncthreads();  // ctrlT read, node data and tables visible
     if (sm.fail) break;
     if (tid == 0 && it + (int)gridDim.x < count) stageCtrl(it + gridDim.x);
-    for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
-      const int q = idx / kNen, a = idx - q * kNen;
-      const int g0 = (q % 3) * 3 + a % 3;  // gi*3 + i
-      const int g1 = ((q / 3) % 3) * 3 + (a / 3) % 3;
-      const int g2 = (q / 9) * 3 + a / 9;
-      const float nx = tn0[g0], ny = tn1[g1], nz = tn2[g2];
-      const float w = sm.X[a][3];
-      sm.u.b.N[q][a] = w * nx * ny * nz;
-      sm.u.b.Du[q][a] = w * td0[g0] * ny * nz;
-      sm.u.b.Dv[q][a] = w * nx * td1[g1] * nz;
-      sm.u.b.Dw[q][a] = w * nx * ny * td2[g2];
+
+    // ---- 2. homogeneous sums at the Gauss points by sum factorisation:
+    //         S[q][c][d] = sum_a (d_d N_a)(q) w_a X_a^c (X^3 = 1); three
+    //         contractions of 3 terms instead of 27 per (point, field, d)
+    for (int t = tid; t < 2 * 4 * 3 * 9; t += blockDim.x) {        // x: [N/D][c][gx][jk]
+      const int jk = t % 9, gx = (t / 9) % 3, c = (t / 27) % 4, dd = t / 108;
+      const float* tbx = sm.tb[0][dd] + gx * 3;
+      const float* w = F.wX[c] + 3 * jk;
+      (&F.A[0][0][0][0])[t] = fmaf(tbx[0], w[0], fmaf(tbx[1], w[1], tbx[2] * w[2]));
+    }
+    __syncthreads();
+    for (int t = tid; t < 3 * 4 * 9 * 3; t += blockDim.x) {        // y: [NN/DN/ND][c][gx gy][k]
+      const int k = t % 3, gxy = (t / 3) % 9, c = (t / 27) % 4, v = t / 108;
+      const int gx = gxy % 3, gy = gxy / 3;
+      const float* tby = sm.tb[1][v == 2] + gy * 3;
+      const float* a = F.A[v == 1][c][gx] + 3 * k;
+      (&F.B[0][0][0][0])[t] = fmaf(tby[0], a[0], fmaf(tby[1], a[1], tby[2] * a[2]));
+    }
+    __syncthreads();
+    for (int t = tid; t < kNq * 16; t += blockDim.x) {              // z: S[q][c][d]
+      const int d = t % 4, c = (t / 4) % 4, q = t / 16;
+      const int gxy = q % 9, gz = q / 9;
+      const int src = d == 1 ? 1 : d == 2 ? 2 : 0;                   // DN, ND, else NN
+      const float* tbz = sm.tb[2][d == 3] + gz * 3;
+      const float* b = F.B[src][c][gxy];
+      (&F.S[0][0][0])[t] = fmaf(tbz[0], b[0], fmaf(tbz[1], b[1], tbz[2] * b[2]));
     }
     __syncthreads();
 
-    // ---- 3. homogeneous sums per Gauss point: sum_a (wN)_a (X_a, 1) and derivatives
-    if (tid < kNq * 4) {
-      const int q = tid >> 2, c = tid & 3;
-      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-#pragma unroll 9
-      for (int a = 0; a < kNen; a++) {
-        const float x = c < 3 ? sm.X[a][c] : 1.f;
-        s0 = fmaf(sm.u.b.N[q][a], x, s0);
-        s1 = fmaf(sm.u.b.Du[q][a], x, s1);
-        s2 = fmaf(sm.u.b.Dv[q][a], x, s2);
-        s3 = fmaf(sm.u.b.Dw[q][a], x, s3);
-      }
-      float* Pq = sc.P + q * 16 + c * 4;
-      Pq[0] = s0;
-      Pq[1] = s1;
-      Pq[2] = s2;
-      Pq[3] = s3;
-    }
-    __syncthreads();
-
-    // ---- 4. Jacobian, FP64 determinant and inverse, integration weight
+    // ---- 3. per Gauss point: Jacobian, determinant and cofactors in FP64
+    //         (from exactly widened FP32 entries), the rest in FP32
     if (tid < kNq) {
       const int q = tid;
-      const float* Pq = sc.P + q * 16;
-      const float iW = 1.f / Pq[12];
-      // J[d*3 + r] = dX_r/du_d (column-major), formed in FP32 and widened
-      // exactly on the integer pipe; the cofactors, determinant and inverse
-      // are FP64 (each FP64 warp instruction costs tens of cycles here, so
-      // the count is kept to the cofactor expansion itself)
-      double J[9];
+      const float* Sq = F.S[q][0];
+      const float iW = 1.f / Sq[12];
+      double J[9];  // J[d*3 + r] = dX_r/du_d, formed in FP32 and widened exactly
+#pragma unroll
       for (int r = 0; r < 3; r++) {
-        const float Xr = Pq[r * 4] * iW;
+        const float Xr = Sq[r * 4] * iW;
+#pragma unroll
         for (int d = 0; d < 3; d++)
-          J[d * 3 + r] = widenF32((Pq[r * 4 + 1 + d] - Xr * Pq[12 + 1 + d]) * iW);
+          J[d * 3 + r] = widenF32((Sq[r * 4 + 1 + d] - Xr * Sq[12 + 1 + d]) * iW);
       }
       const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[1] * J[8] - J[2] * J[7],
                    c2 = J[1] * J[5] - J[2] * J[4];
       const double det = J[0] * c0 - J[3] * c1 + J[6] * c2;
       float w = 0.f;
-      float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // du_d/dx_k at k 3 + d
       if (fabs(det) > kEpsZ) {
-        const double id = 1.0 / det;
-        B[0] = (float)(c0 * id);
-        B[1] = (float)(-c1 * id);
-        B[2] = (float)(c2 * id);
-        B[3] = (float)(-(J[3] * J[8] - J[5] * J[6]) * id);
-        B[4] = (float)((J[0] * J[8] - J[2] * J[6]) * id);
-        B[5] = (float)(-(J[0] * J[5] - J[2] * J[3]) * id);
-        B[6] = (float)((J[3] * J[7] - J[4] * J[6]) * id);
-        B[7] = (float)(-(J[0] * J[7] - J[1] * J[6]) * id);
-        B[8] = (float)((J[0] * J[4] - J[1] * J[3]) * id);
+        const float detf = narrowF64(det);
+        const float id = 1.f / detf;
+        B[0] = narrowF64(c0) * id;
+        B[1] = -narrowF64(c1) * id;
+        B[2] = narrowF64(c2) * id;
+        B[3] = -narrowF64(J[3] * J[8] - J[5] * J[6]) * id;
+        B[4] = narrowF64(J[0] * J[8] - J[2] * J[6]) * id;
+        B[5] = -narrowF64(J[0] * J[5] - J[2] * J[3]) * id;
+        B[6] = narrowF64(J[3] * J[7] - J[4] * J[6]) * id;
+        B[7] = -narrowF64(J[0] * J[7] - J[1] * J[6]) * id;
+        B[8] = narrowF64(J[0] * J[4] - J[1] * J[3]) * id;
         // |J| dV w_i w_j w_k in FP32 (dV = span volume / 8)
-        w = (float)det * sm.dVf * P.gwf[0][q % 3] * P.gwf[1][(q / 3) % 3] * P.gwf[2][q / 9];
+        w = detf * sm.dVf * P.gwf[0][q % 3] * P.gwf[1][(q / 3) % 3] * P.gwf[2][q / 9];
         atomicOr(&sm.signs, w > 0.f ? 1 : 2);
       } else {
         atomicAdd(S.counters, 1ull);
       }
       sm.wq[q] = w;
-      for (int c = 0; c < 9; c++) sc.Jinv[q * 9 + c] = B[c];
-      sc.Wq[q * 4 + 0] = iW;
-      sc.Wq[q * 4 + 1] = Pq[13];
-      sc.Wq[q * 4 + 2] = Pq[14];
-      sc.Wq[q * 4 + 3] = Pq[15];
+      F.iW[q] = iW;
+      // dR_a/dx_k = w_a (sum_d dN_a/du_d E_kd - N_a e_k) with N_a the
+      // B-spline products, E_kd = (du_d/dx_k) / W, e_k = sum_d (dW/du_d / W) E_kd
+      const float g0 = Sq[13] * iW, g1 = Sq[14] * iW, g2 = Sq[15] * iW;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float E0 = B[3 * k] * iW, E1 = B[3 * k + 1] * iW, E2 = B[3 * k + 2] * iW;
+        F.E[q][3 * k] = E0;
+        F.E[q][3 * k + 1] = E1;
+        F.E[q][3 * k + 2] = E2;
+        F.E[q][9 + k] = fmaf(g0, E0, fmaf(g1, E1, g2 * E2));
+      }
     }
     __syncthreads();
 
-    // ---- 5. rational basis R and dR/du in place
-    for (int idx = tid; idx < kNq * kNen; idx += blockDim.x) {
-      const int q = idx / kNen, a = idx - q * kNen;
-      const float* Wq = sc.Wq + q * 4;
-      const float R = sm.u.b.N[q][a] * Wq[0];
-      sm.u.b.Du[q][a] = (sm.u.b.Du[q][a] - R * Wq[1]) * Wq[0];
-      sm.u.b.Dv[q][a] = (sm.u.b.Dv[q][a] - R * Wq[2]) * Wq[0];
-      sm.u.b.Dw[q][a] = (sm.u.b.Dw[q][a] - R * Wq[3]) * Wq[0];
-      sm.u.b.N[q][a] = R;
-    }
-    __syncthreads();
-
-    // ---- 6. operand tile and tensor-core Gram matrix, one pass per weight sign
+    // ---- 4. operand tile and tensor-core Gram matrix, one pass per weight sign
     const int signs = sm.signs;
     bool first = true, ok = true;
     for (int pass = 0; pass < 2 && ok; pass++) {
       const float s = pass == 0 ? 1.f : -1.f;
       if (!(signs & (1 << pass))) continue;
-      // C[q] = sqrt(max(s w_q, 0)) Jinv_q
-      if (tid < kNq) {
-        const float ws = s * sm.wq[tid];
-        const float sw = ws > 0.f ? sqrtf(ws) : 0.f;
-#pragma unroll
-        for (int c = 0; c < 9; c++) sc.C[tid * 9 + c] = sw * sc.Jinv[tid * 9 + c];
+      for (int t = tid; t < kNq * 12; t += blockDim.x) {
+        const int q = t / 12;
+        const float ws = s * sm.wq[q];
+        (&F.Es[0][0])[t] = (ws > 0.f ? sqrtf(ws) : 0.f) * (&F.E[0][0])[t];
       }
       __syncthreads();
-      // one operand row per thread: r = 32k + a (k < 3, a < 27), 4 Gauss
-      // points per 16-byte store (conflict-free: lanes cover whole core rows)
-      {
-        const int r = tid, a = r & 31, k = r >> 5;
-        if (a < kNen && k < 3) {
+      // task (a, g): function a, Gauss points 4g..4g+3 (16-byte stores of
+      // each row 32k + a); the three rows k of a from one basis evaluation
+      for (int task = tid; task < kNen * 7; task += blockDim.x) {
+        const int a = task % kNen, g = task / kNen;
+        const int ia = a % 3, ja = (a / 3) % 3, ka = a / 9;
+        const float wa = sm.X[a][3];
+        float hi[3][4], lo[3][4];
 #pragma unroll
-          for (int kb = 0; kb < 7; kb++) {
-            float hi[4], lo[4];
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-              const int q = kb * 4 + j;
-              float v = 0.f;
-              if (q < kNq) {
-                const float* C = sc.C + q * 9 + k * 3;
-                v = sm.u.b.Du[q][a] * C[0] + sm.u.b.Dv[q][a] * C[1] + sm.u.b.Dw[q][a] * C[2];
-              }
-              splitTF32(v, hi[j], lo[j]);
-            }
-            const int o = kmaj(r, kb * 4);
-            *reinterpret_cast<float4*>(sm.Thi + o) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<float4*>(sm.Tlo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        for (int u = 0; u < 4; u++) {
+          const int q = 4 * g + u;
+          float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+          if (q < kNq) {
+            const int gx = q % 3, gy = (q / 3) % 3, gz = q / 9;
+            const float nx = sm.tb[0][0][3 * gx + ia], dx = sm.tb[0][1][3 * gx + ia];
+            const float ny = sm.tb[1][0][3 * gy + ja], dy = sm.tb[1][1][3 * gy + ja];
+            const float nz = sm.tb[2][0][3 * gz + ka], dz = sm.tb[2][1][3 * gz + ka];
+            const float nyz = wa * ny * nz;
+            const float du = dx * nyz, dv = wa * nx * dy * nz, dw = wa * nx * ny * dz;
+            const float n = nx * nyz;
+            const float4 E0 = *reinterpret_cast<const float4*>(F.Es[q]);
+            const float4 E1 = *reinterpret_cast<const float4*>(F.Es[q] + 4);
+            const float4 E2 = *reinterpret_cast<const float4*>(F.Es[q] + 8);
+            // E_kd at 3k + d, e_k at 9 + k
+            t0 = fmaf(du, E0.x, fmaf(dv, E0.y, fmaf(dw, E0.z, -n * E2.y)));
+            t1 = fmaf(du, E0.w, fmaf(dv, E1.x, fmaf(dw, E1.y, -n * E2.z)));
+            t2 = fmaf(du, E1.z, fmaf(dv, E1.w, fmaf(dw, E2.x, -n * E2.w)));
           }
+          splitTF32(t0, hi[0][u], lo[0][u]);
+          splitTF32(t1, hi[1][u], lo[1][u]);
+          splitTF32(t2, hi[2][u], lo[2][u]);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          const int o = kmaj(32 * k + a, 4 * g);
+          *reinterpret_cast<float4*>(sm.Thi + o) = make_float4(hi[k][0], hi[k][1], hi[k][2], hi[k][3]);
+          *reinterpret_cast<float4*>(sm.Tlo + o) = make_float4(lo[k][0], lo[k][1], lo[k][2], lo[k][3]);
         }
       }
       fenceProxyAsync();
@@ -367,28 +361,33 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       sm.fail = 1;
     }
 
-    // element load vector (body force)
+    // ---- 5. element load vector: body force, Fe[a][k] = b_k sum_q R_a w_q
+    //         (R_a = w_a N_a / W), and Neumann traction on the patch faces
+    //         this element touches
     float fe = 0.f;
     if (tid < kNen * 3) {
       const int a = tid / 3, k = tid % 3;
       const float bk = P.bodyf[k];
       if (bk != 0.f) {
+        const int ia = a % 3, ja = (a / 3) % 3, ka = a / 9;
         float acc = 0.f;
-        for (int q = 0; q < kNq; q++) acc = fmaf(sm.u.b.N[q][a], sm.wq[q], acc);
-        fe = bk * acc;
+        for (int q = 0; q < kNq; q++) {
+          const float n = sm.tb[0][0][3 * (q % 3) + ia] * sm.tb[1][0][3 * ((q / 3) % 3) + ja] *
+                          sm.tb[2][0][3 * (q / 9) + ka];
+          acc = fmaf(n * F.iW[q], sm.wq[q], acc);
+        }
+        fe = bk * sm.X[a][3] * acc;
       }
     }
-
-    // Neumann faces of the patch that this element touches: constant
-    // traction t, Fe += t R dS w at the 3x3 face points (face overload of
-    // ASMs3D::integrate, src/ASM/ASMs3D.C:2547-2812)
+    // constant traction t: Fe += t R dS w at the 3x3 face points (face
+    // overload of ASMs3D::integrate, src/ASM/ASMs3D.C:2547-2812)
     for (int f = 0; f < P.nneu; f++) {
       const int face = P.neuFace[f];
       const int nd0 = (face - 1) >> 1, side = (face - 1) & 1;
       const int ee[3] = {e1, e2, e3};
       if (ee[nd0] != (side ? P.nel[nd0] - 1 : 0)) continue;  // uniform in the CTA
-      float* fR = sc.P;            // [9][27] rational basis at the face points
-      float* fW = sc.P + 9 * 27;   // [9] dS * weights
+      float* fR = F.face;            // [9][27] rational basis at the face points
+      float* fW = F.face + 9 * 27;   // [9] dS * weights
       if (tid < 9) {
         const int ta = nd0 == 0 ? 1 : 0, tb = nd0 == 2 ? 1 : 2;
         int g[3] = {0, 0, 0};
@@ -453,9 +452,9 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       }
       __syncthreads();
     }
-    __syncthreads();  // the Gram stage below overlays the basis arrays
+    __syncthreads();  // the element block below overlays the front-end arrays
 
-    // ---- 7. tensor memory -> exactly symmetric Gram matrix in the element
+    // ---- 6. tensor memory -> exactly symmetric Gram matrix in the element
     //         block layout: row r = 3a + k keeps its entries at and right of
     //         the diagonal (c = 3b + l >= r) and mirrors them (the MMA's FP32
     //         sums of G_rc and G_cr need not agree), so the element matrix and
@@ -488,7 +487,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     if (sm.fail) break;
     if (it + (int)gridDim.x < count) nextItem = items[it + gridDim.x];
 
-    // ---- 8. the element block to the scratch (16-byte stores)
+    // ---- 7. the element block to the scratch (16-byte stores)
     {
       float4* dst = reinterpret_cast<float4*>(P.elm + (size_t)e * P.elmStride);
       const float4* src = reinterpret_cast<const float4*>(Gc);
