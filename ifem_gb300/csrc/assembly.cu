@@ -889,7 +889,6 @@ ifemgpu_status upload(ifemgpu_ctx* ctx, T** dst, const T* src, size_t n)
   return IFEMGPU_OK;
 }
 
-#define IFEMGPU_TRY(x) do { ifemgpu_status s_ = (x); if (s_ != IFEMGPU_OK) return s_; } while (0)
 
 ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
 {
@@ -1446,6 +1445,18 @@ static ifemgpu_status autotune(ifemgpu_ctx* ctx)
                        t[1] * 1e-3, t[2] * 1e-3, ctx->useFlow ? "persistent" : "per colour");
     }
   }
+  return IFEMGPU_OK;
+}
+
+// Every kernel of one assembly on the context's stream, without timing events
+// (for the capture of a whole assemble -> solve step); the autotuner has run.
+ifemgpu_status enqueueAssembly(ifemgpu_ctx* ctx)
+{
+  if (!ctx->tuned) return setError(ctx, IFEMGPU_NOT_READY, "internal: assembly not tuned");
+  bool hasSeg[3] = {true, false, false};
+  for (const Pass& p : ctx->passes) hasSeg[p.face ? 2 : 1] = true;
+  for (int seg = 0; seg < 3; seg++)
+    if (hasSeg[seg]) IFEMGPU_TRY(enqueueSegment(ctx, seg));
   return IFEMGPU_OK;
 }
 

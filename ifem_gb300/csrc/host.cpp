@@ -86,6 +86,7 @@ void freeDevice(ifemgpu_ctx* ctx)
   ctx->d_items = nullptr;
   ctx->d_neumann = nullptr;
   ctx->d_counters = nullptr;
+  dropStep(ctx);
   freeSolver(ctx);
   freeNorms(ctx);
   destroyLearn(ctx);

@@ -241,6 +241,12 @@ struct ifemgpu_ctx {
   double* h_pinned = nullptr;
   // captured inner-solve loops: [0] FP32 Jacobi-PCG, [1 + fine + 2 coarse] FP32
   // flexible CG (fine: 0 Jacobi, 1 Kronecker; coarse: learned correction on)
+  // one captured assemble -> solve step (ifemgpu_graph_capture)
+  cudaGraph_t stepGraph = nullptr;
+  cudaGraphExec_t stepExec = nullptr;
+  ifemgpu_solver_options stepOpts{};
+  const void* stepKey = nullptr;  // workspace the step was captured on
+  int stepGen = -1;
   static constexpr int kLoops = 5;
   cudaGraphExec_t loopExec[kLoops] = {};
   const void* loopKey[kLoops] = {};
@@ -276,6 +282,7 @@ ifemgpu_status cudaFail(ifemgpu_ctx* ctx, cudaError_t e, const char* what);
 // assembly.cu
 ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx);
 ifemgpu_status launchAssembly(ifemgpu_ctx* ctx);
+ifemgpu_status enqueueAssembly(ifemgpu_ctx* ctx);
 ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs);
 
 // tc_volume.cu
@@ -298,6 +305,9 @@ ifemgpu_status gatherLaunch(ifemgpu_ctx* ctx, const GatherList& g);
 // solver.cu
 ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o,
                         double* x, ifemgpu_solve_info* info, const double* bdev = nullptr);
+ifemgpu_status captureStep(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o);
+ifemgpu_status launchStep(ifemgpu_ctx* ctx, double* x, ifemgpu_solve_info* info);
+void dropStep(ifemgpu_ctx* ctx);
 ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* xstar,
                             int stride, int maxit, double rtol, int precond);
 void freeSolver(ifemgpu_ctx* ctx);
@@ -352,4 +362,10 @@ int fdLaunches(const ifemgpu_ctx* ctx);
   do {                                                            \
     cudaError_t e_ = (call);                                      \
     if (e_ != cudaSuccess) return ifemgpu::cudaFail(ctx, e_, #call); \
+  } while (0)
+
+#define IFEMGPU_TRY(x)                                            \
+  do {                                                            \
+    ifemgpu_status s_ = (x);                                      \
+    if (s_ != IFEMGPU_OK) return s_;                              \
   } while (0)

@@ -726,85 +726,121 @@ static inline unsigned* hostTickets(const Work& w)
 
 static void spmv32(ifemgpu_ctx* ctx, const Work& w, const float* p, float* q, int shift);
 
-// FP32 Jacobi-PCG on rhs r64 / sqrt(scal[9]) from x = 0 (captured loop)
-static ifemgpu_status loopPCG32(ifemgpu_ctx* ctx, const Work& w, double rtol, int maxit,
-                                int* iters)
+// One FP32 Jacobi-PCG iteration (the body of the captured loop), and its start
+// on rhs r64 / sqrt(scal[9]) from x = 0.
+static ifemgpu_status pcgIteration(ifemgpu_ctx* ctx, const Work& w)
 {
   cudaStream_t s = ctx->stream;
   const int n = ctx->neq;
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
-  auto body = [&]() -> ifemgpu_status {
-    spmv32(ctx, w, w.p32, w.q32, 1);
-    g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32,
-                                                w.scal, n, w.part);
-    g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
-    IFEMGPU_CUDA(ctx, cudaGetLastError());
-    return IFEMGPU_OK;
-  };
-  ifemgpu_status st = captureLoop(ctx, 0, ctx->workGen, body);
-  if (st != IFEMGPU_OK) return st;
+  spmv32(ctx, w, w.p32, w.q32, 1);
+  g_pcg_update<float><<<vb, kThreads, 0, s>>>(w.x32, w.r32, w.z32, w.p32, w.q32, w.dinv32, w.scal,
+                                              n, w.part);
+  g_pcg_dir<float><<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.scal, n);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  return IFEMGPU_OK;
+}
+
+static ifemgpu_status pcgStart(ifemgpu_ctx* ctx, const Work& w, double rtol, int maxit)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
   k_loop_init<<<1, 1, 0, s>>>(w.scal, rtol * rtol, (double)maxit, 0.0);
   g_pcg_start<float><<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.dinv32,
                                              n, w.part);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
+  return IFEMGPU_OK;
+}
+
+// FP32 Jacobi-PCG on rhs r64 / sqrt(scal[9]) from x = 0 (captured loop)
+static ifemgpu_status loopPCG32(ifemgpu_ctx* ctx, const Work& w, double rtol, int maxit,
+                                int* iters)
+{
+  ifemgpu_status st = captureLoop(ctx, 0, ctx->workGen, [&]() { return pcgIteration(ctx, w); });
+  if (st != IFEMGPU_OK) return st;
+  if ((st = pcgStart(ctx, w, rtol, maxit)) != IFEMGPU_OK) return st;
   int flag = 0;
   if ((st = replayLoop(ctx, w, 0, maxit, iters, &flag)) != IFEMGPU_OK) return st;
   if (flag == 2) return setError(ctx, IFEMGPU_NOT_CONVERGED, "PCG breakdown (NaN)");
   return IFEMGPU_OK;
 }
 
-// FP32 flexible CG (captured loop).  Preconditioner: the fine level (Jacobi,
-// or the Kronecker preconditioner when kron) plus, when learned, the network's
-// coarse correction.  *nan is set when the recurrence produced NaN.
-static ifemgpu_status loopFCG(ifemgpu_ctx* ctx, const Work& w, bool kron, bool learned,
-                              double rtol, int maxit, int* iters, bool* nan)
+// z = M r of flexible CG after the Jacobi step of the update kernel: the fine
+// level (Jacobi, or the Kronecker preconditioner when kron) plus, when
+// learned, the network's coarse correction; withDot: (z, q) -> S_ZQ and beta
+static ifemgpu_status fcgPrecondition(ifemgpu_ctx* ctx, const Work& w, bool kron, bool learned,
+                                      bool withDot)
 {
   cudaStream_t s = ctx->stream;
   const int n = ctx->neq;
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
   unsigned* tk = hostTickets(w);
   const double* guard = w.scal + S_DONE;
-  // z = M r after the Jacobi step of the update kernel; (z, q) -> S_ZQ and beta
-  auto precondition = [&](bool withDot) -> ifemgpu_status {
-    ifemgpu_status st2;
-    if (kron && !learned && withDot && fdCanDot(ctx)) {  // (z, q) inside the last FD kernel
-      FdDot dot;
-      dot.q = w.q32;
-      dot.part = w.part;
-      dot.counter = tk + 2;
-      dot.out = w.scal + S_ZQ;
-      dot.pq = w.scal + S_PQ;
-      dot.beta = reinterpret_cast<float*>(w.scal + S_RAT) + 1;
-      return fdApply(ctx, w.r32, w.z32, guard, &dot);
-    }
-    if (kron && (st2 = fdApply(ctx, w.r32, w.z32, guard)) != IFEMGPU_OK) return st2;
-    if (learned)
-      return learnApply(ctx, w.r32, w.z32, withDot ? w.q32 : nullptr, w.part, vb, tk + 2,
-                        w.scal + S_ZQ, w.scal + S_PQ,
-                        reinterpret_cast<float*>(w.scal + S_RAT) + 1, guard);
-    if (withDot) g_dot<<<vb, kThreads, 0, s>>>(w.z32, w.q32, n, w.part, tk + 2, w.scal);
-    return IFEMGPU_OK;
-  };
-  auto body = [&]() -> ifemgpu_status {
-    spmv32(ctx, w, w.p32, w.q32, 0);
-    g_fcg_update<<<vb, kThreads, 0, s>>>(w.x32, w.r32, kron ? nullptr : w.z32, w.p32, w.q32,
-                                         w.dinv32, w.scal, n, w.part);
-    ifemgpu_status st2 = precondition(true);
-    if (st2 != IFEMGPU_OK) return st2;
-    g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
-    IFEMGPU_CUDA(ctx, cudaGetLastError());
-    return IFEMGPU_OK;
-  };
-  const int slot = 1 + (kron ? 1 : 0) + (learned ? 2 : 0);
-  ifemgpu_status st = captureLoop(ctx, slot, ctx->workGen * 65536 + (learned ? ctx->learnGen : 0), body);
-  if (st != IFEMGPU_OK) return st;
+  ifemgpu_status st2;
+  if (kron && !learned && withDot && fdCanDot(ctx)) {  // (z, q) inside the last FD kernel
+    FdDot dot;
+    dot.q = w.q32;
+    dot.part = w.part;
+    dot.counter = tk + 2;
+    dot.out = w.scal + S_ZQ;
+    dot.pq = w.scal + S_PQ;
+    dot.beta = reinterpret_cast<float*>(w.scal + S_RAT) + 1;
+    return fdApply(ctx, w.r32, w.z32, guard, &dot);
+  }
+  if (kron && (st2 = fdApply(ctx, w.r32, w.z32, guard)) != IFEMGPU_OK) return st2;
+  if (learned)
+    return learnApply(ctx, w.r32, w.z32, withDot ? w.q32 : nullptr, w.part, vb, tk + 2,
+                      w.scal + S_ZQ, w.scal + S_PQ,
+                      reinterpret_cast<float*>(w.scal + S_RAT) + 1, guard);
+  if (withDot) g_dot<<<vb, kThreads, 0, s>>>(w.z32, w.q32, n, w.part, tk + 2, w.scal);
+  return IFEMGPU_OK;
+}
+
+// one flexible-CG iteration (the body of the captured loop)
+static ifemgpu_status fcgIteration(ifemgpu_ctx* ctx, const Work& w, bool kron, bool learned)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  spmv32(ctx, w, w.p32, w.q32, 0);
+  g_fcg_update<<<vb, kThreads, 0, s>>>(w.x32, w.r32, kron ? nullptr : w.z32, w.p32, w.q32,
+                                       w.dinv32, w.scal, n, w.part);
+  ifemgpu_status st2 = fcgPrecondition(ctx, w, kron, learned, true);
+  if (st2 != IFEMGPU_OK) return st2;
+  g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  return IFEMGPU_OK;
+}
+
+// flexible CG start on rhs r64 / sqrt(scal[9]) from x = p = q = 0
+static ifemgpu_status fcgStart(ifemgpu_ctx* ctx, const Work& w, bool kron, bool learned,
+                               double rtol, int maxit)
+{
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
   // a learned loop must keep shrinking its residual or it stops (and the
   // caller continues without the network)
   k_loop_init<<<1, 1, 0, s>>>(w.scal, rtol * rtol, (double)maxit, learned ? 1.0 : 0.0);
   g_fcg_start<<<vb, kThreads, 0, s>>>(w.r64, w.scal, w.r32, w.x32, w.z32, w.p32, w.q32, w.dinv32, n);
-  if ((st = precondition(false)) != IFEMGPU_OK) return st;  // p = q = 0: (z, q) = 0
+  ifemgpu_status st = fcgPrecondition(ctx, w, kron, learned, false);  // p = q = 0: (z, q) = 0
+  if (st != IFEMGPU_OK) return st;
   g_fcg_dir<<<vb, kThreads, 0, s>>>(w.p32, w.z32, w.r32, w.scal, n, w.part);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
+  return IFEMGPU_OK;
+}
+
+// FP32 flexible CG (captured loop).  *nan is set when the recurrence produced
+// NaN or (learned) stagnated.
+static ifemgpu_status loopFCG(ifemgpu_ctx* ctx, const Work& w, bool kron, bool learned,
+                              double rtol, int maxit, int* iters, bool* nan)
+{
+  const int slot = 1 + (kron ? 1 : 0) + (learned ? 2 : 0);
+  ifemgpu_status st = captureLoop(ctx, slot, ctx->workGen * 65536 + (learned ? ctx->learnGen : 0),
+                                  [&]() { return fcgIteration(ctx, w, kron, learned); });
+  if (st != IFEMGPU_OK) return st;
+  if ((st = fcgStart(ctx, w, kron, learned, rtol, maxit)) != IFEMGPU_OK) return st;
   int flag = 0;
   if ((st = replayLoop(ctx, w, slot, maxit, iters, &flag)) != IFEMGPU_OK) return st;
   *nan = flag >= 2;  // NaN or stagnation
@@ -1099,6 +1135,238 @@ ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o, doubl
   return IFEMGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// One captured assemble -> solve step (ifemgpu_graph_capture / _launch): the
+// pair SIMbase::assembleSystem -> SIMbase::solveEqSystem as a single CUDA
+// graph.  Its nodes: the assembly's kernels, the solver prologue, and the
+// FP64 refinement loop as a conditional WHILE node whose body runs one FP32
+// inner solve -- itself a WHILE node over blocks of kLoopBlock iterations --
+// then the FP64 residual.  Kernels decide both loop conditions from the same
+// device scalars the host-driven solve reads (same FP64 operations), so a
+// replay takes the same decisions as ifemgpu_assemble + ifemgpu_solve and
+// gives the same bits.  Both loops end by construction: the inner stop flag
+// is set at max_inner iterations (or NaN), the outer loop stops after
+// max_outer refinement steps or on a failed inner solve.
+namespace {
+
+enum : int { S_OUT = 20, S_INN = 21, S_REL = 22, S_FAIL = 23 };
+
+__global__ void k_step_init(cudaGraphConditionalHandle outer, double* s, double rtol, int maxOuter)
+{
+  s[S_OUT] = 0.0;
+  s[S_INN] = 0.0;
+  s[S_FAIL] = 0.0;
+  const double bn = sqrt(s[8]);
+  const double rel = bn > 0.0 ? 1.0 : 0.0;
+  s[S_REL] = rel;
+  cudaGraphSetConditional(outer, (bn > 0.0 && rel > rtol && maxOuter > 0) ? 1u : 0u);
+}
+
+__global__ void k_step_inner_cond(cudaGraphConditionalHandle inner, const double* s)
+{
+  cudaGraphSetConditional(inner, s[S_DONE] == 0.0 ? 1u : 0u);
+}
+
+// after an inner solve: count it; a breakdown (NaN or stagnation) ends the step
+__global__ void k_step_inner_done(double* s)
+{
+  s[S_OUT] += 1.0;
+  s[S_INN] += s[S_ITS];
+  if (s[S_DONE] >= 2.0) s[S_FAIL] = 1.0;
+}
+
+// x64 += sqrt(scal[9]) x32 unless the inner solve failed
+__global__ void k_step_accumulate(double* __restrict__ x64, const float* __restrict__ x32,
+                                  const double* __restrict__ s, int n)
+{
+  if (s[S_FAIL] != 0.0) return;
+  const double sc = sqrt(s[9]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x64[i] += sc * (double)x32[i];
+}
+
+// relative FP64 residual of the step and the outer loop condition
+__global__ void k_step_outer_cond(cudaGraphConditionalHandle outer, double* s, double rtol,
+                                  int maxOuter)
+{
+  if (s[S_FAIL] == 0.0) s[S_REL] = sqrt(s[9]) / sqrt(s[8]);
+  const bool more = s[S_FAIL] == 0.0 && s[S_REL] > rtol && s[S_OUT] < (double)maxOuter;
+  cudaGraphSetConditional(outer, more ? 1u : 0u);
+}
+
+}  // namespace
+
+void dropStep(ifemgpu_ctx* ctx)
+{
+  if (ctx->stepExec) cudaGraphExecDestroy(ctx->stepExec);
+  if (ctx->stepGraph) cudaGraphDestroy(ctx->stepGraph);
+  ctx->stepExec = nullptr;
+  ctx->stepGraph = nullptr;
+  ctx->stepKey = nullptr;
+  ctx->stepGen = -1;
+}
+
+// the current capture's dependency set -> a new node of `params` -> the new
+// dependency set (the node itself)
+static ifemgpu_status addNodeToCapture(ifemgpu_ctx* ctx, cudaGraphNodeParams* params,
+                                       cudaGraphNode_t* node)
+{
+  cudaStream_t s = ctx->stream;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  IFEMGPU_CUDA(ctx, cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+  if (cs != cudaStreamCaptureStatusActive)
+    return setError(ctx, IFEMGPU_CUDA_ERROR, "internal: stream not capturing");
+  IFEMGPU_CUDA(ctx, cudaGraphAddNode(node, g, deps, nullptr, ndeps, params));
+  IFEMGPU_CUDA(ctx, cudaStreamUpdateCaptureDependencies(s, node, nullptr, 1,
+                                                        cudaStreamSetCaptureDependencies));
+  return IFEMGPU_OK;
+}
+
+// a WHILE node on `handle` appended to the capture; *body receives its body graph
+static ifemgpu_status addWhile(ifemgpu_ctx* ctx, cudaGraphConditionalHandle handle,
+                               cudaGraph_t* body)
+{
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = handle;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  IFEMGPU_TRY(addNodeToCapture(ctx, &p, &node));
+  *body = p.conditional.phGraph_out[0];
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status captureStep(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o)
+{
+  if (o->method != IFEMGPU_PCG_MIXED)
+    return setError(ctx, IFEMGPU_UNSUPPORTED,
+                    "graph_capture: the captured step takes the mixed-precision method");
+  if (o->precond != IFEMGPU_PRECOND_JACOBI && o->precond != IFEMGPU_PRECOND_KRONECKER)
+    return setError(ctx, IFEMGPU_INVALID_ARG, "graph_capture: unknown preconditioner");
+  if (o->max_inner < 1) return setError(ctx, IFEMGPU_INVALID_ARG, "graph_capture: max_inner < 1");
+  const int n = ctx->neq;
+  if (n == 0) return setError(ctx, IFEMGPU_INVALID_ARG, "graph_capture: no equations");
+  const bool kron = o->precond == IFEMGPU_PRECOND_KRONECKER;
+  dropStep(ctx);
+  // settle everything a capture cannot do: the assembly's tuning, the
+  // workspace, the inner-loop variants and the preconditioner set-up
+  if (!ctx->tuned) {
+    IFEMGPU_TRY(launchAssembly(ctx));
+    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  ifemgpu_status st = ensureWork(ctx, true);
+  if (st != IFEMGPU_OK) return st;
+  if (kron && (st = fdSetup(ctx)) != IFEMGPU_OK) return st;
+  const Work w = carve(ctx);
+  const int maxOuter = std::max(1, o->max_outer);
+  const double innerTol = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
+  const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
+  const int sb = std::min(kRedBlocks, (n + 7) / 8);
+  cudaStream_t s = ctx->stream;
+  cudaGraph_t g = nullptr;
+  IFEMGPU_CUDA(ctx, cudaGraphCreate(&g, 0));
+  ctx->stepGraph = g;
+  cudaGraphConditionalHandle hOuter, hInner;  // each made on the graph that holds its node
+  IFEMGPU_CUDA(ctx, cudaGraphConditionalHandleCreate(&hOuter, g, 0, 0));
+  auto fail = [&](ifemgpu_status e) {
+    cudaGraph_t junk = nullptr;
+    cudaStreamCaptureStatus cs;
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+      cudaStreamEndCapture(s, &junk);
+    cudaGetLastError();
+    dropStep(ctx);
+    return e;
+  };
+  // assembly, prologue, refinement loop
+  IFEMGPU_CUDA(ctx, cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+  if ((st = enqueueAssembly(ctx)) != IFEMGPU_OK) return fail(st);
+  k_convert<float><<<1024, kThreads, 0, s>>>(ctx->d_K, ctx->d_K32, ctx->nnz);
+  k_diag<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K,
+                                                              n, w.d64, w.dinv32);
+  cudaMemsetAsync(w.x64, 0, sizeof(double) * n, s);
+  k_norm2<double><<<vb, kThreads, 0, s>>>(ctx->d_b, n, w.part);
+  k_finish<<<1, kThreads, 0, s>>>(w.part, vb, 1, w.scal + 8);
+  cudaMemcpyAsync(w.r64, ctx->d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(w.scal + 9, w.scal + 8, sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (kron && (st = fdRescale(ctx, w.d64)) != IFEMGPU_OK) return fail(st);
+  k_step_init<<<1, 1, 0, s>>>(hOuter, w.scal, o->rtol, maxOuter);
+  if (cudaGetLastError() != cudaSuccess) return fail(setError(ctx, IFEMGPU_CUDA_ERROR, "graph_capture: prologue"));
+  cudaGraph_t outerBody = nullptr;
+  if ((st = addWhile(ctx, hOuter, &outerBody)) != IFEMGPU_OK) return fail(st);
+  cudaGraph_t top = nullptr;
+  IFEMGPU_CUDA(ctx, cudaStreamEndCapture(s, &top));
+  IFEMGPU_CUDA(ctx, cudaGraphConditionalHandleCreate(&hInner, outerBody, 0, 0));
+  // outer body: inner start, inner WHILE, accumulate, FP64 residual, condition
+  IFEMGPU_CUDA(ctx, cudaStreamBeginCaptureToGraph(s, outerBody, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+  st = kron ? fcgStart(ctx, w, true, false, innerTol, o->max_inner)
+            : pcgStart(ctx, w, innerTol, o->max_inner);
+  if (st != IFEMGPU_OK) return fail(st);
+  k_step_inner_cond<<<1, 1, 0, s>>>(hInner, w.scal);
+  cudaGraph_t innerBody = nullptr;
+  if ((st = addWhile(ctx, hInner, &innerBody)) != IFEMGPU_OK) return fail(st);
+  k_step_inner_done<<<1, 1, 0, s>>>(w.scal);
+  k_step_accumulate<<<vb, kThreads, 0, s>>>(w.x64, w.x32, w.scal, n);
+  k_residual<<<sb, kThreads, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K, w.x64, ctx->d_b, w.r64,
+                                     n, w.part, ctx->d_rowPat, ctx->d_patStart, ctx->d_patOff);
+  k_finish<<<1, kThreads, 0, s>>>(w.part, sb, 1, w.scal + 9);
+  k_step_outer_cond<<<1, 1, 0, s>>>(hOuter, w.scal, o->rtol, maxOuter);
+  if (cudaGetLastError() != cudaSuccess) return fail(setError(ctx, IFEMGPU_CUDA_ERROR, "graph_capture: outer body"));
+  cudaGraph_t ob = nullptr;
+  IFEMGPU_CUDA(ctx, cudaStreamEndCapture(s, &ob));
+  // inner body: kLoopBlock iterations, then the inner condition
+  IFEMGPU_CUDA(ctx, cudaStreamBeginCaptureToGraph(s, innerBody, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < kLoopBlock && st == IFEMGPU_OK; k++)
+    st = kron ? fcgIteration(ctx, w, true, false) : pcgIteration(ctx, w);
+  if (st != IFEMGPU_OK) return fail(st);
+  k_step_inner_cond<<<1, 1, 0, s>>>(hInner, w.scal);
+  if (cudaGetLastError() != cudaSuccess) return fail(setError(ctx, IFEMGPU_CUDA_ERROR, "graph_capture: inner body"));
+  cudaGraph_t ib = nullptr;
+  IFEMGPU_CUDA(ctx, cudaStreamEndCapture(s, &ib));
+  const cudaError_t e = cudaGraphInstantiate(&ctx->stepExec, g, 0);
+  if (e != cudaSuccess) return fail(cudaFail(ctx, e, "cudaGraphInstantiate (assemble -> solve step)"));
+  ctx->stepOpts = *o;
+  ctx->stepKey = ctx->d_work;
+  ctx->stepGen = ctx->workGen;
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status launchStep(ifemgpu_ctx* ctx, double* xh, ifemgpu_solve_info* info)
+{
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  if (!ctx->stepExec) return setError(ctx, IFEMGPU_NOT_READY, "graph_launch before graph_capture");
+  if (ctx->stepKey != ctx->d_work || ctx->stepGen != ctx->workGen) {  // the workspace moved
+    const ifemgpu_solver_options o = ctx->stepOpts;
+    IFEMGPU_TRY(captureStep(ctx, &o));
+  }
+  cudaStream_t s = ctx->stream;
+  const int n = ctx->neq;
+  const Work w = carve(ctx);
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->stepExec, s));
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + S_OUT, 4 * sizeof(double),
+                                    cudaMemcpyDeviceToHost, s));
+  if (xh) IFEMGPU_CUDA(ctx, cudaMemcpyAsync(xh, w.x64, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
+  ctx->assembled = true;
+  const double* h = ctx->h_pinned;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+  const double relres = h[2];
+  if (info) *info = ifemgpu_solve_info{(int)h[0], (int)h[1], relres, (double)ms, 0};
+  if (h[3] != 0.0) return setError(ctx, IFEMGPU_NOT_CONVERGED, "graph step: inner solve broke down");
+  if (relres > ctx->stepOpts.rtol)
+    return setError(ctx, IFEMGPU_NOT_CONVERGED, "relative residual above tolerance");
+  return IFEMGPU_OK;
+}
+
 // z = M r for the FP32 preconditioner precond of the assembled matrix (host
 // vectors; diagnostic)
 ifemgpu_status applyPreconditioner(ifemgpu_ctx* ctx, int precond, const double* r, double* z)
@@ -1387,4 +1655,19 @@ extern "C" ifemgpu_status ifemgpu_solve_noalloc(ifemgpu_ctx* ctx, double rtol, i
     return ifemgpu::setError(ctx, IFEMGPU_NOT_READY, "solve before assemble");
   IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
   return ifemgpu::solveNoAlloc(ctx, rtol, max_iter, x, info);
+}
+
+extern "C" ifemgpu_status ifemgpu_graph_capture(ifemgpu_ctx* ctx, const ifemgpu_solver_options* opts)
+{
+  if (!ctx || !opts) return IFEMGPU_INVALID_ARG;
+  if (!ctx->preprocessed || ctx->opts.device < 0)
+    return ifemgpu::setError(ctx, IFEMGPU_NOT_READY, "graph_capture before preprocess");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  return ifemgpu::captureStep(ctx, opts);
+}
+
+extern "C" ifemgpu_status ifemgpu_graph_launch(ifemgpu_ctx* ctx, double* x, ifemgpu_solve_info* info)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  return ifemgpu::launchStep(ctx, x, info);
 }

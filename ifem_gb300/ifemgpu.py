@@ -79,6 +79,7 @@ EXPORTS = [
     "ifemgpu_learn_evaluate", "ifemgpu_learn_gradients", "ifemgpu_learn_info",
     "ifemgpu_learn_get_weights", "ifemgpu_learn_set_weights", "ifemgpu_patch_update_field",
     "ifemgpu_learn_get_pairs", "ifemgpu_apply_preconditioner", "ifemgpu_copy_matrix_bsr",
+    "ifemgpu_graph_capture", "ifemgpu_graph_launch",
 ]
 
 
@@ -135,6 +136,8 @@ def load_library(path: str | None = None):
         "ifemgpu_get_stream": (I, [P, C.POINTER(C.c_void_p)]),
         "ifemgpu_selftest_tc_gemm": (I, [V, V, V]),
         "ifemgpu_solve_noalloc": (I, [P, D, I, V, C.POINTER(SolveInfo)]),
+        "ifemgpu_graph_capture": (I, [P, C.POINTER(SolverOptions)]),
+        "ifemgpu_graph_launch": (I, [P, V, C.POINTER(SolveInfo)]),
         "ifemgpu_learn_setup": (I, [P, C.POINTER(LearnOptions)]),
         "ifemgpu_learn_collect": (I, [P, V, V, I, I, D, I, C.POINTER(I)]),
         "ifemgpu_learn_clear": (I, [P]),
@@ -414,6 +417,21 @@ class SIM:
         o = SolverOptions(method, rtol, max_outer, max_inner, inner_rtol, precond)
         info = SolveInfo()
         st = self.lib.ifemgpu_solve(self.ctx, C.byref(o), _ptr(x), C.byref(info))
+        if check:
+            self._check(st)
+        return x, info
+
+    def graph_capture(self, rtol=1e-10, max_outer=20, max_inner=20000, inner_rtol=1e-4,
+                      precond=PRECOND_JACOBI):
+        """Captures one assemble -> solve step (mixed-precision PCG / FCG)."""
+        o = SolverOptions(PCG_MIXED, rtol, max_outer, max_inner, inner_rtol, precond)
+        self._check(self.lib.ifemgpu_graph_capture(self.ctx, C.byref(o)))
+
+    def graph_launch(self, check=True):
+        """Replays the captured step: (solution, info)."""
+        x = np.zeros(self.sizes.neq, dtype=np.float64)
+        info = SolveInfo()
+        st = self.lib.ifemgpu_graph_launch(self.ctx, _ptr(x), C.byref(info))
         if check:
             self._check(st)
         return x, info

@@ -387,6 +387,31 @@ ifemgpu_status ifemgpu_solve(ifemgpu_ctx* ctx,
 ifemgpu_status ifemgpu_solve_noalloc(ifemgpu_ctx* ctx, double rtol, int max_iter,
                                      double* x, ifemgpu_solve_info* info);
 
+/* ---- captured assemble -> solve step ----------------------------------- */
+
+/* Captures one assembly of the model followed by a solve of the assembled
+ * system into a single CUDA graph owned by the context, for loops that
+ * re-assemble and re-solve a model whose values change between steps
+ * (ifemgpu_patch_update_coefs, ifemgpu_patch_update_field): the assembly's
+ * kernels, the solver's prologue, and the FP64 refinement loop as a
+ * device-driven conditional loop (CUDA conditional WHILE nodes) around the
+ * FP32 inner solve, itself a conditional loop over blocks of iterations.  The
+ * device takes the loop decisions from the same FP64 quantities as
+ * ifemgpu_solve, so a replay gives the bits of ifemgpu_assemble followed by
+ * ifemgpu_solve with the same options.  Method IFEMGPU_PCG_MIXED with the
+ * Jacobi or Kronecker preconditioner.  The first capture of a context runs
+ * one assembly (it settles the assembly's launch tuning).  Replaces the pair
+ * SIMbase::assembleSystem -> SIMbase::solveEqSystem
+ * (src/SIM/SIMbase.C:1229-1429, :1487-1550) of IFEM's time and parameter
+ * loops.                                                                   */
+ifemgpu_status ifemgpu_graph_capture(ifemgpu_ctx* ctx, const ifemgpu_solver_options* opts);
+
+/* Replays the captured step on the context's stream and copies the solution
+ * (neq values, FP64, equation order) to x (may be null); info as for
+ * ifemgpu_solve (device_ms covers assembly and solve).  The assembled system
+ * stays on the device as after ifemgpu_assemble.                          */
+ifemgpu_status ifemgpu_graph_launch(ifemgpu_ctx* ctx, double* x, ifemgpu_solve_info* info);
+
 /* Equation order -> DOF order, fixed DOFs 0 and prescribed DOFs their value
  * times scale; replaces SAM::expandSolution (src/LinAlg/SAM.C:768-810).   */
 ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
