@@ -16,8 +16,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libifemgpu.so")
 OBJDIR = os.path.join(HERE, "_build")
 
-SOURCES = ["host.cpp", "assembly.cu", "solver.cu", "tc_volume.cu", "tc_poisson.cu", "gather.cu",
-           "learned.cu", "fdprec.cu", "norms.cu"]
+SOURCES = ["host.cpp", "assembly.cu", "solver.cu", "tc_volume.cu", "tc_poisson.cu", "tc_elast3.cu",
+           "gather.cu", "learned.cu", "fdprec.cu", "norms.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "-I", INCLUDE]
 

@@ -212,6 +212,8 @@ struct SysView {
   unsigned long long* counters;  // [0] singular points [1] pattern misses [2] timeouts [3] work
   const int* F;  // free DOFs before each node
   int* flags;    // per-element done flags of the persistent pass
+  unsigned flagSpin;  // polls per flag wait
+  int withhold;       // flag slot that is never published (test hook), -1 none
 };
 
 constexpr uint32_t kGenFlagSpin = 1u << 20;  // x 64 ns sleeps: about 0.1 s per wait
@@ -296,7 +298,7 @@ __device__ void waitNeighbours(const DevPatch& P, int e, const SysView& S)
     uint32_t spin = 0;
     waited = true;
     while (genLoadRelaxed(flag) == 0) {
-      if (++spin > kGenFlagSpin) {
+      if (++spin > S.flagSpin) {
         atomicAdd(S.counters + 2, 1ull);
         break;
       }
@@ -723,7 +725,7 @@ __device__ void volumeElement(const DevPatch& P, const Item it, const SysView& S
   }
   if (kFlow) {  // publish: this element's contributions are all issued
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && P.flagBase + e != S.withhold) {
       __threadfence();
       genStoreRelease(S.flags + P.flagBase + e, 1);
     }
@@ -997,7 +999,14 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     DevPatch& D = ctx->h_devpatches[pi];
     onTc[pi] = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcSupports(D) && D.mass == 0.0 &&
                D.lineOff != nullptr && D.faceTables && ctx->patches[pi].neumann.size() <= 6;
-    if (onTc[pi]) onTc[pi] = tcUploadPatch(ctx, ctx->patches[pi], D);  // node tables, TMA maps
+    if (onTc[pi]) onTc[pi] = tcUploadPatch(ctx, ctx->patches[pi], D);  // control-net TMA map
+    if (!onTc[pi] && ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32 && tcElast3Supports(D) &&
+        D.mass == 0.0 && D.lineOff != nullptr && D.faceTables &&
+        ctx->patches[pi].neumann.size() <= 6 &&
+        tcPoissonUpload(ctx, ctx->patches[pi], D, 3)) {  // (p+1)^3 control-net boxes
+      onTc[pi] = 1;
+      tcDeg[pi] = kTcElast3;
+    }
     if (!onTc[pi] && ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32) {
       const int deg = tcPoissonDegree(D, ctx->patches[pi]);
       if (deg && tcPoissonUpload(ctx, ctx->patches[pi], D, deg)) {
@@ -1057,7 +1066,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     D.flagBase = nflags;
     D.tile = 4;
     if (!onTc[pi] && flow) nflags += ctx->patches[pi].nelAll;
-    if (onTc[pi] && tcDeg[pi] == 0) {
+    if (onTc[pi] && (tcDeg[pi] == 0 || tcDeg[pi] == kTcElast3)) {
       // the element kernel integrates this patch's Neumann faces itself
       D.nneu = (int)ctx->patches[pi].neumann.size();
       for (int f = 0; f < D.nneu; f++) {
@@ -1078,8 +1087,10 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
           if (pc.active[e]) out.push_back({pi, e, 0, 0});
         }
   };
-  for (int deg : {0, 2, 3}) {  // one persistent launch per tensor-core kernel, elements in order
-    Pass pass{(int)vol.size(), 0, 0, deg ? 1 : 81, deg ? tcPoissonSmem(deg) : tcVolumeSmem(), true};
+  for (int deg : {0, kTcElast3, 2, 3}) {  // one persistent launch per tensor-core kernel
+    const size_t smem = deg == 0 ? tcVolumeSmem() : deg == kTcElast3 ? tcElast3Smem()
+                                                                      : tcPoissonSmem(deg);
+    Pass pass{(int)vol.size(), 0, 0, deg == 0 ? 81 : deg == kTcElast3 ? 192 : 1, smem, true};
     pass.tcDeg = deg;
     for (int pi = 0; pi < np; pi++)
       if (onTc[pi] && tcDeg[pi] == deg)
@@ -1246,6 +1257,7 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     if (p.tc) {
       IFEMGPU_TRY(tcPrepare(ctx));
       IFEMGPU_TRY(tcPoissonPrepare(ctx));
+      IFEMGPU_TRY(tcElast3Prepare(ctx));
       break;
     }
   for (auto& g : ctx->gathers) IFEMGPU_TRY(gatherPrepare(ctx, g));
@@ -1280,6 +1292,16 @@ ifemgpu_status updateCoefs(ifemgpu_ctx* ctx, int pi, const double* coefs)
   return IFEMGPU_OK;
 }
 
+static SysView sysView(ifemgpu_ctx* ctx)
+{
+  int withhold = -1;
+  if (ctx->dbg.patch >= 0 && ctx->dbg.patch < (int)ctx->h_devpatches.size() && ctx->dbg.elem >= 0)
+    withhold = ctx->h_devpatches[ctx->dbg.patch].flagBase + ctx->dbg.elem;
+  return SysView{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
+                 ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore,
+                 ctx->d_flags, ctx->dbg.flagSpin ? ctx->dbg.flagSpin : kGenFlagSpin, withhold};
+}
+
 // The kernel sequence of one assembly in three segments -- prologue (zeroing,
 // basis tables), volume passes, face passes -- each captured once into a CUDA
 // graph; the timing events are recorded between the graph launches.
@@ -1303,13 +1325,13 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
     IFEMGPU_CUDA(ctx, cudaGetLastError());
     return IFEMGPU_OK;
   }
-  SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
-            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore, ctx->d_flags};
+  SysView S = sysView(ctx);
   const bool split = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32;
   if (seg == 1) {  // element kernels of the tensor-core patches, then their gathers
     for (const Pass& p : ctx->passes) {
       if (!p.tc) continue;
-      if (p.tcDeg) IFEMGPU_TRY(tcPoissonLaunch(ctx, p, p.tcDeg));
+      if (p.tcDeg == kTcElast3) IFEMGPU_TRY(tcElast3Launch(ctx, p));
+      else if (p.tcDeg) IFEMGPU_TRY(tcPoissonLaunch(ctx, p, p.tcDeg));
       else IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
     }
     for (const GatherList& g : ctx->gathers) IFEMGPU_TRY(gatherLaunch(ctx, g));
@@ -1351,8 +1373,7 @@ static ifemgpu_status autotune(ifemgpu_ctx* ctx)
   if (!pp) return IFEMGPU_OK;
   const bool split = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32;
   cudaStream_t s = ctx->stream;
-  SysView S{ctx->d_madof, ctx->d_meqn, ctx->nceq ? ctx->d_c0 : nullptr, ctx->d_colptr,
-            ctx->d_rowidx, ctx->d_K, ctx->d_b, ctx->d_counters, ctx->d_freeBefore, ctx->d_flags};
+  SysView S = sysView(ctx);
   const int np = (int)ctx->h_devpatches.size();
   // grid > 0: the persistent pass with that grid; grid = 0: its colour passes
   auto timePass = [&](int grid, float* ms) -> ifemgpu_status {

@@ -34,6 +34,25 @@ ifemgpu_status cudaFail(ifemgpu_ctx* ctx, cudaError_t e, const char* what)
                                                       : IFEMGPU_CUDA_ERROR, msg);
 }
 
+// Reads the wait counters of the last assembly once: a bounded device wait
+// that gave up leaves the system invalid (IFEMGPU_DEVICE_TIMEOUT, and calls
+// that need an assembled system report IFEMGPU_NOT_READY until the next
+// assembly).
+ifemgpu_status verifyAssembly(ifemgpu_ctx* ctx)
+{
+  if (!ctx->checkPending) return IFEMGPU_OK;
+  ctx->checkPending = false;
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  unsigned long long c[4] = {0, 0, 0, 0};
+  IFEMGPU_CUDA(ctx, cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+  if (c[2]) {
+    ctx->assembled = false;
+    return setError(ctx, IFEMGPU_DEVICE_TIMEOUT,
+                    "a bounded device wait gave up: the assembled system is invalid");
+  }
+  return IFEMGPU_OK;
+}
+
 }  // namespace ifemgpu
 
 namespace {
@@ -791,12 +810,28 @@ ifemgpu_status ifemgpu_assemble(ifemgpu_ctx* ctx, int sync)
   ifemgpu_status st = launchAssembly(ctx);
   if (st != IFEMGPU_OK) return st;
   ctx->assembled = true;
-  if (sync) {
-    IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    unsigned long long c[4] = {0, 0, 0, 0};
-    IFEMGPU_CUDA(ctx, cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
-    if (c[2]) return setError(ctx, IFEMGPU_DEVICE_TIMEOUT, "a bounded device wait gave up");
+  ctx->checkPending = true;
+  return sync ? verifyAssembly(ctx) : IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_debug_waits(ifemgpu_ctx* ctx, unsigned flag_spin, unsigned copy_spin,
+                                   int patch_id, int element)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (patch_id < 0 || patch_id > (int)ctx->patches.size() || (patch_id > 0 && element < 0))
+    return setError(ctx, IFEMGPU_INVALID_ARG, "debug_waits: bad patch or element");
+  ctx->dbg.flagSpin = flag_spin;
+  ctx->dbg.mbarSpin = copy_spin;
+  ctx->dbg.patch = patch_id - 1;
+  ctx->dbg.elem = patch_id > 0 ? element : -1;
+  // the captured kernel sequences hold the old parameters
+  for (int g = 0; g < 3; g++) {
+    if (ctx->graphExec[g]) cudaGraphExecDestroy(ctx->graphExec[g]);
+    if (ctx->graph[g]) cudaGraphDestroy(ctx->graph[g]);
+    ctx->graphExec[g] = nullptr;
+    ctx->graph[g] = nullptr;
   }
+  dropStep(ctx);
   return IFEMGPU_OK;
 }
 
@@ -806,6 +841,7 @@ ifemgpu_status ifemgpu_last_assembly_stats(ifemgpu_ctx* ctx, double* total_ms,
 {
   if (!ctx) return IFEMGPU_INVALID_ARG;
   if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
+  IFEMGPU_TRY(verifyAssembly(ctx));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   float t0 = 0.f, t1 = 0.f;
   IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[3]));
@@ -824,6 +860,7 @@ ifemgpu_status ifemgpu_copy_matrix(ifemgpu_ctx* ctx, double* values)
   if (!ctx || !values) return IFEMGPU_INVALID_ARG;
   if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
   IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  IFEMGPU_TRY(verifyAssembly(ctx));
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(values, ctx->d_K, sizeof(double) * ctx->nnz,
                                     cudaMemcpyDeviceToHost, ctx->stream));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -873,6 +910,7 @@ ifemgpu_status ifemgpu_copy_rhs(ifemgpu_ctx* ctx, double* rhs)
   if (!ctx || !rhs) return IFEMGPU_INVALID_ARG;
   if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
   IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  IFEMGPU_TRY(verifyAssembly(ctx));
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(rhs, ctx->d_b, sizeof(double) * ctx->neq,
                                     cudaMemcpyDeviceToHost, ctx->stream));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -998,6 +1036,7 @@ ifemgpu_status ifemgpu_solve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* opt
   if (!ctx || !opts || !x) return IFEMGPU_INVALID_ARG;
   if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "solve before assemble");
   IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  IFEMGPU_TRY(verifyAssembly(ctx));
   return runSolve(ctx, opts, x, info);
 }
 

@@ -140,6 +140,8 @@ struct HostPatch {
   int* d_lineOff = nullptr;
 };
 
+constexpr int kTcElast3 = 13;  // Pass::tcDeg of the p = 3 elasticity kernel
+
 // One colour pass of the volume or face integration.
 struct Pass {
   int first;   // offset into the item array
@@ -148,9 +150,21 @@ struct Pass {
   int maxNd;   // largest element DOF count in the pass
   size_t smem; // dynamic shared memory of the pass' launch
   bool tc;     // volume pass on a tensor-core kernel
-  int tcDeg = 0;  // 0: elasticity p = 2 kernel; 2, 3: Poisson kernel of that degree
+  int tcDeg = 0;  // 0: elasticity p = 2 kernel; 2, 3: Poisson kernel of that degree;
+                  // kTcElast3: elasticity p = 3 kernel
   bool persistent = false;  // one colour-major launch ordered by done flags
   bool altColour = false;   // colour pass over a part of the persistent pass' items
+};
+
+// Test hooks of the bounded device waits (ifemgpu_debug_waits): shorter
+// limits, and one element (patch index, patch-local element) whose done flag
+// is never published (persistent generic pass) or whose control points are
+// never copied (tensor-core kernels), so that the waits for it run out.
+struct DebugWaits {
+  unsigned flagSpin = 0;  // polls per neighbour-flag wait (0: default)
+  unsigned mbarSpin = 0;  // polls per mbarrier wait for a copy (0: default)
+  int patch = -1;
+  int elem = -1;
 };
 
 // Node-wise gather launch of one (degree, npv) class of tensor-core patches:
@@ -213,6 +227,8 @@ struct ifemgpu_ctx {
   size_t elmFloats = 0;
   std::vector<ifemgpu::GatherList> gathers;
   bool zeroSystem = true;        // some patch adds into the system (generic kernels)
+  ifemgpu::DebugWaits dbg;       // test hooks of the bounded device waits
+  bool checkPending = false;     // an assembly's wait counters not yet read
   // statistics of the last assembly
   double last_total_ms = 0.0, last_volume_ms = 0.0;
   unsigned long long last_singular = 0;
@@ -277,6 +293,7 @@ struct ifemgpu_ctx {
 namespace ifemgpu {
 
 ifemgpu_status setError(ifemgpu_ctx* ctx, ifemgpu_status st, const std::string& msg);
+ifemgpu_status verifyAssembly(ifemgpu_ctx* ctx);
 ifemgpu_status cudaFail(ifemgpu_ctx* ctx, cudaError_t e, const char* what);
 
 // assembly.cu
@@ -296,6 +313,11 @@ size_t tcPoissonSmem(int deg);
 ifemgpu_status tcPoissonPrepare(ifemgpu_ctx* ctx);
 ifemgpu_status tcPoissonLaunch(ifemgpu_ctx* ctx, const Pass& p, int deg);
 ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int grid);
+// tc_elast3.cu: tensor-core elasticity kernel, p = 3
+bool tcElast3Supports(const DevPatch& P);
+size_t tcElast3Smem();
+ifemgpu_status tcElast3Prepare(ifemgpu_ctx* ctx);
+ifemgpu_status tcElast3Launch(ifemgpu_ctx* ctx, const Pass& p);
 
 // gather.cu
 size_t elementBlockFloats(int p, int npv);

@@ -1356,6 +1356,8 @@ ifemgpu_status launchStep(ifemgpu_ctx* ctx, double* xh, ifemgpu_solve_info* info
   if (xh) IFEMGPU_CUDA(ctx, cudaMemcpyAsync(xh, w.x64, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
   ctx->assembled = true;
+  ctx->checkPending = true;
+  IFEMGPU_TRY(verifyAssembly(ctx));
   const double* h = ctx->h_pinned;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);

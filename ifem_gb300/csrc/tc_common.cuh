@@ -86,10 +86,11 @@ __device__ __forceinline__ bool mbarTryWait(uint32_t mbar, uint32_t parity)
   return ok != 0;
 }
 
-// Polls the barrier phase at most kSpinLimit times; false on give-up.
-__device__ __forceinline__ bool mbarWait(uint32_t mbar, uint32_t parity)
+// Polls the barrier phase at most `limit` times (each try_wait may suspend
+// the thread for a while); false on give-up.
+__device__ __forceinline__ bool mbarWait(uint32_t mbar, uint32_t parity, uint32_t limit = kSpinLimit)
 {
-  for (uint32_t i = 0; i < kSpinLimit; i++)
+  for (uint32_t i = 0; i < limit; i++)
     if (mbarTryWait(mbar, parity)) return true;
   return false;
 }

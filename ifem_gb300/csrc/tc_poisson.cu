@@ -105,6 +105,8 @@ static_assert(PCfg<3>::BLOCK % 4 == 0 && PCfg<2>::BLOCK % 4 == 0, "16-byte eleme
 
 struct PoisSys {
   unsigned long long* counters;  // [0] singular points, [2] device timeouts
+  unsigned mbarSpin;             // polls per wait for a copy
+  int wPatch, wElem;             // element whose copy is never issued (test hook), -1 none
 };
 
 template <int P>
@@ -142,6 +144,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     const int f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
     const int f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
     const char* tm = static_cast<const char*>(Pn.tmaps);
+    if (nx.patch == S.wPatch && nx.elem == S.wElem) return;  // withheld: the wait runs out
     if (nx.patch != mapPatch) {
       tmapAcquire(tm);
       mapPatch = nx.patch;
@@ -179,7 +182,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       if (hasG) gv = (float)Pt.logk[node];
       if (hasN) nv = (float)Pt.noise[node];
     }
-    if (mbarWait(ctrlbar, cphase)) {
+    if (mbarWait(ctrlbar, cphase, S.mbarSpin)) {
       cphase ^= 1u;
       ctrlOut = false;
     } else {
@@ -475,7 +478,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     __syncthreads();  // the next element's node data overwrite the tile
   }
   // after a timeout: a copy still in flight lands before the CTA exits
-  if (tid == 0 && ctrlOut) mbarWait(ctrlbar, cphase);
+  if (tid == 0 && ctrlOut) mbarWait(ctrlbar, cphase, S.mbarSpin);
   tcFenceBefore();
   __syncthreads();
   tcFenceAfter();
@@ -537,7 +540,8 @@ ifemgpu_status tcPoissonPrepare(ifemgpu_ctx* ctx)
 ifemgpu_status tcPoissonLaunch(ifemgpu_ctx* ctx, const Pass& p, int deg)
 {
   if (deg != 2 && deg != 3) return setError(ctx, IFEMGPU_INVALID_ARG, "internal: Poisson kernel degree");
-  PoisSys S{ctx->d_counters};
+  PoisSys S{ctx->d_counters, ctx->dbg.mbarSpin ? ctx->dbg.mbarSpin : kSpinLimit, ctx->dbg.patch,
+          ctx->dbg.elem};
   const void* fn = deg == 2 ? (const void*)k_volume_tc_poisson<2> : (const void*)k_volume_tc_poisson<3>;
   const size_t smem = tcPoissonSmem(deg);
   const int cap = deg == 2 ? PCfg<2>::PER_SM : PCfg<3>::PER_SM;

@@ -103,6 +103,8 @@ static_assert(offsetof(TcSmem, Tlo) == offsetof(TcSmem, Thi) + sizeof(float) * k
 
 struct TcSys {
   unsigned long long* counters;  // [0] singular points, [2] device timeouts
+  unsigned mbarSpin;             // polls per wait for a copy
+  int wPatch, wElem;             // element whose copy is never issued (test hook), -1 none
 };
 
 __global__ void __launch_bounds__(128)
@@ -145,6 +147,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     const int f2 = (nx.elem / Pn.nel[0]) % Pn.nel[1];
     const int f3 = nx.elem / (Pn.nel[0] * Pn.nel[1]);
     const char* tm = static_cast<const char*>(Pn.tmaps);
+    if (nx.patch == S.wPatch && nx.elem == S.wElem) return;  // withheld: the wait runs out
     if (nx.patch != mapPatch) {
       tmapAcquire(tm);
       mapPatch = nx.patch;
@@ -175,7 +178,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
       const int d = tid / 18, dd = (tid / 9) & 1, g = tid % 9;
       tbv = (dd ? P.tabDf[d] : P.tabNf[d])[(d == 0 ? e1 : d == 1 ? e2 : e3) * 9 + g];
     }
-    if (mbarWait(ctrlbar, cphase)) {
+    if (mbarWait(ctrlbar, cphase, S.mbarSpin)) {
       cphase ^= 1u;
       ctrlOut = false;
     } else {
@@ -496,7 +499,7 @@ k_volume_tc_elast_p2(const DevPatch* __restrict__ patches, const Item* __restric
     __syncthreads();  // the next element's step 1 overwrites the block
   }
   // after a timeout: a copy still in flight lands before the CTA exits
-  if (tid == 0 && ctrlOut) mbarWait(ctrlbar, cphase);
+  if (tid == 0 && ctrlOut) mbarWait(ctrlbar, cphase, S.mbarSpin);
 
   // release tensor memory (all tcgen05 traffic of this CTA has completed)
   tcFenceBefore();
@@ -649,7 +652,8 @@ ifemgpu_status tcPrepare(ifemgpu_ctx* ctx)
 
 ifemgpu_status tcLaunchVolume(ifemgpu_ctx* ctx, const Pass& p, int)
 {
-  TcSys S{ctx->d_counters};
+  TcSys S{ctx->d_counters, ctx->dbg.mbarSpin ? ctx->dbg.mbarSpin : kSpinLimit, ctx->dbg.patch,
+          ctx->dbg.elem};
   // as many CTAs as fit at once (shared memory, registers and the 4 x 128
   // tensor-memory columns of an SM); no CTA waits for another
   cudaFuncAttributes fa{};

@@ -79,7 +79,7 @@ EXPORTS = [
     "ifemgpu_learn_evaluate", "ifemgpu_learn_gradients", "ifemgpu_learn_info",
     "ifemgpu_learn_get_weights", "ifemgpu_learn_set_weights", "ifemgpu_patch_update_field",
     "ifemgpu_learn_get_pairs", "ifemgpu_apply_preconditioner", "ifemgpu_copy_matrix_bsr",
-    "ifemgpu_graph_capture", "ifemgpu_graph_launch",
+    "ifemgpu_graph_capture", "ifemgpu_graph_launch", "ifemgpu_debug_waits",
 ]
 
 
@@ -138,6 +138,7 @@ def load_library(path: str | None = None):
         "ifemgpu_solve_noalloc": (I, [P, D, I, V, C.POINTER(SolveInfo)]),
         "ifemgpu_graph_capture": (I, [P, C.POINTER(SolverOptions)]),
         "ifemgpu_graph_launch": (I, [P, V, C.POINTER(SolveInfo)]),
+        "ifemgpu_debug_waits": (I, [P, C.c_uint, C.c_uint, I, I]),
         "ifemgpu_learn_setup": (I, [P, C.POINTER(LearnOptions)]),
         "ifemgpu_learn_collect": (I, [P, V, V, I, I, D, I, C.POINTER(I)]),
         "ifemgpu_learn_clear": (I, [P]),

@@ -524,6 +524,21 @@ ifemgpu_status ifemgpu_patch_update_field(ifemgpu_ctx* ctx, int patch_id,
 ifemgpu_status ifemgpu_apply_preconditioner(ifemgpu_ctx* ctx, int precond,
                                             const double* r, double* z);
 
+/* Test hooks of the bounded device waits.  Every wait of a device kernel on
+ * another's progress is bounded; one that gives up counts a timeout, the
+ * kernel returns, and the next call that needs the assembled system
+ * (ifemgpu_assemble with sync, ifemgpu_copy_matrix, ifemgpu_solve, ...)
+ * reports IFEMGPU_DEVICE_TIMEOUT and marks the system invalid.  This sets
+ * the limits -- flag_spin polls per wait for a neighbour's done flag in the
+ * persistent generic pass (0: the default, about 0.1 s), copy_spin polls per
+ * wait for a tensor-core kernel's control-point copy (0: the default) -- and
+ * picks one element (patch_id 1-based, patch-local element; patch_id 0:
+ * none) whose done flag is never published and whose copy is never issued,
+ * so that the waits for it run out.  No IFEM counterpart: it exercises the
+ * failure path without faulting the GPU.                                  */
+ifemgpu_status ifemgpu_debug_waits(ifemgpu_ctx* ctx, unsigned flag_spin, unsigned copy_spin,
+                                   int patch_id, int element);
+
 /* Runs the tensor-core building block of the element kernel once on the
  * current device: D (128 x 96) = A (128 x 32) * B (96 x 32)^T in 3xTF32
  * split precision with FP32 accumulation, all row-major host arrays.  No

@@ -41,6 +41,7 @@ def lib():
         P, I, D, V = C.c_void_p, C.c_int, C.c_double, C.c_void_p
         sig = {
             "ifo_create": (P, [I]), "ifo_destroy": (None, [P]),
+            "ifo_set_bisect": (None, [P, I]),
             "ifo_add_patch": (I, [P, I, V, V, V, V, I]),
             "ifo_set_material": (I, [P, I, I, D, D, I, D, D, V]),
             "ifo_set_field": (I, [P, I, I, V]),
@@ -157,6 +158,11 @@ class OracleModel:
         out = np.zeros(nel * nen, dtype=np.int32)
         self.L.ifo_get_mnpc(self.h, pid, _p(out))
         return out.reshape(nel, nen)
+
+    def set_bisect(self, on: bool = True):
+        """Entry lookup of the scatter by binary search instead of IFEM's
+        linear std::find (same sums; for parity tests of large models)."""
+        self.L.ifo_set_bisect(self.h, int(on))
 
     def assemble(self, threads: int = 1, max_elements: int = 0) -> int:
         return self.L.ifo_assemble(self.h, threads, max_elements)

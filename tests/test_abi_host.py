@@ -216,3 +216,20 @@ def test_oracle_parallel_pattern_equals_set_couplings(oracle_lib, name):
         pats.append(orc.pattern())
     np.testing.assert_array_equal(pats[0][0], pats[1][0])
     np.testing.assert_array_equal(pats[0][1], pats[1][1])
+
+
+@pytest.mark.parametrize("name", ["cfg2_p3", "cfg4_small", "cfg3_small"])
+def test_oracle_binary_search_scatter_equals_linear(oracle_lib, name):
+    """The oracle's binary-search entry lookup (used by the large parity tests)
+    gives bitwise the sums of IFEM's linear std::find lookup."""
+    import oracle
+    patches, ng = CASES[name]()
+    out = []
+    for bis in (False, True):
+        orc = oracle.OracleModel(ng)
+        W.load_into(orc, patches)
+        orc.preprocess()
+        orc.set_bisect(bis)
+        orc.assemble(4)
+        out.append(orc.system())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])

@@ -33,6 +33,7 @@ def oracle_system(patches, ng):
     orc = oracle.OracleModel(ng)
     W.load_into(orc, patches)
     orc.preprocess()
+    orc.set_bisect(True)       # same entries and sums as IFEM's linear search, faster
     orc.assemble(THREADS)
     return orc
 

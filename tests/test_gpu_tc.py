@@ -196,10 +196,25 @@ def test_split_multipatch_mixed(gpulib, oracle_lib):
     split_vs_oracle(patches, ng)
 
 
-def test_split_elasticity_p3_generic(gpulib, oracle_lib):
-    """p=3 elasticity is not on the tensor-core kernel: the FP32 generic
-    kernel assembles it."""
-    split_vs_oracle(*W.config2(nel=3, p=3))
+@pytest.mark.parametrize("nel", [3, 6])
+def test_split_elasticity_p3_tensor_core(gpulib, oracle_lib, nel):
+    """p=3 elasticity (192 DOFs per element) on its tensor-core kernel: two
+    MMA blocks (rows 0..127 x 192, rows 128..191 x 64), the element block
+    mirrored from the upper triangle, with the traction face and a body
+    force; basis tables, element kernel and gather are the only launches."""
+    patches, ng = W.config2(nel=nel, p=3)
+    patches[0].body = (0.2, 0.0, -0.5)
+    sim, orc = split_vs_oracle(patches, ng)
+    K = sim.matrix_values()
+    big = np.abs(K) > 1e-3 * np.abs(K).max()
+    Ko, _ = orc.system()
+    assert (np.abs(K[big] - Ko[big]) / np.abs(Ko[big])).max() < 1e-4
+    _, _, singular = sim.assembly_stats()
+    assert singular == 0
+    assert sim.kernel_launches <= 3
+    assert_exactly_symmetric(sim, K)
+    sim.assembleSystem()
+    assert np.array_equal(sim.matrix_values(), K)
 
 
 def test_config4_family_solve_matches_direct(gpulib, oracle_lib):
