@@ -64,6 +64,14 @@ __device__ __forceinline__ void dfAdd(float& hi, float& lo, float x)
   lo = __fadd_rn(lo, err);
 }
 
+// the same on a shared (hi, lo) pair: one 8-byte load and store
+__device__ __forceinline__ void dfAdd(float2* acc, float x)
+{
+  float2 v = *acc;
+  dfAdd(v.x, v.y, x);
+  *acc = v;
+}
+
 }  // namespace
 
 size_t elementBlockFloats(int p, int npv)
@@ -94,8 +102,7 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
   constexpr int Q = C::Q, NEN = C::NEN, W = C::W, NS = C::NS, KL = C::KL;
   extern __shared__ float gsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* accHi = gsm + warp * 2 * KL * NS;  // [kl][slot]
-  float* accLo = accHi + KL * NS;
+  float2* acc = reinterpret_cast<float2*>(gsm) + warp * KL * NS;  // [kl][slot] (hi, lo)
   for (int t = blockIdx.x * C::WARPS + warp; t < total; t += gridDim.x * C::WARPS) {
     int r0 = 0, r1 = nranges - 1;
     while (r0 < r1) {
@@ -118,10 +125,7 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
       cpa[k] = eqa[k] > 0 ? S.colptr[eqa[k] - 1] : 0;
     }
     if (!any) continue;  // no column: fixed or prescribed DOFs only
-    for (int i = lane; i < KL * NS; i += 32) {
-      accHi[i] = 0.f;
-      accLo[i] = 0.f;
-    }
+    for (int i = lane; i < KL * NS; i += 32) acc[i] = make_float2(0.f, 0.f);
     float feHi = 0.f, feLo = 0.f;  // lane k < NPV: load vector of DOF k
     const float lamf = Pt.lamf, muf = Pt.muf;
     const int ex0 = max(0, ax - P), cx = min(ax, Pt.nel[0] - 1) - ex0 + 1;
@@ -182,10 +186,10 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
 #pragma unroll
                 for (int l = 0; l < 3; l++) {
                   const float ke = fmaf(lamf, gg[3 * k + l], fmaf(muf, gg[3 * l + k], k == l ? tr : 0.f));
-                  dfAdd(accHi[(3 * k + l) * NS + s], accLo[(3 * k + l) * NS + s], ke);
+                  dfAdd(acc + (3 * k + l) * NS + s, ke);
                 }
             } else {
-              dfAdd(accHi[s], accLo[s], gg[0]);
+              dfAdd(acc + s, gg[0]);
             }
           }
         }
@@ -214,7 +218,8 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
         for (int k = 0; k < NPV; k++) {
           if (eqa[k] <= 0) continue;
           const int kl = k * NPV + l;
-          const double v = tc::widenF32(accHi[kl * NS + s]) + tc::widenF32(accLo[kl * NS + s]);
+          const float2 hl = acc[kl * NS + s];
+          const double v = tc::widenF32(hl.x) + tc::widenF32(hl.y);
           if (eqb > 0)
             S.K[cpa[k] + pos + rank] = v;
           else if (S.c0)
