@@ -66,8 +66,9 @@ def test_persistent_launch_equals_colour_passes(gpulib, ke, kind):
     assert np.array_equal(s1.matrix_values(), K1) and np.array_equal(s1.rhs(), b1)
     s1.assembly_stats()
     s2.assembly_stats()
-    if ke == G.KE_SPLIT_TF32 and kind == 1:  # every patch on the tensor-core Poisson kernels
+    if ke == G.KE_SPLIT_TF32:  # every patch on the tensor-core kernels (p = 2 and 3)
         assert s1.kernel_launches == s2.kernel_launches
+        assert s1.kernel_launches <= 5  # basis tables, one element kernel and one gather per degree
     else:
         assert s1.kernel_launches < s2.kernel_launches
 
@@ -103,3 +104,4 @@ def test_full_config3_persistent(gpulib):
               f"persistent {t1:.2f} ms ({s1.kernel_launches} launches), "
               f"colour passes {t2:.2f} ms ({s2.kernel_launches} launches), "
               f"autotuned {t3:.2f} ms ({s3.kernel_launches} launches)")
+        assert s3.kernel_launches <= 5   # one element launch and one gather per degree
