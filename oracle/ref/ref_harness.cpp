@@ -283,6 +283,60 @@ RH_API int rh_poisson_element(void* p, int iel, int nq, const double* N, const d
   return skipped;
 }
 
+// Secondary solution at the Gauss points of one element from IFEM's
+// utl::Jacobian (src/Utility/CoordinateMapping.C:24-63): per point q the
+// spatial gradients dNdX of the element functions, then for Poisson (nf = 1)
+// the flux -kappa[q] grad u, for isotropic elasticity (nf = dim = 3) the
+// stress lambda tr(eps) I + 2 mu eps in Voigt order xx yy zz xy yz zx, from
+// the element's solution values ue[a][c].  N[q][a], dNdu[q][d][a], X[a][3] as
+// for rh_poisson_element; out[q][.]; zero at singular points.  The
+// application integrands that evaluate these (IFEM-Poisson, IFEM-Elasticity)
+// are outside the IFEM tree; the constitutive step is the same one the
+// element matrices use.
+RH_API int rh_secondary_points(int dim, int nen, int nq, const double* N, const double* dNdu,
+                               const double* X, int nf, const double* ue, const double* kappa,
+                               double lam, double mu, double* out)
+{
+  Matrix Xnod(dim, nen);
+  for (int a = 0; a < nen; a++)
+    for (int r = 0; r < dim; r++) Xnod(r + 1, a + 1) = X[(size_t)a * 3 + r];
+  Matrix J, dNdX, dNdu_m(nen, dim);
+  const int ncomp = nf == 1 ? dim : 6;
+  int skipped = 0;
+  for (int q = 0; q < nq; q++) {
+    (void)N;
+    for (int a = 0; a < nen; a++)
+      for (int d = 0; d < dim; d++) dNdu_m(a + 1, d + 1) = dNdu[((size_t)q * dim + d) * nen + a];
+    double* o = out + (size_t)q * ncomp;
+    for (int c = 0; c < ncomp; c++) o[c] = 0.0;
+    const double detJ = utl::Jacobian(J, dNdX, Xnod, dNdu_m);
+    if (detJ == 0.0) {
+      skipped++;
+      continue;
+    }
+    if (nf == 1) {
+      for (int k = 0; k < dim; k++) {
+        double g = 0.0;
+        for (int a = 0; a < nen; a++) g += dNdX(a + 1, k + 1) * ue[a];
+        o[k] = -kappa[q] * g;
+      }
+    } else {
+      double G[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // G[c][k] = du_c/dx_k
+      for (int a = 0; a < nen; a++)
+        for (int c = 0; c < 3; c++)
+          for (int k = 0; k < 3; k++) G[c][k] += ue[(size_t)a * 3 + c] * dNdX(a + 1, k + 1);
+      const double tr = G[0][0] + G[1][1] + G[2][2];
+      o[0] = lam * tr + 2.0 * mu * G[0][0];
+      o[1] = lam * tr + 2.0 * mu * G[1][1];
+      o[2] = lam * tr + 2.0 * mu * G[2][2];
+      o[3] = mu * (G[0][1] + G[1][0]);
+      o[4] = mu * (G[1][2] + G[2][1]);
+      o[5] = mu * (G[2][0] + G[0][2]);
+    }
+  }
+  return skipped;
+}
+
 // Assemble a given element matrix (column-major, nd x nd with nd = nf * nen)
 // and load vector through SAM::assembleSystem.
 RH_API int rh_assemble(void* p, int iel, const double* eKin, const double* eSin)

@@ -52,6 +52,7 @@ def lib():
             "rh_collapse": (I, [P, I, I, I, I]), "rh_neighbours": (None, [P, I, I]),
             "rh_renumber": (I, [P]), "rh_fix_patch": (I, [P, I, I, I]),
             "rh_node_id": (I, [P, I, I]), "rh_elm_id": (I, [P, I, I]),
+            "rh_secondary_points": (I, [I, I, I, V, V, V, I, V, V, C.c_double, C.c_double, V]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -303,3 +304,76 @@ def _poisson_elements(L, h, orc, patch, n_gauss, mnpc, nen, pid=1, iel=None):
         L.rh_poisson_element(h, iel[e] if iel else e + 1, nq, _p(np.ascontiguousarray(Nq)),
                              _p(np.ascontiguousarray(dNq)), _p(wfac), _p(kap), _p(f),
                              float(patch.mass), _p(Xe), _p(eK), _p(eS))
+
+
+def reference_secondary(patch, n_gauss: int, u_dof):
+    """Secondary solution of u (DOF order, npv values per node) at every Gauss
+    point of one patch with IFEM's utl::Jacobian: Poisson flux -kappa grad u,
+    elasticity stress (Voigt xx yy zz xy yz zx).  Shape (nel, nq, ncomp),
+    elements and points first index fastest.  Basis values at IFEM's Gauss
+    points come from the oracle (IFEM takes them from GoTools)."""
+    import oracle
+    from ifem_gb300 import workloads as W
+
+    orc = oracle.OracleModel(n_gauss)
+    W.load_into(orc, [patch])
+    orc.preprocess()
+    dim, p = patch.dim, patch.degree
+    nen = int(np.prod([q + 1 for q in p]))
+    nf = 1 if patch.kind == 1 else dim
+    ncomp = dim if nf == 1 else 6
+    mnpc = orc.mnpc(1, patch.nel, nen)
+    ng = [n_gauss if n_gauss > 0 else p[d] + 1 for d in range(dim)]
+    rules = [gauss(n) for n in ng]
+    nel_d = [patch.ncoef[d] - p[d] for d in range(dim)]
+    X = np.zeros((patch.nnod, 3))
+    X[:, :dim] = patch.coefs[:, :dim]
+    logk = None if patch.log_kappa is None else np.asarray(patch.log_kappa)
+    lam = patch.E * patch.nu / ((1 + patch.nu) * (1 - 2 * patch.nu))
+    mu = patch.E / (2 * (1 + patch.nu))
+    u_dof = np.asarray(u_dof, dtype=np.float64).reshape(patch.nnod, nf)
+    nq = int(np.prod(ng))
+    out = np.zeros((patch.nel, nq, ncomp))
+    Nq = np.zeros((nq, nen))
+    dNq = np.zeros((nq, dim, nen))
+    kap = np.zeros(nq)
+    u = np.zeros(3)
+    Nb = np.zeros(nen)
+    dNb = np.zeros(nen * dim)
+    nodes = np.zeros(nen, dtype=np.int32)
+    L = lib()
+    try:
+        for e in range(patch.nel):
+            idx, r = [], e
+            for d in range(dim):
+                idx.append(r % nel_d[d])
+                r //= nel_d[d]
+            spans = [(patch.knots[d][p[d] + idx[d]], patch.knots[d][p[d] + idx[d] + 1])
+                     for d in range(dim)]
+            q = 0
+            for gk in range(ng[2] if dim == 3 else 1):
+                for gj in range(ng[1]):
+                    for gi in range(ng[0]):
+                        g = (gi, gj, gk)
+                        for d in range(dim):
+                            xi, _ = rules[d]
+                            b0, b1 = spans[d]
+                            u[d] = 0.5 * ((b1 - b0) * xi[g[d]] + b1 + b0)
+                        orc.L.ifo_basis(orc.h, 1, _p(u), _p(Nb), _p(dNb), _p(nodes))
+                        Nq[q] = Nb
+                        dNq[q] = dNb.reshape(dim, nen)
+                        k = patch.kappa
+                        if logk is not None:
+                            k *= np.exp(Nb @ logk[mnpc[e]])
+                        kap[q] = k
+                        q += 1
+            ue = np.ascontiguousarray(u_dof[mnpc[e]].ravel())
+            res = np.zeros((nq, ncomp))
+            L.rh_secondary_points(dim, nen, nq, _p(np.ascontiguousarray(Nq)),
+                                  _p(np.ascontiguousarray(dNq)),
+                                  _p(np.ascontiguousarray(X[mnpc[e]])), nf, _p(ue), _p(kap),
+                                  lam, mu, _p(res))
+            out[e] = res
+    finally:
+        orc.close()
+    return out

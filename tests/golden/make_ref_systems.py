@@ -16,6 +16,9 @@ Cases (the seeded synthetic models of ifem_gb300/workloads.py):
   c10_connected_elast    three connected p=2 elasticity cubes, rotated, clamped at x=0
 Cases are (patches, n_gauss) or (patches, n_gauss, connections).
 Stored per case: IA, JA (0-based compressed columns), A, b (Poisson), MADOF, MEQN.
+For the single-patch 3D cases in SECONDARY also a seeded DOF vector u
+(key "u") and the secondary solution of u at every Gauss point (key "sec":
+Poisson flux, elasticity stress) evaluated with IFEM's utl::Jacobian.
 For c0_poisson2d_small (2D Poisson p=2, 4x4 elements) also the text dumps
 IFEM's SparseMatrix::dump / StdVector::dump write, in ref_dump/ (FLAT,
 MATLAB, MATRIX_MARKET; zero print tolerance 1e-12).
@@ -61,6 +64,16 @@ def cases():
     }
 
 
+# single-patch cases whose Gauss-point secondary solution is stored
+SECONDARY = ("c4_poisson3d_p3", "c3_poisson3d_nurbs", "c2_elast3d_p2")
+
+
+def secondary_input(patch):
+    """The seeded DOF vector whose secondary solution is stored."""
+    nf = 1 if patch.kind == 1 else patch.dim
+    return np.random.default_rng(W.BASE_SEED + 40).standard_normal(patch.nnod * nf)
+
+
 def main():
     from oracle import refmodel
     from oracle.ref import build_ref
@@ -84,6 +97,10 @@ def main():
         for k, v in ref.items():
             if v is not None:
                 out[f"{name}/{k}"] = v
+        if name in SECONDARY:
+            u = secondary_input(patches[0])
+            out[f"{name}/u"] = u
+            out[f"{name}/sec"] = refmodel.reference_secondary(patches[0], ng, u)
         print(f"{name}: neq {len(ref['IA']) - 1}, nnz {len(ref['A'])}")
     np.savez_compressed(os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                      "ref_systems.npz"), **out)

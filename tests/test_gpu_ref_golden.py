@@ -80,3 +80,25 @@ def test_gpu_dump_round_trip(gpulib, tmp_path):
     np.testing.assert_array_equal(ent[:, 2], sim.matrix_values())
     b = np.array([float(v) for v in (tmp_path / "b.mtx").read_text().split()[7:]])
     np.testing.assert_array_equal(b, sim.rhs())
+
+
+SEC = sorted(n for n in CASES if "sec" in golden(n))
+
+
+@pytest.mark.parametrize("ke,tol", [(G.KE_FP64, 1e-10), (G.KE_SPLIT_TF32, 2e-5)],
+                         ids=["fp64", "split"])
+@pytest.mark.parametrize("name", SEC)
+def test_gpu_secondary_matches_reference(gpulib, name, ke, tol):
+    """Gauss-point flux (Poisson) / stress (elasticity) of a seeded DOF vector
+    against the values evaluated with IFEM's own utl::Jacobian (fixture key
+    "sec"): FP64 mode to 1e-10, split mode (FP32 point arithmetic) to 2e-5 of
+    the largest value."""
+    patches, ng = CASES[name][:2]
+    ref = golden(name)
+    sim = G.SIM(n_gauss=ng, ke_precision=ke)
+    W.load_into(sim, patches)
+    sim.preprocess()
+    sim.assembleSystem()
+    nel, nq, ncomp = ref["sec"].shape
+    sec = sim.secondary_solution(1, ref["u"], nq, ncomp)
+    assert np.abs(sec - ref["sec"]).max() <= tol * np.abs(ref["sec"]).max()

@@ -72,4 +72,28 @@ def test_reference_build_reproduces_fixture(oracle_lib):
         else:
             new = refmodel.reference_system(case[0][0], case[1])
         for k, v in ref.items():
+            if k in ("u", "sec"):
+                continue
             np.testing.assert_array_equal(new[k], v, err_msg=f"{name}/{k}")
+        if "sec" in ref:
+            sec = refmodel.reference_secondary(case[0][0], case[1], ref["u"])
+            np.testing.assert_array_equal(sec, ref["sec"], err_msg=f"{name}/sec")
+
+
+SEC = sorted(n for n in CASES if "sec" in golden(n))
+
+
+@pytest.mark.parametrize("name", SEC)
+def test_oracle_secondary_matches_reference(oracle_lib, name):
+    """Gauss-point flux / stress of a seeded DOF vector: the oracle's
+    restatement against IFEM's utl::Jacobian (the fixture's "sec")."""
+    import oracle
+    patches, ng = CASES[name][:2]
+    ref = golden(name)
+    pc = patches[0]
+    orc = oracle.OracleModel(ng)
+    W.load_into(orc, patches)
+    orc.preprocess()
+    nel, nq, ncomp = ref["sec"].shape
+    sec = orc.secondary(1, ref["u"], nel, nq, ncomp)
+    assert np.abs(sec - ref["sec"]).max() <= 1e-12 * np.abs(ref["sec"]).max()
