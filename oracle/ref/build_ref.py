@@ -99,3 +99,17 @@ def build(force: bool = False) -> str | None:
 
 if __name__ == "__main__":
     print(build(force=True))
+
+
+def check_adapter(header: str) -> tuple[bool, str]:
+    """g++ -fsyntax-only of the IFEM-side adapter header against IFEM's own
+    headers (src/{ASM,LinAlg,SIM,Utility}) and include/ifemgpu.h: every
+    function marked override must override a virtual that IFEM declares with
+    the same signature.  (ok, compiler output)."""
+    repo = os.path.dirname(os.path.dirname(HERE))
+    inc = [f"-I{os.path.join(IFEM_ROOT, d)}" for d in
+           ("src", "src/ASM", "src/LinAlg", "src/SIM", "src/Utility")]
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-x", "c++", "-DReal=double", "-DepsZ=1e-12",
+           f"-I{os.path.join(repo, 'include')}", *inc, header]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    return res.returncode == 0, res.stdout + res.stderr
