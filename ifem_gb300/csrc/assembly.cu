@@ -5,15 +5,25 @@
 //                       every knot span (Cox-de Boor, FP64), per patch and
 //                       direction -- the GPU replacement of IFEM's
 //                       BasisFunctionCache (src/ASM/ASMs3D.C:3996-4143).
-//   2. volume passes    one launch per element colour.  Elements of one
-//                       colour share no node, so every CTA adds its element
-//                       matrix into the matrix without atomics and the sum
+//   2. volume passes    tensor-core patches: one element-kernel launch per
+//                       kernel class (tc_volume.cu, tc_poisson.cu,
+//                       tc_elast3.cu), each element's FP32 matrix and load
+//                       vector written to the element scratch, then one
+//                       node-wise gather per (degree, field) class
+//                       (gather.cu) that sums them into the matrix in a fixed
+//                       order.  Other patches (2D, p other than 2/3, mass
+//                       terms, repeated knots, the FP64 mode): the generic
+//                       kernels below, one launch per element colour or one
+//                       persistent colour-major launch ordered by done flags;
+//                       elements of one colour share no node, so the sum
 //                       order is fixed (deterministic).  Replaces the element
 //                       loop of ASMs3D::integrate (src/ASM/ASMs3D.C:2118-2325)
 //                       and the scatter of assemSparse
 //                       (src/LinAlg/SparseMatrix.C:614-688).
-//   3. face passes      Neumann (traction / flux) integration on patch faces
-//                       (src/ASM/ASMs3D.C:2547-2812), also colour by colour.
+//   3. face passes      Neumann (traction / flux) integration on the faces of
+//                       generic patches (src/ASM/ASMs3D.C:2547-2812), colour
+//                       by colour; tensor-core elasticity kernels integrate
+//                       their tractions in the element kernel.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>

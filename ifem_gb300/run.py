@@ -5,7 +5,8 @@ timings as one JSON line.
   python -m ifem_gb300.run --config 3 --kind 2 --colour-passes 1
 
 --config 1  2D Poisson p=2 (sine source with control-point noise)
---config 2  3D NURBS elasticity p=2 (clamped w=0, traction on w=1)
+--config 2  3D NURBS elasticity, p=2 or --degree 3 (clamped w=0, traction on
+            w=1; Gauss rule p+1)
 --config 3  64 independent patches of uneven size and degree; --kind picks the
             Poisson (1) or the elasticity (2) system
 --config 4  3D Poisson p=3 with a log-normal conductivity field
@@ -26,7 +27,8 @@ def build_model(args):
     if args.config == 1:
         return W.config1(nel=args.nel or 32)
     if args.config == 2:
-        return W.config2(nel=args.nel or 24)
+        patches, ng = W.config2(nel=args.nel or 24, p=args.degree)
+        return patches, (ng if args.degree == 2 else 0)
     if args.config == 3:
         patches, ng = W.config3()
         return [p for p in patches if p.kind == args.kind], ng
@@ -38,6 +40,8 @@ def main(argv=None):
     ap.add_argument("--config", type=int, choices=[1, 2, 3, 4], default=4)
     ap.add_argument("--nel", type=int, default=0, help="elements per direction (0: default)")
     ap.add_argument("--kind", type=int, choices=[1, 2], default=1)
+    ap.add_argument("--degree", type=int, choices=[2, 3], default=2,
+                    help="spline degree of --config 2")
     ap.add_argument("--precision", choices=["split", "fp64"], default="split")
     ap.add_argument("--colour-passes", type=int, choices=[0, 1, 2], default=0)
     ap.add_argument("--assemblies", type=int, default=3)
