@@ -1516,6 +1516,7 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
     if (hasSeg[seg]) IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[seg], s));
   }
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+  ctx->assemblies++;
   int used = 0;
   for (const Pass& p : ctx->passes)
     used += !((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow));

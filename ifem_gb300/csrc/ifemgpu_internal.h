@@ -233,6 +233,7 @@ struct ifemgpu_ctx {
   double last_total_ms = 0.0, last_volume_ms = 0.0;
   unsigned long long last_singular = 0;
   int launches_per_assembly = 0;
+  int assemblies = 0;  // assemblies launched (versions of K and b)
   int numSMs = 1;
   // persistent generic pass: grid (autotuned with the tile shapes at the first assembly)
   int genGrid = 0;
@@ -343,10 +344,13 @@ void destroyLearn(ifemgpu_ctx* ctx);
 double* learnXstar(ifemgpu_ctx* ctx);
 // fine: the fine preconditioner's output for r (used by complement targets)
 ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx,
-                           const float* fine);
-ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* q,
-                          double* part, int nparts, unsigned* counter, double* dotOut,
-                          const double* pq, float* betaOut, const double* guard);
+                           const float* fine, const float* t);
+ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* t,
+                          const float* q, double* part, int nparts, unsigned* counter,
+                          unsigned* counter2, double* dotOut, const double* pq, float* betaOut,
+                          const double* guard);
+float* learnT(ifemgpu_ctx* ctx);
+ifemgpu_status learnGalerkin(ifemgpu_ctx* ctx);
 ifemgpu_status learnTrain(ifemgpu_ctx* ctx, int epochs, int B, float lr, unsigned seed,
                           float* lossOut);
 ifemgpu_status learnEvaluate(ifemgpu_ctx* ctx, float* mse);

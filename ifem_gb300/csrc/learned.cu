@@ -72,7 +72,17 @@ struct LearnState {
   int* perm = nullptr;
   // solve scratch
   float *rc = nullptr, *h1 = nullptr, *h2 = nullptr, *yc = nullptr;
-  float* nrm = nullptr;        // [0] |rc| of the last restriction, [1] S
+  float* nrm = nullptr;        // [0] |rc| of the last restriction, [1] S, [2] alpha
+  // energy-optimal step: t = A z1, rc1 = R (r - t), the Galerkin coarse
+  // matrix Ac = R A R^T (banded: 125 npv entries per row, columns at vertex
+  // offsets -2..2 per direction) and its factor B = A R^T (per equation a
+  // box of 4^3 vertices per component, from the equation's cell - 1)
+  int reach = 0;               // max cell distance of two coupled equations
+  float* t = nullptr;
+  float* rc1 = nullptr;
+  float* Bm = nullptr;
+  float* Ac = nullptr;
+  int acAssembly = -1;         // assembly count Ac was formed from
 };
 
 namespace {
@@ -95,6 +105,185 @@ __global__ void k_restrict(const int* __restrict__ vPtr, const int* __restrict__
   for (int k = vPtr[warp] + lane; k < vPtr[warp + 1]; k += 32) s += vW[k] * r[vEq[k]];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) rc[warp] = s;
+}
+
+// rc1 = R (r - t), and rc = R r (sub = 0) or rc1 (sub != 0): warp per coarse
+// unknown, fixed order
+__global__ void k_restrict2(const int* __restrict__ vPtr, const int* __restrict__ vEq,
+                            const float* __restrict__ vW, const float* __restrict__ r,
+                            const float* __restrict__ t, int sub, float* __restrict__ rc,
+                            float* __restrict__ rc1, int nc, const double* guard)
+{
+  if (stopped(guard)) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nc) return;
+  float a = 0.f, b = 0.f;
+  for (int k = vPtr[warp] + lane; k < vPtr[warp + 1]; k += 32) {
+    const int e = vEq[k];
+    const float w = vW[k], re = r[e];
+    a += w * re;
+    b += w * (re - t[e]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    rc[warp] = sub ? b : a;
+    rc1[warp] = b;
+  }
+}
+
+// B = A R^T, one row block per (equation i, component c): warp per item,
+// lanes over the row's entries.  Slot (sx, sy, sz) of the item's 4^3 box is
+// the coarse vertex cell(i) - 1 + (sx, sy, sz); an entry j of component c
+// adds A_ij times its trilinear weights, which sit at the slots
+// cell(j) - cell(i) + 1 + {0, 1} per direction (coupled equations lie at most
+// one cell apart: checked on the host).  Per-lane sums, then a butterfly:
+// the same order on every run.
+__global__ void __launch_bounds__(kT)
+k_galerkin_rows(const int* __restrict__ colptr, const int* __restrict__ rowidx,
+                const double* __restrict__ A, const int* __restrict__ eqCell,
+                const float4* __restrict__ eqFrac, int m, int npv, int n, float* __restrict__ Bm)
+{
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < n * npv;
+       item += warps) {
+    const int i = item / npv, c = item - i * npv;
+    const int ci = eqCell[i];
+    const int cix = ci % m, ciy = (ci / m) % m, ciz = ci / (m * m);
+    float acc[64];
+#pragma unroll
+    for (int q = 0; q < 64; q++) acc[q] = 0.f;
+    for (int k = colptr[i] + lane; k < colptr[i + 1]; k += 32) {
+      const int j = rowidx[k];
+      const float4 f = eqFrac[j];
+      if ((int)f.w != c) continue;
+      const int cj = eqCell[j];
+      const int dx = cj % m - cix + 1, dy = (cj / m) % m - ciy + 1, dz = cj / (m * m) - ciz + 1;
+      const float a = (float)A[k];
+      float hx[4], hy[4], hz[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        hx[q] = q == dx ? a * (1.f - f.x) : (q == dx + 1 ? a * f.x : 0.f);
+        hy[q] = q == dy ? 1.f - f.y : (q == dy + 1 ? f.y : 0.f);
+        hz[q] = q == dz ? 1.f - f.z : (q == dz + 1 ? f.z : 0.f);
+      }
+#pragma unroll
+      for (int qz = 0; qz < 4; qz++)
+#pragma unroll
+        for (int qy = 0; qy < 4; qy++) {
+          const float yz = hy[qy] * hz[qz];
+#pragma unroll
+          for (int qx = 0; qx < 4; qx++)
+            acc[(qz * 4 + qy) * 4 + qx] = fmaf(hx[qx], yz, acc[(qz * 4 + qy) * 4 + qx]);
+        }
+    }
+    float v0 = 0.f, v1 = 0.f;
+#pragma unroll
+    for (int q = 0; q < 32; q++) {
+      float a0 = acc[q], a1 = acc[q + 32];
+      for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      }
+      if (q == lane) {
+        v0 = a0;
+        v1 = a1;
+      }
+    }
+    float* out = Bm + (size_t)item * 64;
+    out[lane] = v0;
+    out[lane + 32] = v1;
+  }
+}
+
+// Ac = R B, banded: warp per coarse unknown (vertex v, component c); the
+// equations of v's support in list order, lanes over the slots of their B
+// rows.  Column (v + o - 2, c') is stored at o npv + c' with o the vertex
+// offset (0..4 per direction); the slots of one B row land on distinct
+// columns, so every column is summed in list order.
+__global__ void __launch_bounds__(kT)
+k_galerkin_coarse(const int* __restrict__ vPtr, const int* __restrict__ vEq,
+                  const float* __restrict__ vW, const int* __restrict__ eqCell,
+                  const float* __restrict__ Bm, int m, int npv, int nc, float* __restrict__ Ac)
+{
+  extern __shared__ float gacc[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int band = 125 * npv;
+  float* acc = gacc + wib * band;
+  const int row = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (row >= nc) return;
+  for (int q = lane; q < band; q += 32) acc[q] = 0.f;
+  __syncwarp();
+  const int m1 = m + 1, v = row / npv;
+  const int vx = v % m1, vy = (v / m1) % m1, vz = v / (m1 * m1);
+  for (int k = vPtr[row]; k < vPtr[row + 1]; k++) {
+    const int i = vEq[k];
+    const float w = vW[k];
+    const int ci = eqCell[i];
+    // offset of slot 0 from v, plus 2: in 0..1 since v is a corner of cell(i)
+    const int bx = ci % m + 1 - vx, by = (ci / m) % m + 1 - vy, bz = ci / (m * m) + 1 - vz;
+    const float* Bi = Bm + (size_t)i * npv * 64;
+    for (int q = lane; q < 64 * npv; q += 32) {
+      const int cp = q >> 6, sl = q & 63;
+      const int o = ((bz + (sl >> 4)) * 5 + by + ((sl >> 2) & 3)) * 5 + bx + (sl & 3);
+      acc[o * npv + cp] += w * Bi[q];
+    }
+    __syncwarp();
+  }
+  float* out = Ac + (size_t)row * band;
+  for (int q = lane; q < band; q += 32) out[q] = acc[q];
+}
+
+// alpha = (y, rc1) / (y, Ac y) for the coarse direction y (0 when the
+// denominator is not positive or not finite): warp per coarse row, per-block
+// partials of both sums in part[b] and part[nb + b], the last block sums
+// them in fixed order.  With y = R^T-prolonged network output c, alpha is
+// the coefficient that minimises the energy norm of the error after
+// z = z1 + alpha c.
+__global__ void __launch_bounds__(kT)
+k_coarse_alpha(const float* __restrict__ Ac, const float* __restrict__ y,
+               const float* __restrict__ rc1, int m, int npv, int nc, double* __restrict__ part,
+               unsigned* counter, float* alphaOut, const double* guard)
+{
+  if (stopped(guard)) return;
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31, m1 = m + 1, band = 125 * npv;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  float num = 0.f, den = 0.f;
+  for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < nc; row += warps) {
+    const int v = row / npv;
+    const int vx = v % m1, vy = (v / m1) % m1, vz = v / (m1 * m1);
+    const float* a = Ac + (size_t)row * band;
+    float e = 0.f;
+    for (int q = lane; q < band; q += 32) {
+      const int o = q / npv, cp = q - o * npv;
+      const int ux = vx + o % 5 - 2, uy = vy + (o / 5) % 5 - 2, uz = vz + o / 25 - 2;
+      if (ux < 0 || ux > m || uy < 0 || uy > m || uz < 0 || uz > m) continue;
+      e += a[q] * y[((uz * m1 + uy) * m1 + ux) * npv + cp];
+    }
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+    if (lane == 0) {
+      den += y[row] * e;
+      num += y[row] * rc1[row];
+    }
+  }
+  const double tn = blockReduceSumF(num, sh);
+  const double td = blockReduceSumF(den, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = tn;
+    part[gridDim.x + blockIdx.x] = td;
+  }
+  if (lastBlock(counter)) {
+    const double n2 = finalSum(part, gridDim.x, sh);
+    const double d2 = finalSum(part + gridDim.x, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      const double al = n2 / d2;
+      *alphaOut = (d2 > 0.0 && al == al && al < 1e30 && al > -1e30) ? (float)al : 0.f;
+    }
+  }
 }
 
 // ec = Rn (x* sx - x) for the error of an iterate
@@ -144,7 +333,7 @@ __global__ void k_store_pair(const float* __restrict__ rc, const float* __restri
   for (int i = threadIdx.x; i < nf; i += blockDim.x) X[nc + i] = feat[i];
 }
 
-// z_e += S |rc| sum_v w_ve y_(v,c); with q != 0 also (z, q): per-block
+// z_e += alpha sum_v w_ve y_(v,c); with q != 0 also (z, q): per-block
 // partials, summed in fixed order by the last block into *dotOut
 __global__ void __launch_bounds__(kT)
 k_prolong_add(const int* __restrict__ eqCell, const float4* __restrict__ eqFrac,
@@ -155,7 +344,7 @@ k_prolong_add(const int* __restrict__ eqCell, const float4* __restrict__ eqFrac,
 {
   if (stopped(guard)) return;
   __shared__ double sh[32];
-  const float sc = nrm[0] * nrm[1];  // |rc| S
+  const float sc = nrm[2];  // the energy-optimal coefficient of the direction
   const int m1 = m + 1;
   float dot = 0.f;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
@@ -381,7 +570,7 @@ void freeLearn(LearnState* L)
   void* ptrs[] = {L->eqCell, L->eqFrac, L->vPtr, L->vEq, L->vW, L->vWn, L->theta, L->grad,
                   L->am, L->av, L->wbf, L->X, L->Y, L->xstar, L->Xb, L->Yb, L->H1, L->H2,
                   L->Yp, L->dH1, L->dH2, L->dY, L->loss, L->perm, L->rc, L->h1, L->h2,
-                  L->yc, L->nrm, L->feat};
+                  L->yc, L->nrm, L->feat, L->t, L->rc1, L->Bm, L->Ac};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -495,6 +684,17 @@ ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigne
       gr[d][i] = p > 0 ? (s / p - u0) / (u1 - u0) : 0.0;
     }
   }
+  // coupling reach in coarse cells: nodes at most p apart in one direction
+  // (the box couplings of one patch) lie in cells at most `reach` apart
+  L->reach = 0;
+  for (int d = 0; d < 3; d++) {
+    auto cellOf = [&](int i) {
+      return std::min(m - 1, std::max(0, (int)std::floor(gr[d][i] * m)));
+    };
+    for (int i = 0; i < pc.n[d]; i++)
+      for (int j = i + 1; j <= std::min(pc.n[d] - 1, i + pc.p[d]); j++)
+        L->reach = std::max(L->reach, std::abs(cellOf(j) - cellOf(i)));
+  }
   std::vector<int> cell(neq, 0);
   std::vector<float4> frac(neq, make_float4(0.f, 0.f, 0.f, 0.f));
   std::vector<std::vector<std::pair<int, float>>> vlist(nc);
@@ -596,10 +796,13 @@ ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigne
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->perm, sizeof(int) * capacity));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->loss, sizeof(float) * kLossParts));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->rc, sizeof(float) * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->rc1, sizeof(float) * nc));
+  IFEMGPU_CUDA(ctx, cudaMalloc(&L->t, sizeof(float) * std::max(neq, 1)));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->yc, sizeof(float) * nc));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->h1, sizeof(float) * nh));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->h2, sizeof(float) * nh));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->nrm, sizeof(float) * 4));
+  IFEMGPU_CUDA(ctx, cudaMemset(L->nrm, 0, sizeof(float) * 4));
   IFEMGPU_CUDA(ctx, cudaMemcpy(L->nrm + 1, &L->scale, sizeof(float), cudaMemcpyHostToDevice));
   return IFEMGPU_OK;
 }
@@ -625,19 +828,27 @@ ifemgpu_status learnPrepare(ifemgpu_ctx* ctx)
   return IFEMGPU_OK;
 }
 
-// one plain-PCG iterate (r, x of the system scaled by sx) -> one pair
+// one iterate (r, x of the system scaled by sx; fine = the fine
+// preconditioner's output for r, t = A fine) -> one pair: input R r (target
+// ERROR) or R (r - t) (target COMPLEMENT), target Rn (x* sx - x) or
+// Rn (x* sx - x - fine)
 ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, double sx,
-                           const float* fine)
+                           const float* fine, const float* t)
 {
   LearnState* L = ctx->learn;
   if (!L || L->count >= L->cap) return IFEMGPU_OK;
   cudaStream_t s = ctx->stream;
   const int nc = L->nc;
   const int blocks = (nc * 32 + kT - 1) / kT;
-  k_restrict<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, L->rc, nc, nullptr);
+  const bool comp = L->target == IFEMGPU_LEARN_TARGET_COMPLEMENT;
+  if (comp && (!fine || !t))
+    return setError(ctx, IFEMGPU_INVALID_ARG, "internal: complement pair without the fine step");
+  if (comp)
+    k_restrict2<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, t, 1, L->rc, L->rc1, nc, nullptr);
+  else
+    k_restrict<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, L->rc, nc, nullptr);
   k_restrict_err<<<blocks, kT, 0, s>>>(L->vPtr, L->vEq, L->vWn, L->xstar, sx, x,
-                                       L->target == IFEMGPU_LEARN_TARGET_COMPLEMENT ? fine : nullptr,
-                                       L->yc, nc);
+                                       comp ? fine : nullptr, L->yc, nc);
   k_store_pair<<<1, kT, 0, s>>>(L->rc, L->yc, L->feat, L->X + (size_t)L->count * L->nin,
                                 L->Y + (size_t)L->count * nc, nc, L->nf);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
@@ -645,18 +856,60 @@ ifemgpu_status learnRecord(ifemgpu_ctx* ctx, const float* r, const float* x, dou
   return IFEMGPU_OK;
 }
 
-// z += coarse correction of r with the BF16 network.  With q != 0 the
-// prolongation also forms (z, q) over its grid of nparts blocks and the last
-// block stores it in *dotOut and -(z, q) / *pq in *betaOut.  Every kernel
-// returns at once when *guard != 0.
-ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* q,
-                          double* part, int nparts, unsigned* counter, double* dotOut,
-                          const double* pq, float* betaOut, const double* guard)
+float* learnT(ifemgpu_ctx* ctx) { return ctx->learn ? ctx->learn->t : nullptr; }
+
+// The Galerkin coarse matrix Ac = R A R^T of the assembled matrix (through
+// B = A R^T), formed once per assembly; it prices the network's direction in
+// the energy norm.
+ifemgpu_status learnGalerkin(ifemgpu_ctx* ctx)
+{
+  LearnState* L = ctx->learn;
+  if (L->acAssembly == ctx->assemblies) return IFEMGPU_OK;
+  if (L->reach > 1)
+    return setError(ctx, IFEMGPU_UNSUPPORTED,
+                    "learned correction: coarse cells narrower than the matrix coupling "
+                    "(use fewer coarse cells)");
+  const int n = ctx->neq, npv = L->npv, nc = L->nc;
+  if (!L->Bm) {
+    IFEMGPU_CUDA(ctx, cudaMalloc(&L->Bm, sizeof(float) * 64 * (size_t)npv * std::max(n, 1)));
+    IFEMGPU_CUDA(ctx, cudaMalloc(&L->Ac, sizeof(float) * 125 * (size_t)npv * nc));
+  }
+  cudaStream_t s = ctx->stream;
+  int sms = 0;
+  IFEMGPU_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->opts.device));
+  const long long items = (long long)n * npv;
+  const int wpb = kT / 32;
+  const int rb = (int)std::min<long long>((items + wpb - 1) / wpb, (long long)sms * 16);
+  if (rb > 0)
+    k_galerkin_rows<<<rb, kT, 0, s>>>(ctx->d_colptr, ctx->d_rowidx, ctx->d_K, L->eqCell, L->eqFrac,
+                                      L->m, npv, n, L->Bm);
+  const size_t sm = sizeof(float) * wpb * 125 * npv;
+  k_galerkin_coarse<<<(nc + wpb - 1) / wpb, kT, sm, s>>>(L->vPtr, L->vEq, L->vW, L->eqCell, L->Bm,
+                                                         L->m, npv, nc, L->Ac);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  L->acAssembly = ctx->assemblies;
+  return IFEMGPU_OK;
+}
+
+// z = z1 + alpha R^T y: y the BF16 network's coarse direction for the input
+// R r (target ERROR) or R (r - t) (target COMPLEMENT), t = A z1 computed by
+// the caller, alpha = (y, R (r - t)) / (y, Ac y) the coefficient that
+// minimises the energy norm of the error after the step (0 when the
+// direction carries no energy).  With q != 0 the prolongation also forms
+// (z, q) over its grid of nparts blocks and the last block stores it in
+// *dotOut and -(z, q) / *pq in *betaOut.  Every kernel returns at once when
+// *guard != 0.
+ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const float* t,
+                          const float* q, double* part, int nparts, unsigned* counter,
+                          unsigned* counter2, double* dotOut, const double* pq, float* betaOut,
+                          const double* guard)
 {
   LearnState* L = ctx->learn;
   cudaStream_t s = ctx->stream;
   const int nc = L->nc, nh = L->nh;
-  k_restrict<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, L->rc, nc, guard);
+  const int comp = L->target == IFEMGPU_LEARN_TARGET_COMPLEMENT ? 1 : 0;
+  k_restrict2<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, t, comp, L->rc,
+                                                     L->rc1, nc, guard);
   k_gemv_bf16<<<(nh * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW1, L->theta + L->ob1, L->rc,
                                                       nc, L->feat, L->nf, L->h1, nh, 1, L->nrm,
                                                       guard);
@@ -664,6 +917,9 @@ ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const floa
                                                       nh, nullptr, 0, L->h2, nh, 1, nullptr, guard);
   k_gemv_bf16<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW3, L->theta + L->ob3, L->h2,
                                                       nh, nullptr, 0, L->yc, nc, 0, nullptr, guard);
+  const int ab = std::min(nparts, (nc + 7) / 8);
+  k_coarse_alpha<<<ab, kT, 0, s>>>(L->Ac, L->yc, L->rc1, L->m, L->npv, nc, part, counter2,
+                                   L->nrm + 2, guard);
   k_prolong_add<<<nparts, kT, 0, s>>>(L->eqCell, L->eqFrac, L->yc, L->nrm, L->m, L->npv,
                                       z, ctx->neq, q, part, counter, dotOut, pq, betaOut, guard);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
@@ -810,6 +1066,34 @@ void learnClear(ifemgpu_ctx* ctx)
 }
 
 }  // namespace ifemgpu
+
+extern "C" ifemgpu_status ifemgpu_learn_coarse_matrix(ifemgpu_ctx* ctx, float* Ac)
+{
+  using namespace ifemgpu;
+  if (!ctx || !Ac) return IFEMGPU_INVALID_ARG;
+  if (!ctx->learn) return setError(ctx, IFEMGPU_NOT_READY, "learn_coarse_matrix before learn_setup");
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "learn_coarse_matrix before assemble");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  IFEMGPU_TRY(verifyAssembly(ctx));
+  IFEMGPU_TRY(learnGalerkin(ctx));
+  LearnState* L = ctx->learn;
+  const int nc = L->nc, npv = L->npv, m1 = L->m + 1, band = 125 * npv;
+  std::vector<float> b((size_t)nc * band);
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaMemcpy(b.data(), L->Ac, sizeof(float) * b.size(), cudaMemcpyDeviceToHost));
+  std::fill(Ac, Ac + (size_t)nc * nc, 0.f);
+  for (int row = 0; row < nc; row++) {
+    const int v = row / npv;
+    const int vx = v % m1, vy = (v / m1) % m1, vz = v / (m1 * m1);
+    for (int q = 0; q < band; q++) {
+      const int o = q / npv, cp = q % npv;
+      const int ux = vx + o % 5 - 2, uy = vy + (o / 5) % 5 - 2, uz = vz + o / 25 - 2;
+      if (ux < 0 || ux >= m1 || uy < 0 || uy >= m1 || uz < 0 || uz >= m1) continue;
+      Ac[(size_t)row * nc + ((uz * m1 + uy) * m1 + ux) * npv + cp] = b[(size_t)row * band + q];
+    }
+  }
+  return IFEMGPU_OK;
+}
 
 extern "C" ifemgpu_status ifemgpu_learn_info(const ifemgpu_ctx* ctx, int* coarse_unknowns,
                                              int* inputs, int* hidden, int* nparam, int* pairs)

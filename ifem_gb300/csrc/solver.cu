@@ -350,6 +350,7 @@ g_spmv(const int* __restrict__ colptr, const int* __restrict__ rowidx, const T* 
       dot += (float)(acc * p[row]);
     }
   }
+  if (shift < 0) return;  // plain product: no dot, no scalars
   const double t = blockReduceSumF(dot, sh);
   if (lastBlockDone(part, t, tickets(s) + 0)) {
     const double v = finalSum(part, gridDim.x, sh);
@@ -363,7 +364,7 @@ g_spmv(const int* __restrict__ colptr, const int* __restrict__ rowidx, const T* 
 
 // q = A p with 16-bit column offsets relative to the row (banded spline
 // patterns), four independent load chains per lane; (p, q) -> S_PQ, alpha,
-// with shift also S_RZ <- S_RZN.  kPat: the offsets of row r are pattern
+// with shift > 0 also S_RZ <- S_RZN, with shift < 0 the product only.  kPat: the offsets of row r are pattern
 // rowPat[r] of the row-pattern dictionary (4 bytes per entry from HBM, the
 // dictionary stays in L2); otherwise one offset per entry (6 bytes per entry).
 template <bool kPat>
@@ -413,6 +414,7 @@ g_spmvOff(const int* __restrict__ colptr, const int* __restrict__ rowPat,
       dot += acc * p[row];
     }
   }
+  if (shift < 0) return;  // plain product: no dot, no scalars
   const double t = blockReduceSumF(dot, sh);
   if (lastBlockDone(part, t, tickets(s) + 0)) {
     const double v = finalSum(part, gridDim.x, sh);
@@ -767,8 +769,10 @@ static ifemgpu_status loopPCG32(ifemgpu_ctx* ctx, const Work& w, double rtol, in
 }
 
 // z = M r of flexible CG after the Jacobi step of the update kernel: the fine
-// level (Jacobi, or the Kronecker preconditioner when kron) plus, when
-// learned, the network's coarse correction; withDot: (z, q) -> S_ZQ and beta
+// level z1 (Jacobi, or the Kronecker preconditioner when kron) and, when
+// learned, the network's coarse direction added with its energy-optimal
+// coefficient (a multiplicative two-level step); withDot: (z, q) -> S_ZQ
+// and beta
 static ifemgpu_status fcgPrecondition(ifemgpu_ctx* ctx, const Work& w, bool kron, bool learned,
                                       bool withDot)
 {
@@ -789,10 +793,13 @@ static ifemgpu_status fcgPrecondition(ifemgpu_ctx* ctx, const Work& w, bool kron
     return fdApply(ctx, w.r32, w.z32, guard, &dot);
   }
   if (kron && (st2 = fdApply(ctx, w.r32, w.z32, guard)) != IFEMGPU_OK) return st2;
-  if (learned)
-    return learnApply(ctx, w.r32, w.z32, withDot ? w.q32 : nullptr, w.part, vb, tk + 2,
-                      w.scal + S_ZQ, w.scal + S_PQ,
+  if (learned) {  // two-level step: t = A z1, then z = z1 + alpha R^T y
+    float* t = learnT(ctx);
+    spmv32(ctx, w, w.z32, t, -1);
+    return learnApply(ctx, w.r32, w.z32, t, withDot ? w.q32 : nullptr, w.part, vb, tk + 2,
+                      tk + 5, w.scal + S_ZQ, w.scal + S_PQ,
                       reinterpret_cast<float*>(w.scal + S_RAT) + 1, guard);
+  }
   if (withDot) g_dot<<<vb, kThreads, 0, s>>>(w.z32, w.q32, n, w.part, tk + 2, w.scal);
   return IFEMGPU_OK;
 }
@@ -1073,6 +1080,8 @@ ifemgpu_status runSolve(ifemgpu_ctx* ctx, const ifemgpu_solver_options* o, doubl
   Work w = carve(ctx);
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+  // the coarse Galerkin matrix of this assembly (timed with the solve)
+  if (learned && (st = learnGalerkin(ctx)) != IFEMGPU_OK) return st;
   double bn = 0.0;
   if ((st = solvePrologue(ctx, w, b, mixed, &bn)) != IFEMGPU_OK) return st;
   if (kron && (st = fdRescale(ctx, w.d64)) != IFEMGPU_OK) return st;
@@ -1350,6 +1359,7 @@ ifemgpu_status launchStep(ifemgpu_ctx* ctx, double* xh, ifemgpu_solve_info* info
   const Work w = carve(ctx);
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
   IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->stepExec, s));
+  ctx->assemblies++;
   IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
   IFEMGPU_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, w.scal + S_OUT, 4 * sizeof(double),
                                     cudaMemcpyDeviceToHost, s));
@@ -1403,8 +1413,9 @@ ifemgpu_status applyPreconditioner(ifemgpu_ctx* ctx, int precond, const double* 
 // Training pairs from one FP32 solve of A x = rhs (the assembled b when rhs
 // is null) from x = 0 -- Jacobi-PCG, or flexible CG with the Kronecker
 // preconditioner (the iteration the network will serve): every stride-th
-// iterate gives (R r_k, Rn (x* - x_k)).  x* is the caller's reference
-// solution, or the FP64-refined mixed solve to 1e-12 when xstar is null.
+// iterate gives one pair (learnRecord).  x* is the caller's reference
+// solution, or the FP64-refined mixed solve to 1e-12 with the same
+// preconditioner when xstar is null.
 ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* xstar, int stride,
                             int maxit, double rtol, int precond)
 {
@@ -1426,7 +1437,7 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
     IFEMGPU_CUDA(ctx, cudaMemcpy(xs, xstar, sizeof(double) * n, cudaMemcpyHostToDevice));
   } else {
     std::vector<double> xh(n);
-    ifemgpu_solver_options so{IFEMGPU_PCG_MIXED, 1e-12, 40, 100000, 1e-5};
+    ifemgpu_solver_options so{IFEMGPU_PCG_MIXED, 1e-12, 40, 100000, 1e-5, precond};
     ifemgpu_solve_info si{};
     st = runSolve(ctx, &so, xh.data(), &si, b);
     if (st != IFEMGPU_OK && !(st == IFEMGPU_NOT_CONVERGED && si.relres < 1e-9)) return st;
@@ -1439,23 +1450,22 @@ ifemgpu_status collectPairs(ifemgpu_ctx* ctx, const double* rhs, const double* x
   if ((st = solvePrologue(ctx, w, b, true, &bn)) != IFEMGPU_OK) return st;
   if (!(bn > 0)) return IFEMGPU_OK;
   const bool kron = precond == IFEMGPU_PRECOND_KRONECKER;
-  // complement targets subtract the Kronecker preconditioner's output for r_k:
-  // z itself along flexible CG, a separate application into q (free between
-  // iterations) along Jacobi-PCG
+  // complement pairs take the collecting iteration's fine preconditioner
+  // output for r_k (z: Kronecker along flexible CG, Jacobi along PCG) and
+  // its product t = A z
   const bool complement = learnTarget(ctx) == IFEMGPU_LEARN_TARGET_COMPLEMENT;
-  if (kron || complement) {
+  if (kron) {
     if ((st = fdSetup(ctx)) != IFEMGPU_OK) return st;
     if ((st = fdRescale(ctx, w.d64)) != IFEMGPU_OK) return st;
   }
   const double sx = 1.0 / bn;  // the loop solves the system scaled by 1/||b||
   auto record = [&]() -> ifemgpu_status {
-    const float* fine = nullptr;
+    float* t = nullptr;
     if (complement) {
-      ifemgpu_status st2;
-      if (!kron && (st2 = fdApply(ctx, w.r32, w.q32, nullptr)) != IFEMGPU_OK) return st2;
-      fine = kron ? w.z32 : w.q32;
+      t = learnT(ctx);
+      spmv32(ctx, w, w.z32, t, -1);
     }
-    return learnRecord(ctx, w.r32, w.x32, sx, fine);
+    return learnRecord(ctx, w.r32, w.x32, sx, complement ? w.z32 : nullptr, t);
   };
   const int vb = std::min(kRedBlocks, (n + kThreads - 1) / kThreads);
   unsigned* tk = hostTickets(w);

@@ -422,11 +422,19 @@ ifemgpu_status ifemgpu_expand_solution(const ifemgpu_ctx* ctx, const double* x,
  * methods with algebraic preconditioners.  For a context of one 3D patch a
  * small network maps the residual, restricted to a coarse grid of
  * (m+1)^3 vertices over the patch's parameter domain (trilinear weights at
- * the Greville points, npv values per vertex), to a coarse error estimate
- * that is interpolated back and added to the Jacobi step of flexible CG
- * (IFEMGPU_FCG_LEARNED).  The network (3 layers of width `hidden`, ReLU) is
- * trained on the device by the library's own kernels on (residual, error)
- * pairs that plain PCG solves of the same patch generate.                 */
+ * the Greville points, R; npv values per vertex), to a coarse direction y.
+ * Flexible CG (IFEMGPU_FCG_LEARNED) applies it as a two-level step after
+ * the fine preconditioner's z1 (Jacobi or Kronecker):
+ *   t = A z1,  y = net(R r) or net(R (r - t)),
+ *   z = z1 + alpha R^T y,  alpha = (y, R (r - t)) / (y, Ac y),
+ * Ac = R A R^T the Galerkin coarse matrix of the assembly (formed on the
+ * device at the first learned solve after each assembly): alpha minimises
+ * the energy norm of the error after the step, so a poor direction costs
+ * its work but no convergence.  The network (3 layers of width `hidden`,
+ * ReLU) is trained on the device by the library's own kernels on
+ * (residual, error) pairs that solves of the same patch generate.  The
+ * coarse cells must be at least as wide as the matrix coupling (p
+ * Greville spacings), else the learned solve reports IFEMGPU_UNSUPPORTED. */
 
 typedef struct ifemgpu_learn_options {
   int coarse_cells;   /* m, coarse cells per direction (1..32)            */
@@ -446,10 +454,11 @@ ifemgpu_status ifemgpu_learn_setup(ifemgpu_ctx* ctx, const ifemgpu_learn_options
  * from x = 0 to the relative residual rtol (at most max_iter iterations)
  * with FP32 Jacobi-PCG (precond IFEMGPU_PRECOND_JACOBI) or flexible CG with
  * the Kronecker preconditioner (IFEMGPU_PRECOND_KRONECKER: the iteration the
- * network is added to) and stores one pair per stride-th iterate:
- * (R r_k / |R r_k|, Rn (x* - x_k) / |R r_k|), Rn the weight-normalised
- * restriction.  x* is xstar (neq host values) or, when null, the library's
- * FP64-refined solve to 1e-12.  *pairs receives the stored total.          */
+ * network is added to) and stores one pair per stride-th iterate (see
+ * ifemgpu_learn_set_target; Rn is the weight-normalised restriction).  x*
+ * is xstar (neq host values) or, when null, the library's FP64-refined
+ * solve to 1e-12 with the same preconditioner.  *pairs receives the
+ * stored total.                                                           */
 ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs,
                                      const double* xstar, int stride,
                                      int max_iter, double rtol, int precond,
@@ -458,12 +467,15 @@ ifemgpu_status ifemgpu_learn_collect(ifemgpu_ctx* ctx, const double* rhs,
 /* Forgets the stored pairs (the network is kept).                         */
 ifemgpu_status ifemgpu_learn_clear(ifemgpu_ctx* ctx);
 
-/* What the stored targets are (default IFEMGPU_LEARN_TARGET_ERROR):
- *   ERROR       Rn (x* - x_k) / |R r_k|, the whole coarse error;
- *   COMPLEMENT  Rn (x* - x_k - M r_k) / |R r_k| with M the Kronecker
- *               preconditioner: the part of the error that the fine level
- *               of flexible CG does not already supply, so that the added
- *               correction does not count the coarse error twice.
+/* What the stored pairs are (default IFEMGPU_LEARN_TARGET_ERROR):
+ *   ERROR       input R r_k, target Rn (x* - x_k) / |R r_k|: the whole
+ *               coarse error;
+ *   COMPLEMENT  input R (r_k - A z_k), target Rn (x* - x_k - z_k) /
+ *               |R (r_k - A z_k)|, z_k = M r_k the collecting iteration's
+ *               fine preconditioner output (Kronecker along flexible CG,
+ *               Jacobi along PCG): the part of the error that the fine step
+ *               leaves, seen through the residual it leaves.
+ * The learned solve feeds the network the input of the same mode.
  * Changing the mode forgets the stored pairs; learn_setup restores the
  * default.                                                                */
 enum ifemgpu_learn_target {
@@ -494,6 +506,12 @@ ifemgpu_status ifemgpu_learn_evaluate(ifemgpu_ctx* ctx, float* mse);
 ifemgpu_status ifemgpu_learn_gradients(ifemgpu_ctx* ctx, const float* X,
                                        const float* Y, int n, float* grad,
                                        float* loss);
+
+/* The Galerkin coarse matrix Ac = R A R^T of the assembled system as a
+ * dense row-major nc x nc FP32 array (nc = coarse_unknowns): the matrix
+ * the learned step prices its direction with, formed on the device from
+ * the FP64 matrix.  Diagnostic; no IFEM counterpart.                       */
+ifemgpu_status ifemgpu_learn_coarse_matrix(ifemgpu_ctx* ctx, float* Ac);
 
 /* Sizes of the coarse problem and the network; null pointers skipped.     */
 ifemgpu_status ifemgpu_learn_info(const ifemgpu_ctx* ctx, int* coarse_unknowns,

@@ -204,30 +204,92 @@ def test_pairs_from_kronecker_iterates(gpulib):
     assert np.isfinite(Xk).all() and np.isfinite(Yk).all()
 
 
-def test_complement_targets_subtract_the_kronecker_step(gpulib):
-    """Complement targets: the first pair's target is the whole-error target
-    minus the weight-normalised restriction of the Kronecker preconditioner's
-    output for the first residual, on the same scale."""
+def csc_matrix(sim):
+    import scipy.sparse as sp
+    sam = sim.getSAM()
+    n = sim.sizes.neq
+    return sp.csc_matrix((sim.matrix_values(), sam.rowidx, sam.colptr), shape=(n, n))
+
+
+def test_complement_pairs_of_the_kronecker_step(gpulib):
+    """Complement pairs along flexible CG with the Kronecker preconditioner:
+    the first pair (x = 0, r0 = b/|b|, z0 = M r0) has the input
+    R (r0 - A z0) / |R (r0 - A z0)| and the target
+    Rn (x*/|b| - z0) / |R (r0 - A z0)|."""
     sim, patches = poisson_model(nel=8)
     m = 3
     sim.learn_setup(coarse_cells=m, hidden=16, capacity=64, seed=1, field_inputs=0)
     x_ref, _ = sim.solveSystem(method=G.PCG_FP64, rtol=1e-12, max_inner=20000)
-    sim.learn_collect(xstar=x_ref, stride=4, rtol=1e-6)
-    Xe, Ye = sim.learn_pairs()
+    sim.learn_collect(xstar=x_ref, stride=4, rtol=1e-6, precond=G.PRECOND_KRONECKER)
     sim.learn_set_target(G.LEARN_TARGET_COMPLEMENT)
     assert sim.learn_info()["pairs"] == 0          # changing the mode forgets the pairs
-    sim.learn_collect(xstar=x_ref, stride=4, rtol=1e-6)
+    sim.learn_collect(xstar=x_ref, stride=4, rtol=1e-6, precond=G.PRECOND_KRONECKER)
     Xc, Yc = sim.learn_pairs()
-    assert np.array_equal(Xc[0], Xe[0])
     sam = sim.getSAM()
     pc = patches[0]
     R = mlp.restriction(pc.knots, pc.degree, pc.ncoef, sam.meqn, sam.madof, 1, m)
     Rn = R / np.maximum(R.sum(1, keepdims=True), 1e-300)
+    A = csc_matrix(sim)
     b = sim.rhs()
     r0 = b / np.linalg.norm(b)
     z0 = sim.apply_preconditioner(r0, G.PRECOND_KRONECKER)
-    nrm = np.linalg.norm(R @ r0)
-    want = Ye[0] - (Rn @ z0) / nrm
-    assert np.abs(Yc[0] - want).max() <= 1e-4 * np.abs(Ye[0]).max()
+    rc1 = R @ (r0 - A @ z0)
+    nrm = np.linalg.norm(rc1)
+    assert np.abs(Xc[0] - rc1 / nrm).max() <= 1e-4
+    want = Rn @ (x_ref / np.linalg.norm(b) - z0) / nrm
+    assert np.abs(Yc[0] - want).max() <= 1e-3 * np.abs(want).max()
     with pytest.raises(G.IfemGpuError):
         sim.learn_set_target(7)
+
+
+@pytest.mark.parametrize("kind", ["poisson", "elasticity"])
+def test_galerkin_coarse_matrix(gpulib, kind):
+    """The learned step's Galerkin coarse matrix R A R^T against numpy's
+    product of the FP64 matrix with the oracle's restriction (FP32 sums:
+    1e-5 of the largest entry)."""
+    if kind == "poisson":
+        sim, patches = poisson_model(nel=8)
+        npv = 1
+    else:
+        patches, ng = W.config2(nel=8)
+        sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
+        W.load_into(sim, patches)
+        sim.preprocess()
+        sim.assembleSystem()
+        npv = 3
+    m = 2
+    sim.learn_setup(coarse_cells=m, hidden=16, capacity=8, seed=1, field_inputs=0)
+    Ac = sim.learn_coarse_matrix()
+    sam = sim.getSAM()
+    pc = patches[0]
+    R = mlp.restriction(pc.knots, pc.degree, pc.ncoef, sam.meqn, sam.madof, npv, m)
+    ref = (R @ (csc_matrix(sim) @ R.T))
+    assert Ac.shape == ref.shape
+    assert np.abs(Ac - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+def test_untrained_network_costs_no_convergence(gpulib):
+    """The energy-optimal coefficient: a network with its initial random
+    weights still reaches the FP64 residual with about the Kronecker
+    iteration count (the step along a useless direction is near zero)."""
+    sim, _ = poisson_model(nel=16)
+    sim.learn_setup(coarse_cells=4, hidden=64, capacity=8, seed=3, field_inputs=1)
+    theta, scale = sim.learn_get_weights()
+    sim.learn_set_weights(theta, scale)                # marks the network usable
+    xk, ik = sim.solveSystem(method=G.PCG_MIXED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    xl, il = sim.solveSystem(method=G.FCG_LEARNED, rtol=1e-10, precond=G.PRECOND_KRONECKER)
+    print(f"\nKronecker FCG {ik.inner_iters} its, with an untrained network {il.inner_iters} its")
+    assert il.relres <= 1e-10 and il.fallbacks == 0
+    assert il.inner_iters <= 1.25 * ik.inner_iters + 4
+    assert np.abs(xl - xk).max() <= 1e-8 * np.abs(xk).max()
+
+
+def test_learned_rejects_coarse_cells_narrower_than_coupling(gpulib):
+    sim, _ = poisson_model(nel=8)
+    sim.learn_setup(coarse_cells=4, hidden=16, capacity=8, seed=1, field_inputs=0)
+    theta, scale = sim.learn_get_weights()
+    sim.learn_set_weights(theta, scale)
+    x = np.zeros(sim.sizes.neq)
+    info = G.SolveInfo()
+    o = G.SolverOptions(G.FCG_LEARNED, 1e-10, 20, 1000, 1e-4, G.PRECOND_KRONECKER)
+    assert sim.lib.ifemgpu_solve(sim.ctx, G.C.byref(o), G._ptr(x), G.C.byref(info)) == G.UNSUPPORTED
