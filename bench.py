@@ -647,9 +647,9 @@ def main():
     ap.add_argument("--solve-reps", type=int, default=3)
     ap.add_argument("--ref-solve", type=int, default=1,
                     help="1: FP64 reference solutions and CPU solve baselines by the oracle")
-    ap.add_argument("--train-seeds", type=int, default=600)
+    ap.add_argument("--train-seeds", type=int, default=200)
     ap.add_argument("--coarse-cells", type=int, default=8)
-    ap.add_argument("--elast-seeds", type=int, default=300,
+    ap.add_argument("--elast-seeds", type=int, default=60,
                     help="seeded loads for the learned elasticity leg (0: skip it)")
     args = ap.parse_args()
     if args.impl == "reference":
