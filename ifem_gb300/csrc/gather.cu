@@ -47,11 +47,15 @@ struct GCfg {
   static constexpr int W = 2 * P + 1;
   static constexpr int NS = W * W * W;           // neighbour slots of a node
   static constexpr int KL = NPV * NPV;
-  static constexpr int WARPS = (P == 3 && NPV == 3) ? 4 : 8;
+  // warps per CTA, elements whose loads are issued together, CTAs per SM:
+  // measured on 64^3 (32^3 for p = 3 elasticity) models; more elements in
+  // flight only add registers (p = 2 elasticity spilled with three) where
+  // the warps of an SM already keep enough loads in flight
+  static constexpr int WARPS = (P == 3 && NPV == 3) ? 4 : (P == 3 ? 6 : 8);
   static constexpr int NB = (NEN + 31) / 32;           // element functions per lane
-  static constexpr int U = NPV == 3 ? 3 : (P == 3 ? 4 : 6);  // elements in flight per warp
+  static constexpr int U = NPV == 3 ? (P == 2 ? 1 : 3) : (P == 3 ? 1 : 6);
   static constexpr size_t SMEM = sizeof(float) * 2 * KL * NS * WARPS;
-  static constexpr int MINB = (P == 3 && NPV == 3) ? 2 : (NPV == 3 ? 3 : 4);  // CTAs per SM
+  static constexpr int MINB = (P == 3 && NPV == 3) ? 2 : (NPV == 3 ? 3 : (P == 3 ? 5 : 4));
 };
 
 // hi + lo += x (TwoSum: the rounding error of hi + x goes to lo)
