@@ -384,7 +384,10 @@ g_spmvOff(const int* __restrict__ colptr, const int* __restrict__ rowPat,
     const int so = kPat ? patStart[rowPat[row]] - b : 0;  // offset of entry k: off[k + so]
     float acc = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
     int k = b + lane;
-    // values stream (no L1 allocation: the offsets and p stay in L1)
+    // values stream (no L1 allocation: the offsets and p stay in L1); two
+    // rounds unrolled so that their loads are issued together (-4% per
+    // product on the 64^3 p=3 Poisson system)
+#pragma unroll 2
     for (; k + 96 < e; k += 128) {
       const int o0 = off[k + so], o1 = off[k + so + 32], o2 = off[k + so + 64], o3 = off[k + so + 96];
       const float a0 = __ldcs(A + k), a1 = __ldcs(A + k + 32), a2 = __ldcs(A + k + 64),
