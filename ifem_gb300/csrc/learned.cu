@@ -7,15 +7,19 @@
 //   restriction   rc_(v,c) = sum_e w_ve r_e     over the free equations e of
 //                                               component c; w_ve is the
 //                                               trilinear weight of vertex v
-//                                               at e's Greville point
-//   network       y = MLP([rc / |rc|, g])       3 layers, width nh, ReLU
-//   prolongation  z_e += S |rc| sum_v w_ve y_(v,c(e))
+//                                               at e's Greville point (R)
+//   network       y = MLP([rc / |rc|, g])       3 layers, width nh, ReLU;
+//                                               BF16 tcgen05 inference with
+//                                               FP32 accumulation
+//   two-level step  after the fine step z1 and t = A z1, rc = R (r - t):
+//                 z = z1 + alpha R^T y, alpha = (y, rc) / (y, Ac y) with the
+//                 Galerkin coarse matrix Ac = R A R^T of the assembly
 // g (optional) is the patch's log-conductivity field restricted to the
 // coarse vertices, so that one network can serve many coefficient fields.
-// The network is trained by the kernels of this file on pairs
+// The network is trained by the FP32 kernels of this file on pairs
 // ([rc/|rc|, g], ec/|rc|), ec the weight-normalised restriction of the error
-// x* - x_k of plain PCG iterates; S, the RMS of the targets, keeps the
-// network's outputs of order one.
+// of the method's own iterates (learnRecord); S, the RMS of the targets,
+// keeps the network's outputs of order one.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -26,6 +30,7 @@
 
 #include "ifemgpu_internal.h"
 #include "reduce.cuh"
+#include "tc_common.cuh"
 
 namespace ifemgpu {
 
@@ -50,12 +55,19 @@ struct LearnState {
   int* vEq = nullptr;
   float* vW = nullptr;        // trilinear weights
   float* vWn = nullptr;       // weights divided by their sum per coarse unknown
-  // network: FP32 master weights, BF16 copy for the solve
+  // network: FP32 master weights; for the solve a BF16 copy packed in
+  // 128 x 64 tensor-core operand tiles per layer (layer l: Mt[l] row tiles x
+  // nKT[l] K tiles at element offset pOff[l]), per-tile partial sums and the
+  // tickets of the row tiles' last CTAs
   float* theta = nullptr;
   float* grad = nullptr;
   float* am = nullptr;
   float* av = nullptr;
-  __nv_bfloat16* wbf = nullptr;
+  __nv_bfloat16* wtc = nullptr;
+  size_t pOff[3] = {0, 0, 0};
+  int Mt[3] = {0, 0, 0}, nKT[3] = {0, 0, 0};
+  float* tpart = nullptr;
+  unsigned* tick = nullptr;
   int adamStep = 0;
   float scale = 1.f;          // S
   bool trained = false;
@@ -376,44 +388,145 @@ k_prolong_add(const int* __restrict__ eqCell, const float4* __restrict__ eqFrac,
 
 // ---- network kernels -----------------------------------------------------------
 
-// y = act(W [x / |x|, x2] + b) with |x| taken when normOut != 0 (first
-// layer; block 0 stores it), else y = act(W [x, x2] + b); W rows hold
-// cols + cols2 weights.  Warp per output row, BF16 weights, FP32 sums.
-__global__ void __launch_bounds__(kT)
-k_gemv_bf16(const __nv_bfloat16* __restrict__ W, const float* __restrict__ b,
-            const float* __restrict__ x, int cols, const float* __restrict__ x2, int cols2,
-            float* __restrict__ y, int rows, int relu, float* normOut, const double* guard)
+// ---- tensor-core inference ----------------------------------------------------
+// One network layer y = act(W [x / |x|, x2] + b) on tcgen05 (kind::f16: BF16
+// operands, FP32 accumulation in tensor memory).  W is packed in BF16 as
+// 128 x 64 operand tiles (K-major core matrices, no swizzle), row tile major;
+// the input vector is the MMA's B operand with N = 16 (row 0, zero rows
+// 1..15): one right-hand side per solve iteration.  CTA (m, t) multiplies row
+// tile m by K tile t (one bulk copy of 16 KB, four MMAs of K = 16) and stores
+// its 128 partial sums; the last CTA of row tile m sums the partials of all K
+// tiles in tile order, adds the bias and applies the activation.
+constexpr int kTileRows = 128, kTileK = 64;
+constexpr int kTileElems = kTileRows * kTileK;
+
+struct InferSmem {
+  __nv_bfloat16 A[kTileElems];   // one packed W tile (16 KB)
+  __nv_bfloat16 B[16 * kTileK];  // the input slice as row 0 of 16
+  unsigned long long mbarA, mbarD;
+  uint32_t tmemSlot;
+  int ok, last;
+  float red[4];
+};
+
+// element offset of (row r, k) inside a packed tile (r < 128, k < 64)
+__device__ __forceinline__ int tileOff(int r, int k)
 {
-  if (stopped(guard)) return;
-  __shared__ float sh[32];
-  float inv = 1.f;
-  if (normOut) {
-    float s = 0.f;
-    for (int i = threadIdx.x; i < cols; i += blockDim.x) s += x[i] * x[i];
-    const float nx = sqrtf(blockSumF(s, sh));
-    if (blockIdx.x == 0 && threadIdx.x == 0) normOut[0] = nx;
-    inv = nx > 0.f ? 1.f / nx : 0.f;
-  }
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= rows) return;
-  const __nv_bfloat16* w = W + (size_t)warp * (cols + cols2);
-  float s = 0.f, s2 = 0.f;
-  for (int k = lane; k < cols; k += 32) s = fmaf(__bfloat162float(w[k]), x[k], s);
-  for (int k = lane; k < cols2; k += 32) s2 = fmaf(__bfloat162float(w[cols + k]), x2[k], s2);
-  for (int o = 16; o > 0; o >>= 1) {
-    s += __shfl_down_sync(0xffffffffu, s, o);
-    s2 += __shfl_down_sync(0xffffffffu, s2, o);
-  }
-  if (lane == 0) {
-    const float v = s * inv + s2 + b[warp];
-    y[warp] = relu ? fmaxf(v, 0.f) : v;
+  return (r >> 3) * 512 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+// W (rows x cols, FP32 row-major) -> packed BF16 tiles (zero padding)
+__global__ void k_pack_bf16(const float* __restrict__ W, int rows, int cols, int nKT,
+                            __nv_bfloat16* __restrict__ out, size_t total)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t tile = i / kTileElems;
+    const int e = (int)(i - tile * kTileElems);
+    const int mt = (int)(tile / nKT), kt = (int)(tile - (size_t)mt * nKT);
+    const int rem = e & 511, rem2 = rem & 63;
+    const int r = ((e >> 9) << 3) | (rem2 >> 3), k = ((rem >> 6) << 3) | (rem2 & 7);
+    const int row = mt * kTileRows + r, col = kt * kTileK + k;
+    out[i] = __float2bfloat16(row < rows && col < cols ? W[(size_t)row * cols + col] : 0.f);
   }
 }
 
-__global__ void k_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, int n)
+__global__ void __launch_bounds__(128)
+k_mlp_tc(const __nv_bfloat16* __restrict__ Wp, int nKT, const float* __restrict__ bias,
+         const float* __restrict__ x, int cols1, const float* __restrict__ x2, int cols2,
+         int normFirst, float* __restrict__ part, unsigned* __restrict__ tick,
+         float* __restrict__ y, int rows, int relu, float* normOut, unsigned spin,
+         const double* guard)
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = __float2bfloat16(a[i]);
+  if (stopped(guard)) return;
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  InferSmem& sm = *reinterpret_cast<InferSmem*>(smraw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x, kt = blockIdx.y;
+  const uint32_t mbarA = smemAddr(&sm.mbarA), mbarD = smemAddr(&sm.mbarD);
+  if (tid == 0) {
+    mbarInit(mbarA, 1);
+    mbarInit(mbarD, 1);
+  }
+  if (warp == 0) tmemAlloc(&sm.tmemSlot, 32);
+  float inv = 1.f;
+  if (normFirst) {  // |x| over the first cols1 inputs
+    float q = 0.f;
+    for (int i = tid; i < cols1; i += blockDim.x) q += x[i] * x[i];
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if (lane == 0) sm.red[warp] = q;
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = sm.tmemSlot;
+  if (normFirst) {
+    const float nx = sqrtf((sm.red[0] + sm.red[1]) + (sm.red[2] + sm.red[3]));
+    inv = nx > 0.f ? 1.f / nx : 0.f;
+    if (mt == 0 && kt == 0 && tid == 0 && normOut) *normOut = nx;
+  }
+  if (tid == 0) {
+    mbarExpectTx(mbarA, kTileElems * 2);
+    bulkLoad(smemAddr(sm.A), Wp + ((size_t)mt * nKT + kt) * kTileElems, kTileElems * 2, mbarA);
+  }
+  // the input slice in BF16 as row 0 of the B operand
+  for (int e = tid; e < 16 * kTileK; e += blockDim.x) {
+    const int rem = e & 511, rem2 = rem & 63;
+    const int n = ((e >> 9) << 3) | (rem2 >> 3), k = ((rem >> 6) << 3) | (rem2 & 7);
+    float v = 0.f;
+    if (n == 0) {
+      const int col = kt * kTileK + k;
+      v = col < cols1 ? x[col] * inv : (col < cols1 + cols2 ? x2[col - cols1] : 0.f);
+    }
+    sm.B[e] = __float2bfloat16(v);
+  }
+  fenceProxyAsync();
+  __syncthreads();
+  if (tid == 0) {
+    int ok = mbarWait(mbarA, 0, spin) ? 1 : 0;
+    if (ok) {
+      tcFenceAfter();
+      const uint32_t idesc = instrDescBF16(kTileRows, 16);
+      const uint32_t a0 = smemAddr(sm.A), b0 = smemAddr(sm.B);
+#pragma unroll
+      for (int s = 0; s < kTileK / 16; s++)  // K = 16 BF16 = 32 bytes: two core matrices
+        mmaBF16(tmem, smemDesc(a0 + s * 256), smemDesc(b0 + s * 256), idesc, s > 0 ? 1u : 0u);
+      mmaCommit(mbarD);
+      ok = mbarWait(mbarD, 0, spin) ? 2 : 0;
+    }
+    sm.ok = ok;
+  }
+  __syncthreads();
+  tcFenceAfter();
+  float v[16];
+  if (sm.ok == 2) {
+    tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16), v);
+  } else {
+    v[0] = __int_as_float(0x7FC00000);  // a wait gave up: NaN ends the solve's learned step
+  }
+  const int row = mt * kTileRows + warp * 32 + lane;
+  if (row < rows) part[(size_t)kt * rows + row] = v[0];
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) sm.last = atomicAdd(tick + mt, 1u) == gridDim.y - 1;
+  __syncthreads();
+  if (sm.last) {
+    __threadfence();
+    if (row < rows) {
+      float acc = 0.f;
+      for (int t = 0; t < (int)gridDim.y; t++) acc += __ldcg(part + (size_t)t * rows + row);
+      acc += bias[row];
+      y[row] = relu ? fmaxf(acc, 0.f) : acc;
+    }
+    if (tid == 0) tick[mt] = 0u;
+  }
+  // a copy still in flight after a give-up lands before the CTA exits
+  if (tid == 0 && sm.ok == 0) mbarWait(mbarA, 0, spin);
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (warp == 0) tmemDealloc(tmem, 32);
 }
 
 // C (M x N) = op(A) op(B) (+ C when accumulate); row-major; op transposes
@@ -568,7 +681,7 @@ void sgemm(cudaStream_t s, const float* A, const float* B, float* C, int M, int 
 void freeLearn(LearnState* L)
 {
   void* ptrs[] = {L->eqCell, L->eqFrac, L->vPtr, L->vEq, L->vW, L->vWn, L->theta, L->grad,
-                  L->am, L->av, L->wbf, L->X, L->Y, L->xstar, L->Xb, L->Yb, L->H1, L->H2,
+                  L->am, L->av, L->wtc, L->tpart, L->tick, L->X, L->Y, L->xstar, L->Xb, L->Yb, L->H1, L->H2,
                   L->Yp, L->dH1, L->dH2, L->dY, L->loss, L->perm, L->rc, L->h1, L->h2,
                   L->yc, L->nrm, L->feat, L->t, L->rc1, L->Bm, L->Ac};
   for (void* p : ptrs)
@@ -603,6 +716,18 @@ void batchPass(cudaStream_t s, LearnState* L, int Bn, float invS, bool grad)
   k_relu_back<<<256, kT, 0, s>>>(L->dH1, L->H1, (size_t)Bn * nh);
   sgemm(s, L->dH1, L->Xb, g + L->oW1, nh, nin, Bn, nh, nin, nin, 1, 0, 0);
   k_colsum<<<(nh + kT - 1) / kT, kT, 0, s>>>(L->dH1, g + L->ob1, Bn, nh);
+}
+
+// the BF16 operand tiles of the three layers from the FP32 master weights
+void packWeights(cudaStream_t s, LearnState* L)
+{
+  const int rows[3] = {L->nh, L->nh, L->nc}, cols[3] = {L->nin, L->nh, L->nh};
+  const int off[3] = {L->oW1, L->oW2, L->oW3};
+  for (int l = 0; l < 3; l++) {
+    const size_t total = (size_t)L->Mt[l] * L->nKT[l] * kTileElems;
+    k_pack_bf16<<<512, kT, 0, s>>>(L->theta + off[l], rows[l], cols[l], L->nKT[l],
+                                   L->wtc + L->pOff[l], total);
+  }
 }
 
 ifemgpu_status readLoss(ifemgpu_ctx* ctx, LearnState* L, double denom, double* out)
@@ -787,7 +912,25 @@ ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigne
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->av, sizeof(float) * L->nparam));
   IFEMGPU_CUDA(ctx, cudaMemset(L->am, 0, sizeof(float) * L->nparam));
   IFEMGPU_CUDA(ctx, cudaMemset(L->av, 0, sizeof(float) * L->nparam));
-  IFEMGPU_CUDA(ctx, cudaMalloc(&L->wbf, sizeof(__nv_bfloat16) * L->nparam));
+  {
+    const int rows[3] = {nh, nh, nc}, cols[3] = {nin, nh, nh};
+    size_t at = 0;
+    int parts = 0, tiles = 0;
+    for (int l = 0; l < 3; l++) {
+      L->Mt[l] = (rows[l] + kTileRows - 1) / kTileRows;
+      L->nKT[l] = (cols[l] + kTileK - 1) / kTileK;
+      L->pOff[l] = at;
+      at += (size_t)L->Mt[l] * L->nKT[l] * kTileElems;
+      parts = std::max(parts, L->nKT[l] * rows[l]);
+      tiles = std::max(tiles, L->Mt[l]);
+    }
+    IFEMGPU_CUDA(ctx, cudaMalloc(&L->wtc, sizeof(__nv_bfloat16) * at));
+    IFEMGPU_CUDA(ctx, cudaMalloc(&L->tpart, sizeof(float) * parts));
+    IFEMGPU_CUDA(ctx, cudaMalloc(&L->tick, sizeof(unsigned) * tiles));
+    IFEMGPU_CUDA(ctx, cudaMemset(L->tick, 0, sizeof(unsigned) * tiles));
+    IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(InferSmem) + 1024));
+  }
   L->cap = capacity;
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->X, sizeof(float) * (size_t)capacity * nin));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->Y, sizeof(float) * (size_t)capacity * nc));
@@ -891,6 +1034,26 @@ ifemgpu_status learnGalerkin(ifemgpu_ctx* ctx)
   return IFEMGPU_OK;
 }
 
+// the network's three layers on the tensor cores: L->rc (and the field
+// features) -> L->yc
+void inferTC(ifemgpu_ctx* ctx, const double* guard)
+{
+  LearnState* L = ctx->learn;
+  cudaStream_t s = ctx->stream;
+  const int nc = L->nc, nh = L->nh;
+  const unsigned spin = ctx->dbg.mbarSpin ? ctx->dbg.mbarSpin : tc::kSpinLimit;
+  const size_t sm = sizeof(InferSmem);
+  k_mlp_tc<<<dim3(L->Mt[0], L->nKT[0]), 128, sm, s>>>(
+      L->wtc + L->pOff[0], L->nKT[0], L->theta + L->ob1, L->rc, nc, L->feat, L->nf, 1, L->tpart,
+      L->tick, L->h1, nh, 1, L->nrm, spin, guard);
+  k_mlp_tc<<<dim3(L->Mt[1], L->nKT[1]), 128, sm, s>>>(
+      L->wtc + L->pOff[1], L->nKT[1], L->theta + L->ob2, L->h1, nh, nullptr, 0, 0, L->tpart,
+      L->tick, L->h2, nh, 1, nullptr, spin, guard);
+  k_mlp_tc<<<dim3(L->Mt[2], L->nKT[2]), 128, sm, s>>>(
+      L->wtc + L->pOff[2], L->nKT[2], L->theta + L->ob3, L->h2, nh, nullptr, 0, 0, L->tpart,
+      L->tick, L->yc, nc, 0, nullptr, spin, guard);
+}
+
 // z = z1 + alpha R^T y: y the BF16 network's coarse direction for the input
 // R r (target ERROR) or R (r - t) (target COMPLEMENT), t = A z1 computed by
 // the caller, alpha = (y, R (r - t)) / (y, Ac y) the coefficient that
@@ -910,13 +1073,7 @@ ifemgpu_status learnApply(ifemgpu_ctx* ctx, const float* r, float* z, const floa
   const int comp = L->target == IFEMGPU_LEARN_TARGET_COMPLEMENT ? 1 : 0;
   k_restrict2<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->vPtr, L->vEq, L->vW, r, t, comp, L->rc,
                                                      L->rc1, nc, guard);
-  k_gemv_bf16<<<(nh * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW1, L->theta + L->ob1, L->rc,
-                                                      nc, L->feat, L->nf, L->h1, nh, 1, L->nrm,
-                                                      guard);
-  k_gemv_bf16<<<(nh * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW2, L->theta + L->ob2, L->h1,
-                                                      nh, nullptr, 0, L->h2, nh, 1, nullptr, guard);
-  k_gemv_bf16<<<(nc * 32 + kT - 1) / kT, kT, 0, s>>>(L->wbf + L->oW3, L->theta + L->ob3, L->h2,
-                                                      nh, nullptr, 0, L->yc, nc, 0, nullptr, guard);
+  inferTC(ctx, guard);
   const int ab = std::min(nparts, (nc + 7) / 8);
   k_coarse_alpha<<<ab, kT, 0, s>>>(L->Ac, L->yc, L->rc1, L->m, L->npv, nc, part, counter2,
                                    L->nrm + 2, guard);
@@ -968,7 +1125,8 @@ ifemgpu_status learnTrain(ifemgpu_ctx* ctx, int epochs, int B, float lr, unsigne
     IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
   }
   IFEMGPU_CUDA(ctx, cudaGetLastError());
-  k_to_bf16<<<512, kT, 0, s>>>(L->theta, L->wbf, L->nparam);
+  packWeights(s, L);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(s));
   L->trained = true;
   if (lossOut) *lossOut = (float)lastLoss;
@@ -1037,7 +1195,8 @@ ifemgpu_status learnWeights(ifemgpu_ctx* ctx, float* theta, int* count, float* s
     IFEMGPU_CUDA(ctx, cudaMemcpy(L->theta, theta, sizeof(float) * L->nparam, cudaMemcpyHostToDevice));
     if (scale) L->scale = *scale;
     IFEMGPU_CUDA(ctx, cudaMemcpy(L->nrm + 1, &L->scale, sizeof(float), cudaMemcpyHostToDevice));
-    k_to_bf16<<<512, kT, 0, ctx->stream>>>(L->theta, L->wbf, L->nparam);
+    packWeights(ctx->stream, L);
+    IFEMGPU_CUDA(ctx, cudaGetLastError());
     IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     L->trained = true;
   } else {
@@ -1066,6 +1225,25 @@ void learnClear(ifemgpu_ctx* ctx)
 }
 
 }  // namespace ifemgpu
+
+extern "C" ifemgpu_status ifemgpu_learn_forward(ifemgpu_ctx* ctx, const float* rc, float* y)
+{
+  using namespace ifemgpu;
+  if (!ctx || !rc || !y) return IFEMGPU_INVALID_ARG;
+  if (!ctx->learn || !ctx->learn->trained)
+    return setError(ctx, IFEMGPU_NOT_READY, "learn_forward without a trained network");
+  IFEMGPU_CUDA(ctx, cudaSetDevice(ctx->opts.device));
+  IFEMGPU_TRY(learnPrepare(ctx));
+  LearnState* L = ctx->learn;
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(L->rc, rc, sizeof(float) * L->nc, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+  inferTC(ctx, nullptr);
+  IFEMGPU_CUDA(ctx, cudaGetLastError());
+  IFEMGPU_CUDA(ctx, cudaMemcpyAsync(y, L->yc, sizeof(float) * L->nc, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return IFEMGPU_OK;
+}
 
 extern "C" ifemgpu_status ifemgpu_learn_coarse_matrix(ifemgpu_ctx* ctx, float* Ac)
 {

@@ -1,12 +1,13 @@
 // tc_common.cuh -- inline-PTX building blocks for the sm_103a tensor-core
-// path: tcgen05 MMA (kind::tf32, cta_group::1), tensor-memory allocation and
-// loads, mbarrier waits with an iteration bound, and the shared-memory
-// operand layout.
+// path: tcgen05 MMA (kind::tf32, and kind::f16 with BF16 operands;
+// cta_group::1), tensor-memory allocation and loads, mbarrier waits with an
+// iteration bound, bulk copies, and the shared-memory operand layout.
 //
-// Operand layout ("K-major, no swizzle"): a tile of R rows x 32 K-elements
-// (FP32/TF32) is stored as 8x4 core matrices of 128 bytes; the core matrices
-// of one 8-row group are adjacent along K (leading byte offset 128 B) and the
-// 8-row groups follow each other every 1024 B (stride byte offset).
+// Operand layout ("K-major, no swizzle"): a tile of R rows x 128 bytes of K
+// (32 FP32/TF32 or 64 BF16 elements) is stored as core matrices of 8 rows x
+// 16 bytes; the core matrices of one 8-row group are adjacent along K
+// (leading byte offset 128 B) and the 8-row groups follow each other every
+// 1024 B (stride byte offset).
 #pragma once
 
 #include <cstdint>
@@ -54,6 +55,26 @@ __device__ __forceinline__ void mmaTF32(uint32_t tmemD, uint64_t adesc, uint64_t
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+      :
+      : "r"(tmemD), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// instruction descriptor, kind::f16 with BF16 A and B (format 1 at bits 7-9
+// and 10-12), D f32, both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t instrDescBF16(int M, int N)
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mmaBF16(uint32_t tmemD, uint64_t adesc, uint64_t bdesc,
+                                        uint32_t idesc, uint32_t accumulate)
+{
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
       :
       : "r"(tmemD), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
@@ -110,6 +131,16 @@ __device__ __forceinline__ void tmaLoad4d(uint32_t dst, const void* tmap, int c0
       "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3, %4, %5}], [%6];"
       : : "r"(dst), "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(mbar) : "memory");
+}
+
+// untiled bulk copy global -> shared of `bytes` (both addresses 16-byte
+// aligned, bytes a multiple of 16), completing on an mbarrier
+__device__ __forceinline__ void bulkLoad(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t mbar)
+{
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      : : "r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
 }
 
 // tensor maps written to global memory by copies before the launch: order

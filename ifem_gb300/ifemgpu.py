@@ -77,7 +77,7 @@ EXPORTS = [
     "ifemgpu_selftest_tc_gemm", "ifemgpu_solve_noalloc", "ifemgpu_learn_setup",
     "ifemgpu_learn_collect", "ifemgpu_learn_clear", "ifemgpu_learn_set_target", "ifemgpu_learn_train",
     "ifemgpu_learn_evaluate", "ifemgpu_learn_gradients", "ifemgpu_learn_info",
-    "ifemgpu_learn_coarse_matrix",
+    "ifemgpu_learn_coarse_matrix", "ifemgpu_learn_forward",
     "ifemgpu_learn_get_weights", "ifemgpu_learn_set_weights", "ifemgpu_patch_update_field",
     "ifemgpu_learn_get_pairs", "ifemgpu_apply_preconditioner", "ifemgpu_copy_matrix_bsr",
     "ifemgpu_graph_capture", "ifemgpu_graph_launch", "ifemgpu_debug_waits",
@@ -157,6 +157,7 @@ def load_library(path: str | None = None):
         "ifemgpu_learn_get_weights": (I, [P, V, C.POINTER(I), C.POINTER(C.c_float)]),
         "ifemgpu_learn_set_weights": (I, [P, V, I, C.c_float]),
         "ifemgpu_learn_coarse_matrix": (I, [P, V]),
+        "ifemgpu_learn_forward": (I, [P, V, V]),
         "ifemgpu_patch_update_field": (I, [P, I, I, V]),
     }
     for name, (res, args) in sig.items():
@@ -501,6 +502,14 @@ class SIM:
         Ac = np.zeros((nc, nc), dtype=np.float32)
         self._check(self.lib.ifemgpu_learn_coarse_matrix(self.ctx, _ptr(Ac)))
         return Ac
+
+    def learn_forward(self, rc: np.ndarray) -> np.ndarray:
+        """The network's output for a coarse input through the solve's
+        tensor-core inference path."""
+        rc = np.ascontiguousarray(rc, dtype=np.float32)
+        y = np.zeros(self.learn_info()["coarse_unknowns"], dtype=np.float32)
+        self._check(self.lib.ifemgpu_learn_forward(self.ctx, _ptr(rc), _ptr(y)))
+        return y
 
     def learn_clear(self):
         self._check(self.lib.ifemgpu_learn_clear(self.ctx))

@@ -507,6 +507,13 @@ ifemgpu_status ifemgpu_learn_gradients(ifemgpu_ctx* ctx, const float* X,
                                        const float* Y, int n, float* grad,
                                        float* loss);
 
+/* The trained network's output y (coarse_unknowns floats) for a coarse
+ * input rc (coarse_unknowns floats, normalised inside as in the solve; the
+ * field features of the current field appended) through the solve's
+ * inference path: BF16 tcgen05 products with FP32 accumulation, weights and
+ * inputs of each layer rounded to BF16.  Diagnostic; no IFEM counterpart. */
+ifemgpu_status ifemgpu_learn_forward(ifemgpu_ctx* ctx, const float* rc, float* y);
+
 /* The Galerkin coarse matrix Ac = R A R^T of the assembled system as a
  * dense row-major nc x nc FP32 array (nc = coarse_unknowns): the matrix
  * the learned step prices its direction with, formed on the device from

@@ -293,3 +293,38 @@ def test_learned_rejects_coarse_cells_narrower_than_coupling(gpulib):
     info = G.SolveInfo()
     o = G.SolverOptions(G.FCG_LEARNED, 1e-10, 20, 1000, 1e-4, G.PRECOND_KRONECKER)
     assert sim.lib.ifemgpu_solve(sim.ctx, G.C.byref(o), G._ptr(x), G.C.byref(info)) == G.UNSUPPORTED
+
+
+def bf16(a):
+    """Round to BF16 (nearest even), returned as float64."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("hidden", [160, 256])
+def test_tensor_core_inference_matches_bf16_reference(gpulib, hidden):
+    """The solve's inference path (BF16 tcgen05 products, FP32 accumulation in
+    tensor memory, weights and each layer's inputs in BF16) against an FP64
+    evaluation of the same rounded operands: 2e-3 of the largest output (FP32
+    sums of up to a few hundred products).  hidden = 160 pads the row and K
+    tiles; several K tiles are summed by the last CTA of a row tile."""
+    sim, _ = poisson_model(nel=8)
+    info = sim.learn_setup(coarse_cells=2, hidden=hidden, capacity=4, seed=4, field_inputs=1)
+    nc, nin, nh = info["coarse_unknowns"], info["inputs"], info["hidden"]
+    theta, scale = sim.learn_get_weights()
+    rng = np.random.default_rng(17)
+    theta = theta + 0.05 * rng.standard_normal(theta.size).astype(np.float32)
+    sim.learn_set_weights(theta, scale)
+    sim.learn_collect(stride=1, rtol=1e-2)
+    X, _ = sim.learn_pairs(0, 1)
+    feat = X[0, nc:].astype(np.float64)
+    rc = rng.standard_normal(nc).astype(np.float32)
+    y = sim.learn_forward(rc)
+    W1, b1, W2, b2, W3, b3 = mlp.unpack(theta, nin, nh, nc)
+    x0 = np.concatenate([rc.astype(np.float64) / np.linalg.norm(rc.astype(np.float64)), feat])
+    h1 = np.maximum(bf16(W1) @ bf16(x0) + b1, 0.0)
+    h2 = np.maximum(bf16(W2) @ bf16(h1) + b2, 0.0)
+    ref = bf16(W3) @ bf16(h2) + b3
+    assert np.isfinite(y).all()
+    assert np.abs(y - ref).max() <= 2e-3 * np.abs(ref).max()
