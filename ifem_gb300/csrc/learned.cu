@@ -16,7 +16,8 @@
 //                 Galerkin coarse matrix Ac = R A R^T of the assembly
 // g (optional) is the patch's log-conductivity field restricted to the
 // coarse vertices, so that one network can serve many coefficient fields.
-// The network is trained by the FP32 kernels of this file on pairs
+// The network is trained by the kernels of this file (3xTF32 tcgen05 GEMMs,
+// FP32 elsewhere) on pairs
 // ([rc/|rc|, g], ec/|rc|), ec the weight-normalised restriction of the error
 // of the method's own iterates (learnRecord); S, the RMS of the targets,
 // keeps the network's outputs of order one.
@@ -530,61 +531,115 @@ k_mlp_tc(const __nv_bfloat16* __restrict__ Wp, int nKT, const float* __restrict_
 }
 
 // C (M x N) = op(A) op(B) (+ C when accumulate); row-major; op transposes
-// when its flag is set (A is M x K or K x M, B is K x N or N x K).  64 x 64
-// tiles, 16 x 16 threads of 4 x 4 outputs, K in steps of 16 through shared
-// memory.
-__global__ void __launch_bounds__(256)
-k_sgemm(const float* __restrict__ A, const float* __restrict__ B, float* __restrict__ C, int M,
-        int N, int K, int lda, int ldb, int ldc, int transA, int transB, int accumulate)
+// when its flag is set (A is M x K or K x M, B is K x N or N x K).  On the
+// tensor cores in 3xTF32 (hi hi + hi lo + lo hi, FP32 accumulation in tensor
+// memory), so the training keeps FP32 accuracy: one CTA of 128 threads per
+// 128 x 128 tile of C, K in chunks of 32 staged by the threads (the loads
+// follow the operand's contiguous direction; split into TF32 hi/lo parts in
+// the K-major core-matrix layout), twelve MMAs per chunk, the accumulator
+// read back by the four warps (32 rows each).
+constexpr int kGT = 128;  // tile of C: rows and columns
+struct GemmSmem {
+  float Ahi[kGT * tc::kK], Alo[kGT * tc::kK], Bhi[kGT * tc::kK], Blo[kGT * tc::kK];
+  unsigned long long mbar;
+  uint32_t tmemSlot;
+  int ok;
+};
+
+__global__ void __launch_bounds__(128)
+k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __restrict__ C, int M,
+          int N, int K, int lda, int ldb, int ldc, int transA, int transB, int accumulate,
+          unsigned spin)
 {
-  __shared__ float As[16][64 + 4];
-  __shared__ float Bs[16][64 + 4];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
-  float acc[4][4] = {{0.f}};
-  for (int k0 = 0; k0 < K; k0 += 16) {
-    for (int i = threadIdx.x; i < 16 * 64; i += 256) {
-      int kk, mm;
-      if (transA) { kk = i / 64; mm = i % 64; }  // consecutive threads along m
-      else { mm = i / 16; kk = i % 16; }         // consecutive threads along k
-      const int gm = m0 + mm, gk = k0 + kk;
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  GemmSmem& sm = *reinterpret_cast<GemmSmem*>(smraw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  const uint32_t mbar = smemAddr(&sm.mbar);
+  if (tid == 0) {
+    mbarInit(mbar, 1);
+    sm.ok = 1;
+  }
+  if (warp == 0) tmemAlloc(&sm.tmemSlot, kGT);
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = sm.tmemSlot;
+  const uint32_t idesc = instrDescTF32(kGT, kGT);
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int k0 = 0; k0 < K && ok; k0 += kK) {
+    // op(A)[m0 + r][k0 + k] and op(B)[k0 + k][n0 + r] for r < 128, k < 32
+    for (int i = tid; i < kGT * kK; i += blockDim.x) {
+      int r, k;
+      if (transA) { k = i / kGT; r = i % kGT; }  // A stored K x M: consecutive threads along m
+      else { r = i / kK; k = i % kK; }          // A stored M x K: along k
+      const int gm = m0 + r, gk = k0 + k;
       float va = 0.f;
       if (gm < M && gk < K) va = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
-      As[kk][mm] = va;
-      int kb, nn;
-      if (transB) { nn = i / 16; kb = i % 16; }
-      else { kb = i / 64; nn = i % 64; }
-      const int gn = n0 + nn, gkb = k0 + kb;
+      float hi, lo;
+      splitTF32(va, hi, lo);
+      sm.Ahi[kmaj(r, k)] = hi;
+      sm.Alo[kmaj(r, k)] = lo;
+      if (transB) { r = i / kK; k = i % kK; }   // B stored N x K: along k
+      else { k = i / kGT; r = i % kGT; }        // B stored K x N: along n
+      const int gn = n0 + r, gkb = k0 + k;
       float vb = 0.f;
       if (gn < N && gkb < K) vb = transB ? B[(size_t)gn * ldb + gkb] : B[(size_t)gkb * ldb + gn];
-      Bs[kb][nn] = vb;
+      splitTF32(vb, hi, lo);
+      sm.Bhi[kmaj(r, k)] = hi;
+      sm.Blo[kmaj(r, k)] = lo;
     }
+    fenceProxyAsync();
     __syncthreads();
+    if (tid == 0) {
+      tcFenceAfter();
+      const uint32_t ah = smemAddr(sm.Ahi), al = smemAddr(sm.Alo);
+      const uint32_t bh = smemAddr(sm.Bhi), bl = smemAddr(sm.Blo);
 #pragma unroll
-    for (int kk = 0; kk < 16; kk++) {
-      float a[4], bv[4];
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        a[i] = As[kk][ty * 4 + i];
-        bv[i] = Bs[kk][tx * 4 + i];
+      for (int st = 0; st < kK / 8; st++) {
+        const uint32_t off = st * 256;
+        mmaTF32(tmem, smemDesc(ah + off), smemDesc(bh + off), idesc, (k0 > 0 || st > 0) ? 1u : 0u);
+        mmaTF32(tmem, smemDesc(ah + off), smemDesc(bl + off), idesc, 1u);
+        mmaTF32(tmem, smemDesc(al + off), smemDesc(bh + off), idesc, 1u);
       }
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], bv[j], acc[i][j]);
+      mmaCommit(mbar);
+      if (!mbarWait(mbar, phase, spin)) sm.ok = 0;
     }
-    __syncthreads();
+    phase ^= 1u;
+    __syncthreads();  // the operand tiles are free again (or the wait gave up)
+    ok = sm.ok != 0;
+    tcFenceAfter();
   }
+  const int gm = m0 + warp * 32 + lane;
+  if (K > 0 && ok) {
+    for (int c16 = 0; c16 < kGT / 16; c16++) {
+      float v[16];
+      tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
+      if (gm < M) {
 #pragma unroll
-  for (int i = 0; i < 4; i++)
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
-      if (gm < M && gn < N) {
-        float* c = C + (size_t)gm * ldc + gn;
-        *c = accumulate ? *c + acc[i][j] : acc[i][j];
+        for (int j = 0; j < 16; j++) {
+          const int gn = n0 + 16 * c16 + j;
+          if (gn < N) {
+            float* c = C + (size_t)gm * ldc + gn;
+            *c = accumulate ? *c + v[j] : v[j];
+          }
+        }
       }
     }
+  } else if (gm < M) {  // no products (K = 0), or a wait gave up (NaN marks it)
+    const float v = K > 0 ? __int_as_float(0x7FC00000) : 0.f;
+    for (int gn = n0; gn < min(N, n0 + kGT); gn++) {
+      float* c = C + (size_t)gm * ldc + gn;
+      *c = (accumulate && K == 0) ? *c : v;
+    }
+  }
+  if (!ok && tid == 0) mbarWait(mbar, phase ^ 1u, spin);  // the MMAs given up on finish first
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (warp == 0) tmemDealloc(tmem, kGT);
 }
 
 // H = act(H + b) row-wise
@@ -674,8 +729,9 @@ __global__ void k_sum_sq(const float* __restrict__ v, size_t n, float* __restric
 void sgemm(cudaStream_t s, const float* A, const float* B, float* C, int M, int N, int K, int lda,
            int ldb, int ldc, int tA, int tB, int acc)
 {
-  dim3 grid((N + 63) / 64, (M + 63) / 64);
-  k_sgemm<<<grid, 256, 0, s>>>(A, B, C, M, N, K, lda, ldb, ldc, tA, tB, acc);
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
+  k_gemm_tc<<<grid, 128, sizeof(GemmSmem), s>>>(A, B, C, M, N, K, lda, ldb, ldc, tA, tB, acc,
+                                                 tc::kSpinLimit);
 }
 
 void freeLearn(LearnState* L)
@@ -928,8 +984,8 @@ ifemgpu_status learnSetup(ifemgpu_ctx* ctx, int m, int nh, int capacity, unsigne
     IFEMGPU_CUDA(ctx, cudaMalloc(&L->tpart, sizeof(float) * parts));
     IFEMGPU_CUDA(ctx, cudaMalloc(&L->tick, sizeof(unsigned) * tiles));
     IFEMGPU_CUDA(ctx, cudaMemset(L->tick, 0, sizeof(unsigned) * tiles));
-    IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)sizeof(InferSmem) + 1024));
+    IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(GemmSmem)));
   }
   L->cap = capacity;
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->X, sizeof(float) * (size_t)capacity * nin));
