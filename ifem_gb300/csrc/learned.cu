@@ -35,6 +35,8 @@
 
 namespace ifemgpu {
 
+constexpr int kGemmTiles = 1024;  // output tiles of one training product with split K
+
 struct LearnState {
   int m = 8;             // coarse cells per direction
   int npv = 1;           // unknowns per node
@@ -69,6 +71,10 @@ struct LearnState {
   int Mt[3] = {0, 0, 0}, nKT[3] = {0, 0, 0};
   float* tpart = nullptr;
   unsigned* tick = nullptr;
+  // split-K partial tiles and tile tickets of the training products
+  float* gws = nullptr;
+  size_t gwsCap = 0;
+  unsigned* gtick = nullptr;
   int adamStep = 0;
   float scale = 1.f;          // S
   bool trained = false;
@@ -534,28 +540,33 @@ k_mlp_tc(const __nv_bfloat16* __restrict__ Wp, int nKT, const float* __restrict_
 // when its flag is set (A is M x K or K x M, B is K x N or N x K).  On the
 // tensor cores in 3xTF32 (hi hi + hi lo + lo hi, FP32 accumulation in tensor
 // memory), so the training keeps FP32 accuracy: one CTA of 128 threads per
-// 128 x 128 tile of C, K in chunks of 32 staged by the threads (the loads
-// follow the operand's contiguous direction; split into TF32 hi/lo parts in
-// the K-major core-matrix layout), twelve MMAs per chunk, the accumulator
-// read back by the four warps (32 rows each).
+// 128 x 128 tile of C and slice of K (gridDim.z slices of kChunks chunks of
+// 32), each chunk staged by the threads (the loads follow the operand's
+// contiguous direction; split into TF32 hi/lo parts in the K-major
+// core-matrix layout) and contracted by twelve MMAs, the accumulator read
+// back by the four warps (32 rows each).  With several slices every CTA
+// stores its partial tile and the last CTA of a tile (ticket) sums the
+// slices in order: the result does not depend on which CTA finishes first.
 constexpr int kGT = 128;  // tile of C: rows and columns
 struct GemmSmem {
   float Ahi[kGT * tc::kK], Alo[kGT * tc::kK], Bhi[kGT * tc::kK], Blo[kGT * tc::kK];
   unsigned long long mbar;
   uint32_t tmemSlot;
-  int ok;
+  int ok, last;
 };
 
 __global__ void __launch_bounds__(128)
 k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __restrict__ C, int M,
           int N, int K, int lda, int ldb, int ldc, int transA, int transB, int accumulate,
-          unsigned spin)
+          int kChunks, float* __restrict__ P, unsigned* __restrict__ tick, unsigned spin)
 {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char smraw[];
   GemmSmem& sm = *reinterpret_cast<GemmSmem*>(smraw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  const int kBeg = blockIdx.z * kChunks * kK, kEnd = min(K, kBeg + kChunks * kK);
+  const int slices = gridDim.z;
   const uint32_t mbar = smemAddr(&sm.mbar);
   if (tid == 0) {
     mbarInit(mbar, 1);
@@ -569,7 +580,7 @@ k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __res
   const uint32_t idesc = instrDescTF32(kGT, kGT);
   uint32_t phase = 0;
   bool ok = true;
-  for (int k0 = 0; k0 < K && ok; k0 += kK) {
+  for (int k0 = kBeg; k0 < kEnd && ok; k0 += kK) {
     // op(A)[m0 + r][k0 + k] and op(B)[k0 + k][n0 + r] for r < 128, k < 32
     for (int i = tid; i < kGT * kK; i += blockDim.x) {
       int r, k;
@@ -577,7 +588,7 @@ k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __res
       else { r = i / kK; k = i % kK; }          // A stored M x K: along k
       const int gm = m0 + r, gk = k0 + k;
       float va = 0.f;
-      if (gm < M && gk < K) va = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+      if (gm < M && gk < kEnd) va = transA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
       float hi, lo;
       splitTF32(va, hi, lo);
       sm.Ahi[kmaj(r, k)] = hi;
@@ -586,7 +597,7 @@ k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __res
       else { k = i / kGT; r = i % kGT; }        // B stored K x N: along n
       const int gn = n0 + r, gkb = k0 + k;
       float vb = 0.f;
-      if (gn < N && gkb < K) vb = transB ? B[(size_t)gn * ldb + gkb] : B[(size_t)gkb * ldb + gn];
+      if (gn < N && gkb < kEnd) vb = transB ? B[(size_t)gn * ldb + gkb] : B[(size_t)gkb * ldb + gn];
       splitTF32(vb, hi, lo);
       sm.Bhi[kmaj(r, k)] = hi;
       sm.Blo[kmaj(r, k)] = lo;
@@ -600,7 +611,8 @@ k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __res
 #pragma unroll
       for (int st = 0; st < kK / 8; st++) {
         const uint32_t off = st * 256;
-        mmaTF32(tmem, smemDesc(ah + off), smemDesc(bh + off), idesc, (k0 > 0 || st > 0) ? 1u : 0u);
+        const uint32_t acc = (k0 > kBeg || st > 0) ? 1u : 0u;
+        mmaTF32(tmem, smemDesc(ah + off), smemDesc(bh + off), idesc, acc);
         mmaTF32(tmem, smemDesc(ah + off), smemDesc(bl + off), idesc, 1u);
         mmaTF32(tmem, smemDesc(al + off), smemDesc(bh + off), idesc, 1u);
       }
@@ -612,27 +624,29 @@ k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __res
     ok = sm.ok != 0;
     tcFenceAfter();
   }
-  const int gm = m0 + warp * 32 + lane;
-  if (K > 0 && ok) {
-    for (int c16 = 0; c16 < kGT / 16; c16++) {
-      float v[16];
+  // this CTA's tile: to C (one slice) or to its partial slot; an empty slice
+  // is zero, a wait that gave up NaN
+  const int r = warp * 32 + lane, gm = m0 + r;
+  const bool any = kEnd > kBeg;
+  float* Pt = P + ((size_t)blockIdx.z * gridDim.x * gridDim.y + blockIdx.y * gridDim.x + blockIdx.x) *
+                  kGT * kGT;
+  for (int c16 = 0; c16 < kGT / 16; c16++) {
+    float v[16];
+    if (any && ok) {
       tmemLoad16(tmem + ((uint32_t)(32 * warp) << 16) + 16 * c16, v);
-      if (gm < M) {
+    } else {
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int gn = n0 + 16 * c16 + j;
-          if (gn < N) {
-            float* c = C + (size_t)gm * ldc + gn;
-            *c = accumulate ? *c + v[j] : v[j];
-          }
-        }
-      }
+      for (int j = 0; j < 16; j++) v[j] = any ? __int_as_float(0x7FC00000) : 0.f;
     }
-  } else if (gm < M) {  // no products (K = 0), or a wait gave up (NaN marks it)
-    const float v = K > 0 ? __int_as_float(0x7FC00000) : 0.f;
-    for (int gn = n0; gn < min(N, n0 + kGT); gn++) {
-      float* c = C + (size_t)gm * ldc + gn;
-      *c = (accumulate && K == 0) ? *c : v;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int c = 16 * c16 + j, gn = n0 + c;
+      if (slices > 1) {
+        Pt[(size_t)r * kGT + c] = v[j];
+      } else if (gm < M && gn < N) {
+        float* cp = C + (size_t)gm * ldc + gn;
+        *cp = accumulate ? *cp + v[j] : v[j];
+      }
     }
   }
   if (!ok && tid == 0) mbarWait(mbar, phase ^ 1u, spin);  // the MMAs given up on finish first
@@ -640,6 +654,25 @@ k_gemm_tc(const float* __restrict__ A, const float* __restrict__ B, float* __res
   __syncthreads();
   tcFenceAfter();
   if (warp == 0) tmemDealloc(tmem, kGT);
+  if (slices == 1) return;
+  __threadfence();
+  __syncthreads();
+  const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+  if (tid == 0) sm.last = atomicAdd(tick + tile, 1u) == (unsigned)slices - 1;
+  __syncthreads();
+  if (!sm.last) return;
+  __threadfence();
+  if (gm < M) {
+    const size_t tstride = (size_t)gridDim.x * gridDim.y * kGT * kGT;
+    const float* P0 = P + (size_t)tile * kGT * kGT + (size_t)r * kGT;
+    for (int c = 0; c < kGT && n0 + c < N; c++) {
+      float acc = 0.f;
+      for (int z = 0; z < slices; z++) acc += __ldcg(P0 + z * tstride + c);
+      float* cp = C + (size_t)gm * ldc + n0 + c;
+      *cp = accumulate ? *cp + acc : acc;
+    }
+  }
+  if (tid == 0) tick[tile] = 0u;
 }
 
 // H = act(H + b) row-wise
@@ -726,12 +759,21 @@ __global__ void k_sum_sq(const float* __restrict__ v, size_t n, float* __restric
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-void sgemm(cudaStream_t s, const float* A, const float* B, float* C, int M, int N, int K, int lda,
-           int ldb, int ldc, int tA, int tB, int acc)
+// K is split into up to 8 slices, for about 96 CTAs per product (the
+// training products have few 128 x 128 tiles and long K; the last CTA of a
+// tile reads every slice's partial tile, which bounds the useful split)
+void sgemm(cudaStream_t s, LearnState* L, const float* A, const float* B, float* C, int M, int N,
+           int K, int lda, int ldb, int ldc, int tA, int tB, int acc)
 {
-  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
-  k_gemm_tc<<<grid, 128, sizeof(GemmSmem), s>>>(A, B, C, M, N, K, lda, ldb, ldc, tA, tB, acc,
-                                                 tc::kSpinLimit);
+  const int tn = (N + kGT - 1) / kGT, tm = (M + kGT - 1) / kGT;
+  const int chunks = std::max(1, (K + tc::kK - 1) / tc::kK);
+  int slices = std::min(std::min(chunks, 8), std::max(1, 96 / (tn * tm)));
+  const int per = (chunks + slices - 1) / slices;
+  slices = (chunks + per - 1) / per;
+  if ((size_t)slices * tn * tm * kGT * kGT > L->gwsCap || tn * tm > kGemmTiles) slices = 1;
+  k_gemm_tc<<<dim3(tn, tm, slices), 128, sizeof(GemmSmem), s>>>(
+      A, B, C, M, N, K, lda, ldb, ldc, tA, tB, acc, slices > 1 ? per : chunks, L->gws, L->gtick,
+      tc::kSpinLimit);
 }
 
 void freeLearn(LearnState* L)
@@ -739,7 +781,7 @@ void freeLearn(LearnState* L)
   void* ptrs[] = {L->eqCell, L->eqFrac, L->vPtr, L->vEq, L->vW, L->vWn, L->theta, L->grad,
                   L->am, L->av, L->wtc, L->tpart, L->tick, L->X, L->Y, L->xstar, L->Xb, L->Yb, L->H1, L->H2,
                   L->Yp, L->dH1, L->dH2, L->dY, L->loss, L->perm, L->rc, L->h1, L->h2,
-                  L->yc, L->nrm, L->feat, L->t, L->rc1, L->Bm, L->Ac};
+                  L->yc, L->nrm, L->feat, L->t, L->rc1, L->Bm, L->Ac, L->gws, L->gtick};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -753,24 +795,24 @@ void batchPass(cudaStream_t s, LearnState* L, int Bn, float invS, bool grad)
   const int nc = L->nc, nh = L->nh, nin = L->nin;
   const float* th = L->theta;
   float* g = L->grad;
-  sgemm(s, L->Xb, th + L->oW1, L->H1, Bn, nh, nin, nin, nin, nh, 0, 1, 0);
+  sgemm(s, L, L->Xb, th + L->oW1, L->H1, Bn, nh, nin, nin, nin, nh, 0, 1, 0);
   k_bias_act<<<256, kT, 0, s>>>(L->H1, th + L->ob1, Bn, nh, 1);
-  sgemm(s, L->H1, th + L->oW2, L->H2, Bn, nh, nh, nh, nh, nh, 0, 1, 0);
+  sgemm(s, L, L->H1, th + L->oW2, L->H2, Bn, nh, nh, nh, nh, nh, 0, 1, 0);
   k_bias_act<<<256, kT, 0, s>>>(L->H2, th + L->ob2, Bn, nh, 1);
-  sgemm(s, L->H2, th + L->oW3, L->Yp, Bn, nc, nh, nh, nh, nc, 0, 1, 0);
+  sgemm(s, L, L->H2, th + L->oW3, L->Yp, Bn, nc, nh, nh, nh, nc, 0, 1, 0);
   k_bias_act<<<256, kT, 0, s>>>(L->Yp, th + L->ob3, Bn, nc, 0);
   k_mse<<<kLossParts, kT, 0, s>>>(L->Yp, L->Yb, invS, grad ? L->dY : nullptr, (size_t)Bn * nc,
                                   L->loss);
   if (!grad) return;
-  sgemm(s, L->dY, L->H2, g + L->oW3, nc, nh, Bn, nc, nh, nh, 1, 0, 0);
+  sgemm(s, L, L->dY, L->H2, g + L->oW3, nc, nh, Bn, nc, nh, nh, 1, 0, 0);
   k_colsum<<<(nc + kT - 1) / kT, kT, 0, s>>>(L->dY, g + L->ob3, Bn, nc);
-  sgemm(s, L->dY, th + L->oW3, L->dH2, Bn, nh, nc, nc, nh, nh, 0, 0, 0);
+  sgemm(s, L, L->dY, th + L->oW3, L->dH2, Bn, nh, nc, nc, nh, nh, 0, 0, 0);
   k_relu_back<<<256, kT, 0, s>>>(L->dH2, L->H2, (size_t)Bn * nh);
-  sgemm(s, L->dH2, L->H1, g + L->oW2, nh, nh, Bn, nh, nh, nh, 1, 0, 0);
+  sgemm(s, L, L->dH2, L->H1, g + L->oW2, nh, nh, Bn, nh, nh, nh, 1, 0, 0);
   k_colsum<<<(nh + kT - 1) / kT, kT, 0, s>>>(L->dH2, g + L->ob2, Bn, nh);
-  sgemm(s, L->dH2, th + L->oW2, L->dH1, Bn, nh, nh, nh, nh, nh, 0, 0, 0);
+  sgemm(s, L, L->dH2, th + L->oW2, L->dH1, Bn, nh, nh, nh, nh, nh, 0, 0, 0);
   k_relu_back<<<256, kT, 0, s>>>(L->dH1, L->H1, (size_t)Bn * nh);
-  sgemm(s, L->dH1, L->Xb, g + L->oW1, nh, nin, Bn, nh, nin, nin, 1, 0, 0);
+  sgemm(s, L, L->dH1, L->Xb, g + L->oW1, nh, nin, Bn, nh, nin, nin, 1, 0, 0);
   k_colsum<<<(nh + kT - 1) / kT, kT, 0, s>>>(L->dH1, g + L->ob1, Bn, nh);
 }
 
@@ -813,6 +855,13 @@ ifemgpu_status ensureBatch(ifemgpu_ctx* ctx, LearnState* L, int B)
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->H2, sizeof(float) * B * nh));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->dH1, sizeof(float) * B * nh));
   IFEMGPU_CUDA(ctx, cudaMalloc(&L->dH2, sizeof(float) * B * nh));
+  // split-K workspace: up to 96 CTAs of 128 x 128 partial tiles
+  if (!L->gws) {
+    L->gwsCap = (size_t)96 * 128 * 128;
+    IFEMGPU_CUDA(ctx, cudaMalloc(&L->gws, sizeof(float) * L->gwsCap));
+    IFEMGPU_CUDA(ctx, cudaMalloc(&L->gtick, sizeof(unsigned) * kGemmTiles));
+    IFEMGPU_CUDA(ctx, cudaMemset(L->gtick, 0, sizeof(unsigned) * kGemmTiles));
+  }
   L->B = B;
   return IFEMGPU_OK;
 }
