@@ -1065,6 +1065,12 @@ ifemgpu_status uploadAssemblyModel(ifemgpu_ctx* ctx)
     GatherList g;
     g.p = cls.first;
     g.npv = cls.second;
+    // each node pair once, mirrored writes: pays where the element work
+    // dominates the scattered mirrored writes (p = 3 elasticity, 32^3: 5.14 ->
+    // 4.78 ms per assembly); p = 2 elasticity and p = 3 Poisson run slower
+    // with it (64^3: 6.80 -> 7.72 and 12.5 -> 13.5 ms); prescribed values
+    // need every warp's full neighbourhood
+    g.half = ctx->nceq == 0 && g.p == 3 && g.npv == 3;
     g.nranges = (int)start.size();
     g.total = total;
     IFEMGPU_TRY(upload(ctx, &g.d_start, start.data(), start.size()));

@@ -54,8 +54,13 @@ struct GCfg {
   static constexpr int WARPS = (P == 3 && NPV == 3) ? 4 : (P == 3 ? 6 : 8);
   static constexpr int NB = (NEN + 31) / 32;           // element functions per lane
   static constexpr int U = NPV == 3 ? (P == 2 ? 1 : 3) : (P == 3 ? 1 : 6);
-  static constexpr size_t SMEM = sizeof(float) * 2 * KL * NS * WARPS;
   static constexpr int MINB = (P == 3 && NPV == 3) ? 2 : (NPV == 3 ? 3 : (P == 3 ? 5 : 4));
+  // neighbour slots summed by a node's warp: all of them, or (half) the
+  // centre and the slots after it, the offsets (dz, dy, dx) >= 0 in
+  // lexicographic order -- each unordered node pair then belongs to exactly
+  // one of its two nodes
+  template <bool HALF> static constexpr int SB = HALF ? NS / 2 : 0;
+  template <bool HALF> static constexpr size_t smem() { return sizeof(float) * 2 * KL * (NS - SB<HALF>) * WARPS; }
 };
 
 // hi + lo += x (TwoSum: the rounding error of hi + x goes to lo)
@@ -96,17 +101,25 @@ struct GatherSys {
 };
 
 // One warp per node of the patches of one (degree, npv) class; node item t
-// belongs to the last range whose start is <= t.
-template <int P, int NPV>
+// belongs to the last range whose start is <= t.  HALF (models without
+// prescribed DOFs): the warp of node a sums only the entries of the node
+// pairs it owns (slots from the centre on) and writes each of them twice,
+// at (a, k; b, l) in its own columns and at (b, l; a, k) in node b's
+// columns: half the loads, additions and accumulators, and the matrix is
+// exactly symmetric by construction.  Otherwise every warp sums all of its
+// node's neighbour entries and writes its own columns, and the prescribed
+// neighbours' terms -c0 K(i, j) go to the right-hand side.
+template <int P, int NPV, bool HALF>
 __global__ void __launch_bounds__(GCfg<P, NPV>::WARPS * 32, GCfg<P, NPV>::MINB)
 k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
          const int* __restrict__ pidx, int nranges, int total, GatherSys S)
 {
   using C = GCfg<P, NPV>;
   constexpr int Q = C::Q, NEN = C::NEN, W = C::W, NS = C::NS, KL = C::KL;
+  constexpr int SB = C::template SB<HALF>, NSH = NS - SB;
   extern __shared__ float gsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float2* acc = reinterpret_cast<float2*>(gsm) + warp * KL * NS;  // [kl][slot] (hi, lo)
+  float2* acc = reinterpret_cast<float2*>(gsm) + warp * KL * NSH;  // [kl][slot - SB] (hi, lo)
   for (int t = blockIdx.x * C::WARPS + warp; t < total; t += gridDim.x * C::WARPS) {
     int r0 = 0, r1 = nranges - 1;
     while (r0 < r1) {
@@ -129,7 +142,7 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
       cpa[k] = eqa[k] > 0 ? S.colptr[eqa[k] - 1] : 0;
     }
     if (!any) continue;  // no column: fixed or prescribed DOFs only
-    for (int i = lane; i < KL * NS; i += 32) acc[i] = make_float2(0.f, 0.f);
+    for (int i = lane; i < KL * NSH; i += 32) acc[i] = make_float2(0.f, 0.f);
     float feHi = 0.f, feLo = 0.f;  // lane k < NPV: load vector of DOF k
     const float lamf = Pt.lamf, muf = Pt.muf;
     const int ex0 = max(0, ax - P), cx = min(ax, Pt.nel[0] - 1) - ex0 + 1;
@@ -167,7 +180,8 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
           for (int bb = 0; bb < C::NB; bb++) {
             const int bl = lane + 32 * bb;
 #pragma unroll
-            for (int kl = 0; kl < KL; kl++) g[u][bb][kl] = bl < NEN ? __ldcs(row + kl * NEN + bl) : 0.f;
+            for (int kl = 0; kl < KL; kl++)
+              g[u][bb][kl] = (bl < NEN && (!HALF || bl >= alU[u])) ? __ldcs(row + kl * NEN + bl) : 0.f;
           }
         }
       }
@@ -179,9 +193,10 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
 #pragma unroll
         for (int bb = 0; bb < C::NB; bb++) {
           const int bl = lane + 32 * bb;
-          if (bl < NEN) {
+          // (local order = slot order: bl >= al exactly for the owned slots)
+          if (bl < NEN && (!HALF || bl >= al)) {
             const int blx = bl % Q, bly = (bl / Q) % Q, blz = bl / (Q * Q);
-            const int s = (blx - alx + P) + W * ((bly - aly + P) + W * (blz - alz + P));
+            const int s = (blx - alx + P) + W * ((bly - aly + P) + W * (blz - alz + P)) - SB;
             const float* gg = g[u][bb];
             if (NPV == 3) {
               const float tr = muf * (gg[0] + gg[4] + gg[8]);
@@ -190,7 +205,7 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
 #pragma unroll
                 for (int l = 0; l < 3; l++) {
                   const float ke = fmaf(lamf, gg[3 * k + l], fmaf(muf, gg[3 * l + k], k == l ? tr : 0.f));
-                  dfAdd(acc + (3 * k + l) * NS + s, ke);
+                  dfAdd(acc + (3 * k + l) * NSH + s, ke);
                 }
             } else {
               dfAdd(acc + s, gg[0]);
@@ -201,33 +216,50 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
         __syncwarp();
       }
     }
-    // write the node's columns; prescribed neighbours feed the right-hand side
+    // write the node's columns (and, HALF, the mirrored entries in the owned
+    // neighbours' columns); prescribed neighbours feed the right-hand side
     double corr[NPV];
+    int rankA[NPV];  // position of a's DOF k among its free DOFs
+    {
+      int r = 0;
 #pragma unroll
-    for (int k = 0; k < NPV; k++) corr[k] = 0.0;
+      for (int k = 0; k < NPV; k++) {
+        corr[k] = 0.0;
+        rankA[k] = r;
+        r += eqa[k] > 0;
+      }
+    }
+    const int Fa = S.F[ga];
     const int* lineOff = Pt.lineOff + (size_t)a * W * W;
-    for (int s = lane; s < NS; s += 32) {
+    for (int s = SB + lane; s < NS; s += 32) {
       const int dx = s % W - P, dy = (s / W) % W - P, dz = s / (W * W) - P;
       const int bx = ax + dx, by = ay + dy, bz = az + dz;
       if (bx < 0 || bx >= n0 || by < 0 || by >= n1 || bz < 0 || bz >= Pt.n[2]) continue;
-      const int gb = Pt.firstNode + (bz * n1 + by) * n0 + bx;
+      const int b = (bz * n1 + by) * n0 + bx;
+      const int gb = Pt.firstNode + b;
       const int db = S.madof[gb] - 1;
       const int pos = lineOff[(dz + P) * W + dy + P] + S.F[gb];
+      const bool mirror = HALF && s != SB;
+      // row (a, k) in node b's columns: b's line towards a, then a's free DOFs
+      const int posB = mirror ? Pt.lineOff[(size_t)b * W * W + (P - dz) * W + P - dy] + Fa : 0;
       int rank = 0;
 #pragma unroll
       for (int l = 0; l < NPV; l++) {
         const int eqb = S.meqn[db + l];
         if (eqb == 0) continue;
+        const int cpb = (mirror && eqb > 0) ? S.colptr[eqb - 1] : 0;
 #pragma unroll
         for (int k = 0; k < NPV; k++) {
           if (eqa[k] <= 0) continue;
           const int kl = k * NPV + l;
-          const float2 hl = acc[kl * NS + s];
+          const float2 hl = acc[kl * NSH + s - SB];
           const double v = tc::widenF32(hl.x) + tc::widenF32(hl.y);
-          if (eqb > 0)
+          if (eqb > 0) {
             S.K[cpa[k] + pos + rank] = v;
-          else if (S.c0)
+            if (mirror) S.K[cpb + posB + rankA[k]] = v;
+          } else if (S.c0) {
             corr[k] = fma(S.c0[-eqb - 1], v, corr[k]);
+          }
         }
         rank += eqb > 0;
       }
@@ -252,31 +284,43 @@ k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
 
 namespace {
 
-template <int P, int NPV>
+template <int P, int NPV, bool HALF>
 ifemgpu_status prepareOne(ifemgpu_ctx* ctx, GatherList& g)
 {
   using C = GCfg<P, NPV>;
-  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_gather<P, NPV>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)C::SMEM));
+  const size_t smem = C::template smem<HALF>();
+  IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_gather<P, NPV, HALF>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int perSM = 0;
-  IFEMGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_gather<P, NPV>,
-                                                                  C::WARPS * 32, C::SMEM));
+  IFEMGPU_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_gather<P, NPV, HALF>,
+                                                                  C::WARPS * 32, smem));
   const int need = (g.total + C::WARPS - 1) / C::WARPS;
   g.grid = std::max(1, std::min(need, std::max(1, perSM) * ctx->numSMs));
   return IFEMGPU_OK;
 }
 
-template <int P, int NPV>
+template <int P, int NPV, bool HALF>
 ifemgpu_status launchOne(ifemgpu_ctx* ctx, const GatherList& g)
 {
   using C = GCfg<P, NPV>;
   GatherSys S{ctx->d_madof, ctx->d_meqn, ctx->d_freeBefore, ctx->nceq ? ctx->d_c0 : nullptr,
               ctx->d_colptr, ctx->d_K, ctx->d_b};
-  k_gather<P, NPV><<<g.grid, C::WARPS * 32, C::SMEM, ctx->stream>>>(
+  k_gather<P, NPV, HALF><<<g.grid, C::WARPS * 32, C::template smem<HALF>(), ctx->stream>>>(
       ctx->d_patches, g.d_start, g.d_pidx, g.nranges, g.total, S);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
   return IFEMGPU_OK;
+}
+
+template <int P, int NPV>
+ifemgpu_status prepareAny(ifemgpu_ctx* ctx, GatherList& g)
+{
+  return g.half ? prepareOne<P, NPV, true>(ctx, g) : prepareOne<P, NPV, false>(ctx, g);
+}
+
+template <int P, int NPV>
+ifemgpu_status launchAny(ifemgpu_ctx* ctx, const GatherList& g)
+{
+  return g.half ? launchOne<P, NPV, true>(ctx, g) : launchOne<P, NPV, false>(ctx, g);
 }
 
 }  // namespace
@@ -284,20 +328,20 @@ ifemgpu_status launchOne(ifemgpu_ctx* ctx, const GatherList& g)
 // kernel attributes and grid of a gather launch (before any capture)
 ifemgpu_status gatherPrepare(ifemgpu_ctx* ctx, GatherList& g)
 {
-  if (g.p == 2 && g.npv == 3) return prepareOne<2, 3>(ctx, g);
-  if (g.p == 2 && g.npv == 1) return prepareOne<2, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 1) return prepareOne<3, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 3) return prepareOne<3, 3>(ctx, g);
+  if (g.p == 2 && g.npv == 3) return prepareAny<2, 3>(ctx, g);
+  if (g.p == 2 && g.npv == 1) return prepareAny<2, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 1) return prepareAny<3, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 3) return prepareAny<3, 3>(ctx, g);
   return setError(ctx, IFEMGPU_INVALID_ARG, "internal: gather class");
 }
 
 ifemgpu_status gatherLaunch(ifemgpu_ctx* ctx, const GatherList& g)
 {
   if (g.total == 0) return IFEMGPU_OK;
-  if (g.p == 2 && g.npv == 3) return launchOne<2, 3>(ctx, g);
-  if (g.p == 2 && g.npv == 1) return launchOne<2, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 1) return launchOne<3, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 3) return launchOne<3, 3>(ctx, g);
+  if (g.p == 2 && g.npv == 3) return launchAny<2, 3>(ctx, g);
+  if (g.p == 2 && g.npv == 1) return launchAny<2, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 1) return launchAny<3, 1>(ctx, g);
+  if (g.p == 3 && g.npv == 3) return launchAny<3, 3>(ctx, g);
   return setError(ctx, IFEMGPU_INVALID_ARG, "internal: gather class");
 }
 

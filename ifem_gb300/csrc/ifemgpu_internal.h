@@ -171,6 +171,7 @@ struct DebugWaits {
 // node item t belongs to patch pidx[r] for the last range r with start[r] <= t.
 struct GatherList {
   int p = 0, npv = 0;
+  bool half = false;   // each node pair summed once, written to both columns
   int* d_start = nullptr;
   int* d_pidx = nullptr;
   int nranges = 0;
