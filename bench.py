@@ -62,9 +62,12 @@ SAMPLE_LAYERS = 8
 WORKLOAD = "3D linear elasticity, 1 NURBS patch, p=2, 64^3 elements, 3x3x3 Gauss"
 METRIC = "elements/s assembled; time to 1e-10 residual, learned vs plain PCG, 1 GB300"
 DATA = "synthetic (seeded NURBS patch: Greville points + U(-0.1h, 0.1h), weights U[0.8, 1.2])"
-# dram__bytes_read.sum + dram__bytes_write.sum of the dominant kernel per
-# 64^3 assembly (ncu capture of a smaller case scaled by the element count)
-TRAFFIC_PER_ELEMENT = None
+# dram__bytes_read.sum + dram__bytes_write.sum per element of the dominant
+# kernel (the p=2 elasticity element kernel): 4.7 MB + 1,641.7 MB for the
+# 64,000 elements of the 40^3 model (one ncu capture), scaled by the element
+# count; about 97% of its 26,576-byte element blocks (the rest is still in L2
+# when the kernel ends)
+TRAFFIC_PER_ELEMENT = 25725
 
 
 def config_of(s):
@@ -493,7 +496,7 @@ def run_gpu(args):
     # ---- device-resident steps (inputs larger than L2) ----------------------
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    vol_ms = []
+    vol_ms, elem_ms, gath_ms = [], [], []
     barrier()
     with ClockSampler(local) as clk:
         wall0 = time.perf_counter()
@@ -504,7 +507,10 @@ def run_gpu(args):
             with torch.cuda.stream(stream):
                 ends[i].record(stream)
             _, v, _ = sim.assembly_stats()            # synchronises; volume-pass time
+            e_ms, g_ms = sim.assembly_phases()         # element kernel, gather
             vol_ms.append(v)
+            elem_ms.append(e_ms)
+            gath_ms.append(g_ms)
         barrier()
         wall = time.perf_counter() - wall0
     step_ms = float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)]))
@@ -535,7 +541,9 @@ def run_gpu(args):
     del Kh, bh
 
     # ---- max over ranks ----------------------------------------------------
-    step_ms, e2e_ms, vmax = max_over_ranks([step_ms, e2e_ms, float(np.mean(vol_ms))], "cuda")
+    step_ms, e2e_ms, vmax, emax, gmax = max_over_ranks(
+        [step_ms, e2e_ms, float(np.mean(vol_ms)), float(np.mean(elem_ms)),
+         float(np.mean(gath_ms))], "cuda")
 
     if rank == 0:
         hbm, bf16, src = measured_peaks()
@@ -546,6 +554,8 @@ def run_gpu(args):
         achieved = traffic_alg / (vmax * 1e-3) / 1e9
         nq, ndof_e, ns = 27, 81, 6     # p=2 elasticity: Gauss points, element DOFs, stresses
         flops_el = 2 * nq * (ns * ndof_e ** 2 + ns ** 2 * ndof_e)
+        tflops_el = flops_el * sz.nel / (emax * 1e-3) / 1e12
+        gbs_gather = traffic_alg / (gmax * 1e-3) / 1e9
         value = world * sz.nel / (step_ms * 1e-3)
         # host baseline on the same workload (bounded sample), then the oracle's
         # full FP64 assembly as the reference of the accuracy object
@@ -574,21 +584,28 @@ def run_gpu(args):
             "e2e": {"value": world * sz.nel / (e2e_ms * 1e-3), "unit": "elements/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm,
-                         "traffic": (TRAFFIC_PER_ELEMENT * sz.nel if TRAFFIC_PER_ELEMENT
-                                     else None),
-                         "kernel": "volume integration + scatter passes",
-                         "kernel_ms": vmax, "algorithmic_bytes": traffic_alg,
-                         "peak_source": src},
-            "roofline_tensor": {
-                "bound": "tensor", "achieved": flops_el * sz.nel / (vmax * 1e-3) / 1e12,
-                "peak": bf16, "unit": "TFLOP/s",
-                "frac": flops_el * sz.nel / (vmax * 1e-3) / 1e12 / bf16,
-                "flops_per_element": flops_el,
-                "note": "element stiffness contraction 2 nq (ns ndof^2 + ns^2 ndof), ns = 6, "
-                        "counted once although 3xTF32 issues three MMAs per product; peak = "
-                        "measured dense bf16 rate (TF32 runs at half of it)"},
+            "roofline": {
+                "bound": "tensor", "achieved": tflops_el, "peak": bf16, "unit": "TFLOP/s",
+                "frac": tflops_el / bf16,
+                "traffic": (TRAFFIC_PER_ELEMENT * sz.nel if TRAFFIC_PER_ELEMENT else None),
+                "kernel": "k_volume_tc_elast_p2 (element kernel, the dominant kernel)",
+                "kernel_ms": emax, "flops_per_element": flops_el,
+                "algorithmic": "Ke contraction 2 nq (ns ndof^2 + ns^2 ndof), ns = 6, ndof = 81, "
+                               "nq = 27, counted once although 3xTF32 issues three MMAs per "
+                               "product",
+                "peak_source": src + " (dense bf16 burst; TF32 runs at half of it)"},
+            "roofline_gather": {
+                "bound": "hbm", "achieved": gbs_gather, "peak": hbm, "unit": "GB/s",
+                "frac": gbs_gather / hbm, "kernel": "k_gather<2, 3> (node-wise sums)",
+                "kernel_ms": gmax, "algorithmic_bytes": traffic_alg,
+                "algorithmic": "compulsory bytes of the scatter: nnz (8 value + 4 row index) "
+                               "+ 4 (neq + 1) + 8 neq; the element blocks it reads "
+                               "(26,576 B per element) are not counted",
+                "peak_source": src},
+            "roofline_assembly": {
+                "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "kernel": "element kernel + gather (one assembly)",
+                "kernel_ms": vmax, "algorithmic_bytes": traffic_alg, "peak_source": src},
             "cpu_baseline": {"value": cpu_v, "unit": "elements/s", "cores": threads,
                              "kind": "port",
                              "sample": f"{args.cpu_reps} samples: " +

@@ -1318,9 +1318,10 @@ static SysView sysView(ifemgpu_ctx* ctx)
                  ctx->d_flags, ctx->dbg.flagSpin ? ctx->dbg.flagSpin : kGenFlagSpin, withhold};
 }
 
-// The kernel sequence of one assembly in three segments -- prologue (zeroing,
-// basis tables), volume passes, face passes -- each captured once into a CUDA
-// graph; the timing events are recorded between the graph launches.
+// The kernel sequence of one assembly in four segments -- prologue (zeroing,
+// basis tables), element kernels and generic volume passes, gathers, face
+// passes -- each captured once into a CUDA graph; the timing events are
+// recorded between the graph launches.
 static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
 {
   cudaStream_t s = ctx->stream;
@@ -1343,18 +1344,21 @@ static ifemgpu_status enqueueSegment(ifemgpu_ctx* ctx, int seg)
   }
   SysView S = sysView(ctx);
   const bool split = ctx->opts.ke_precision == IFEMGPU_KE_SPLIT_TF32;
-  if (seg == 1) {  // element kernels of the tensor-core patches, then their gathers
+  if (seg == 1) {  // element kernels of the tensor-core patches
     for (const Pass& p : ctx->passes) {
       if (!p.tc) continue;
       if (p.tcDeg == kTcElast3) IFEMGPU_TRY(tcElast3Launch(ctx, p));
       else if (p.tcDeg) IFEMGPU_TRY(tcPoissonLaunch(ctx, p, p.tcDeg));
       else IFEMGPU_TRY(tcLaunchVolume(ctx, p, 0));
     }
+  }
+  if (seg == 2) {  // their gathers
     for (const GatherList& g : ctx->gathers) IFEMGPU_TRY(gatherLaunch(ctx, g));
+    return IFEMGPU_OK;
   }
   for (const Pass& p : ctx->passes) {
     if (p.tc) continue;
-    if ((p.face != 0) != (seg == 2)) continue;
+    if ((p.face != 0) != (seg == 3)) continue;
     if ((p.persistent && !ctx->useFlow) || (p.altColour && ctx->useFlow)) continue;
     if (p.persistent && split)
       k_volume_gen_flow<float><<<std::min(p.count, ctx->genGrid), 256, p.smem, s>>>(
@@ -1490,9 +1494,9 @@ static ifemgpu_status autotune(ifemgpu_ctx* ctx)
 ifemgpu_status enqueueAssembly(ifemgpu_ctx* ctx)
 {
   if (!ctx->tuned) return setError(ctx, IFEMGPU_NOT_READY, "internal: assembly not tuned");
-  bool hasSeg[3] = {true, false, false};
-  for (const Pass& p : ctx->passes) hasSeg[p.face ? 2 : 1] = true;
-  for (int seg = 0; seg < 3; seg++)
+  bool hasSeg[4] = {true, false, !ctx->gathers.empty(), false};
+  for (const Pass& p : ctx->passes) hasSeg[p.face ? 3 : 1] = true;
+  for (int seg = 0; seg < 4; seg++)
     if (hasSeg[seg]) IFEMGPU_TRY(enqueueSegment(ctx, seg));
   return IFEMGPU_OK;
 }
@@ -1501,9 +1505,9 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
 {
   cudaStream_t s = ctx->stream;
   if (!ctx->tuned) IFEMGPU_TRY(autotune(ctx));
-  bool hasSeg[3] = {true, false, false};
-  for (const Pass& p : ctx->passes) hasSeg[p.face ? 2 : 1] = true;
-  for (int seg = 0; seg < 3; seg++) {
+  bool hasSeg[4] = {true, false, !ctx->gathers.empty(), false};
+  for (const Pass& p : ctx->passes) hasSeg[p.face ? 3 : 1] = true;
+  for (int seg = 0; seg < 4; seg++) {
     if (ctx->graphExec[seg] || !hasSeg[seg]) continue;
     IFEMGPU_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     ifemgpu_status st = enqueueSegment(ctx, seg);
@@ -1517,11 +1521,11 @@ ifemgpu_status launchAssembly(ifemgpu_ctx* ctx)
     ctx->graph[seg] = g;
     IFEMGPU_CUDA(ctx, cudaGraphInstantiate(&ctx->graphExec[seg], g, 0));
   }
-  for (int seg = 0; seg < 3; seg++) {
+  for (int seg = 0; seg < 4; seg++) {
     IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[seg], s));
     if (hasSeg[seg]) IFEMGPU_CUDA(ctx, cudaGraphLaunch(ctx->graphExec[seg], s));
   }
-  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+  IFEMGPU_CUDA(ctx, cudaEventRecord(ctx->ev[4], s));
   ctx->assemblies++;
   int used = 0;
   for (const Pass& p : ctx->passes)

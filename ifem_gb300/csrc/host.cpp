@@ -91,7 +91,7 @@ void freeDevice(ifemgpu_ctx* ctx)
   ctx->d_freeBefore = nullptr;
   ctx->d_flags = nullptr;
   ctx->d_basisStart = nullptr;
-  for (int g = 0; g < 3; g++) {
+  for (int g = 0; g < 4; g++) {
     if (ctx->graphExec[g]) cudaGraphExecDestroy(ctx->graphExec[g]);
     if (ctx->graph[g]) cudaGraphDestroy(ctx->graph[g]);
     ctx->graphExec[g] = nullptr;
@@ -825,13 +825,28 @@ ifemgpu_status ifemgpu_debug_waits(ifemgpu_ctx* ctx, unsigned flag_spin, unsigne
   ctx->dbg.patch = patch_id - 1;
   ctx->dbg.elem = patch_id > 0 ? element : -1;
   // the captured kernel sequences hold the old parameters
-  for (int g = 0; g < 3; g++) {
+  for (int g = 0; g < 4; g++) {
     if (ctx->graphExec[g]) cudaGraphExecDestroy(ctx->graphExec[g]);
     if (ctx->graph[g]) cudaGraphDestroy(ctx->graph[g]);
     ctx->graphExec[g] = nullptr;
     ctx->graph[g] = nullptr;
   }
   dropStep(ctx);
+  return IFEMGPU_OK;
+}
+
+ifemgpu_status ifemgpu_last_assembly_phases(ifemgpu_ctx* ctx, double* element_ms,
+                                            double* gather_ms)
+{
+  if (!ctx) return IFEMGPU_INVALID_ARG;
+  if (!ctx->assembled) return setError(ctx, IFEMGPU_NOT_READY, "no assembly yet");
+  IFEMGPU_TRY(verifyAssembly(ctx));
+  IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  float t0 = 0.f, t1 = 0.f;
+  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t0, ctx->ev[1], ctx->ev[2]));
+  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t1, ctx->ev[2], ctx->ev[3]));
+  if (element_ms) *element_ms = t0;
+  if (gather_ms) *gather_ms = t1;
   return IFEMGPU_OK;
 }
 
@@ -844,8 +859,8 @@ ifemgpu_status ifemgpu_last_assembly_stats(ifemgpu_ctx* ctx, double* total_ms,
   IFEMGPU_TRY(verifyAssembly(ctx));
   IFEMGPU_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   float t0 = 0.f, t1 = 0.f;
-  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[3]));
-  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t1, ctx->ev[1], ctx->ev[2]));
+  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t0, ctx->ev[0], ctx->ev[4]));
+  IFEMGPU_CUDA(ctx, cudaEventElapsedTime(&t1, ctx->ev[1], ctx->ev[3]));
   unsigned long long s = 0;
   IFEMGPU_CUDA(ctx, cudaMemcpy(&s, ctx->d_counters, sizeof(s), cudaMemcpyDeviceToHost));
   if (total_ms) *total_ms = t0;

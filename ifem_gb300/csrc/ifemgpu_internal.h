@@ -192,7 +192,7 @@ struct ifemgpu_ctx {
   ifemgpu_options opts{};
   std::string err;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<ifemgpu::HostPatch> patches;
   std::vector<ifemgpu::HostConnection> conns;  // patch connections (topology)
   bool preprocessed = false;
@@ -205,8 +205,10 @@ struct ifemgpu_ctx {
   std::vector<int> colptr, rowidx;
   std::vector<int> freeBefore;  // F(n): free DOFs of the nodes before node n (nnod+1)
   int* d_freeBefore = nullptr;
-  cudaGraph_t graph[3] = {nullptr, nullptr, nullptr};  // captured assembly segments
-  cudaGraphExec_t graphExec[3] = {nullptr, nullptr, nullptr};
+  // captured assembly segments: prologue, element kernels (and generic
+  // volume passes), gathers, face passes
+  cudaGraph_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaGraphExec_t graphExec[4] = {nullptr, nullptr, nullptr, nullptr};
   // device model
   int* d_madof = nullptr;
   int* d_meqn = nullptr;

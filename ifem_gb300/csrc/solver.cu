@@ -610,7 +610,7 @@ static Work carve(ifemgpu_ctx* ctx)
 
 static void dropLoopGraphs(ifemgpu_ctx* ctx)
 {
-  for (int g = 0; g < 3; g++) {
+  for (int g = 0; g < ifemgpu_ctx::kLoops; g++) {  // every captured inner loop
     if (ctx->loopExec[g]) cudaGraphExecDestroy(ctx->loopExec[g]);
     ctx->loopExec[g] = nullptr;
     ctx->loopKey[g] = nullptr;

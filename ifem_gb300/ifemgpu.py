@@ -71,7 +71,8 @@ EXPORTS = [
     "ifemgpu_patch_constrain_face", "ifemgpu_patch_add_neumann", "ifemgpu_preprocess",
     "ifemgpu_get_sizes", "ifemgpu_get_madof", "ifemgpu_get_meqn", "ifemgpu_get_mnpc",
     "ifemgpu_get_pattern", "ifemgpu_assemble", "ifemgpu_copy_matrix", "ifemgpu_copy_rhs",
-    "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_solve",
+    "ifemgpu_device_system", "ifemgpu_last_assembly_stats", "ifemgpu_last_assembly_phases",
+    "ifemgpu_solve",
     "ifemgpu_copy_system_async", "ifemgpu_copy_wait",
     "ifemgpu_expand_solution", "ifemgpu_patch_update_coefs", "ifemgpu_get_stream",
     "ifemgpu_selftest_tc_gemm", "ifemgpu_solve_noalloc", "ifemgpu_learn_setup",
@@ -131,6 +132,7 @@ def load_library(path: str | None = None):
         "ifemgpu_device_system": (I, [P, V, V, V, V]),
         "ifemgpu_last_assembly_stats": (I, [P, C.POINTER(D), C.POINTER(D),
                                             C.POINTER(C.c_longlong), C.POINTER(I)]),
+        "ifemgpu_last_assembly_phases": (I, [P, C.POINTER(D), C.POINTER(D)]),
         "ifemgpu_solve": (I, [P, C.POINTER(SolverOptions), V, C.POINTER(SolveInfo)]),
         "ifemgpu_expand_solution": (I, [P, V, V, D]),
         "ifemgpu_patch_update_coefs": (I, [P, I, V]),
@@ -346,6 +348,12 @@ class SIM:
                                                          C.byref(s), C.byref(n)))
         self.kernel_launches = n.value
         return t.value, v.value, s.value
+
+    def assembly_phases(self):
+        """(element-kernel ms, gather ms) of the last assembly."""
+        e, g = C.c_double(), C.c_double()
+        self._check(self.lib.ifemgpu_last_assembly_phases(self.ctx, C.byref(e), C.byref(g)))
+        return e.value, g.value
 
     def matrix_values(self) -> np.ndarray:
         out = np.zeros(self.sizes.nnz, dtype=np.float64)

@@ -303,6 +303,13 @@ ifemgpu_status ifemgpu_last_assembly_stats(ifemgpu_ctx* ctx, double* total_ms,
                                            long long* singular_points,
                                            int* kernel_launches);
 
+/* Device time of the last assembly's two phases on the tensor-core path:
+ * the element kernels (with the generic volume passes of other patches)
+ * and the node-wise gathers, from events between the captured segments.
+ * No IFEM counterpart (timing diagnostics).                               */
+ifemgpu_status ifemgpu_last_assembly_phases(ifemgpu_ctx* ctx, double* element_ms,
+                                            double* gather_ms);
+
 /* Block-CSR copy of the assembled matrix for models whose free DOFs come in
  * whole nodes of `block` DOFs (e.g. block 3 for elasticity with fully
  * clamped faces): block rows in equation order, column indices ascending,
