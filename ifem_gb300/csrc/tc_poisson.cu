@@ -223,7 +223,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     //         derivatives, fields 4, 5 (w g, w n) values only.
     float* sA = sFw + 6 * C::NEN;  // blocks 2f + [N, D] (f < 4), 8 + (f - 4): [k][j][gi]
     float* sB = sA + 10 * Q3;      // blocks 3f + [NN, DN, ND] (f < 4), 12 + (f - 4): [k][gj][gi]
-    float* sP = sB + 14 * Q3;      // [q][6][value, d/du, d/dv, d/dw]
+    float* sP = sB + 14 * Q3;      // [6][value, d/du, d/dv, d/dw][q]: slot-major
     for (int t = tid; t < 10 * Q3; t += blockDim.x) {
       const int blk = t / Q3, r = t - blk * Q3;
       const int gi = r % Q, j = (r / Q) % Q, k = r / Q2;
@@ -256,8 +256,10 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       sB[t] = acc;
     }
     __syncthreads();
+    // lanes over the Gauss points of one output slot: the lanes of a warp
+    // read one source block (no bank conflicts) and store consecutive words
     for (int t = tid; t < C::NQ * 18; t += blockDim.x) {
-      const int q = t / 18, r = t - q * 18;
+      const int r = t / C::NQ, q = t - r * C::NQ;
       const int gi = q % Q, gj = (q / Q) % Q, gk = q / Q2;
       int src, d2, slot;
       if (r < 16) {
@@ -275,7 +277,7 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       float acc = 0.f;
 #pragma unroll
       for (int kk = 0; kk < Q; kk++) acc = fmaf(tb[kk], b[kk * Q2], acc);
-      sP[q * 24 + slot] = acc;
+      sP[slot * C::NQ + q] = acc;
     }
     __syncthreads();
 
@@ -283,13 +285,15 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
     //         weight, conductivity kappa = kappa0 exp(sum R g), source
     if (tid < C::NQ) {
       const int q = tid;
-      const float* Pq = sP + q * 24;
-      const float iW = 1.f / Pq[12];
+      auto Pq = [&](int k) { return sP[k * C::NQ + q]; };
+      const float iW = 1.f / Pq(12);
       double J[9];  // J[d*3 + r] = dX_r/du_d, formed in FP32 and widened exactly
+#pragma unroll
       for (int r = 0; r < 3; r++) {
-        const float Xr = Pq[r * 4] * iW;
+        const float Xr = Pq(r * 4) * iW;
+#pragma unroll
         for (int d = 0; d < 3; d++)
-          J[d * 3 + r] = widenF32((Pq[r * 4 + 1 + d] - Xr * Pq[12 + 1 + d]) * iW);
+          J[d * 3 + r] = widenF32((Pq(r * 4 + 1 + d) - Xr * Pq(12 + 1 + d)) * iW);
       }
       const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[1] * J[8] - J[2] * J[7],
                    c2 = J[1] * J[5] - J[2] * J[4];
@@ -297,34 +301,38 @@ k_volume_tc_poisson(const DevPatch* __restrict__ patches, const Item* __restrict
       float w = 0.f;
       float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (fabs(det) > kEpsZ) {
-        const double id = 1.0 / det;
-        B[0] = (float)(c0 * id);
-        B[1] = (float)(-c1 * id);
-        B[2] = (float)(c2 * id);
-        B[3] = (float)(-(J[3] * J[8] - J[5] * J[6]) * id);
-        B[4] = (float)((J[0] * J[8] - J[2] * J[6]) * id);
-        B[5] = (float)(-(J[0] * J[5] - J[2] * J[3]) * id);
-        B[6] = (float)((J[3] * J[7] - J[4] * J[6]) * id);
-        B[7] = (float)(-(J[0] * J[7] - J[1] * J[6]) * id);
-        B[8] = (float)((J[0] * J[4] - J[1] * J[3]) * id);
-        w = (float)det * sm.dVf * Pt.gwf[0][q % Q] * Pt.gwf[1][(q / Q) % Q] * Pt.gwf[2][q / Q2];
+        // cofactors and determinant narrowed on the integer pipe, the
+        // quotients in FP32 (an FP64 division and nine FP64 products and
+        // conversions would occupy the scarce FP64 units)
+        const float detf = narrowF64(det);
+        const float id = 1.f / detf;
+        B[0] = narrowF64(c0) * id;
+        B[1] = -narrowF64(c1) * id;
+        B[2] = narrowF64(c2) * id;
+        B[3] = -narrowF64(J[3] * J[8] - J[5] * J[6]) * id;
+        B[4] = narrowF64(J[0] * J[8] - J[2] * J[6]) * id;
+        B[5] = -narrowF64(J[0] * J[5] - J[2] * J[3]) * id;
+        B[6] = narrowF64(J[3] * J[7] - J[4] * J[6]) * id;
+        B[7] = -narrowF64(J[0] * J[7] - J[1] * J[6]) * id;
+        B[8] = narrowF64(J[0] * J[4] - J[1] * J[3]) * id;
+        w = detf * sm.dVf * Pt.gwf[0][q % Q] * Pt.gwf[1][(q / Q) % Q] * Pt.gwf[2][q / Q2];
       } else {
         atomicAdd(S.counters, 1ull);
       }
       float kap = (float)Pt.kappa;
-      if (hasG) kap *= expf(Pq[16] * iW);
+      if (hasG) kap *= expf(Pq(16) * iW);
       float f = (float)Pt.source;
       if (Pt.source_shape == IFEMGPU_SOURCE_SINE)
-        for (int c = 0; c < 3; c++) f *= sinpif((float)((double)(Pq[c * 4] * iW) + sm.c00[c]));
-      if (hasN) f *= 1.f + Pq[20] * iW;
+        for (int c = 0; c < 3; c++) f *= sinpif((float)((double)(Pq(c * 4) * iW) + sm.c00[c]));
+      if (hasN) f *= 1.f + Pq(20) * iW;
       const float kw = kap * w;
       if (kw != 0.f) atomicOr(&sm.signs, kw > 0.f ? 1 : 2);
       sm.t.pt.kw[q] = kw;
       sm.t.pt.fw[q] = f * w;
       sm.t.pt.Wq[q][0] = iW;
-      sm.t.pt.Wq[q][1] = Pq[13];
-      sm.t.pt.Wq[q][2] = Pq[14];
-      sm.t.pt.Wq[q][3] = Pq[15];
+      sm.t.pt.Wq[q][1] = Pq(13);
+      sm.t.pt.Wq[q][2] = Pq(14);
+      sm.t.pt.Wq[q][3] = Pq(15);
       for (int c = 0; c < 9; c++) sm.t.pt.Ji[q][c] = B[c];
     }
     __syncthreads();
