@@ -20,8 +20,13 @@ Extra objects of the GPU line:
                  host), per entry and in the max norm;
   assembly_24    the same model at 24^3 (device-resident, L2 flushed);
   elasticity_64  time to the FP64 relative residual 1e-10 on the 64^3 system
-                 (plain mixed PCG, Kronecker FCG), solutions against the
-                 oracle's FP64 PCG solution;
+                 (plain mixed PCG, Kronecker FCG, and the learned two-level
+                 step trained on seeded loads, the traction load held out),
+                 solutions against the oracle's FP64 PCG solution;
+  roofline       the dominant kernel (the element kernel) against the tensor
+                 peak; roofline_gather and roofline_assembly the gather and the
+                 whole assembly against HBM (events between the captured
+                 segments time each phase);
   solve          the second half of the metric: wall time to 1e-10 on the
                  64^3 p=3 log-normal Poisson system, plain Jacobi mixed PCG
                  against flexible CG with the Kronecker preconditioner and with
