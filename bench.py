@@ -19,6 +19,8 @@ Extra objects of the GPU line:
                  the oracle (IFEM's integrate + assemSparse restated on the
                  host), per entry and in the max norm;
   assembly_24    the same model at 24^3 (device-resident, L2 flushed);
+  batched_64_patches  64 patches of uneven size and degree, one system per
+                 integrand: ms per assembly and kernel launches;
   elasticity_64  time to the FP64 relative residual 1e-10 on the 64^3 system
                  (plain mixed PCG, Kronecker FCG, and the learned two-level
                  step trained on seeded loads, the traction load held out),
@@ -408,6 +410,34 @@ def run_assembly_24(args, G, W):
             "l2": "flushed between steps (256 MB write, untimed)"}
 
 
+def run_batched(args, G, W):
+    """The batched configuration: 64 independent patches of 8^3..32^3
+    elements, p = 2 and 3, Poisson and elasticity, assembled as two systems
+    (one per integrand, as the patch kinds need different DOF counts); each
+    assembly is the basis tables, one element-kernel launch per kernel class
+    over all its patches and one gather per (degree, field) class."""
+    patches, ng = W.config3()
+    out = {}
+    for kind, name in ((1, "poisson"), (2, "elasticity")):
+        sub = [pc for pc in patches if pc.kind == kind]
+        sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
+        W.load_into(sim, sub)
+        sz = sim.preprocess()
+        for _ in range(3):
+            sim.assembleSystem()
+        ts = []
+        for _ in range(max(3, args.steps // 2)):
+            sim.assembleSystem()
+            ts.append(sim.assembly_stats()[0])
+        ms = float(np.median(ts))
+        out[name] = {"patches": len(sub), "nel": sz.nel, "neq": sz.neq, "nnz": sz.nnz,
+                     "ms_per_assembly": ms, "elements_per_s": sz.nel / (ms * 1e-3),
+                     "kernel_launches": sim.kernel_launches,
+                     "degrees": sorted({int(pc.degree[0]) for pc in sub})}
+        del sim
+    return out
+
+
 def seeded_loads(W, patch, sam, seed):
     """A smooth random load per displacement component: a Gaussian random
     field (sigma 1, correlation 0.1) at the control points, as nodal values
@@ -625,6 +655,7 @@ def run_gpu(args):
         line["elasticity_64"] = run_elasticity_solves(args, G, W, sim, patches, xref)
         del sim
         line["assembly_24"] = run_assembly_24(args, G, W)
+        line["batched_64_patches"] = run_batched(args, G, W)
         if args.solve_nel > 0:
             line["solve"] = run_solve(args, G, W, threads)
             if "cpu_solve" in line["solve"]:
