@@ -78,6 +78,7 @@ struct Tc3Sys {
   unsigned long long* counters;  // [0] singular points, [2] device timeouts
   unsigned mbarSpin;
   int wPatch, wElem;             // element whose copy is never issued (test hook)
+  int upper;                     // write only the node pairs b >= a (the gather's half mode)
 };
 
 __global__ void __launch_bounds__(kThreads3, 2)
@@ -429,7 +430,10 @@ k_volume_tc_elast_p3(const DevPatch* __restrict__ patches, const Item* __restric
 
     // ---- 6. tensor memory -> element block: every entry with c >= r at
     //         (r, c) and its mirror (c, r); warps 0..3 block 1, warps 4, 5
-    //         block 2, warps 6, 7 the load vector
+    //         block 2, warps 6, 7 the load vector.  With S.upper the gather
+    //         reads only the node pairs b >= a of each row block (a row
+    //         (a, k), columns (b, l)), so only those positions are written:
+    //         half the stores
     float* blk = P.elm + (size_t)e * P.elmStride;
     if (warp < 4) {
       const int r = 32 * warp + lane, k = r >> 6, a = r & 63;
@@ -441,7 +445,8 @@ k_volume_tc_elast_p3(const DevPatch* __restrict__ patches, const Item* __restric
 #pragma unroll
           for (int i = 0; i < 16; i++) v[i] = 0.f;
         const int l = c16 >> 2, b0 = (c16 & 3) * 16;
-        if (l > k) {
+        const bool full = l > k && (!S.upper || b0 >= a);  // the 16 direct values, 16-byte stores
+        if (full) {
 #pragma unroll
           for (int i = 0; i < 16; i += 4)
             *reinterpret_cast<float4*>(rowOut + l * 64 + b0 + i) =
@@ -450,8 +455,9 @@ k_volume_tc_elast_p3(const DevPatch* __restrict__ patches, const Item* __restric
 #pragma unroll
         for (int i = 0; i < 16; i++) {
           const int b = b0 + i;
-          if (l == k && b >= a) rowOut[l * 64 + b] = v[i];
-          if (l > k || b > a) blk[(size_t)((3 * b + l) * 3 + k) * 64 + a] = v[i];
+          if (!full && b >= a && l >= k) rowOut[l * 64 + b] = v[i];
+          if ((l > k || b > a) && (!S.upper || b <= a))
+            blk[(size_t)((3 * b + l) * 3 + k) * 64 + a] = v[i];
         }
       }
     } else if (warp < 6) {
@@ -467,7 +473,7 @@ k_volume_tc_elast_p3(const DevPatch* __restrict__ patches, const Item* __restric
         for (int i = 0; i < 16; i++) {
           const int b = 16 * c16 + i;
           if (b >= a) rowOut[b] = v[i];
-          if (b > a) blk[(size_t)((3 * b + 2) * 3 + 2) * 64 + a] = v[i];
+          if (b > a && !S.upper) blk[(size_t)((3 * b + 2) * 3 + 2) * 64 + a] = v[i];
         }
       }
     } else {
@@ -508,8 +514,10 @@ ifemgpu_status tcElast3Prepare(ifemgpu_ctx* ctx)
 
 ifemgpu_status tcElast3Launch(ifemgpu_ctx* ctx, const Pass& p)
 {
+  // without prescribed values the gather of this class sums each node pair
+  // once (half mode) and reads only the pairs b >= a
   Tc3Sys S{ctx->d_counters, ctx->dbg.mbarSpin ? ctx->dbg.mbarSpin : kSpinLimit, ctx->dbg.patch,
-           ctx->dbg.elem};
+           ctx->dbg.elem, ctx->nceq == 0 ? 1 : 0};
   // two CTAs per SM (2 x 256 tensor-memory columns, shared memory)
   const int grid = std::min(p.count, 2 * ctx->numSMs);
   const DevPatch* patches = ctx->d_patches;
