@@ -237,3 +237,21 @@ def test_config4_family_solve_matches_direct(gpulib, oracle_lib):
     Kmo = sp.csc_matrix((Ko, sam.rowidx, sam.colptr), shape=(sim.sizes.neq,) * 2)
     xo = sla.spsolve(Kmo, bo)
     assert np.abs(x - xo).max() <= 1e-5 * np.abs(xo).max()
+
+
+def test_assembly_phase_timings(gpulib):
+    """The element-kernel and gather phases of a tensor-core assembly are
+    timed by events between their captured segments: both positive, and
+    together the volume time of the assembly statistics."""
+    patches, ng = W.config2(nel=12)
+    sim = G.SIM(n_gauss=ng, ke_precision=G.KE_SPLIT_TF32)
+    W.load_into(sim, patches)
+    sim.preprocess()
+    for _ in range(2):
+        sim.assembleSystem()
+    total, volume, _ = sim.assembly_stats()
+    elem, gath = sim.assembly_phases()
+    assert sim.kernel_launches == 3          # basis tables, element kernel, gather
+    assert elem > 0.0 and gath > 0.0
+    assert abs((elem + gath) - volume) <= 1e-3 * volume + 1e-3
+    assert volume <= total
