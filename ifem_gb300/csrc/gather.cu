@@ -40,27 +40,28 @@ namespace ifemgpu {
 
 namespace {
 
-template <int P, int NPV>
+template <int P, int NPV, bool HALF>
 struct GCfg {
   static constexpr int Q = P + 1;
   static constexpr int NEN = Q * Q * Q;
   static constexpr int W = 2 * P + 1;
   static constexpr int NS = W * W * W;           // neighbour slots of a node
   static constexpr int KL = NPV * NPV;
+  // neighbour slots summed by a node's warp: all of them, or (HALF) the
+  // centre and the slots after it, the offsets (dz, dy, dx) >= 0 in
+  // lexicographic order -- each unordered node pair then belongs to exactly
+  // one of its two nodes
+  static constexpr int SB = HALF ? NS / 2 : 0;
+  static constexpr bool E3 = P == 3 && NPV == 3;
   // warps per CTA, elements whose loads are issued together, CTAs per SM:
   // measured on 64^3 (32^3 for p = 3 elasticity) models; more elements in
   // flight only add registers (p = 2 elasticity spilled with three) where
   // the warps of an SM already keep enough loads in flight
-  static constexpr int WARPS = (P == 3 && NPV == 3) ? 4 : (P == 3 ? 6 : 8);
+  static constexpr int WARPS = E3 ? (HALF ? 6 : 4) : (P == 3 ? 6 : 8);
   static constexpr int NB = (NEN + 31) / 32;           // element functions per lane
-  static constexpr int U = NPV == 3 ? (P == 2 ? 1 : 3) : (P == 3 ? 1 : 6);
-  static constexpr int MINB = (P == 3 && NPV == 3) ? 2 : (NPV == 3 ? 3 : (P == 3 ? 5 : 4));
-  // neighbour slots summed by a node's warp: all of them, or (half) the
-  // centre and the slots after it, the offsets (dz, dy, dx) >= 0 in
-  // lexicographic order -- each unordered node pair then belongs to exactly
-  // one of its two nodes
-  template <bool HALF> static constexpr int SB = HALF ? NS / 2 : 0;
-  template <bool HALF> static constexpr size_t smem() { return sizeof(float) * 2 * KL * (NS - SB<HALF>) * WARPS; }
+  static constexpr int U = NPV == 3 ? (P == 2 || HALF ? 1 : 3) : (P == 3 ? 1 : 6);
+  static constexpr int MINB = E3 ? (HALF ? 3 : 2) : (NPV == 3 ? 3 : (P == 3 ? 5 : 4));
+  static constexpr size_t SMEM = sizeof(float) * 2 * KL * (NS - SB) * WARPS;
 };
 
 // hi + lo += x (TwoSum: the rounding error of hi + x goes to lo)
@@ -110,13 +111,13 @@ struct GatherSys {
 // node's neighbour entries and writes its own columns, and the prescribed
 // neighbours' terms -c0 K(i, j) go to the right-hand side.
 template <int P, int NPV, bool HALF>
-__global__ void __launch_bounds__(GCfg<P, NPV>::WARPS * 32, GCfg<P, NPV>::MINB)
+__global__ void __launch_bounds__(GCfg<P, NPV, HALF>::WARPS * 32, GCfg<P, NPV, HALF>::MINB)
 k_gather(const DevPatch* __restrict__ patches, const int* __restrict__ start,
          const int* __restrict__ pidx, int nranges, int total, GatherSys S)
 {
-  using C = GCfg<P, NPV>;
+  using C = GCfg<P, NPV, HALF>;
   constexpr int Q = C::Q, NEN = C::NEN, W = C::W, NS = C::NS, KL = C::KL;
-  constexpr int SB = C::template SB<HALF>, NSH = NS - SB;
+  constexpr int SB = C::SB, NSH = NS - SB;
   extern __shared__ float gsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float2* acc = reinterpret_cast<float2*>(gsm) + warp * KL * NSH;  // [kl][slot - SB] (hi, lo)
@@ -287,8 +288,8 @@ namespace {
 template <int P, int NPV, bool HALF>
 ifemgpu_status prepareOne(ifemgpu_ctx* ctx, GatherList& g)
 {
-  using C = GCfg<P, NPV>;
-  const size_t smem = C::template smem<HALF>();
+  using C = GCfg<P, NPV, HALF>;
+  const size_t smem = C::SMEM;
   IFEMGPU_CUDA(ctx, cudaFuncSetAttribute(k_gather<P, NPV, HALF>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int perSM = 0;
@@ -302,10 +303,10 @@ ifemgpu_status prepareOne(ifemgpu_ctx* ctx, GatherList& g)
 template <int P, int NPV, bool HALF>
 ifemgpu_status launchOne(ifemgpu_ctx* ctx, const GatherList& g)
 {
-  using C = GCfg<P, NPV>;
+  using C = GCfg<P, NPV, HALF>;
   GatherSys S{ctx->d_madof, ctx->d_meqn, ctx->d_freeBefore, ctx->nceq ? ctx->d_c0 : nullptr,
               ctx->d_colptr, ctx->d_K, ctx->d_b};
-  k_gather<P, NPV, HALF><<<g.grid, C::WARPS * 32, C::template smem<HALF>(), ctx->stream>>>(
+  k_gather<P, NPV, HALF><<<g.grid, C::WARPS * 32, C::SMEM, ctx->stream>>>(
       ctx->d_patches, g.d_start, g.d_pidx, g.nranges, g.total, S);
   IFEMGPU_CUDA(ctx, cudaGetLastError());
   return IFEMGPU_OK;
