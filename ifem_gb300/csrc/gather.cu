@@ -312,37 +312,35 @@ ifemgpu_status launchOne(ifemgpu_ctx* ctx, const GatherList& g)
   return IFEMGPU_OK;
 }
 
-template <int P, int NPV>
-ifemgpu_status prepareAny(ifemgpu_ctx* ctx, GatherList& g)
-{
-  return g.half ? prepareOne<P, NPV, true>(ctx, g) : prepareOne<P, NPV, false>(ctx, g);
-}
-
-template <int P, int NPV>
-ifemgpu_status launchAny(ifemgpu_ctx* ctx, const GatherList& g)
-{
-  return g.half ? launchOne<P, NPV, true>(ctx, g) : launchOne<P, NPV, false>(ctx, g);
-}
-
 }  // namespace
 
-// kernel attributes and grid of a gather launch (before any capture)
+// kernel attributes and grid of a gather launch (before any capture); the
+// half-pair mode is built for p = 3 elasticity only, the one class that
+// takes it (for the others the mirrored writes cost more than they save)
 ifemgpu_status gatherPrepare(ifemgpu_ctx* ctx, GatherList& g)
 {
-  if (g.p == 2 && g.npv == 3) return prepareAny<2, 3>(ctx, g);
-  if (g.p == 2 && g.npv == 1) return prepareAny<2, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 1) return prepareAny<3, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 3) return prepareAny<3, 3>(ctx, g);
+  if (g.half) {
+    if (g.p == 3 && g.npv == 3) return prepareOne<3, 3, true>(ctx, g);
+    return setError(ctx, IFEMGPU_INVALID_ARG, "internal: half-pair gather class");
+  }
+  if (g.p == 2 && g.npv == 3) return prepareOne<2, 3, false>(ctx, g);
+  if (g.p == 2 && g.npv == 1) return prepareOne<2, 1, false>(ctx, g);
+  if (g.p == 3 && g.npv == 1) return prepareOne<3, 1, false>(ctx, g);
+  if (g.p == 3 && g.npv == 3) return prepareOne<3, 3, false>(ctx, g);
   return setError(ctx, IFEMGPU_INVALID_ARG, "internal: gather class");
 }
 
 ifemgpu_status gatherLaunch(ifemgpu_ctx* ctx, const GatherList& g)
 {
   if (g.total == 0) return IFEMGPU_OK;
-  if (g.p == 2 && g.npv == 3) return launchAny<2, 3>(ctx, g);
-  if (g.p == 2 && g.npv == 1) return launchAny<2, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 1) return launchAny<3, 1>(ctx, g);
-  if (g.p == 3 && g.npv == 3) return launchAny<3, 3>(ctx, g);
+  if (g.half) {
+    if (g.p == 3 && g.npv == 3) return launchOne<3, 3, true>(ctx, g);
+    return setError(ctx, IFEMGPU_INVALID_ARG, "internal: half-pair gather class");
+  }
+  if (g.p == 2 && g.npv == 3) return launchOne<2, 3, false>(ctx, g);
+  if (g.p == 2 && g.npv == 1) return launchOne<2, 1, false>(ctx, g);
+  if (g.p == 3 && g.npv == 1) return launchOne<3, 1, false>(ctx, g);
+  if (g.p == 3 && g.npv == 3) return launchOne<3, 3, false>(ctx, g);
   return setError(ctx, IFEMGPU_INVALID_ARG, "internal: gather class");
 }
 
