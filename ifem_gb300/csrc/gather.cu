@@ -62,6 +62,9 @@ struct GCfg {
   static constexpr int U = NPV == 3 ? (P == 2 || HALF ? 1 : 3) : (P == 3 ? 1 : 6);
   static constexpr int MINB = E3 ? (HALF ? 3 : 2) : (NPV == 3 ? 3 : (P == 3 ? 5 : 4));
   static constexpr size_t SMEM = sizeof(float) * 2 * KL * (NS - SB) * WARPS;
+  // MINB CTAs per SM must fit in its 228 KB of shared memory (1 KB of each
+  // CTA's share is reserved by the system)
+  static_assert(MINB * (SMEM + 1024) <= 228 * 1024, "gather accumulators exceed shared memory");
 };
 
 // hi + lo += x (TwoSum: the rounding error of hi + x goes to lo)
